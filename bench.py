@@ -1,0 +1,293 @@
+"""Benchmark: P+B boxes/s of the PBI4 estimator path on GB300.
+
+Workload (one "step" = one box through the whole path): 2,097,152 particles
+(128^3 lattice) displaced by the Zel'dovich approximation (P(k) ~ k^-1.5, rms
+displacement 5 Mpc/h, RSD along z with f = 0.7) in L = 1000 Mpc/h; grid 256^3,
+PCS with interlacing; P(k) multipoles l = 0,2,4 with dk = kf (128 bins);
+bispectrum B0,B2,B4 over all (open) triangles with dk = 3 kf up to 0.5 k_Nyq
+(21 shells, 1156 triangles).  Triangle counts depend only on the binning and
+are computed once per plan (the reference caches them in its cfile).
+
+Lines printed (rank 0): one JSON line for our arm, or for ``--impl reference``
+the CPU restatement of the reference (oracle/, serial loops as in the Fortran,
+FFTs on all host cores) timed on a bounded sample and extrapolated per box.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(workload="zeldovich_256_pcs_interlaced_P024_B024", particles=128 ** 3, box=1000.0, grid=256,
+                nintp=4, interlacing=True, multipoles=True, los=[0.0, 0.0, 1.0], kbin_ps=1.0, kcenter_ps=1.0,
+                nbins_ps=128, kbin_bs=3.0, kcenter_bs=3.0, nbins_bs=21, iopen=True)
+METRIC = "P+B boxes/s @256^3 PCS interlaced (P l=0,2,4 + B l=0,2,4)"
+
+
+def make_positions(quick=False):
+    from pbi4_gb300 import synthetic
+    n = 32 if quick else 128
+    return synthetic.zeldovich_box(n, WORKLOAD["box"], n_s=-1.5, rms_disp=5.0, f_growth=0.7, seed=2)
+
+
+def est_config(precision, grid=None):
+    from pbi4_gb300.estimator import EstimatorConfig
+    w = WORKLOAD
+    return EstimatorConfig(grid=grid or w["grid"], box=w["box"], nintp=w["nintp"], interlacing=w["interlacing"],
+                           multipoles=w["multipoles"], los=tuple(w["los"]), kbin_ps=w["kbin_ps"],
+                           kcenter_ps=w["kcenter_ps"], nbins_ps=w["nbins_ps"] if grid is None else None,
+                           do_bispectrum=True, kbin_bs=w["kbin_bs"], kcenter_bs=w["kcenter_bs"],
+                           nbins_bs=w["nbins_bs"] if grid is None else None, iopen=w["iopen"], precision=precision)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    def __init__(self, index=0):
+        self.index, self.rows, self.proc = index, [], None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows if len(r) >= 9 for k in range(4) if r[5 + k] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+# ------------------------------------------------------------ CPU legs ---
+def cpu_reference_box_seconds(pos, budget_s=20.0):
+    """Seconds per box of the CPU restatement of the reference, from a bounded
+    sample: assignment (full), one density FFT, fcomb, one of the 21
+    multipole FFTs (x22), measure_pk_multipoles, one shell-map FFT (x63) and a
+    subset of the triangle sums (extrapolated to all 1156 x 3 sums)."""
+    import scipy.fft
+
+    from oracle import pbi4_oracle as O
+    w = WORKLOAD
+    N, cores = w["grid"], os.cpu_count() or 1
+    p = dict(grid=N, box=w["box"], interpolation=w["nintp"], interlacing=w["interlacing"], multipoles=True,
+             kbin=w["kbin_ps"], kcenter=w["kcenter_ps"], iopen=True, los=w["los"], cross=False, om=0.3, ol=0.7,
+             z=0.5)
+    p.update(O.derived_params(p))
+    t = {}
+    t0 = time.perf_counter()
+    npart, dcl = O.assign_grid(pos, p)
+    t["assign"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    f = scipy.fft.fftn(dcl / npart, workers=cores)
+    t["fft"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    d = O.fcomb(N, w["nintp"], True, w["box"], f)
+    t["fcomb"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    dx = scipy.fft.ifftn(d, workers=cores)
+    q = O.compute_q2k(N, w["box"], scipy.fft.fftn(dx * 1.0, workers=cores), 3, 3)
+    t["multipoles"] = (time.perf_counter() - t0) * 22  # 1 ifftn + 21 fftn/q-factor passes
+    d2 = -0.5 * d + 1.5 * q
+    t0 = time.perf_counter()
+    O.measure_pk_multipoles(N, w["box"], 1.0, 1.0, w["nbins_ps"], d, d2, d2)
+    t["pk"] = time.perf_counter() - t0
+    nb = w["nbins_bs"]
+    full = O.hermitian_full_grid(d)
+    shell = O.shell_index(N, w["kbin_bs"], w["kcenter_bs"])
+    t0 = time.perf_counter()
+    m = scipy.fft.fftn(np.where(shell == 5, full, 0.0), workers=cores).real.ravel()
+    t["maps"] = (time.perf_counter() - t0) * 3 * nb
+    # triangle sums: time a few triangles of the serial FP64 loop (bispectrumI4.f90:484-488)
+    maps = np.stack([m, m, m])
+    ntri = 0
+    t0 = time.perf_counter()
+    counts = np.ones(1, dtype=np.float32)
+    bout = np.zeros((11, 1))
+    while time.perf_counter() - t0 < min(budget_s, 6.0) and ntri < 50:
+        O.lib().or_bk_multipoles_last_sum(1, 3.0, 3.0, 1, 0.00628, int(npart), N ** 3,
+                                          counts.ctypes.data_as(O._f), O._p(maps), O._p(maps), O._p(maps),
+                                          O._p(np.zeros(1)), O._p(bout))
+        ntri += 1
+    per_tri = (time.perf_counter() - t0) / ntri
+    t["triangle_sums"] = per_tri * 1156
+    total = sum(t.values())
+    sample = (f"full assignment + 1 density FFT + fcomb + P binning; 1 of 22 multipole FFT passes (x22), 1 of 63 "
+              f"shell-map FFTs (x63), {ntri} of 1156 triangle triple-sums (x1156/{ntri}); FFTs on {cores} threads, "
+              f"Fortran loops serial as in the reference")
+    return total, t, sample, cores
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import pbi4_oracle as O
+    O.build()
+    pos = make_positions(quick=args.quick)
+    vals = []
+    for k in range(args.warmup + args.steps):
+        sec, stages, sample, cores = cpu_reference_box_seconds(pos, budget_s=5.0)
+        if k >= args.warmup:
+            vals.append(sec)
+    sec = statistics.median(vals)
+    value = 1.0 / sec
+    line = {"metric": METRIC, "value": value, "unit": "boxes/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Zel'dovich box)",
+            "config": {**{k: v for k, v in WORKLOAD.items()}, "parallelism": "cpu"},
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "boxes/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "boxes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "stages_s": stages}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------ GPU arm ---
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    from pbi4_gb300.estimator import Estimator
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    pos = make_positions(quick=args.quick)
+    npart = pos.shape[1]
+    cfg = est_config(args.precision, grid=64 if args.quick else None)
+    est = Estimator(cfg)
+    dpos = torch.from_numpy(pos).cuda()
+    pout, bout = est.alloc_outputs()
+    # warm-up: plan tables, triangle counts, cuFFT plans
+    for _ in range(args.warmup):
+        est.run_device(npart, dpos, pout, bout)
+    torch.cuda.synchronize()
+    est.enable_timing(True)
+    est.stage_times()
+    launches0 = est.launches
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        start.record()
+        for _ in range(args.steps):
+            est.run_device(npart, dpos, pout, bout)
+        stop.record()
+        torch.cuda.synchronize()
+    barrier()
+    ms = start.elapsed_time(stop)
+    launches = est.launches - launches0
+    stages = est.stage_times()
+    est.enable_timing(False)
+    t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = world * args.steps / (ms_max / 1e3)
+
+    # e2e: host (pinned) positions in, host results out, through the C-ABI call
+    hpos = torch.from_numpy(pos).pin_memory().numpy()
+    for _ in range(2):
+        est.run_host(hpos)
+    barrier()
+    t0 = time.perf_counter()
+    e2e_steps = max(2, args.steps // 2)
+    for _ in range(e2e_steps):
+        p_h, b_h = est.run_host(hpos)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    te = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+    if world > 1:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e_value = world / float(te.item())
+
+    # roofline of the dominant kernel stage
+    from pbi4_gb300 import roofline
+    rl = roofline.for_stages(stages, args.steps, cfg, npart)
+    clocks = clk.summary()
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline:
+            sec, _, sample, cores = cpu_reference_box_seconds(pos, budget_s=10.0)
+            cpu = {"value": 1.0 / sec, "unit": "boxes/s", "cores": cores, "kind": "port", "sample": sample}
+        line = {"metric": METRIC, "value": value, "unit": "boxes/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else args.precision,
+                "data": "synthetic (seeded Zel'dovich box, positions resident in HBM)",
+                "config": {**WORKLOAD, "precision": args.precision, "parallelism": f"replicas{world}",
+                           "l2": "working set > L2 (shell maps %.1f GB per box)" % (
+                               3 * WORKLOAD["nbins_bs"] * 256 * 256 * 129 * 8 / 1e9),
+                           "triangle_counts": "computed once per plan (input independent)"},
+                "e2e": {"value": e2e_value, "unit": "boxes/s", "h2d_bytes_per_step": int(pos.nbytes),
+                        "d2h_bytes_per_step": int(p_h.nbytes + b_h.nbytes)},
+                "gpu_launches": int(launches), "clocks": clocks, "roofline": rl, "cpu_baseline": cpu,
+                "stages_ms_per_box": {k: round(v[0] / max(1, args.steps), 4) for k, v in stages.items()}}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "fp16split", "bf16"])
+    ap.add_argument("--quick", action="store_true", help="small box (debug only)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

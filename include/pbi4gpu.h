@@ -1,0 +1,184 @@
+/*
+ * pbi4gpu.h -- C ABI of the GB300 (sm_103a) PBI4 estimator library (libpbi4gpu.so).
+ *
+ * Two groups of entry points:
+ *
+ *  1. Drop-ins for the f2py routines the reference's pbi4/pbi4.py imports
+ *     (`from powerI4 import ...`, `from bispectrumI4 import ...`, pbi4.py:12-14).
+ *     Same arguments, same meaning, host buffers in and out, Fortran-ordered
+ *     3-D grids (a(ix,iy,iz) with ix fastest), complex grids as interleaved
+ *     (re, im) float64.  Outputs are fully written (f2py zero-fills them).
+ *     The computation runs on the current CUDA device; copies are inside.
+ *
+ *  2. A device-resident estimator plan (the throughput path): positions in
+ *     HBM -> density -> P(k) multipoles -> bispectrum, with FFT plans, shell
+ *     tables and triangle counts kept resident between boxes.
+ *
+ * Every function returns PBI4G_OK (0) or a PBI4G_ERR_* code and never exits the
+ * process; pbi4g_last_error() gives the message of the calling thread's last
+ * failure.  Scalar kinds follow the Fortran interfaces: `real` -> float,
+ * `real(kind=8)` -> double, `integer` -> int32_t, `integer(kind=8)` -> int64_t,
+ * `logical` -> int32_t (0/1).
+ */
+#ifndef PBI4GPU_H
+#define PBI4GPU_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PBI4G_OK 0
+#define PBI4G_ERR_INVALID 1     /* bad argument (sizes, ranges, null pointers) */
+#define PBI4G_ERR_CUDA 2        /* CUDA runtime error */
+#define PBI4G_ERR_NOMEM 3       /* device allocation failed */
+#define PBI4G_ERR_CUFFT 4       /* cuFFT error */
+#define PBI4G_ERR_TIMEOUT 5     /* a bounded device wait gave up */
+#define PBI4G_ERR_UNSUPPORTED 6 /* option not supported by this build / device */
+#define PBI4G_ERR_RANGE 7       /* input outside the documented range (e.g. fixed-point bound) */
+
+/* Arithmetic of the shell maps and triangle sums (and of the FFTs for FP64). */
+#define PBI4G_PREC_FP32 0      /* plain form: FP32 FFTs, maps and products, FP64 bin reductions */
+#define PBI4G_PREC_FP64 1      /* FP64 everywhere (GPU oracle form) */
+#define PBI4G_PREC_FP16SPLIT 2 /* mixed: maps as FP16 hi+lo, tensor-core sums, FP32 accumulate */
+#define PBI4G_PREC_BF16 3      /* mixed: maps as BF16, tensor-core sums, FP32 accumulate */
+
+const char *pbi4g_last_error(void);
+int pbi4g_version(void);
+/* Precision used by the drop-in bispectrum entry points (default FP32). */
+int pbi4g_set_dropin_precision(int32_t precision);
+
+/* ---------------- 1. f2py drop-ins: powerI4 ---------------- */
+
+/* replaces powerI4.f90:68-140 assign_single_grid.  pos: (3, npart) float64,
+ * C order (pos[c*npart + i]); weight: npart float64; dtl: grid^3 float64.
+ * Accumulation is 64-bit fixed point, so dtl is bit-reproducible. */
+int pbi4g_assign_single_grid(int32_t grid, int32_t nintp, int64_t npart, const double *pos,
+                             const double *weight, double *dtl);
+/* replaces powerI4.f90:142-249 assign_double_grid; dcl: grid^3 complex128,
+ * Re = grid at x, Im = grid at x - 1/2 cell. */
+int pbi4g_assign_double_grid(int32_t grid, int32_t nintp, int64_t npart, const double *pos,
+                             const double *weight, double *dcl);
+/* replaces powerI4.f90:251-378 fcomb (interlacing combine + window deconvolution
+ * of a full complex FFT); fdcl and dcl: grid^3 complex128 (may alias). */
+int pbi4g_fcomb(int32_t grid, int32_t nintp, int32_t interlacing, float box, const double *fdcl,
+                double *dcl);
+/* replaces powerI4.f90:380-407 reduce_array; din: L^3, dout: grid^3 complex128. */
+int pbi4g_reduce_array(int32_t L, const double *din, int32_t grid, double *dout);
+/* replaces powerI4.f90:409-458 compute_q2k (1-based i, j). */
+int pbi4g_compute_q2k(int32_t grid, float box, const double *deltak, int32_t i, int32_t j, double *q2k);
+/* replaces powerI4.f90:460-508 compute_q4k (1-based i, j, l, k). */
+int pbi4g_compute_q4k(int32_t grid, float box, const double *deltak, int32_t i, int32_t j, int32_t l,
+                      int32_t k, double *q4k);
+/* replaces powerI4.f90:510-594 measure_pk; pout: (5, nbins) float64, Fortran order. */
+int pbi4g_measure_pk(int32_t grid, float box, float kbin, float kcenter, int32_t nbins, const double *dcl1,
+                     const double *dcl2, double *pout);
+/* replaces powerI4.f90:596-693 measure_pk_multipoles. */
+int pbi4g_measure_pk_multipoles(int32_t grid, float box, float kbin, float kcenter, int32_t nbins,
+                                const double *dcl, const double *dcl2, const double *dcl4, double *pout);
+
+/* ---------------- 1. f2py drop-ins: bispectrumI4 ---------------- */
+
+/* replaces bispectrumI4.f90:763-915 count_triangles; counts: itot float64
+ * (= grid^3 x exact integer triangle count). npool is accepted and ignored. */
+int pbi4g_count_triangles(int32_t nbins, int32_t grid, float kbin, float kcenter, int32_t iopen,
+                          int32_t cross, int32_t npool, int64_t itot, double *counts);
+/* replaces bispectrumI4.f90:1-198 measure_bk; bout: (9, itot) float64 Fortran order. */
+int pbi4g_measure_bk(int32_t nbins, int32_t grid, float kbin, float kcenter, int32_t iopen, float kf,
+                     int32_t npool, int64_t itot, int64_t npart, const float *counts, const double *dcl,
+                     double *bout);
+/* replaces bispectrumI4.f90:200-516 measure_bk_multipoles; bout: (11, itot). */
+int pbi4g_measure_bk_multipoles(int32_t nbins, int32_t grid, float kbin, float kcenter, int32_t iopen,
+                                float kf, int32_t npool, int64_t itot, int64_t npart, const float *counts,
+                                const double *dcl, const double *dcl2, const double *dcl4, double *bout);
+/* replaces bispectrumI4.f90:518-761 measure_bk_cross; bout: (5, itot). */
+int pbi4g_measure_bk_cross(int32_t nbins, int32_t grid, float kbin, float kcenter, int32_t iopen, float kf,
+                           int32_t npool, int64_t itot, int64_t npart, const float *counts,
+                           const double *dcl1, const double *dcl2, double *bout);
+
+/* ---------------- 2. device-resident estimator plan ---------------- */
+
+/* One estimator configuration: the params dict of pbi4.py (IO.derived_params,
+ * pbi4.py:86-119) reduced to what the hot path reads.  P and B may use
+ * different binnings (the reference shares kbin/kcenter; pass equal values to
+ * reproduce it). */
+typedef struct pbi4g_config {
+    int32_t grid;        /* N */
+    float box;           /* L in Mpc/h (real(4), as the reference passes it) */
+    int32_t nintp;       /* 1 NGP, 2 CIC, 3 TSC, 4 PCS */
+    int32_t interlacing; /* 0/1 */
+    int32_t multipoles;  /* 0: P0 / B0 (real space); 1: P0,P2,P4 / B0,B2,B4 */
+    double los[3];       /* params['los'] after derived_params: los / (los . los) */
+    float kbin_ps, kcenter_ps;
+    int32_t nbins_ps;
+    int32_t do_bispectrum; /* 0: P only */
+    float kbin_bs, kcenter_bs;
+    int32_t nbins_bs;
+    int32_t iopen;
+    int32_t precision;   /* PBI4G_PREC_* of the shell maps / triangle sums */
+    int32_t reserved[7]; /* must be zero */
+} pbi4g_config;
+
+typedef struct pbi4g_plan pbi4g_plan;
+
+/* Device bytes a plan for cfg needs for boxes of up to npart_max particles
+ * (admission control).  Does not allocate. */
+int pbi4g_plan_footprint(const pbi4g_config *cfg, int64_t npart_max, int64_t *bytes);
+/* Create a plan on the current device (allocates its buffers, cuFFT plans,
+ * bin/shell tables; triangle counts are computed on first use and cached). */
+int pbi4g_plan_create(const pbi4g_config *cfg, pbi4g_plan **out);
+int pbi4g_plan_destroy(pbi4g_plan *plan);
+/* Work of the plan is issued on this stream (a cudaStream_t; NULL = legacy default). */
+int pbi4g_plan_set_stream(pbi4g_plan *plan, void *stream);
+/* Output sizes: pout is (5, nbins_ps), bout is (brows, itot), Fortran order. */
+int pbi4g_plan_shape(const pbi4g_plan *plan, int32_t *nbins_ps, int64_t *itot, int32_t *brows);
+/* Exact integer triangle counts of the plan's binning (computed once, cached). */
+int pbi4g_plan_triangle_counts(pbi4g_plan *plan, int64_t *counts_host);
+
+/* Density stage (pbi4.py:290-341 + 343-388): positions (3, npart) float64 in
+ * [0,1) on the device (pos[c*npart+i]); weight device float64 or NULL (ones).
+ * Leaves delta(k) on the kx >= 0 half resident in the plan. */
+int pbi4g_plan_density(pbi4g_plan *plan, int64_t npart, const double *d_pos, const double *d_weight);
+/* P(k) stage (pbi4.py:405-461): d_pout device (5, nbins_ps) float64: rows avgk,
+ * P0 (not shot-noise subtracted, as measure_pk*), P2, P4, Nmodes. */
+int pbi4g_plan_powerspectrum(pbi4g_plan *plan, double *d_pout);
+/* B stage (pbi4.py:478-553): d_bout device (brows, itot) float64, rows as
+ * measure_bk (9) / measure_bk_multipoles (11). */
+int pbi4g_plan_bispectrum(pbi4g_plan *plan, double *d_bout);
+/* Whole box on device buffers: density + P (+ B when configured). */
+int pbi4g_plan_run_device(pbi4g_plan *plan, int64_t npart, const double *d_pos, const double *d_weight,
+                          double *d_pout, double *d_bout);
+/* Whole box from host buffers (pinned or pageable): copies in, runs, copies
+ * pout/bout back, synchronises the plan's stream. */
+int pbi4g_plan_run_host(pbi4g_plan *plan, int64_t npart, const double *pos, const double *weight,
+                        double *pout, double *bout);
+/* Copy the resident delta(k) half spectrum (N, N, N/2+1) complex128, C order
+ * [z][y][x], to host memory. */
+int pbi4g_plan_get_delta_half(pbi4g_plan *plan, double *host_half);
+/* Launches of this library's kernels issued by this plan since creation. */
+int64_t pbi4g_plan_kernel_launches(const pbi4g_plan *plan);
+
+/* Stage timing with CUDA events on the plan's stream (off by default).
+ * Stages: 0 assign, 1 grid convert, 2 forward FFT, 3 fcomb, 4 P(k) binning,
+ * 5 triangle counts, 6 shell spectra, 7 inverse FFT, 8 triangle sums,
+ * 9 output rows.  pbi4g_plan_stage_times synchronises the stream, writes the
+ * summed milliseconds and the number of timed calls per stage since the last
+ * query (arrays of PBI4G_NSTAGES) and resets them. */
+#define PBI4G_NSTAGES 10
+int pbi4g_plan_enable_timing(pbi4g_plan *plan, int32_t enable);
+int pbi4g_plan_stage_times(pbi4g_plan *plan, double *ms, int64_t *calls);
+
+#ifdef __cplusplus
+}
+#endif
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+
+#endif /* PBI4GPU_H */

@@ -1,0 +1,545 @@
+// bispec.cu -- shell tables, shell-filtered k-maps, CUDA-core triangle sums,
+// exact triangle counts and the bispectrum output rows.
+//
+// Reference: bispectrumI4.f90 measure_bk (1-198), measure_bk_multipoles
+// (200-516), measure_bk_cross (518-761), count_triangles (763-915).
+//
+// k-maps: the reference expands the kx >= 0 half spectrum to a full Hermitian
+// grid, zeroes the imaginary part at the 8 self-conjugate points, and keeps the
+// real part of a complex FFT of each shell-masked copy (:116-157).  The real
+// part of a complex FFT equals the FFT of the input's Hermitian part, so here
+// the masked half spectrum is Hermitian-symmetrised on the kx = 0 and kx = N/2
+// planes and transformed with one batched C2R (cuFFT).  The reference's
+// FORWARD transform and its x<->z transposed layout map x -> -x and permute
+// axes; every output is a sum over all x, which neither changes.
+#include "bispec.cuh"
+
+#include <float.h>
+#include <math.h>
+#include <algorithm>
+#include <map>
+
+namespace pbi4g {
+
+constexpr int kTP = 4;   // pairs per thread tile
+constexpr int kTQ = 8;   // q maps per thread tile
+constexpr int kKC = 32;  // contraction points per shared-memory chunk
+constexpr int kGroupThreads = 256;
+
+// ------------------------------------------------------------- Shells ---
+int Shells::build(int N_, float kbin_, float kcenter_, int nb_, int iopen_, int cross_, cudaStream_t st) {
+    if (N == N_ && kbin == kbin_ && kcenter == kcenter_ && nb == nb_ && iopen == iopen_ && cross == cross_ && lut.p)
+        return PBI4G_OK;
+    if (nb_ < 1 || nb_ > 4096 || !(kbin_ > 0) || N_ < 4 || (N_ & 1))
+        return set_error(PBI4G_ERR_INVALID, "shells: grid=%d nbins=%d kbin=%g", N_, nb_, kbin_);
+    N = N_; kbin = kbin_; kcenter = kcenter_; nb = nb_; iopen = iopen_; cross = cross_;
+    counts.clear();
+    const double kck = (double)(kcenter / kbin);
+    const int h = N / 2;
+    k2max = 3 * h * h;
+    lut_h.assign(k2max + 1, 0);
+    for (int k2 = 0; k2 <= k2max; k2++) {
+        // idist = nint(dsqrt(di*di+dj*dj+dl*dl)/kbin - kcenter/kbin - tiny) + 1
+        // (bispectrumI4.f90:73); di^2+dj^2+dl^2 is exact, so idist depends on k2 only.
+        long long b = llround(sqrt((double)k2) / (double)kbin - kck - (double)FLT_MIN) + 1;
+        lut_h[k2] = (b >= 1 && b <= nb) ? (int)b : 0;
+    }
+    // full-grid modes per shell: multiplicity of |k_axis| = d is 1 for d in {0, N/2}, else 2
+    nmodes.assign(nb, 0);
+    for (int dz = 0; dz <= h; dz++)
+        for (int dy = 0; dy <= h; dy++)
+            for (int dx = 0; dx <= h; dx++) {
+                int b = lut_h[dx * dx + dy * dy + dz * dz];
+                if (!b) continue;
+                int m = (dx == 0 || dx == h ? 1 : 2) * (dy == 0 || dy == h ? 1 : 2) * (dz == 0 || dz == h ? 1 : 2);
+                nmodes[b - 1] += m;
+            }
+    ishift = (int)(kcenter / kbin) + (iopen ? 1 : 0);  // bispectrumI4.f90:38-42
+    tri.clear();
+    for (int l = 1; l <= nb; l++)
+        for (int j = 1; j <= l; j++) {
+            int imax = cross ? std::min(nb, j + l - 1 + ishift) : j;
+            for (int i = std::max(1, l - j + 1 - ishift); i <= imax; i++) {
+                tri.push_back(l);
+                tri.push_back(j);
+                tri.push_back(i);
+            }
+        }
+    itot = (int64_t)tri.size() / 3;
+    PBI4G_CHECK(lut.ensure(sizeof(int) * (k2max + 1)));
+    PBI4G_CUDA(cudaMemcpyAsync(lut.p, lut_h.data(), sizeof(int) * (k2max + 1), cudaMemcpyHostToDevice, st));
+    std::vector<double> nm(nb);
+    for (int b = 0; b < nb; b++) nm[b] = (double)nmodes[b];
+    PBI4G_CHECK(tri_d.ensure(sizeof(int) * std::max<size_t>(3, tri.size())));
+    PBI4G_CUDA(cudaMemcpyAsync(tri_d.p, tri.data(), sizeof(int) * tri.size(), cudaMemcpyHostToDevice, st));
+    PBI4G_CHECK(nmodes_d.ensure(sizeof(double) * nb));
+    PBI4G_CUDA(cudaMemcpyAsync(nmodes_d.p, nm.data(), sizeof(double) * nb, cudaMemcpyHostToDevice, st));
+    PBI4G_CUDA(cudaStreamSynchronize(st));
+    return PBI4G_OK;
+}
+
+// ------------------------------------------------------------ TriPlan ---
+// Output slot (m, s) = m * nsets + s.  Non-cross: S = sum M_i M_j Q_{s,l}, pair
+// (i, j) of set-0 maps, q = map s*nb + l-1.  Cross: S = sum Q_i M_j M_l, pair
+// (j, l) of set-0 maps, q = map qset*nb + i-1.
+int TriPlan::build(const Shells &sh, int nsets_, int cross_) {
+    nsets = nsets_;
+    cross = cross_;
+    const int nb = sh.nb;
+    std::map<std::pair<int, int>, int> pidx;  // pair -> index in first-appearance order
+    std::vector<int2> plist;
+    std::vector<int> qlist;
+    std::map<int, int> qidx;
+    struct E { int p, q, slot; };
+    std::vector<E> ents;
+    for (int64_t m = 0; m < sh.itot; m++) {
+        const int l = sh.tri[3 * m], j = sh.tri[3 * m + 1], i = sh.tri[3 * m + 2];
+        for (int s = 0; s < nsets; s++) {
+            int pa, pb, qm;
+            if (!cross) { pa = i - 1; pb = j - 1; qm = s * nb + l - 1; }
+            else { pa = j - 1; pb = l - 1; qm = cross * nb + i - 1; }  // cross = set index of the q field
+            auto pk = std::make_pair(pb, pa);
+            auto it = pidx.find(pk);
+            int p;
+            if (it == pidx.end()) { p = (int)plist.size(); pidx[pk] = p; plist.push_back(make_int2(pa, pb)); }
+            else p = it->second;
+            qidx[qm] = 0;
+            ents.push_back({p, qm, (int)(m * nsets + s)});
+        }
+    }
+    // q order: sorted map index
+    for (auto &kv : qidx) { kv.second = (int)qlist.size(); qlist.push_back(kv.first); }
+    for (auto &e : ents) e.q = qidx[e.q];
+    np = (int)plist.size();
+    nq = (int)qlist.size();
+    nslots = (int)(sh.itot * nsets);
+    // tiles
+    std::map<std::pair<int, int>, int> tidx;
+    std::vector<int4> tl;
+    std::vector<int> stab;
+    for (auto &e : ents) {
+        auto key = std::make_pair(e.p / kTP, e.q / kTQ);
+        auto it = tidx.find(key);
+        int t;
+        if (it == tidx.end()) {
+            t = (int)tl.size();
+            tidx[key] = t;
+            tl.push_back(make_int4(key.first * kTP, key.second * kTQ, 0, t * kTP * kTQ));
+            stab.resize(stab.size() + kTP * kTQ, -1);
+        } else t = it->second;
+        stab[(size_t)t * kTP * kTQ + (e.p % kTP) * kTQ + (e.q % kTQ)] = e.slot;
+    }
+    // order tiles by (pair tile, q tile) and cut into groups of <= 256 tiles and <= 256 pairs
+    std::vector<int> order(tl.size());
+    for (size_t k = 0; k < order.size(); k++) order[k] = (int)k;
+    std::sort(order.begin(), order.end(), [&](int a, int b) {
+        return tl[a].x != tl[b].x ? tl[a].x < tl[b].x : tl[a].y < tl[b].y;
+    });
+    std::vector<int4> tiles_sorted;
+    std::vector<int> stab_sorted;
+    std::vector<int4> gl;
+    int g_t0 = 0, g_p0 = -1;
+    for (size_t k = 0; k < order.size(); k++) {
+        int4 t = tl[order[k]];
+        if (g_p0 < 0) g_p0 = t.x;
+        const int ntile_g = (int)tiles_sorted.size() - g_t0;
+        if (ntile_g >= kGroupThreads || t.x + kTP - g_p0 > 256) {
+            gl.push_back(make_int4(g_t0, (int)tiles_sorted.size(), g_p0, tiles_sorted.back().x + kTP));
+            g_t0 = (int)tiles_sorted.size();
+            g_p0 = t.x;
+        }
+        int ns = (int)tiles_sorted.size();
+        stab_sorted.insert(stab_sorted.end(), stab.begin() + (size_t)t.w, stab.begin() + (size_t)t.w + kTP * kTQ);
+        t.z = (int)gl.size();
+        t.w = ns * kTP * kTQ;
+        tiles_sorted.push_back(t);
+    }
+    if ((int)tiles_sorted.size() > g_t0)
+        gl.push_back(make_int4(g_t0, (int)tiles_sorted.size(), g_p0, tiles_sorted.back().x + kTP));
+    ntiles = (int)tiles_sorted.size();
+    ngroups = (int)gl.size();
+    max_group_pairs = 0;
+    for (auto &g : gl) max_group_pairs = std::max(max_group_pairs, g.w - g.z);
+    // pad pair list to a multiple of kTP with a harmless pair (0,0)
+    while ((int)plist.size() % kTP) plist.push_back(make_int2(0, 0));
+    while ((int)qlist.size() % kTQ) qlist.push_back(qlist.empty() ? 0 : qlist[0]);
+    PBI4G_CHECK(pairs.ensure(sizeof(int2) * plist.size()));
+    PBI4G_CUDA(cudaMemcpy(pairs.p, plist.data(), sizeof(int2) * plist.size(), cudaMemcpyHostToDevice));
+    PBI4G_CHECK(qmap.ensure(sizeof(int) * qlist.size()));
+    PBI4G_CUDA(cudaMemcpy(qmap.p, qlist.data(), sizeof(int) * qlist.size(), cudaMemcpyHostToDevice));
+    PBI4G_CHECK(tiles.ensure(sizeof(int4) * std::max<size_t>(1, tiles_sorted.size())));
+    PBI4G_CUDA(cudaMemcpy(tiles.p, tiles_sorted.data(), sizeof(int4) * tiles_sorted.size(), cudaMemcpyHostToDevice));
+    PBI4G_CHECK(slots.ensure(sizeof(int) * std::max<size_t>(1, stab_sorted.size())));
+    PBI4G_CUDA(cudaMemcpy(slots.p, stab_sorted.data(), sizeof(int) * stab_sorted.size(), cudaMemcpyHostToDevice));
+    PBI4G_CHECK(groups.ensure(sizeof(int4) * std::max<size_t>(1, gl.size())));
+    PBI4G_CUDA(cudaMemcpy(groups.p, gl.data(), sizeof(int4) * gl.size(), cudaMemcpyHostToDevice));
+    return PBI4G_OK;
+}
+
+// ------------------------------------------------------- map spectra ---
+template <class C> __device__ __forceinline__ C czero() { C c; c.x = 0; c.y = 0; return c; }
+
+template <class R>
+__global__ void build_map_spectra_kernel(int N, int nb, const int *__restrict__ lut, int m0, int count,
+                                         const typename Cx<R>::T *__restrict__ s0,
+                                         const typename Cx<R>::T *__restrict__ s1,
+                                         const typename Cx<R>::T *__restrict__ s2, int f0, int f1, int f2, double l0,
+                                         double l1, double l2, typename Cx<R>::T *__restrict__ out,
+                                         double *__restrict__ powsum) {
+    using C = typename Cx<R>::T;
+    extern __shared__ double spow[];
+    if (powsum)
+        for (int b = threadIdx.x; b < nb; b += blockDim.x) spow[b] = 0.0;
+    __syncthreads();
+    const int NH = N / 2 + 1;
+    const size_t HC = (size_t)N * N * NH;
+    for (size_t cell = blockIdx.x * (size_t)blockDim.x + threadIdx.x; cell < HC;
+         cell += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(cell % NH), y = (int)((cell / NH) % N), z = (int)(cell / ((size_t)NH * N));
+        const int ay = kabs0(y, N), az = kabs0(z, N);
+        const int sb = lut[x * x + ay * ay + az * az];
+        const int s_lo = m0 / nb, s_hi = (m0 + count - 1) / nb;
+        if (sb == 0) {
+            for (int j = 0; j < count; j++) out[(size_t)j * HC + cell] = czero<C>();
+            continue;
+        }
+        const bool herm = (x == 0 || x == N / 2);
+        const size_t mc = ((size_t)kneg0(z, N) * N + kneg0(y, N)) * NH + x;
+        const int ky = kfreq0(y, N), kz = kfreq0(z, N);
+        const int k2 = x * x + ky * ky + kz * kz;
+        const double lk = l0 * x + l1 * ky + l2 * kz;
+        const R mu2 = k2 > 0 ? (R)(lk * lk / (double)k2) : (R)0;
+        // one value per set present in the chunk
+        C val[3];
+#pragma unroll
+        for (int s = 0; s < 3; s++) {
+            val[s] = czero<C>();
+            if (s < s_lo || s > s_hi) continue;
+            const C *src = s == 0 ? s0 : (s == 1 ? s1 : s2);
+            const int fac = s == 0 ? f0 : (s == 1 ? f1 : f2);
+            C v = src[cell];
+            if (herm) {
+                const C w = src[mc];
+                v.x = (v.x + w.x) * (R)0.5;
+                v.y = (v.y - w.y) * (R)0.5;
+            }
+            R L = 1;
+            if (fac == 2) L = (R)-0.5 + (R)1.5 * mu2;
+            else if (fac == 4) L = (R)0.375 + mu2 * ((R)-3.75 + (R)4.375 * mu2);
+            v.x *= L;
+            v.y *= L;
+            val[s] = v;
+        }
+        for (int j = 0; j < count; j++) {
+            const int m = m0 + j, s = m / nb, b = m % nb + 1;
+            out[(size_t)j * HC + cell] = (b == sb) ? val[s] : czero<C>();
+        }
+        if (powsum && s_lo == 0 && (sb - 1) >= m0 && (sb - 1) < m0 + count) {
+            const C v = val[0];
+            atomicAdd(&spow[sb - 1], (herm ? 1.0 : 2.0) * ((double)v.x * v.x + (double)v.y * v.y));
+        }
+    }
+    if (powsum) {
+        __syncthreads();
+        for (int b = threadIdx.x; b < nb; b += blockDim.x)
+            if (spow[b] != 0.0) atomicAdd(powsum + b, spow[b]);
+    }
+}
+
+template <class R>
+int build_map_spectra(const Shells &sh, int m0, int count, const typename Cx<R>::T *const src[3], const int fac[3],
+                      const double los[3], typename Cx<R>::T *out, double *powsum, cudaStream_t st,
+                      int64_t *launches) {
+    const int N = sh.N;
+    const size_t smem = powsum ? sizeof(double) * sh.nb : 0;
+    build_map_spectra_kernel<R><<<grid_blocks(half_cells(N), 256, 152 * 8), 256, smem, st>>>(
+        N, sh.nb, sh.lut.as<int>(), m0, count, src[0], src[1], src[2], fac[0], fac[1], fac[2], los ? los[0] : 0,
+        los ? los[1] : 0, los ? los[2] : 0, out, powsum);
+    PBI4G_LAUNCH_CHECK();
+    ++*launches;
+    return PBI4G_OK;
+}
+
+template int build_map_spectra<float>(const Shells &, int, int, const float2 *const[3], const int[3], const double[3],
+                                      float2 *, double *, cudaStream_t, int64_t *);
+template int build_map_spectra<double>(const Shells &, int, int, const double2 *const[3], const int[3],
+                                       const double[3], double2 *, double *, cudaStream_t, int64_t *);
+
+template <class R>
+__global__ void build_indicator_kernel(int N, const int *__restrict__ lut, int m0, int count,
+                                       typename Cx<R>::T *__restrict__ out) {
+    using C = typename Cx<R>::T;
+    const int NH = N / 2 + 1;
+    const size_t HC = (size_t)N * N * NH;
+    for (size_t cell = blockIdx.x * (size_t)blockDim.x + threadIdx.x; cell < HC;
+         cell += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(cell % NH), ay = kabs0((int)((cell / NH) % N), N),
+                  az = kabs0((int)(cell / ((size_t)NH * N)), N);
+        const int sb = lut[x * x + ay * ay + az * az];
+        for (int j = 0; j < count; j++) {
+            C v = czero<C>();
+            if (sb == m0 + j + 1) v.x = 1;
+            out[(size_t)j * HC + cell] = v;
+        }
+    }
+}
+
+template <class R>
+int build_indicator_spectra(const Shells &sh, int m0, int count, typename Cx<R>::T *out, cudaStream_t st,
+                            int64_t *launches) {
+    build_indicator_kernel<R><<<grid_blocks(half_cells(sh.N), 256, 152 * 8), 256, 0, st>>>(sh.N, sh.lut.as<int>(), m0,
+                                                                                         count, out);
+    PBI4G_LAUNCH_CHECK();
+    ++*launches;
+    return PBI4G_OK;
+}
+template int build_indicator_spectra<float>(const Shells &, int, int, float2 *, cudaStream_t, int64_t *);
+template int build_indicator_spectra<double>(const Shells &, int, int, double2 *, cudaStream_t, int64_t *);
+
+// ------------------------------------------------------ triangle sums ---
+// four consecutive values from 16-byte-aligned shared memory
+__device__ __forceinline__ void load4(const float *p, float v[4]) {
+    const float4 a = *reinterpret_cast<const float4 *>(p);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+}
+__device__ __forceinline__ void load4(const double *p, double v[4]) {
+    const double2 a = *reinterpret_cast<const double2 *>(p), b = *reinterpret_cast<const double2 *>(p + 2);
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+
+// Accumulation of one chunk into the running sum: Kahan-compensated for FP32.
+template <class T> struct Runner {
+    T sum = 0, comp = 0;
+    __device__ __forceinline__ void add(T v) {
+        T y = v - comp;
+        T t = sum + y;
+        comp = (t - sum) - y;
+        sum = t;
+    }
+};
+template <> struct Runner<double> {
+    double sum = 0, comp = 0;
+    __device__ __forceinline__ void add(double v) { sum += v; }
+};
+
+template <class T>
+__global__ void __launch_bounds__(kGroupThreads) trisum_kernel(
+    int N, const T *__restrict__ maps, size_t mstride, int rs, int nb, int nq, int qpad, const int *__restrict__ qmap,
+    const int2 *__restrict__ pairs, const int4 *__restrict__ tiles, const int4 *__restrict__ groups,
+    const int *__restrict__ slots, int ngroups, int ksplit, long long K, int nslots, int gpad,
+    double *__restrict__ partial) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *sQ = reinterpret_cast<T *>(smem_raw);                 // [kKC][qpad]
+    T *sA = sQ + (size_t)kKC * qpad;                         // [nb][kKC]   set-0 maps (pair sources)
+    T *sP = sA + (size_t)nb * kKC;                           // [kKC][gpad] pair products of this group
+    const int g = blockIdx.x % ngroups, split = blockIdx.x / ngroups;
+    const int4 G = groups[g];
+    const int ntile = G.y - G.x, p0g = G.z, npg = G.w - G.z;
+    const int my = threadIdx.x;
+    int4 tile = make_int4(0, 0, 0, 0);
+    if (my < ntile) tile = tiles[G.x + my];
+    const int tp = tile.x - p0g, tq = tile.y;
+
+    long long kb = (K * split) / ksplit, ke = (K * (split + 1)) / ksplit;
+    kb = kb / kKC * kKC;
+    if (split + 1 < ksplit) ke = ke / kKC * kKC;
+
+    T acc[kTP][kTQ];
+    Runner<T> run[kTP][kTQ];
+#pragma unroll
+    for (int a = 0; a < kTP; a++)
+#pragma unroll
+        for (int b = 0; b < kTQ; b++) acc[a][b] = 0;
+
+    for (long long k0 = kb; k0 < ke; k0 += kKC) {
+        // stage q maps (transposed) and pair-source maps
+        for (int idx = threadIdx.x; idx < nq * kKC; idx += blockDim.x) {
+            const int q = idx / kKC, kk = idx % kKC;
+            const long long p = k0 + kk;
+            T v = 0;
+            if (p < ke) v = maps[(size_t)qmap[q] * mstride + (size_t)(p / N) * rs + (size_t)(p % N)];
+            sQ[(size_t)kk * qpad + q] = v;
+        }
+        for (int idx = threadIdx.x; idx < nb * kKC; idx += blockDim.x) {
+            const int a = idx / kKC, kk = idx % kKC;
+            const long long p = k0 + kk;
+            T v = 0;
+            if (p < ke) v = maps[(size_t)a * mstride + (size_t)(p / N) * rs + (size_t)(p % N)];
+            sA[idx] = v;
+        }
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < npg * kKC; idx += blockDim.x) {
+            const int pp = idx / kKC, kk = idx % kKC;
+            const int2 pr = pairs[p0g + pp];
+            sP[(size_t)kk * gpad + pp] = sA[pr.x * kKC + kk] * sA[pr.y * kKC + kk];
+        }
+        __syncthreads();
+        if (my < ntile) {
+#pragma unroll 4
+            for (int kk = 0; kk < kKC; kk++) {
+                T av[4], qv[8];
+                load4(sP + (size_t)kk * gpad + tp, av);
+                load4(sQ + (size_t)kk * qpad + tq, qv);
+                load4(sQ + (size_t)kk * qpad + tq + 4, qv + 4);
+#pragma unroll
+                for (int a = 0; a < kTP; a++)
+#pragma unroll
+                    for (int b = 0; b < kTQ; b++) acc[a][b] = fma(av[a], qv[b], acc[a][b]);
+            }
+#pragma unroll
+            for (int a = 0; a < kTP; a++)
+#pragma unroll
+                for (int b = 0; b < kTQ; b++) {
+                    run[a][b].add(acc[a][b]);
+                    acc[a][b] = 0;
+                }
+        }
+        __syncthreads();
+    }
+    if (my < ntile) {
+        const int *st = slots + tile.w;
+#pragma unroll
+        for (int a = 0; a < kTP; a++)
+#pragma unroll
+            for (int b = 0; b < kTQ; b++) {
+                const int s = st[a * kTQ + b];
+                if (s >= 0) partial[(size_t)split * nslots + s] = (double)run[a][b].sum - (double)run[a][b].comp;
+            }
+    }
+}
+
+__global__ void reduce_partial_kernel(int nslots, int ksplit, const double *__restrict__ partial,
+                                      double *__restrict__ S) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nslots; s += gridDim.x * blockDim.x) {
+        double v = 0;
+        for (int k = 0; k < ksplit; k++) v += partial[(size_t)k * nslots + s];
+        S[s] = v;
+    }
+}
+
+template <class T>
+int triangle_sums(const Shells &sh, const TriPlan &tp, const T *maps, size_t mstride, int rs, DevBuf &partial,
+                  double *S, cudaStream_t st, int64_t *launches) {
+    const int N = sh.N;
+    const long long K = (long long)N * N * N;
+    const int qpad = ((tp.nq + kTQ - 1) / kTQ) * kTQ + 4;        // +4: fewer bank conflicts on transposed stores
+    const int gpad = ((tp.max_group_pairs + kTP - 1) / kTP) * kTP + 4;
+    const size_t smem = sizeof(T) * ((size_t)kKC * qpad + (size_t)sh.nb * kKC + (size_t)kKC * gpad);
+    if (smem > 220 * 1024) return set_error(PBI4G_ERR_UNSUPPORTED, "triangle sums: %zu B shared memory", smem);
+    const int target = 152 * 3;
+    int ksplit = std::max(1, target / std::max(1, tp.ngroups));
+    ksplit = (int)std::min<long long>(ksplit, std::max<long long>(1, K / (kKC * 16)));
+    PBI4G_CHECK(partial.ensure(sizeof(double) * (size_t)ksplit * tp.nslots));
+    auto kern = trisum_kernel<T>;
+    PBI4G_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<tp.ngroups * ksplit, kGroupThreads, smem, st>>>(
+        N, maps, mstride, rs, sh.nb, tp.nq, qpad, tp.qmap.as<int>(), tp.pairs.as<int2>(), tp.tiles.as<int4>(),
+        tp.groups.as<int4>(), tp.slots.as<int>(), tp.ngroups, ksplit, K, tp.nslots, gpad, partial.as<double>());
+    PBI4G_LAUNCH_CHECK();
+    reduce_partial_kernel<<<(tp.nslots + 255) / 256, 256, 0, st>>>(tp.nslots, ksplit, partial.as<double>(), S);
+    PBI4G_LAUNCH_CHECK();
+    *launches += 2;
+    return PBI4G_OK;
+}
+
+template int triangle_sums<float>(const Shells &, const TriPlan &, const float *, size_t, int, DevBuf &, double *,
+                                  cudaStream_t, int64_t *);
+template int triangle_sums<double>(const Shells &, const TriPlan &, const double *, size_t, int, DevBuf &, double *,
+                                   cudaStream_t, int64_t *);
+
+// ------------------------------------------------------------ outputs ---
+__global__ void bk_finalize_kernel(int64_t itot, int nb, int nsets, int cross, const int *__restrict__ tri,
+                                   const double *__restrict__ S, const double *__restrict__ powsum,
+                                   const double *__restrict__ nmodes, double kf3, double powSN, double gridD,
+                                   double kcenter, double kbin, const float *__restrict__ counts,
+                                   double *__restrict__ bout) {
+    const double powSN2 = powSN * powSN;
+    for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < itot; m += (int64_t)gridDim.x * blockDim.x) {
+        const int l = tri[3 * m], j = tri[3 * m + 1], i = tri[3 * m + 2];
+        const double c = (double)counts[m];
+        const double tl = kcenter + (double)(l - 1) * kbin, tj = kcenter + (double)(j - 1) * kbin,
+                     ti = kcenter + (double)(i - 1) * kbin;
+        if (cross) {
+            double *o = bout + 5 * m;
+            o[0] = tl; o[1] = tj; o[2] = ti;
+            o[3] = kf3 * S[m * nsets] / c;
+            o[4] = (double)(float)(c / gridD);
+            continue;
+        }
+        // pow(i) = kf3*avg/dble(gridd)/dble(nmodes) - powSN, avg = sum_x m^2 = gridD * sum_k |H|^2
+        auto pw = [&](int b) { return kf3 * (gridD * powsum[b - 1]) / gridD / nmodes[b - 1] - powSN; };
+        const double pl = pw(l), pj = pw(j), pi = pw(i);
+        const double bispSN = (pi + pj + pl) * powSN + powSN2;
+        const int rows = nsets == 3 ? 11 : 9;
+        double *o = bout + (size_t)rows * m;
+        o[0] = tl; o[1] = tj; o[2] = ti;
+        o[3] = pl; o[4] = pj; o[5] = pi;
+        o[6] = kf3 * S[m * nsets] / c + bispSN;
+        o[7] = bispSN;
+        o[8] = (double)(float)(c / gridD);
+        if (nsets == 3) {
+            o[9] = 5 * kf3 * S[m * nsets + 1] / c;
+            o[10] = 9 * kf3 * S[m * nsets + 2] / c;
+        }
+    }
+}
+
+int bk_finalize(const Shells &sh, int nsets, int cross, const double *S, const double *powsum, float kf,
+                int64_t npart, const float *counts_f32, double *bout, cudaStream_t st, int64_t *launches) {
+    const float kf3f = kf * kf * kf;
+    const double kf3 = (double)kf3f;
+    const double powSN = 1.0 / (double)npart / kf3;
+    const double gridD = (double)sh.N * sh.N * sh.N;
+    bk_finalize_kernel<<<grid_blocks(sh.itot, 128), 128, 0, st>>>(
+        sh.itot, sh.nb, nsets, cross, sh.tri_d.as<int>(), S, powsum, sh.nmodes_d.as<double>(), kf3, powSN, gridD,
+        (double)sh.kcenter, (double)sh.kbin, counts_f32, bout);
+    PBI4G_LAUNCH_CHECK();
+    ++*launches;
+    return PBI4G_OK;
+}
+
+// ------------------------------------------------------------- counts ---
+int triangle_counts(Shells &sh, cudaStream_t st, int64_t *launches) {
+    if (!sh.counts.empty()) return PBI4G_OK;
+    const int N = sh.N, nb = sh.nb, NH = N / 2 + 1;
+    const size_t HC = half_cells(N);
+    DevBuf maps, partial, S;
+    PBI4G_CHECK(maps.ensure(sizeof(double2) * HC * nb));
+    PBI4G_CHECK(build_indicator_spectra<double>(sh, 0, nb, maps.as<double2>(), st, launches));
+    cufftHandle plan;
+    int n[3] = {N, N, N}, inembed[3] = {N, N, NH}, onembed[3] = {N, N, 2 * NH};
+    PBI4G_CUFFT(cufftPlanMany(&plan, 3, n, inembed, 1, (int)HC, onembed, 1, (int)(2 * HC), CUFFT_Z2D, nb));
+    cufftSetStream(plan, st);
+    cufftResult r = cufftExecZ2D(plan, maps.as<cufftDoubleComplex>(), maps.as<cufftDoubleReal>());
+    cufftDestroy(plan);
+    if (r != CUFFT_SUCCESS) return set_error(PBI4G_ERR_CUFFT, "counts: cufftExecZ2D failed (%d)", (int)r);
+    // all three factors are indicator maps of the same set (also for the cross
+    // enumeration, bispectrumI4.f90:887-896), so the non-cross pair layout applies
+    TriPlan tp;
+    PBI4G_CHECK(tp.build(sh, 1, 0));
+    PBI4G_CHECK(S.ensure(sizeof(double) * tp.nslots));
+    PBI4G_CHECK(triangle_sums<double>(sh, tp, maps.as<double>(), 2 * HC, 2 * NH, partial, S.as<double>(), st, launches));
+    std::vector<double> Sh(tp.nslots);
+    PBI4G_CUDA(cudaMemcpyAsync(Sh.data(), S.p, sizeof(double) * tp.nslots, cudaMemcpyDeviceToHost, st));
+    PBI4G_CUDA(cudaStreamSynchronize(st));
+    const double gridD = (double)N * N * N;
+    sh.counts.resize(sh.itot);
+    std::vector<float> c32(sh.itot);
+    double maxdev = 0;
+    for (int64_t m = 0; m < sh.itot; m++) {
+        double v = Sh[m] / gridD;
+        long long c = llround(v);
+        maxdev = std::max(maxdev, fabs(v - (double)c));
+        sh.counts[m] = c;
+        c32[m] = (float)(gridD * (double)c);
+    }
+    if (maxdev > 0.25) {
+        sh.counts.clear();
+        return set_error(PBI4G_ERR_RANGE, "triangle counts not resolved to integers (max deviation %g)", maxdev);
+    }
+    PBI4G_CHECK(sh.counts_f32.ensure(sizeof(float) * sh.itot));
+    PBI4G_CUDA(cudaMemcpy(sh.counts_f32.p, c32.data(), sizeof(float) * sh.itot, cudaMemcpyHostToDevice));
+    return PBI4G_OK;
+}
+
+}  // namespace pbi4g

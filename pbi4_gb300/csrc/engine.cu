@@ -1,0 +1,398 @@
+// engine.cu -- the plan (device-resident estimator) and the bispectrum engine.
+//
+// Density   : assign (fixed point) -> real grids -> batched R2C -> fcomb_half
+//             (pbi4.py:290-341, powerI4.f90:68-378)
+// P(k)      : pk_measure on the half spectrum, multipoles by the per-mode
+//             constant-LOS factors (pbi4.py:343-461, powerI4.f90:596-693)
+// B(k)      : shell spectra -> one batched C2R -> triangle sums -> output rows
+//             (pbi4.py:478-553, bispectrumI4.f90)
+#include "engine.cuh"
+#include "assign.cuh"
+
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+#include <algorithm>
+
+namespace pbi4g {
+
+static thread_local char g_err[1024] = "";
+
+int set_error(int code, const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof g_err, fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+Prof::~Prof() {
+    for (auto e : pool) cudaEventDestroy(e);
+    for (auto &r : recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+}
+
+cudaEvent_t Prof::get() {
+    if (!pool.empty()) {
+        cudaEvent_t e = pool.back();
+        pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+void Prof::begin(int stage, cudaStream_t st) {
+    if (!on) return;
+    cur_a = get();
+    cur_stage = stage;
+    cudaEventRecord(cur_a, st);
+}
+
+void Prof::end(cudaStream_t st) {
+    if (!on || cur_stage < 0) return;
+    cudaEvent_t b = get();
+    cudaEventRecord(b, st);
+    recs.push_back({cur_stage, cur_a, b});
+    cur_stage = -1;
+}
+
+size_t BkEngine::footprint(int N, int nb, int nsets, int cross, bool fp64) {
+    const size_t HC = half_cells(N);
+    const int nm = cross ? 2 * nb : nsets * nb;
+    const size_t cs = fp64 ? 16 : 8;
+    // maps + a cuFFT work area of about one batch of the same size (upper estimate)
+    return 2 * (size_t)nm * HC * cs + (size_t)nb * 8 + (size_t)1 << 26;
+}
+
+template <class R>
+int BkEngine::run(const typename Cx<R>::T *const src[3], const int fac[3], const double los[3], float kf,
+                  int64_t npart, const float *counts_f32, double *d_bout, cudaStream_t st, int64_t *launches,
+                  Prof *prof) {
+    using C = typename Cx<R>::T;
+    Prof dummy;
+    Prof &pf = prof ? *prof : dummy;
+    const int N = sh.N, NH = N / 2 + 1, nb = sh.nb;
+    const size_t HC = half_cells(N);
+    const int nm = nmaps();
+    const bool fp64 = sizeof(R) == 8;
+    if (tp_nsets != nsets || tp_cross != cross) {
+        PBI4G_CHECK(tp.build(sh, cross ? 1 : nsets, cross));
+        tp_nsets = nsets;
+        tp_cross = cross;
+    }
+    PBI4G_CHECK(maps.ensure(sizeof(C) * HC * nm));
+    PBI4G_CHECK(powsum.ensure(sizeof(double) * nb));
+    PBI4G_CHECK(S.ensure(sizeof(double) * std::max(1, tp.nslots)));
+    pf.begin(6, st);
+    PBI4G_CUDA(cudaMemsetAsync(powsum.p, 0, sizeof(double) * nb, st));
+    PBI4G_CHECK(build_map_spectra<R>(sh, 0, nm, src, fac, los, maps.as<C>(), powsum.as<double>(), st, launches));
+    pf.end(st);
+    if (!inv || inv_batch != nm || inv_N != N || inv_fp64 != (int)fp64) {
+        if (inv) cufftDestroy(inv);
+        inv = 0;
+        int n[3] = {N, N, N}, inembed[3] = {N, N, NH}, onembed[3] = {N, N, 2 * NH};
+        PBI4G_CUFFT(cufftPlanMany(&inv, 3, n, inembed, 1, (int)HC, onembed, 1, (int)(2 * HC),
+                                  fp64 ? CUFFT_Z2D : CUFFT_C2R, nm));
+        inv_batch = nm;
+        inv_N = N;
+        inv_fp64 = fp64;
+    }
+    PBI4G_CUFFT(cufftSetStream(inv, st));
+    pf.begin(7, st);
+    if (fp64)
+        PBI4G_CUFFT(cufftExecZ2D(inv, maps.as<cufftDoubleComplex>(), maps.as<cufftDoubleReal>()));
+    else
+        PBI4G_CUFFT(cufftExecC2R(inv, maps.as<cufftComplex>(), maps.as<cufftReal>()));
+    pf.end(st);
+    pf.begin(8, st);
+    PBI4G_CHECK(triangle_sums<R>(sh, tp, maps.as<R>(), 2 * HC, 2 * NH, partial, S.as<double>(), st, launches));
+    pf.end(st);
+    pf.begin(9, st);
+    PBI4G_CHECK(bk_finalize(sh, cross ? 1 : nsets, cross, S.as<double>(), powsum.as<double>(), kf, npart, counts_f32,
+                            d_bout, st, launches));
+    pf.end(st);
+    return PBI4G_OK;
+}
+
+template int BkEngine::run<float>(const float2 *const[3], const int[3], const double[3], float, int64_t, const float *,
+                                  double *, cudaStream_t, int64_t *, Prof *);
+template int BkEngine::run<double>(const double2 *const[3], const int[3], const double[3], float, int64_t,
+                                   const float *, double *, cudaStream_t, int64_t *, Prof *);
+
+}  // namespace pbi4g
+
+using namespace pbi4g;
+
+// ================================================================ plan ===
+struct pbi4g_plan {
+    pbi4g_config cfg;
+    cudaStream_t st = 0;
+    int64_t launches = 0;
+    bool fp64 = false;
+    int N = 0, G = 1;
+    AssignWork aw;
+    DevBuf real_grids, spec, delta;
+    DevBuf pos_stage, w_stage, pout_d, bout_d;
+    cufftHandle fwd = 0;
+    PkBins pk;
+    BkEngine bk;
+    bool have_delta = false;
+    int64_t npart = 0;
+    Prof prof;
+    ~pbi4g_plan() {
+        if (fwd) cufftDestroy(fwd);
+    }
+};
+
+static int check_config(const pbi4g_config *c) {
+    if (!c) return set_error(PBI4G_ERR_INVALID, "null config");
+    if (c->grid < 4 || (c->grid & 1) || c->grid > 2048)
+        return set_error(PBI4G_ERR_INVALID, "grid must be even and in [4, 2048] (got %d)", c->grid);
+    if (c->nintp < 1 || c->nintp > 4) return set_error(PBI4G_ERR_INVALID, "interpolation must be 1..4");
+    if (!(c->box > 0)) return set_error(PBI4G_ERR_INVALID, "box must be > 0");
+    if (c->nbins_ps < 1 || !(c->kbin_ps > 0)) return set_error(PBI4G_ERR_INVALID, "bad P binning");
+    if (c->do_bispectrum && (c->nbins_bs < 1 || !(c->kbin_bs > 0)))
+        return set_error(PBI4G_ERR_INVALID, "bad B binning");
+    if (c->precision < PBI4G_PREC_FP32 || c->precision > PBI4G_PREC_BF16)
+        return set_error(PBI4G_ERR_INVALID, "unknown precision %d", c->precision);
+    for (int k = 0; k < 7; k++)
+        if (c->reserved[k]) return set_error(PBI4G_ERR_INVALID, "reserved config fields must be zero");
+    return PBI4G_OK;
+}
+
+extern "C" {
+
+const char *pbi4g_last_error(void) { return g_err; }
+int pbi4g_version(void) { return 100; }
+
+int pbi4g_plan_footprint(const pbi4g_config *cfg, int64_t npart_max, int64_t *bytes) {
+    PBI4G_CHECK(check_config(cfg));
+    if (!bytes || npart_max < 0) return set_error(PBI4G_ERR_INVALID, "bad footprint arguments");
+    const int N = cfg->grid, G = cfg->interlacing ? 2 : 1;
+    const bool fp64 = cfg->precision == PBI4G_PREC_FP64;
+    const size_t rs = fp64 ? 8 : 4, cs = 2 * rs, HC = half_cells(N), FC = full_cells(N);
+    size_t b = AssignWork::footprint(N, npart_max, cfg->interlacing) + G * FC * rs + G * HC * cs + HC * cs;
+    b += 2 * G * HC * cs;  // cuFFT work area (upper estimate)
+    b += (size_t)npart_max * 32 + 5 * (size_t)cfg->nbins_ps * 8 * 1300;
+    if (cfg->do_bispectrum) {
+        b += BkEngine::footprint(N, cfg->nbins_bs, cfg->multipoles ? 3 : 1, 0, fp64);
+        b += (size_t)FC * 8 * (size_t)0;  // counts use a temporary FP64 map set, freed after the first box
+    }
+    *bytes = (int64_t)b;
+    return PBI4G_OK;
+}
+
+int pbi4g_plan_create(const pbi4g_config *cfg, pbi4g_plan **out) {
+    PBI4G_CHECK(check_config(cfg));
+    if (!out) return set_error(PBI4G_ERR_INVALID, "null out");
+    pbi4g_plan *p = new pbi4g_plan();
+    p->cfg = *cfg;
+    p->N = cfg->grid;
+    p->G = cfg->interlacing ? 2 : 1;
+    p->fp64 = cfg->precision == PBI4G_PREC_FP64;
+    int rc = PBI4G_OK;
+    do {
+        const int N = p->N;
+        const size_t rs = p->fp64 ? 8 : 4, HC = half_cells(N), FC = full_cells(N);
+        if ((rc = p->real_grids.ensure(p->G * FC * rs))) break;
+        if ((rc = p->spec.ensure(p->G * HC * 2 * rs))) break;
+        if ((rc = p->delta.ensure(HC * 2 * rs))) break;
+        int n[3] = {N, N, N};
+        cufftResult r = cufftPlanMany(&p->fwd, 3, n, nullptr, 1, (int)FC, nullptr, 1, (int)HC,
+                                      p->fp64 ? CUFFT_D2Z : CUFFT_R2C, p->G);
+        if (r != CUFFT_SUCCESS) { rc = set_error(PBI4G_ERR_CUFFT, "R2C plan failed (%d)", (int)r); p->fwd = 0; break; }
+        if ((rc = p->pk.build(N, cfg->box, cfg->kbin_ps, cfg->kcenter_ps, cfg->nbins_ps, p->st, &p->launches))) break;
+        if (cfg->do_bispectrum) {
+            if ((rc = p->bk.sh.build(N, cfg->kbin_bs, cfg->kcenter_bs, cfg->nbins_bs, cfg->iopen, 0, p->st))) break;
+            p->bk.nsets = cfg->multipoles ? 3 : 1;
+            p->bk.cross = 0;
+        }
+        cudaError_t e = cudaStreamSynchronize(p->st);
+        if (e != cudaSuccess) { rc = set_error(PBI4G_ERR_CUDA, "plan create: %s", cudaGetErrorString(e)); break; }
+    } while (0);
+    if (rc) {
+        delete p;
+        return rc;
+    }
+    *out = p;
+    return PBI4G_OK;
+}
+
+int pbi4g_plan_destroy(pbi4g_plan *plan) {
+    delete plan;
+    return PBI4G_OK;
+}
+
+int pbi4g_plan_set_stream(pbi4g_plan *plan, void *stream) {
+    if (!plan) return set_error(PBI4G_ERR_INVALID, "null plan");
+    plan->st = (cudaStream_t)stream;
+    return PBI4G_OK;
+}
+
+int pbi4g_plan_shape(const pbi4g_plan *plan, int32_t *nbins_ps, int64_t *itot, int32_t *brows) {
+    if (!plan) return set_error(PBI4G_ERR_INVALID, "null plan");
+    if (nbins_ps) *nbins_ps = plan->cfg.nbins_ps;
+    if (itot) *itot = plan->cfg.do_bispectrum ? plan->bk.sh.itot : 0;
+    if (brows) *brows = plan->cfg.do_bispectrum ? (plan->cfg.multipoles ? 11 : 9) : 0;
+    return PBI4G_OK;
+}
+
+int64_t pbi4g_plan_kernel_launches(const pbi4g_plan *plan) { return plan ? plan->launches : -1; }
+
+int pbi4g_plan_triangle_counts(pbi4g_plan *plan, int64_t *counts_host) {
+    if (!plan || !plan->cfg.do_bispectrum) return set_error(PBI4G_ERR_INVALID, "plan has no bispectrum");
+    PBI4G_CHECK(triangle_counts(plan->bk.sh, plan->st, &plan->launches));
+    if (counts_host) memcpy(counts_host, plan->bk.sh.counts.data(), sizeof(int64_t) * plan->bk.sh.itot);
+    return PBI4G_OK;
+}
+
+int pbi4g_plan_density(pbi4g_plan *p, int64_t npart, const double *d_pos, const double *d_weight) {
+    if (!p) return set_error(PBI4G_ERR_INVALID, "null plan");
+    if (npart < 1) return set_error(PBI4G_ERR_INVALID, "npart must be >= 1");
+    const int N = p->N;
+    int bits;
+    p->prof.begin(0, p->st);
+    PBI4G_CHECK(assign_fixed(p->aw, N, p->cfg.nintp, p->G == 2, p->fp64, npart, d_pos, d_weight, &bits, p->st,
+                             &p->launches));
+    p->prof.end(p->st);
+    p->prof.begin(1, p->st);
+    PBI4G_CHECK(fixed_to_real(p->aw, N, p->G == 2, bits, p->fp64, p->real_grids.p, p->st, &p->launches));
+    p->prof.end(p->st);
+    PBI4G_CUFFT(cufftSetStream(p->fwd, p->st));
+    p->prof.begin(2, p->st);
+    if (p->fp64)
+        PBI4G_CUFFT(cufftExecD2Z(p->fwd, p->real_grids.as<cufftDoubleReal>(), p->spec.as<cufftDoubleComplex>()));
+    else
+        PBI4G_CUFFT(cufftExecR2C(p->fwd, p->real_grids.as<cufftReal>(), p->spec.as<cufftComplex>()));
+    p->prof.end(p->st);
+    p->prof.begin(3, p->st);
+    if (p->fp64)
+        PBI4G_CHECK(fcomb_half<double>(N, p->cfg.nintp, p->G == 2, p->cfg.box, (double)npart, p->spec.as<double2>(),
+                                       p->delta.as<double2>(), p->st, &p->launches));
+    else
+        PBI4G_CHECK(fcomb_half<float>(N, p->cfg.nintp, p->G == 2, p->cfg.box, (double)npart, p->spec.as<float2>(),
+                                      p->delta.as<float2>(), p->st, &p->launches));
+    p->prof.end(p->st);
+    p->have_delta = true;
+    p->npart = npart;
+    return PBI4G_OK;
+}
+
+int pbi4g_plan_powerspectrum(pbi4g_plan *p, double *d_pout) {
+    if (!p || !d_pout) return set_error(PBI4G_ERR_INVALID, "null plan/output");
+    if (!p->have_delta) return set_error(PBI4G_ERR_INVALID, "powerspectrum before density");
+    const int mode = p->cfg.multipoles ? 1 : 0;
+    p->prof.begin(4, p->st);
+    int rc;
+    if (p->fp64)
+        rc = pk_measure<double>(p->pk, mode, p->cfg.los, p->delta.as<double2>(), p->delta.as<double2>(), nullptr,
+                                d_pout, p->st, &p->launches);
+    else
+        rc = pk_measure<float>(p->pk, mode, p->cfg.los, p->delta.as<float2>(), p->delta.as<float2>(), nullptr, d_pout,
+                               p->st, &p->launches);
+    p->prof.end(p->st);
+    return rc;
+}
+
+int pbi4g_plan_bispectrum(pbi4g_plan *p, double *d_bout) {
+    if (!p || !d_bout) return set_error(PBI4G_ERR_INVALID, "null plan/output");
+    if (!p->cfg.do_bispectrum) return set_error(PBI4G_ERR_INVALID, "plan has no bispectrum");
+    if (!p->have_delta) return set_error(PBI4G_ERR_INVALID, "bispectrum before density");
+    if (p->cfg.precision == PBI4G_PREC_FP16SPLIT || p->cfg.precision == PBI4G_PREC_BF16)
+        return set_error(PBI4G_ERR_UNSUPPORTED, "tensor-core precision not built in this library");
+    if (p->bk.sh.counts.empty()) {
+        p->prof.begin(5, p->st);
+        PBI4G_CHECK(triangle_counts(p->bk.sh, p->st, &p->launches));
+        p->prof.end(p->st);
+    }
+    // the reference passes kf = 2 pi / box as real(4) (pbi4.py:100, bispectrumI4.f90:8)
+    const float kf = (float)(2.0 * 3.14159265358979323846 / (double)p->cfg.box);
+    const int fac[3] = {0, 2, 4};
+    if (p->fp64) {
+        const double2 *src[3] = {p->delta.as<double2>(), p->delta.as<double2>(), p->delta.as<double2>()};
+        return p->bk.run<double>(src, fac, p->cfg.los, kf, p->npart, p->bk.sh.counts_f32.as<float>(), d_bout, p->st,
+                                 &p->launches, &p->prof);
+    }
+    const float2 *src[3] = {p->delta.as<float2>(), p->delta.as<float2>(), p->delta.as<float2>()};
+    return p->bk.run<float>(src, fac, p->cfg.los, kf, p->npart, p->bk.sh.counts_f32.as<float>(), d_bout, p->st,
+                            &p->launches, &p->prof);
+}
+
+int pbi4g_plan_run_device(pbi4g_plan *p, int64_t npart, const double *d_pos, const double *d_weight, double *d_pout,
+                          double *d_bout) {
+    PBI4G_CHECK(pbi4g_plan_density(p, npart, d_pos, d_weight));
+    PBI4G_CHECK(pbi4g_plan_powerspectrum(p, d_pout));
+    if (p->cfg.do_bispectrum) PBI4G_CHECK(pbi4g_plan_bispectrum(p, d_bout));
+    return PBI4G_OK;
+}
+
+int pbi4g_plan_run_host(pbi4g_plan *p, int64_t npart, const double *pos, const double *weight, double *pout,
+                        double *bout) {
+    if (!p || !pos || !pout) return set_error(PBI4G_ERR_INVALID, "null argument");
+    if (p->cfg.do_bispectrum && !bout) return set_error(PBI4G_ERR_INVALID, "null bout");
+    PBI4G_CHECK(p->pos_stage.ensure(sizeof(double) * 3 * (size_t)npart));
+    PBI4G_CUDA(cudaMemcpyAsync(p->pos_stage.p, pos, sizeof(double) * 3 * (size_t)npart, cudaMemcpyHostToDevice, p->st));
+    const double *dw = nullptr;
+    if (weight) {
+        PBI4G_CHECK(p->w_stage.ensure(sizeof(double) * (size_t)npart));
+        PBI4G_CUDA(cudaMemcpyAsync(p->w_stage.p, weight, sizeof(double) * (size_t)npart, cudaMemcpyHostToDevice, p->st));
+        dw = p->w_stage.as<double>();
+    }
+    const size_t pb = sizeof(double) * 5 * p->cfg.nbins_ps;
+    const size_t bb = p->cfg.do_bispectrum ? sizeof(double) * (p->cfg.multipoles ? 11 : 9) * p->bk.sh.itot : 0;
+    PBI4G_CHECK(p->pout_d.ensure(pb));
+    if (bb) PBI4G_CHECK(p->bout_d.ensure(bb));
+    PBI4G_CHECK(pbi4g_plan_run_device(p, npart, p->pos_stage.as<double>(), dw, p->pout_d.as<double>(),
+                                      bb ? p->bout_d.as<double>() : nullptr));
+    PBI4G_CUDA(cudaMemcpyAsync(pout, p->pout_d.p, pb, cudaMemcpyDeviceToHost, p->st));
+    if (bb) PBI4G_CUDA(cudaMemcpyAsync(bout, p->bout_d.p, bb, cudaMemcpyDeviceToHost, p->st));
+    PBI4G_CUDA(cudaStreamSynchronize(p->st));
+    return PBI4G_OK;
+}
+
+int pbi4g_plan_enable_timing(pbi4g_plan *p, int32_t enable) {
+    if (!p) return set_error(PBI4G_ERR_INVALID, "null plan");
+    p->prof.on = enable != 0;
+    return PBI4G_OK;
+}
+
+int pbi4g_plan_stage_times(pbi4g_plan *p, double *ms, int64_t *calls) {
+    if (!p || !ms) return set_error(PBI4G_ERR_INVALID, "null argument");
+    PBI4G_CUDA(cudaStreamSynchronize(p->st));
+    for (int s = 0; s < PBI4G_NSTAGES; s++) {
+        ms[s] = 0;
+        if (calls) calls[s] = 0;
+    }
+    for (auto &r : p->prof.recs) {
+        float t = 0;
+        PBI4G_CUDA(cudaEventElapsedTime(&t, r.a, r.b));
+        ms[r.stage] += t;
+        if (calls) calls[r.stage] += 1;
+        p->prof.pool.push_back(r.a);
+        p->prof.pool.push_back(r.b);
+    }
+    p->prof.recs.clear();
+    return PBI4G_OK;
+}
+
+int pbi4g_plan_get_delta_half(pbi4g_plan *p, double *host_half) {
+    if (!p || !host_half) return set_error(PBI4G_ERR_INVALID, "null argument");
+    if (!p->have_delta) return set_error(PBI4G_ERR_INVALID, "no density yet");
+    const size_t HC = half_cells(p->N);
+    if (p->fp64) {
+        PBI4G_CUDA(cudaMemcpyAsync(host_half, p->delta.p, HC * 16, cudaMemcpyDeviceToHost, p->st));
+        PBI4G_CUDA(cudaStreamSynchronize(p->st));
+        return PBI4G_OK;
+    }
+    std::vector<float2> tmp(HC);
+    PBI4G_CUDA(cudaMemcpyAsync(tmp.data(), p->delta.p, HC * 8, cudaMemcpyDeviceToHost, p->st));
+    PBI4G_CUDA(cudaStreamSynchronize(p->st));
+    for (size_t i = 0; i < HC; i++) {
+        host_half[2 * i] = tmp[i].x;
+        host_half[2 * i + 1] = tmp[i].y;
+    }
+    return PBI4G_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,44 @@
+// engine.cuh -- bispectrum engine shared by the plan and the drop-in entry points.
+#pragma once
+#include "bispec.cuh"
+
+namespace pbi4g {
+
+// Per-stage CUDA-event timing on a stream (see pbi4g_plan_enable_timing).
+struct Prof {
+    bool on = false;
+    struct Rec { int stage; cudaEvent_t a, b; };
+    std::vector<cudaEvent_t> pool;
+    std::vector<Rec> recs;
+    cudaEvent_t cur_a = nullptr;
+    int cur_stage = -1;
+    ~Prof();
+    cudaEvent_t get();
+    void begin(int stage, cudaStream_t st);
+    void end(cudaStream_t st);
+};
+
+// Resident state of the bispectrum stage for one (grid, binning, sets) layout.
+struct BkEngine {
+    Shells sh;
+    TriPlan tp;
+    int tp_nsets = -1, tp_cross = -1;
+    int nsets = 1, cross = 0;  // cross: 1 => q maps from the second field
+    DevBuf maps;               // [nmaps][N][N][N/2+1] complex = padded real maps after C2R
+    cufftHandle inv = 0;
+    int inv_batch = 0, inv_N = 0, inv_fp64 = -1;
+    DevBuf powsum, S, partial;
+    ~BkEngine() {
+        if (inv) cufftDestroy(inv);
+    }
+    int nmaps() const { return cross ? 2 * sh.nb : nsets * sh.nb; }
+    static size_t footprint(int N, int nb, int nsets, int cross, bool fp64);
+
+    // src[s]: half spectra (N, N, N/2+1) of set s; fac[s]: 0 none, 2/4 the
+    // multipole factor from `los`.  counts_f32: device float counts[itot].
+    template <class R>
+    int run(const typename Cx<R>::T *const src[3], const int fac[3], const double los[3], float kf, int64_t npart,
+            const float *counts_f32, double *d_bout, cudaStream_t st, int64_t *launches, Prof *prof = nullptr);
+};
+
+}  // namespace pbi4g

@@ -1,0 +1,518 @@
+// spectrum.cu -- Fourier-space kernels of the density stage and P(k) binning.
+//
+//  * fcomb_half   : interlacing combine + window deconvolution + 1/npart, fused
+//                   into one pass over the R2C half spectra (powerI4.f90:251-378).
+//  * fcomb_full   : the same routine on a full complex grid (f2py drop-in).
+//  * pk_measure   : P(k) / P_l binning (powerI4.f90:510-594, 596-693) with the
+//                   constant-LOS multipole factors applied per mode, which equals
+//                   compute_density_multipoles (pbi4.py:343-388 + compute_q2k/q4k)
+//                   without its 22 full FFTs:
+//                   FFT(delta(x) l_i l_j) = l_i l_j delta(k) by linearity, and
+//                   sum_{ij} fac l_i l_j k_i k_j / k^2 = (l.k)^2 / k^2.
+//  * q2k_full, q4k_full, reduce_full : f2py drop-ins on full grids.
+#include "spectrum.cuh"
+
+#include <float.h>
+#include <math.h>
+#include <vector>
+
+namespace pbi4g {
+
+void window_table(int N, int nintp, double *tW) {
+    const double tpiN = (double)kTwoPiF / (double)N;
+    tW[0] = 1.0;
+    for (int i = 2; i <= N / 2 + 1; i++) {
+        double rk = tpiN * (double)(i - 1);
+        double s = sin(rk / 2.0) / (rk / 2.0), r = 1.0;
+        for (int k = 0; k < nintp; k++) r *= s;
+        tW[i - 1] = r;
+    }
+}
+
+double fcomb_kF3(float box) {
+    volatile float t = kTwoPiF * kTwoPiF;  // real(4) arithmetic, powerI4.f90:271
+    t = t * kTwoPiF;
+    t = t / box;
+    t = t / box;
+    t = t / box;
+    return (double)t;
+}
+
+// ------------------------------------------------------------ complex ops ---
+template <class C> __device__ __forceinline__ C cmk(double r, double i) { C c; c.x = r; c.y = i; return c; }
+template <class C> __device__ __forceinline__ C cmul(C a, C b) {
+    C c; c.x = a.x * b.x - a.y * b.y; c.y = a.x * b.y + a.y * b.x; return c;
+}
+template <class C> __device__ __forceinline__ C cadd(C a, C b) { C c; c.x = a.x + b.x; c.y = a.y + b.y; return c; }
+template <class C> __device__ __forceinline__ C csub(C a, C b) { C c; c.x = a.x - b.x; c.y = a.y - b.y; return c; }
+template <class C> __device__ __forceinline__ C cconj(C a) { C c; c.x = a.x; c.y = -a.y; return c; }
+template <class C, class S> __device__ __forceinline__ C cscale(C a, S s) { C c; c.x = a.x * s; c.y = a.y * s; return c; }
+
+__device__ __forceinline__ void sincos_t(float a, float *s, float *c) { sincosf(a, s, c); }
+__device__ __forceinline__ void sincos_t(double a, double *s, double *c) { sincos(a, s, c); }
+
+// The orbit {ix,icx} x {iy,icy} x {iz,icz} of one iteration of fcomb's
+// interlaced loop, with the reference's write order (powerI4.f90:325-342)
+// applied to an 8-entry local copy.  Where ix == icx (etc.) the two slots are
+// one location and later writes win, exactly as in the Fortran.
+template <class R>
+struct Orbit {
+    using C = typename Cx<R>::T;
+    C v[8];
+    int ex, ey, ez;
+    __device__ __forceinline__ int key(int xs, int ys, int zs) const {
+        return (ex ? 0 : xs) | ((ey ? 0 : ys) << 1) | ((ez ? 0 : zs) << 2);
+    }
+    __device__ __forceinline__ void combine(R xa, R ya, R za, R cfac) {
+        // phases xrec = exp(-i pi (ix-1)/N) etc. as angles xa, ya, za
+        R sx, cxr, sy, cyr, sz, czr;
+        sincos_t(xa, &sx, &cxr);
+        sincos_t(ya, &sy, &cyr);
+        sincos_t(za, &sz, &czr);
+        const C xr = cmk<C>(cxr, sx), yr = cmk<C>(cyr, sy), zr = cmk<C>(czr, sz);
+        const C ci = cmk<C>(0, 1), c1 = cmk<C>(1, 0);
+        const C cma = cmul(cmul(cmul(ci, xr), yr), zr);
+        const C cmb = cmul(cmul(cmul(ci, xr), yr), cconj(zr));
+        const C cmc = cmul(cmul(cmul(ci, xr), cconj(yr)), zr);
+        const C cmd = cmul(cmul(ci, xr), cconj(cmul(yr, zr)));
+        const C c000 = cadd(cmul(v[key(0, 0, 0)], csub(c1, cma)), cmul(cconj(v[key(1, 1, 1)]), cadd(c1, cma)));
+        const C c001 = cadd(cmul(v[key(0, 0, 1)], csub(c1, cmb)), cmul(cconj(v[key(1, 1, 0)]), cadd(c1, cmb)));
+        const C c010 = cadd(cmul(v[key(0, 1, 0)], csub(c1, cmc)), cmul(cconj(v[key(1, 0, 1)]), cadd(c1, cmc)));
+        const C c011 = cadd(cmul(v[key(0, 1, 1)], csub(c1, cmd)), cmul(cconj(v[key(1, 0, 0)]), cadd(c1, cmd)));
+        v[key(0, 0, 0)] = cscale(c000, cfac);
+        v[key(0, 0, 1)] = cscale(c001, cfac);
+        v[key(0, 1, 0)] = cscale(c010, cfac);
+        v[key(0, 1, 1)] = cscale(c011, cfac);
+        v[key(1, 0, 0)] = cconj(v[key(0, 1, 1)]);
+        v[key(1, 0, 1)] = cconj(v[key(0, 1, 0)]);
+        v[key(1, 1, 0)] = cconj(v[key(0, 0, 1)]);
+        v[key(1, 1, 1)] = cconj(v[key(0, 0, 0)]);
+    }
+};
+
+// ------------------------------------------------- fcomb on half spectra ---
+// d(k) = F1(k) + i F2(k) is the FFT of the complex grid the reference builds
+// (Re = grid 1, Im = interlaced grid); outside the stored half it is
+// conj(F1(-k)) + i conj(F2(-k)).
+template <class R>
+__device__ __forceinline__ typename Cx<R>::T dsample(const typename Cx<R>::T *__restrict__ F1,
+                                                     const typename Cx<R>::T *__restrict__ F2, int N, int X, int Y,
+                                                     int Z) {
+    using C = typename Cx<R>::T;
+    const int NH = N / 2 + 1;
+    if (X <= N / 2) {
+        const size_t o = ((size_t)Z * N + Y) * NH + X;
+        const C f1 = F1[o], f2 = F2[o];
+        return cmk<C>(f1.x - f2.y, f1.y + f2.x);
+    }
+    const size_t o = ((size_t)kneg0(Z, N) * N + kneg0(Y, N)) * NH + (N - X);
+    const C f1 = F1[o], f2 = F2[o];
+    return cmk<C>(f1.x + f2.y, f2.x - f1.y);
+}
+
+template <class R>
+__global__ void fcomb_interlaced_half_kernel(int N, const typename Cx<R>::T *__restrict__ spec,
+                                             typename Cx<R>::T *__restrict__ delta, const R *__restrict__ iW,
+                                             R cf, double piN) {
+    const int NH = N / 2 + 1;
+    const size_t HC = (size_t)N * N * NH;
+    const typename Cx<R>::T *F1 = spec, *F2 = spec + HC;
+    const size_t total = (size_t)NH * NH * NH;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+        const int ox = (int)(t % NH), oy = (int)((t / NH) % NH), oz = (int)(t / ((size_t)NH * NH));
+        const int cx = kneg0(ox, N), cy = kneg0(oy, N), cz = kneg0(oz, N);
+        Orbit<R> o;
+        o.ex = ox == cx; o.ey = oy == cy; o.ez = oz == cz;
+#pragma unroll
+        for (int s = 0; s < 8; s++) {
+            const int xs = s & 1, ys = (s >> 1) & 1, zs = s >> 2;
+            o.v[o.key(xs, ys, zs)] = dsample<R>(F1, F2, N, xs ? cx : ox, ys ? cy : oy, zs ? cz : oz);
+        }
+        const R cfac = cf * iW[ox] * iW[oy] * iW[oz];
+        o.combine((R)(piN * ox), (R)(piN * oy), (R)(piN * oz), cfac);
+        // store the orbit's locations inside the half (x = ox; x = cx only if equal)
+#pragma unroll
+        for (int s = 0; s < 4; s++) {
+            const int ys = s & 1, zs = s >> 1;
+            if ((ys && o.ey) || (zs && o.ez)) continue;
+            const int Y = ys ? cy : oy, Z = zs ? cz : oz;
+            delta[((size_t)Z * N + Y) * NH + ox] = o.v[o.key(0, ys, zs)];
+        }
+    }
+}
+
+template <class R>
+__global__ void fcomb_plain_half_kernel(int N, const typename Cx<R>::T *__restrict__ spec,
+                                        typename Cx<R>::T *__restrict__ delta, const R *__restrict__ iW, R cf) {
+    const int NH = N / 2 + 1;
+    const size_t HC = (size_t)N * N * NH;
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < HC; c += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(c % NH), y = (int)((c / NH) % N), z = (int)(c / ((size_t)NH * N));
+        const R f = cf * iW[x] * iW[kabs0(y, N)] * iW[kabs0(z, N)];
+        delta[c] = cscale(spec[c], f);
+    }
+}
+
+template <class R>
+int fcomb_half(int N, int nintp, bool interlaced, float box, double norm, const typename Cx<R>::T *spec,
+               typename Cx<R>::T *delta, cudaStream_t st, int64_t *launches) {
+    const int NH = N / 2 + 1;
+    std::vector<double> tW(NH);
+    window_table(N, nintp, tW.data());
+    std::vector<R> iW(NH);
+    for (int i = 0; i < NH; i++) iW[i] = (R)(1.0 / tW[i]);
+    // iW is tiny; keep it in a per-call device buffer that lives in a static
+    // cache keyed by (N, nintp, precision) to avoid an allocation per box.
+    static thread_local DevBuf cache;
+    static thread_local int cN = -1, cn = -1, cs = -1;
+    if (cN != N || cn != nintp || cs != (int)sizeof(R) || !cache.p) {
+        PBI4G_CHECK(cache.ensure(sizeof(R) * NH));
+        PBI4G_CUDA(cudaMemcpy(cache.p, iW.data(), sizeof(R) * NH, cudaMemcpyHostToDevice));
+        cN = N; cn = nintp; cs = (int)sizeof(R);
+    }
+    const double kF3 = fcomb_kF3(box);
+    const double cf = (interlaced ? 1.0 / (4.0 * kF3) : 1.0 / kF3) / norm;
+    if (interlaced) {
+        const double tpiN = (double)kTwoPiF / (double)N;
+        const size_t total = (size_t)NH * NH * NH;
+        fcomb_interlaced_half_kernel<R><<<grid_blocks(total, 256), 256, 0, st>>>(N, spec, delta, cache.as<R>(),
+                                                                                 (R)cf, -tpiN / 2.0);
+    } else {
+        fcomb_plain_half_kernel<R><<<grid_blocks(half_cells(N), 256), 256, 0, st>>>(N, spec, delta, cache.as<R>(),
+                                                                                    (R)cf);
+    }
+    PBI4G_LAUNCH_CHECK();
+    ++*launches;
+    return PBI4G_OK;
+}
+
+template int fcomb_half<float>(int, int, bool, float, double, const float2 *, float2 *, cudaStream_t, int64_t *);
+template int fcomb_half<double>(int, int, bool, float, double, const double2 *, double2 *, cudaStream_t, int64_t *);
+
+// ------------------------------------------------ fcomb on full grids (FP64) ---
+__global__ void fcomb_interlaced_full_kernel(int N, const double2 *in, double2 *out, const double *__restrict__ tW,
+                                             double cf, double piN) {
+    const int NH = N / 2 + 1;
+    const size_t total = (size_t)NH * NH * NH;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+        const int ox = (int)(t % NH), oy = (int)((t / NH) % NH), oz = (int)(t / ((size_t)NH * NH));
+        const int cx = kneg0(ox, N), cy = kneg0(oy, N), cz = kneg0(oz, N);
+        Orbit<double> o;
+        o.ex = ox == cx; o.ey = oy == cy; o.ez = oz == cz;
+#pragma unroll
+        for (int s = 0; s < 8; s++) {
+            const int xs = s & 1, ys = (s >> 1) & 1, zs = s >> 2;
+            const int X = xs ? cx : ox, Y = ys ? cy : oy, Z = zs ? cz : oz;
+            o.v[o.key(xs, ys, zs)] = in[((size_t)Z * N + Y) * N + X];
+        }
+        const double cfac = cf / (tW[ox] * tW[oy] * tW[oz]);
+        // the reference accumulates xrec = recx^(ix-1); the direct angle differs only by rounding
+        o.combine(piN * ox, piN * oy, piN * oz, cfac);
+#pragma unroll
+        for (int s = 0; s < 8; s++) {
+            const int xs = s & 1, ys = (s >> 1) & 1, zs = s >> 2;
+            if ((xs && o.ex) || (ys && o.ey) || (zs && o.ez)) continue;
+            const int X = xs ? cx : ox, Y = ys ? cy : oy, Z = zs ? cz : oz;
+            out[((size_t)Z * N + Y) * N + X] = o.v[o.key(xs, ys, zs)];
+        }
+    }
+}
+
+__global__ void fcomb_plain_full_kernel(int N, const double2 *in, double2 *out, const double *__restrict__ tW,
+                                        double cf) {
+    const size_t n = (size_t)N * N * N;
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(c % N), y = (int)((c / N) % N), z = (int)(c / ((size_t)N * N));
+        double2 v = in[c];
+        if (x <= N / 2) {
+            const double cfac = cf / (tW[x] * tW[kabs0(y, N)] * tW[kabs0(z, N)]);
+            v.x *= cfac;
+            v.y *= cfac;
+        }
+        out[c] = v;
+    }
+}
+
+int fcomb_full(int N, int nintp, bool interlaced, float box, const double2 *in, double2 *out, cudaStream_t st) {
+    const int NH = N / 2 + 1;
+    std::vector<double> tW(NH);
+    window_table(N, nintp, tW.data());
+    DevBuf dW;
+    PBI4G_CHECK(dW.ensure(sizeof(double) * NH));
+    PBI4G_CUDA(cudaMemcpyAsync(dW.p, tW.data(), sizeof(double) * NH, cudaMemcpyHostToDevice, st));
+    const double kF3 = fcomb_kF3(box);
+    if (interlaced) {
+        const double tpiN = (double)kTwoPiF / (double)N;
+        const size_t total = (size_t)NH * NH * NH;
+        fcomb_interlaced_full_kernel<<<grid_blocks(total, 128), 128, 0, st>>>(N, in, out, dW.as<double>(),
+                                                                              1.0 / (4.0 * kF3), -tpiN / 2.0);
+    } else {
+        fcomb_plain_full_kernel<<<grid_blocks(full_cells(N), 256), 256, 0, st>>>(N, in, out, dW.as<double>(),
+                                                                                 1.0 / kF3);
+    }
+    PBI4G_LAUNCH_CHECK();
+    PBI4G_CUDA(cudaStreamSynchronize(st));
+    return PBI4G_OK;
+}
+
+// ------------------------------------------------------------ P(k) bins ---
+struct PkExact {
+    double kF, dk, kck;
+};
+
+// Bin index with the reference's FP64 operation sequence (powerI4.f90:549-566);
+// explicit _rn intrinsics keep the compiler from contracting into FMAs.
+__device__ __forceinline__ int pk_bin_exact(const PkExact &e, int kx, int ky, int kz) {
+    const double rkx = __dmul_rn(e.kF, (double)kx), rky = __dmul_rn(e.kF, (double)ky), rkz = __dmul_rn(e.kF, (double)kz);
+    const double s = __dadd_rn(__dadd_rn(__dmul_rn(rkx, rkx), __dmul_rn(rky, rky)), __dmul_rn(rkz, rkz));
+    const double rk = __dsqrt_rn(s);
+    const double t = __dsub_rn(__dsub_rn(__ddiv_rn(rk, e.dk), e.kck), DBL_MIN);
+    return (int)llround(t) + 1;
+}
+
+__device__ __forceinline__ double pk_rk_exact(const PkExact &e, int kx, int ky, int kz) {
+    const double rkx = __dmul_rn(e.kF, (double)kx), rky = __dmul_rn(e.kF, (double)ky), rkz = __dmul_rn(e.kF, (double)kz);
+    return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(rkx, rkx), __dmul_rn(rky, rky)), __dmul_rn(rkz, rkz)));
+}
+
+// half-space mode selection of powerI4.f90:563
+__device__ __forceinline__ bool pk_keep(int x, int ky, int kz) { return x != 0 || ky > 0 || (ky == 0 && kz > 0); }
+
+__global__ void pk_bins_kernel(int N, int nbins, PkExact e, unsigned long long *__restrict__ co,
+                               double *__restrict__ sumk) {
+    const int NH = N / 2 + 1;
+    const size_t HC = (size_t)N * N * NH;
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < HC; c += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(c % NH), ky = kfreq0((int)((c / NH) % N), N), kz = kfreq0((int)(c / ((size_t)NH * N)), N);
+        if (!pk_keep(x, ky, kz)) continue;
+        const int b = pk_bin_exact(e, x, ky, kz);
+        if (b < 1 || b > nbins) continue;
+        atomicAdd(co + (b - 1), 1ull);
+        atomicAdd(sumk + (b - 1), pk_rk_exact(e, x, ky, kz));
+    }
+}
+
+__global__ void pk_bins_finish_kernel(int nbins, const unsigned long long *co, double *avgk_co) {
+    for (int b = threadIdx.x; b < nbins; b += blockDim.x) avgk_co[nbins + b] = (double)co[b];
+}
+
+int PkBins::build(int N_, float box_, float kbin_, float kcenter_, int nbins_, cudaStream_t st, int64_t *launches) {
+    if (N == N_ && box == box_ && kbin == kbin_ && kcenter == kcenter_ && nbins == nbins_ && lut.p) return PBI4G_OK;
+    if (nbins_ < 1 || nbins_ > 65536 || !(kbin_ > 0)) return set_error(PBI4G_ERR_INVALID, "P bins: nbins=%d kbin=%g", nbins_, kbin_);
+    N = N_; box = box_; kbin = kbin_; kcenter = kcenter_; nbins = nbins_;
+    kF = (double)(kTwoPiF / box);
+    kF3 = kF * kF * kF;
+    dk = (double)kbin * kF;
+    const double kck = (double)(kcenter / kbin);
+    k2max = 3 * (N / 2) * (N / 2);
+    std::vector<int> h(k2max + 1);
+    for (int k2 = 0; k2 <= k2max; k2++) {
+        double t = sqrt((double)k2) / (double)kbin - kck;
+        double f = t - floor(t);
+        if (fabs(f - 0.5) < 1e-7) { h[k2] = -1; continue; }
+        long long b = llround(t) + 1;
+        h[k2] = (b >= 1 && b <= nbins) ? (int)b : 0;
+    }
+    PBI4G_CHECK(lut.ensure(sizeof(int) * (k2max + 1)));
+    PBI4G_CUDA(cudaMemcpyAsync(lut.p, h.data(), sizeof(int) * (k2max + 1), cudaMemcpyHostToDevice, st));
+    PBI4G_CHECK(avgk_co.ensure(sizeof(double) * 2 * nbins + sizeof(unsigned long long) * nbins));
+    double *sumk = avgk_co.as<double>();
+    unsigned long long *co = reinterpret_cast<unsigned long long *>(sumk + 2 * nbins);
+    PBI4G_CUDA(cudaMemsetAsync(avgk_co.p, 0, avgk_co.bytes, st));
+    PkExact e{kF, dk, kck};
+    pk_bins_kernel<<<grid_blocks(half_cells(N), 256), 256, 0, st>>>(N, nbins, e, co, sumk);
+    PBI4G_LAUNCH_CHECK();
+    pk_bins_finish_kernel<<<1, 256, 0, st>>>(nbins, co, sumk);
+    PBI4G_LAUNCH_CHECK();
+    *launches += 2;
+    blocks = grid_blocks(half_cells(N), 256, 152 * 4);
+    PBI4G_CHECK(partial.ensure(sizeof(double) * 3 * nbins * blocks));
+    return PBI4G_OK;
+}
+
+template <class R> struct AccOf { using T = float; };
+template <> struct AccOf<double> { using T = double; };
+
+template <class R, int MODE>
+__global__ void pk_accum_kernel(int N, int nbins, const int *__restrict__ lut, PkExact e, double l0, double l1,
+                                double l2, const typename Cx<R>::T *__restrict__ a,
+                                const typename Cx<R>::T *__restrict__ b, const typename Cx<R>::T *__restrict__ c,
+                                double *__restrict__ partial) {
+    using A = typename AccOf<R>::T;
+    extern __shared__ unsigned char smem_raw[];
+    A *s = reinterpret_cast<A *>(smem_raw);
+    const int nq = MODE == 0 ? 1 : 3;
+    for (int i = threadIdx.x; i < nq * nbins; i += blockDim.x) s[i] = 0;
+    __syncthreads();
+    const int NH = N / 2 + 1;
+    const size_t HC = (size_t)N * N * NH;
+    for (size_t cell = blockIdx.x * (size_t)blockDim.x + threadIdx.x; cell < HC;
+         cell += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(cell % NH), ky = kfreq0((int)((cell / NH) % N), N),
+                  kz = kfreq0((int)(cell / ((size_t)NH * N)), N);
+        if (!pk_keep(x, ky, kz)) continue;
+        const int k2 = x * x + ky * ky + kz * kz;
+        int bin = lut[k2];
+        if (bin < 0) bin = pk_bin_exact(e, x, ky, kz);
+        if (bin < 1 || bin > nbins) continue;
+        const typename Cx<R>::T va = a[cell];
+        if (MODE == 0) {
+            const typename Cx<R>::T vb = b[cell];
+            atomicAdd(&s[bin - 1], (A)(va.x * vb.x + va.y * vb.y));
+        } else if (MODE == 1) {
+            const A p = (A)(va.x * va.x + va.y * va.y);
+            const A lk = (A)(l0 * x + l1 * ky + l2 * kz);
+            const A mu2 = lk * lk / (A)k2;
+            const A L2 = (A)-0.5 + (A)1.5 * mu2;
+            const A L4 = (A)0.375 + mu2 * ((A)-3.75 + (A)4.375 * mu2);
+            atomicAdd(&s[bin - 1], p);
+            atomicAdd(&s[nbins + bin - 1], p * L2);
+            atomicAdd(&s[2 * nbins + bin - 1], p * L4);
+        } else {
+            const typename Cx<R>::T vb = b[cell], vc = c[cell];
+            atomicAdd(&s[bin - 1], (A)(va.x * va.x + va.y * va.y));
+            atomicAdd(&s[nbins + bin - 1], (A)(va.x * vb.x + va.y * vb.y));
+            atomicAdd(&s[2 * nbins + bin - 1], (A)(va.x * vc.x + va.y * vc.y));
+        }
+    }
+    __syncthreads();
+    double *out = partial + (size_t)blockIdx.x * 3 * nbins;
+    for (int i = threadIdx.x; i < 3 * nbins; i += blockDim.x) out[i] = i < nq * nbins ? (double)s[i] : 0.0;
+}
+
+// Deterministic reduction over blocks + the output rows of measure_pk /
+// measure_pk_multipoles (pout Fortran (5, nbins)).
+__global__ void pk_finalize_kernel(int nbins, int blocks, int mode, double kF3, const double *__restrict__ partial,
+                                   const double *__restrict__ avgk_co, double *__restrict__ pout) {
+    for (int bi = blockIdx.x * blockDim.x + threadIdx.x; bi < nbins; bi += gridDim.x * blockDim.x) {
+        double s0 = 0, s2 = 0, s4 = 0;
+        for (int k = 0; k < blocks; k++) {
+            const double *p = partial + (size_t)k * 3 * nbins;
+            s0 += p[bi];
+            s2 += p[nbins + bi];
+            s4 += p[2 * nbins + bi];
+        }
+        const double co = avgk_co[nbins + bi], avgk = avgk_co[bi];
+        double *o = pout + 5 * (size_t)bi;
+        o[0] = avgk / co;
+        o[1] = s0 * kF3 / co;
+        if (mode == 0) {
+            o[2] = co;
+            o[3] = 0.0;
+            o[4] = 0.0;
+        } else {
+            o[2] = 5.0 * s2 * kF3 / co;
+            o[3] = 9.0 * s4 * kF3 / co;
+            o[4] = co;
+        }
+    }
+}
+
+template <class R>
+int pk_measure(PkBins &bins, int mode, const double los[3], const typename Cx<R>::T *a, const typename Cx<R>::T *b,
+               const typename Cx<R>::T *c, double *d_pout, cudaStream_t st, int64_t *launches) {
+    using A = typename AccOf<R>::T;
+    const int nbins = bins.nbins, N = bins.N;
+    const size_t smem = sizeof(A) * (mode == 0 ? 1 : 3) * nbins;
+    if (smem > 200 * 1024) return set_error(PBI4G_ERR_INVALID, "too many P bins (%d)", nbins);
+    PkExact e{bins.kF, bins.dk, (double)(bins.kcenter / bins.kbin)};
+    const double l0 = los ? los[0] : 0, l1 = los ? los[1] : 0, l2 = los ? los[2] : 0;
+    const int blocks = bins.blocks;
+    if (mode == 0) {
+        auto k = pk_accum_kernel<R, 0>;
+        if (smem > 48 * 1024) PBI4G_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k<<<blocks, 256, smem, st>>>(N, nbins, bins.lut.as<int>(), e, l0, l1, l2, a, b ? b : a, c,
+                                     bins.partial.as<double>());
+    } else if (mode == 1) {
+        auto k = pk_accum_kernel<R, 1>;
+        if (smem > 48 * 1024) PBI4G_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k<<<blocks, 256, smem, st>>>(N, nbins, bins.lut.as<int>(), e, l0, l1, l2, a, b, c, bins.partial.as<double>());
+    } else {
+        auto k = pk_accum_kernel<R, 2>;
+        if (smem > 48 * 1024) PBI4G_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k<<<blocks, 256, smem, st>>>(N, nbins, bins.lut.as<int>(), e, l0, l1, l2, a, b, c, bins.partial.as<double>());
+    }
+    PBI4G_LAUNCH_CHECK();
+    pk_finalize_kernel<<<(nbins + 127) / 128, 128, 0, st>>>(nbins, blocks, mode == 0 ? 0 : 1, bins.kF3,
+                                                            bins.partial.as<double>(), bins.avgk_co.as<double>(),
+                                                            d_pout);
+    PBI4G_LAUNCH_CHECK();
+    *launches += 2;
+    return PBI4G_OK;
+}
+
+template int pk_measure<float>(PkBins &, int, const double *, const float2 *, const float2 *, const float2 *, double *,
+                               cudaStream_t, int64_t *);
+template int pk_measure<double>(PkBins &, int, const double *, const double2 *, const double2 *, const double2 *,
+                                double *, cudaStream_t, int64_t *);
+
+// --------------------------------------------------- q2k / q4k / reduce ---
+__global__ void qlk_full_kernel(int N, double kF, const double2 *__restrict__ in, int nidx, int i0, int i1, int i2,
+                                int i3, double2 *__restrict__ out) {
+    const size_t n = (size_t)N * N * N;
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(c % N), y = (int)((c / N) % N), z = (int)(c / ((size_t)N * N));
+        double2 q = in[c];
+        if (x <= N / 2) {
+            if (x + y + z > 0) {
+                const double v[3] = {kF * (double)kfreq0(x, N), kF * (double)kfreq0(y, N), kF * (double)kfreq0(z, N)};
+                double rk2 = __dadd_rn(__dadd_rn(__dmul_rn(v[0], v[0]), __dmul_rn(v[1], v[1])), __dmul_rn(v[2], v[2]));
+                if (nidx == 4) rk2 = rk2 * rk2;
+                const int idx[4] = {i0, i1, i2, i3};
+                for (int k = 0; k < nidx; k++) {
+                    q.x = q.x * v[idx[k]];
+                    q.y = q.y * v[idx[k]];
+                }
+                q.x = q.x / rk2;
+                q.y = q.y / rk2;
+            } else {
+                q = make_double2(0.0, 0.0);
+            }
+        }
+        out[c] = q;
+    }
+}
+
+int q2k_full(int N, float box, const double2 *in, int i, int j, double2 *out, cudaStream_t st) {
+    if (i < 1 || i > 3 || j < 1 || j > 3) return set_error(PBI4G_ERR_INVALID, "compute_q2k: index out of 1..3");
+    qlk_full_kernel<<<grid_blocks(full_cells(N), 256), 256, 0, st>>>(N, (double)(kTwoPiF / box), in, 2, i - 1, j - 1,
+                                                                      0, 0, out);
+    PBI4G_LAUNCH_CHECK();
+    return PBI4G_OK;
+}
+
+int q4k_full(int N, float box, const double2 *in, int i, int j, int l, int k, double2 *out, cudaStream_t st) {
+    if (i < 1 || i > 3 || j < 1 || j > 3 || l < 1 || l > 3 || k < 1 || k > 3)
+        return set_error(PBI4G_ERR_INVALID, "compute_q4k: index out of 1..3");
+    qlk_full_kernel<<<grid_blocks(full_cells(N), 256), 256, 0, st>>>(N, (double)(kTwoPiF / box), in, 4, i - 1, j - 1,
+                                                                      l - 1, k - 1, out);
+    PBI4G_LAUNCH_CHECK();
+    return PBI4G_OK;
+}
+
+// powerI4.f90:380-407, one thread per (ix, iy, iz) in [1, grid/2+1]^3; the four
+// writes keep their order so aliased locations end with the last one.
+__global__ void reduce_full_kernel(int L, const double2 *__restrict__ din, int N, double2 *__restrict__ dout) {
+    const int NH = N / 2 + 1;
+    const size_t total = (size_t)NH * NH * NH;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(t % NH), y = (int)((t / NH) % NH), z = (int)(t / ((size_t)NH * NH));
+        const int icz = kneg0(z, L), jcz = kneg0(z, N), icy = kneg0(y, L), jcy = kneg0(y, N);
+        const size_t LL = (size_t)L;
+        auto src = [&](int yy, int zz) { return din[((size_t)zz * LL + yy) * LL + x]; };
+        auto dst = [&](int yy, int zz) -> double2 & { return dout[((size_t)zz * N + yy) * N + x]; };
+        dst(y, z) = src(y, z);
+        dst(jcy, z) = src(icy, z);
+        dst(y, jcz) = src(y, icz);
+        dst(jcy, jcz) = src(icy, icz);
+    }
+}
+
+int reduce_full(int L, const double2 *din, int N, double2 *dout, cudaStream_t st) {
+    const int NH = N / 2 + 1;
+    reduce_full_kernel<<<grid_blocks((size_t)NH * NH * NH, 256), 256, 0, st>>>(L, din, N, dout);
+    PBI4G_LAUNCH_CHECK();
+    return PBI4G_OK;
+}
+
+}  // namespace pbi4g

@@ -1,0 +1,179 @@
+"""Device-resident estimator: one resident plan per box configuration.
+
+``Estimator`` wraps the ``pbi4g_plan_*`` C ABI.  Positions enter either as a
+CUDA tensor / device pointer of shape (3, npart) float64 in [0, 1)
+(``run_device``: the throughput path, everything stays in HBM) or as a host
+numpy array (``run_host``: copies inside the call).  Outputs follow the
+reference's Fortran arrays: ``pout`` is (5, nbins_ps) with rows
+avgk, P0, P2, P4, Nmodes (measure_pk_multipoles, powerI4.f90:685-691; for real
+space rows avgk, P, Nmodes as measure_pk, :589-592), ``bout`` is (9 or 11, itot)
+as measure_bk / measure_bk_multipoles (bispectrumI4.f90:174-182, 490-500).
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+from math import floor
+
+import numpy as np
+
+from ._lib import PRECISIONS, Config, check, lib, ptr
+
+
+@dataclass
+class EstimatorConfig:
+    grid: int
+    box: float
+    nintp: int = 4
+    interlacing: bool = True
+    multipoles: bool = False
+    los: tuple = (0.0, 0.0, 1.0)      # already divided by (los . los), as IO.derived_params does
+    kbin_ps: float = 1.0
+    kcenter_ps: float = 1.0
+    nbins_ps: int | None = None
+    do_bispectrum: bool = True
+    kbin_bs: float = 1.0
+    kcenter_bs: float = 1.0
+    nbins_bs: int | None = None
+    iopen: bool = True
+    precision: str = "fp32"
+    extra: dict = field(default_factory=dict)
+
+    def __post_init__(self):
+        g = int(self.grid)
+        if self.nbins_ps is None:   # pbi4.py:98
+            self.nbins_ps = floor((g / 2 + self.kbin_ps - self.kcenter_ps) / self.kbin_ps)
+        if self.nbins_bs is None:   # pbi4.py:99
+            self.nbins_bs = floor((g / 3 + self.kbin_bs - self.kcenter_bs) / self.kbin_bs)
+
+    @classmethod
+    def from_params(cls, params: dict, precision: str = "fp32", do_bispectrum: bool = True, **over):
+        """From a reference params dict after IO.derived_params (pbi4.py:86-119)."""
+        kw = dict(grid=int(params["grid"]), box=float(params["box"]), nintp=int(params["interpolation"]),
+                  interlacing=bool(params["interlacing"]), multipoles=bool(params["multipoles"]),
+                  los=tuple(float(x) for x in np.asarray(params["los"], dtype=np.float64)),
+                  kbin_ps=float(params["kbin"]), kcenter_ps=float(params["kcenter"]),
+                  nbins_ps=int(params["nbins_ps"]), do_bispectrum=do_bispectrum,
+                  kbin_bs=float(params["kbin"]), kcenter_bs=float(params["kcenter"]),
+                  nbins_bs=int(params["nbins_bisp"]), iopen=bool(params["iopen"]), precision=precision)
+        kw.update(over)
+        return cls(**kw)
+
+    def to_c(self) -> Config:
+        c = Config()
+        c.grid, c.box, c.nintp = int(self.grid), float(self.box), int(self.nintp)
+        c.interlacing, c.multipoles = int(bool(self.interlacing)), int(bool(self.multipoles))
+        for k in range(3):
+            c.los[k] = float(self.los[k])
+        c.kbin_ps, c.kcenter_ps, c.nbins_ps = float(self.kbin_ps), float(self.kcenter_ps), int(self.nbins_ps)
+        c.do_bispectrum = int(bool(self.do_bispectrum))
+        c.kbin_bs, c.kcenter_bs, c.nbins_bs = float(self.kbin_bs), float(self.kcenter_bs), int(self.nbins_bs)
+        c.iopen = int(bool(self.iopen))
+        c.precision = PRECISIONS[self.precision]
+        return c
+
+    def key(self):
+        return (int(self.grid), float(self.box), int(self.nintp), bool(self.interlacing), bool(self.multipoles),
+                tuple(self.los), float(self.kbin_ps), float(self.kcenter_ps), int(self.nbins_ps),
+                bool(self.do_bispectrum), float(self.kbin_bs), float(self.kcenter_bs), int(self.nbins_bs),
+                bool(self.iopen), self.precision)
+
+
+def footprint(cfg: EstimatorConfig, npart_max: int) -> int:
+    """Device bytes a plan for cfg needs (admission control); allocates nothing."""
+    c = cfg.to_c()
+    out = ctypes.c_int64()
+    check(lib().pbi4g_plan_footprint(ctypes.byref(c), int(npart_max), ctypes.byref(out)))
+    return int(out.value)
+
+
+class Estimator:
+    def __init__(self, cfg: EstimatorConfig, stream=None):
+        self.cfg = cfg
+        self._c = cfg.to_c()
+        h = ctypes.c_void_p()
+        check(lib().pbi4g_plan_create(ctypes.byref(self._c), ctypes.byref(h)))
+        self._h = h
+        if stream is not None:
+            self.set_stream(stream)
+        nb, it, br = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int32()
+        check(lib().pbi4g_plan_shape(self._h, ctypes.byref(nb), ctypes.byref(it), ctypes.byref(br)))
+        self.nbins_ps, self.itot, self.brows = nb.value, it.value, br.value
+
+    # -- lifecycle
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().pbi4g_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream):
+        """stream: a torch.cuda.Stream, an integer cudaStream_t, or None (legacy default)."""
+        s = getattr(stream, "cuda_stream", stream)
+        check(lib().pbi4g_plan_set_stream(self._h, s))
+
+    def enable_timing(self, on: bool = True):
+        check(lib().pbi4g_plan_enable_timing(self._h, int(bool(on))))
+
+    def stage_times(self):
+        """{stage: (summed ms, calls)} since the last query (synchronises the plan's stream)."""
+        from ._lib import NSTAGES, STAGES
+        ms = np.zeros(NSTAGES, dtype=np.float64)
+        calls = np.zeros(NSTAGES, dtype=np.int64)
+        check(lib().pbi4g_plan_stage_times(self._h, ms.ctypes.data, calls.ctypes.data))
+        return {STAGES[k]: (float(ms[k]), int(calls[k])) for k in range(NSTAGES)}
+
+    @property
+    def launches(self) -> int:
+        return int(lib().pbi4g_plan_kernel_launches(self._h))
+
+    # -- stages (device pointers / CUDA tensors)
+    def density(self, npart: int, pos, weight=None):
+        check(lib().pbi4g_plan_density(self._h, int(npart), ptr(pos), ptr(weight)))
+
+    def powerspectrum(self, pout):
+        check(lib().pbi4g_plan_powerspectrum(self._h, ptr(pout)))
+
+    def bispectrum(self, bout):
+        check(lib().pbi4g_plan_bispectrum(self._h, ptr(bout)))
+
+    def run_device(self, npart: int, pos, pout, bout=None, weight=None):
+        check(lib().pbi4g_plan_run_device(self._h, int(npart), ptr(pos), ptr(weight), ptr(pout), ptr(bout)))
+
+    def alloc_outputs(self, device="cuda"):
+        """Device output tensors (pout (5, nbins_ps), bout (brows, itot)) in Fortran layout."""
+        import torch
+        pout = torch.empty((self.nbins_ps, 5), dtype=torch.float64, device=device).t()
+        bout = None
+        if self.itot:
+            bout = torch.empty((self.itot, self.brows), dtype=torch.float64, device=device).t()
+        return pout, bout
+
+    # -- host path
+    def run_host(self, pos: np.ndarray, weight: np.ndarray | None = None):
+        pos = np.ascontiguousarray(pos, dtype=np.float64)
+        if pos.ndim != 2 or pos.shape[0] != 3:
+            raise ValueError("pos must be (3, npart)")
+        npart = pos.shape[1]
+        w = None if weight is None else np.ascontiguousarray(weight, dtype=np.float64)
+        pout = np.empty((5, self.nbins_ps), dtype=np.float64, order="F")
+        bout = np.empty((self.brows, self.itot), dtype=np.float64, order="F") if self.itot else None
+        check(lib().pbi4g_plan_run_host(self._h, npart, pos.ctypes.data, ptr(w), pout.ctypes.data,
+                                        None if bout is None else bout.ctypes.data))
+        return pout, bout
+
+    def triangle_counts(self) -> np.ndarray:
+        out = np.empty(self.itot, dtype=np.int64)
+        check(lib().pbi4g_plan_triangle_counts(self._h, out.ctypes.data))
+        return out
+
+    def delta_half(self) -> np.ndarray:
+        n = int(self.cfg.grid)
+        out = np.empty((n, n, n // 2 + 1), dtype=np.complex128)
+        check(lib().pbi4g_plan_get_delta_half(self._h, out.ctypes.data))
+        return out

@@ -1,0 +1,218 @@
+"""GPU parity: every C-ABI entry point against the FP64 oracle on seeded inputs.
+
+Tolerances (stated per test): integer outputs (mode counts, triangle counts)
+bit-exact; FP64 GPU paths within 1e-9; FP32 paths within 1e-5 relative on P0
+and on B relative to max(|B|, P1P2+P1P3+P2P3) (see tests/_helpers.b_errors).
+"""
+import numpy as np
+import pytest
+
+from oracle import pbi4_oracle as O
+from pbi4_gb300 import bispectrumI4 as B
+from pbi4_gb300 import powerI4 as P
+from pbi4_gb300 import synthetic
+from pbi4_gb300.estimator import Estimator, EstimatorConfig
+
+from ._helpers import b_errors, oracle_density, p_errors, ref_params
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def box_uniform():
+    return synthetic.uniform_box(20000, seed=11)
+
+
+@pytest.fixture(scope="module")
+def box_za():
+    return synthetic.zeldovich_box(24, 1000.0, seed=12)
+
+
+# ------------------------------------------------------------ assignment ---
+@pytest.mark.parametrize("nintp", [1, 2, 3, 4])
+@pytest.mark.parametrize("grid", [8, 16, 32])
+def test_assign_single_grid(box_uniform, nintp, grid):
+    pos = box_uniform
+    w = np.ones(pos.shape[1])
+    ref = O.assign_single_grid(grid, nintp, pos.shape[1], pos, w)
+    got = P.assign_single_grid(grid, nintp, pos.shape[1], pos, w)
+    assert got.shape == ref.shape and got.dtype == ref.dtype
+    assert np.max(np.abs(got - ref)) <= 1e-11 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("nintp", [1, 2, 3, 4])
+@pytest.mark.parametrize("grid", [8, 16, 32])
+def test_assign_double_grid(box_za, nintp, grid):
+    pos = box_za
+    w = np.random.default_rng(13).random(pos.shape[1]) + 0.5
+    ref = O.assign_double_grid(grid, nintp, pos.shape[1], pos, w)
+    got = P.assign_double_grid(grid, nintp, pos.shape[1], pos, w)
+    assert got.dtype == np.complex128
+    assert np.max(np.abs(got - ref)) <= 1e-11 * np.max(np.abs(ref))
+
+
+def test_assign_bit_reproducible_under_permutation(box_uniform):
+    pos = box_uniform
+    w = np.ones(pos.shape[1])
+    a = P.assign_double_grid(32, 4, pos.shape[1], pos, w)
+    perm = np.random.default_rng(1).permutation(pos.shape[1])
+    b = P.assign_double_grid(32, 4, pos.shape[1], np.ascontiguousarray(pos[:, perm]), w)
+    c = P.assign_double_grid(32, 4, pos.shape[1], pos, w)
+    assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+    assert np.array_equal(a.view(np.uint64), c.view(np.uint64))
+
+
+def test_assign_edge_positions():
+    # positions at 0, just below 1 and exactly 1 (pbi4.py:243 can produce 1.0)
+    pos = np.array([[0.0, 1.0 - 2 ** -53, 1.0, 0.5], [0.0, 0.999999, 1.0, 0.25], [1.0, 0.0, 0.5, 0.75]])
+    w = np.ones(4)
+    for nintp in (1, 2, 3, 4):
+        ref = O.assign_double_grid(8, nintp, 4, pos, w)
+        got = P.assign_double_grid(8, nintp, 4, pos, w)
+        assert np.max(np.abs(got - ref)) <= 1e-12
+
+
+# ------------------------------------------------------- fcomb and friends ---
+@pytest.mark.parametrize("interlacing", [False, True])
+@pytest.mark.parametrize("grid,nintp", [(8, 2), (16, 4), (16, 3), (32, 1)])
+def test_fcomb_full(box_za, interlacing, grid, nintp):
+    import scipy.fft
+    p = ref_params(grid, 1000.0, nintp, interlacing, False)
+    npart, dcl = O.assign_grid(box_za, p)
+    f = scipy.fft.fftn(dcl / npart)
+    ref = O.fcomb(grid, nintp, interlacing, 1000.0, f)
+    got = P.fcomb(grid, nintp, interlacing, 1000.0, f)
+    assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+def test_q2k_q4k_reduce(box_za):
+    import scipy.fft
+    rng = np.random.default_rng(3)
+    d = scipy.fft.fftn(rng.standard_normal((16, 16, 16)))
+    for ij in [(1, 1), (2, 1), (3, 2), (3, 3)]:
+        ref = O.compute_q2k(16, 1000.0, d, *ij)
+        got = P.compute_q2k(16, 1000.0, d, *ij)
+        assert np.max(np.abs(got - ref)) <= 1e-13 * np.max(np.abs(ref))
+    for ijlk in [(1, 1, 1, 1), (3, 2, 2, 1), (3, 3, 1, 1)]:
+        ref = O.compute_q4k(16, 1000.0, d, *ijlk)
+        got = P.compute_q4k(16, 1000.0, d, *ijlk)
+        assert np.max(np.abs(got - ref)) <= 1e-13 * np.max(np.abs(ref))
+    big = scipy.fft.fftn(rng.standard_normal((32, 32, 32)))
+    assert np.array_equal(P.reduce_array(32, big, 16), O.reduce_array(32, big, 16))
+
+
+# ------------------------------------------------------------------ P(k) ---
+@pytest.mark.parametrize("kbin,kcenter", [(1.0, 1.0), (2.0, 2.0), (1.5, 0.5)])
+def test_measure_pk_dropin(box_za, kbin, kcenter):
+    p = ref_params(32, 1000.0, 4, True, True, kbin=kbin, kcenter=kcenter)
+    npart, d, d2, d4 = oracle_density(box_za, p)
+    nb = p["nbins_ps"]
+    ref = O.measure_pk_multipoles(32, 1000.0, kbin, kcenter, nb, d, d2, d4)
+    got = P.measure_pk_multipoles(32, 1000.0, kbin, kcenter, nb, d, d2, d4)
+    np.testing.assert_array_equal(got[4], ref[4])
+    assert np.max(np.abs(got[:4] - ref[:4]) / np.abs(ref[:4]).max(axis=1, keepdims=True)) < 1e-12
+    ref1 = O.measure_pk(32, 1000.0, kbin, kcenter, nb, d, d2)
+    got1 = P.measure_pk(32, 1000.0, kbin, kcenter, nb, d, d2)
+    np.testing.assert_array_equal(got1[2], ref1[2])
+    assert np.max(np.abs(got1[:2] - ref1[:2]) / np.abs(ref1[:2]).max(axis=1, keepdims=True)) < 1e-12
+
+
+@pytest.mark.parametrize("precision,tol", [("fp32", 1e-5), ("fp64", 1e-9)])
+@pytest.mark.parametrize("grid,nintp,interlacing,multipoles",
+                         [(32, 4, True, True), (32, 2, False, False), (64, 3, True, True), (16, 1, True, False)])
+def test_plan_powerspectrum(box_za, precision, tol, grid, nintp, interlacing, multipoles):
+    p = ref_params(grid, 1000.0, nintp, interlacing, multipoles, los=(0.0, 2.0, 1.0))
+    npart, d, d2, d4 = oracle_density(box_za, p)
+    nb = p["nbins_ps"]
+    if multipoles:
+        ref = O.measure_pk_multipoles(grid, 1000.0, 1.0, 1.0, nb, d, d2, d4)
+    else:
+        ref = O.measure_pk(grid, 1000.0, 1.0, 1.0, nb, d, d)
+    est = Estimator(EstimatorConfig.from_params(p, precision=precision, do_bispectrum=False))
+    pout, _ = est.run_host(box_za)
+    rows = 4 if multipoles else 2
+    np.testing.assert_array_equal(pout[rows], ref[rows])
+    e0, e2, e4 = p_errors(pout, ref, multipoles)
+    assert e0 < tol and e2 < tol and e4 < tol, (e0, e2, e4)
+    assert np.max(np.abs(pout[0] / ref[0] - 1)) < 1e-12
+
+
+# --------------------------------------------------------------- counts ---
+def test_count_triangles_golden():
+    g = np.load(__import__("os").path.join(__import__("os").path.dirname(__file__), "golden",
+                                           "reference_testdata_cols.npz"))
+    c = B.count_triangles(21, 64, 1.0, 1.0, True, False, 4, 1156)
+    np.testing.assert_array_equal(np.round(c / 64.0 ** 3).astype(np.int64), g["bs_ntr"])
+    assert np.array_equal(c, np.round(c / 64.0 ** 3) * 64.0 ** 3)
+
+
+@pytest.mark.parametrize("grid,nb,kbin,kc,iopen,cross", [(16, 5, 1.0, 1.0, False, False), (32, 8, 2.0, 2.0, True, False),
+                                                         (24, 6, 1.5, 1.5, True, True), (16, 4, 1.0, 1.0, True, True)])
+def test_count_triangles(grid, nb, kbin, kc, iopen, cross):
+    it = O.itot(nb, kbin, kc, iopen, cross)
+    ref = O.count_triangles(nb, grid, kbin, kc, iopen, cross, 1, it)
+    got = B.count_triangles(nb, grid, kbin, kc, iopen, cross, 1, it)
+    np.testing.assert_array_equal(got / grid ** 3, np.round(ref / grid ** 3))
+
+
+# ------------------------------------------------------------ bispectrum ---
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("fp32", 1e-5)])
+def test_measure_bk_dropin(box_za, precision, tol):
+    p = ref_params(32, 1000.0, 4, True, True, kbin=1.0, kcenter=1.0)
+    npart, d, d2, d4 = oracle_density(box_za, p)
+    nb, it = 8, O.itot(8, 1.0, 1.0, True)
+    counts = O.count_triangles(nb, 32, 1.0, 1.0, True, False, 1, it)
+    kf = 2 * np.pi / 1000.0
+    B.set_precision(precision)
+    try:
+        ref = O.measure_bk(nb, 32, 1.0, 1.0, True, kf, 1, it, npart, counts, d)
+        got = B.measure_bk(nb, 32, 1.0, 1.0, True, kf, 1, it, npart, counts, d)
+        np.testing.assert_array_equal(got[[0, 1, 2, 8]], ref[[0, 1, 2, 8]])
+        errs, pw = b_errors(got, ref)
+        assert max(errs) < tol and pw < tol, (errs, pw)
+        refm = O.measure_bk_multipoles(nb, 32, 1.0, 1.0, True, kf, 1, it, npart, counts, d, d2, d4)
+        gotm = B.measure_bk_multipoles(nb, 32, 1.0, 1.0, True, kf, 1, it, npart, counts, d, d2, d4)
+        errs, pw = b_errors(gotm, refm)
+        assert max(errs) < tol and pw < tol, (errs, pw)
+    finally:
+        B.set_precision("fp32")
+
+
+def test_measure_bk_cross_dropin(box_za, box_uniform):
+    p = ref_params(16, 1000.0, 3, True, False)
+    n1, d1, _, _ = oracle_density(box_za, p)
+    n2, d2, _, _ = oracle_density(box_uniform, p)
+    nb, it = 4, O.itot(4, 1.0, 1.0, True, True)
+    counts = O.count_triangles(nb, 16, 1.0, 1.0, True, True, 1, it)
+    kf = 2 * np.pi / 1000.0
+    B.set_precision("fp64")
+    try:
+        ref = O.measure_bk_cross(nb, 16, 1.0, 1.0, True, kf, 1, it, n1, counts, d1, d2)
+        got = B.measure_bk_cross(nb, 16, 1.0, 1.0, True, kf, 1, it, n1, counts, d1, d2)
+    finally:
+        B.set_precision("fp32")
+    np.testing.assert_array_equal(got[[0, 1, 2, 4]], ref[[0, 1, 2, 4]])
+    assert np.max(np.abs(got[3] - ref[3])) <= 1e-9 * np.max(np.abs(ref[3]))
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("fp32", 1e-5)])
+@pytest.mark.parametrize("multipoles", [False, True])
+def test_plan_bispectrum(box_za, precision, tol, multipoles):
+    grid, nb = 32, 8
+    p = ref_params(grid, 1000.0, 4, True, multipoles, kbin=1.0, kcenter=1.0)
+    p["nbins_bisp"] = nb
+    npart, d, d2, d4 = oracle_density(box_za, p)
+    it = O.itot(nb, 1.0, 1.0, True)
+    counts = O.count_triangles(nb, grid, 1.0, 1.0, True, False, 1, it)
+    kf = 2 * np.pi / 1000.0
+    if multipoles:
+        ref = O.measure_bk_multipoles(nb, grid, 1.0, 1.0, True, kf, 1, it, npart, counts, d, d2, d4)
+    else:
+        ref = O.measure_bk(nb, grid, 1.0, 1.0, True, kf, 1, it, npart, counts, d)
+    est = Estimator(EstimatorConfig.from_params(p, precision=precision))
+    pout, bout = est.run_host(box_za)
+    assert bout.shape == ref.shape
+    np.testing.assert_array_equal(est.triangle_counts(), np.round(counts / grid ** 3).astype(np.int64))
+    np.testing.assert_array_equal(bout[[0, 1, 2, 8]], ref[[0, 1, 2, 8]])
+    errs, pw = b_errors(bout, ref)
+    assert max(errs) < tol and pw < tol, (errs, pw)
