@@ -34,9 +34,9 @@ WORKLOAD = dict(workload="zeldovich_256_pcs_interlaced_P024_B024", particles=128
 METRIC = "P+B boxes/s @256^3 PCS interlaced (P l=0,2,4 + B l=0,2,4)"
 
 
-def make_positions(quick=False):
+def make_positions(quick=False, small=False):
     from pbi4_gb300 import synthetic
-    n = 32 if quick else 128
+    n = 32 if quick else (64 if small else 128)
     return synthetic.zeldovich_box(n, WORKLOAD["box"], n_s=-1.5, rms_disp=5.0, f_growth=0.7, seed=2)
 
 
@@ -197,9 +197,9 @@ def run_ours(args):
         if world > 1:
             dist.barrier()
 
-    pos = make_positions(quick=args.quick)
+    pos = make_positions(quick=args.quick, small=args.small)
     npart = pos.shape[1]
-    cfg = est_config(args.precision, grid=64 if args.quick else None)
+    cfg = est_config(args.precision, grid=64 if args.quick else (128 if args.small else None))
     est = Estimator(cfg)
     dpos = torch.from_numpy(pos).cuda()
     pout, bout = est.alloc_outputs()
@@ -279,6 +279,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "fp16split", "bf16"])
     ap.add_argument("--quick", action="store_true", help="small box (debug only)")
+    ap.add_argument("--small", action="store_true",
+                    help="profiling case: 64^3 particles on a 128^3 grid (same kernels, a few hundred MB)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

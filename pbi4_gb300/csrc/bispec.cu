@@ -23,7 +23,6 @@ namespace pbi4g {
 
 constexpr int kTP = 4;   // pairs per thread tile
 constexpr int kTQ = 8;   // q maps per thread tile
-constexpr int kKC = 32;  // contraction points per shared-memory chunk
 constexpr int kGroupThreads = 256;
 
 // ------------------------------------------------------------- Shells ---
@@ -82,7 +81,7 @@ int Shells::build(int N_, float kbin_, float kcenter_, int nb_, int iopen_, int 
 // Output slot (m, s) = m * nsets + s.  Non-cross: S = sum M_i M_j Q_{s,l}, pair
 // (i, j) of set-0 maps, q = map s*nb + l-1.  Cross: S = sum Q_i M_j M_l, pair
 // (j, l) of set-0 maps, q = map qset*nb + i-1.
-int TriPlan::build(const Shells &sh, int nsets_, int cross_) {
+int TriPlan::build(const Shells &sh, int nsets_, int cross_, int max_pairs) {
     nsets = nsets_;
     cross = cross_;
     const int nb = sh.nb;
@@ -129,33 +128,46 @@ int TriPlan::build(const Shells &sh, int nsets_, int cross_) {
         } else t = it->second;
         stab[(size_t)t * kTP * kTQ + (e.p % kTP) * kTQ + (e.q % kTQ)] = e.slot;
     }
-    // order tiles by (pair tile, q tile) and cut into groups of <= 256 tiles and <= 256 pairs
+    // Pair blocks of <= max_pairs consecutive pairs; inside a block tiles are
+    // ordered (q tile, pair tile) so the threads of a warp share a q tile.
+    // Groups are runs of <= kGroupThreads tiles of one block.
     std::vector<int> order(tl.size());
     for (size_t k = 0; k < order.size(); k++) order[k] = (int)k;
+    const int pblk = std::max(kTP, (max_pairs / kTP) * kTP);
     std::sort(order.begin(), order.end(), [&](int a, int b) {
-        return tl[a].x != tl[b].x ? tl[a].x < tl[b].x : tl[a].y < tl[b].y;
+        const int ba = tl[a].x / pblk, bb = tl[b].x / pblk;
+        if (ba != bb) return ba < bb;
+        return tl[a].y != tl[b].y ? tl[a].y < tl[b].y : tl[a].x < tl[b].x;
     });
     std::vector<int4> tiles_sorted;
     std::vector<int> stab_sorted;
     std::vector<int4> gl;
-    int g_t0 = 0, g_p0 = -1;
-    for (size_t k = 0; k < order.size(); k++) {
-        int4 t = tl[order[k]];
-        if (g_p0 < 0) g_p0 = t.x;
-        const int ntile_g = (int)tiles_sorted.size() - g_t0;
-        if (ntile_g >= kGroupThreads || t.x + kTP - g_p0 > 256) {
-            gl.push_back(make_int4(g_t0, (int)tiles_sorted.size(), g_p0, tiles_sorted.back().x + kTP));
-            g_t0 = (int)tiles_sorted.size();
-            g_p0 = t.x;
+    size_t k = 0;
+    while (k < order.size()) {
+        const int blk = tl[order[k]].x / pblk;
+        size_t e = k;
+        while (e < order.size() && tl[order[e]].x / pblk == blk) e++;
+        for (size_t g0 = k; g0 < e; g0 += kGroupThreads) {
+            const size_t g1 = std::min(e, g0 + (size_t)kGroupThreads);
+            int pmin = 1 << 30, pmax = 0;
+            for (size_t u = g0; u < g1; u++) {
+                pmin = std::min(pmin, tl[order[u]].x);
+                pmax = std::max(pmax, tl[order[u]].x + kTP);
+            }
+            const int t0 = (int)tiles_sorted.size();
+            for (size_t u = g0; u < g1; u++) {
+                int4 t = tl[order[u]];
+                const int ns = (int)tiles_sorted.size();
+                stab_sorted.insert(stab_sorted.end(), stab.begin() + (size_t)t.w,
+                                   stab.begin() + (size_t)t.w + kTP * kTQ);
+                t.z = (int)gl.size();
+                t.w = ns * kTP * kTQ;
+                tiles_sorted.push_back(t);
+            }
+            gl.push_back(make_int4(t0, (int)tiles_sorted.size(), pmin, pmax));
         }
-        int ns = (int)tiles_sorted.size();
-        stab_sorted.insert(stab_sorted.end(), stab.begin() + (size_t)t.w, stab.begin() + (size_t)t.w + kTP * kTQ);
-        t.z = (int)gl.size();
-        t.w = ns * kTP * kTQ;
-        tiles_sorted.push_back(t);
+        k = e;
     }
-    if ((int)tiles_sorted.size() > g_t0)
-        gl.push_back(make_int4(g_t0, (int)tiles_sorted.size(), g_p0, tiles_sorted.back().x + kTP));
     ntiles = (int)tiles_sorted.size();
     ngroups = (int)gl.size();
     max_group_pairs = 0;
@@ -297,14 +309,24 @@ template int build_indicator_spectra<float>(const Shells &, int, int, float2 *, 
 template int build_indicator_spectra<double>(const Shells &, int, int, double2 *, cudaStream_t, int64_t *);
 
 // ------------------------------------------------------ triangle sums ---
-// four consecutive values from 16-byte-aligned shared memory
-__device__ __forceinline__ void load4(const float *p, float v[4]) {
+// CUDA-core form (FP32 plain / FP64).  Each CTA owns a group of register
+// tiles (kTP pairs x kTQ q maps per thread) and a contiguous range of the
+// contraction (grid points).  Per chunk of kc points inside one grid row the
+// CTA stages the q maps and the pair-source maps in shared memory (k
+// contiguous), forms the pair products, then every thread runs its tile.
+// FP32 chunk sums are folded into Kahan-compensated running sums.
+template <class T> struct VecOf;
+template <> struct VecOf<float> { static constexpr int W = 4; using V = float4; using V2 = float2; };
+template <> struct VecOf<double> { static constexpr int W = 2; using V = double2; using V2 = double2; };
+
+template <class T> __device__ __forceinline__ void vload(const T *p, T v[VecOf<T>::W]);
+template <> __device__ __forceinline__ void vload<float>(const float *p, float v[4]) {
     const float4 a = *reinterpret_cast<const float4 *>(p);
     v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
 }
-__device__ __forceinline__ void load4(const double *p, double v[4]) {
-    const double2 a = *reinterpret_cast<const double2 *>(p), b = *reinterpret_cast<const double2 *>(p + 2);
-    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+template <> __device__ __forceinline__ void vload<double>(const double *p, double v[2]) {
+    const double2 a = *reinterpret_cast<const double2 *>(p);
+    v[0] = a.x; v[1] = a.y;
 }
 
 // Accumulation of one chunk into the running sum: Kahan-compensated for FP32.
@@ -322,27 +344,33 @@ template <> struct Runner<double> {
     __device__ __forceinline__ void add(double v) { sum += v; }
 };
 
+constexpr int kKCmax = 64;
+
+// Shared layout (k-major, the tile index contiguous): sQ[k][q], sP[k][p], so a
+// warp whose threads share one q tile reads it by broadcast and reads its
+// consecutive pair tiles as one contiguous 512-byte row segment.
 template <class T>
 __global__ void __launch_bounds__(kGroupThreads) trisum_kernel(
-    int N, const T *__restrict__ maps, size_t mstride, int rs, int nb, int nq, int qpad, const int *__restrict__ qmap,
+    int N, int kc, const T *__restrict__ maps, size_t mstride, int rs, int nb, int nq, const int *__restrict__ qmap,
     const int2 *__restrict__ pairs, const int4 *__restrict__ tiles, const int4 *__restrict__ groups,
-    const int *__restrict__ slots, int ngroups, int ksplit, long long K, int nslots, int gpad,
-    double *__restrict__ partial) {
+    const int *__restrict__ slots, int ngroups, int ksplit, long long K, int nslots, double *__restrict__ partial,
+    int qrow, int prow) {
+    using V2 = typename VecOf<T>::V2;
+    constexpr int ARS = kKCmax + (sizeof(T) == 4 ? 4 : 2);  // sA row stride (k contiguous)
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *sQ = reinterpret_cast<T *>(smem_raw);                 // [kKC][qpad]
-    T *sA = sQ + (size_t)kKC * qpad;                         // [nb][kKC]   set-0 maps (pair sources)
-    T *sP = sA + (size_t)nb * kKC;                           // [kKC][gpad] pair products of this group
     const int g = blockIdx.x % ngroups, split = blockIdx.x / ngroups;
     const int4 G = groups[g];
     const int ntile = G.y - G.x, p0g = G.z, npg = G.w - G.z;
+    T *sQ = reinterpret_cast<T *>(smem_raw);  // [kKCmax][qrow]
+    T *sP = sQ + (size_t)kKCmax * qrow;       // [kKCmax][prow]
+    T *sA = sP + (size_t)kKCmax * prow;       // [nb][ARS]
     const int my = threadIdx.x;
     int4 tile = make_int4(0, 0, 0, 0);
     if (my < ntile) tile = tiles[G.x + my];
     const int tp = tile.x - p0g, tq = tile.y;
 
-    long long kb = (K * split) / ksplit, ke = (K * (split + 1)) / ksplit;
-    kb = kb / kKC * kKC;
-    if (split + 1 < ksplit) ke = ke / kKC * kKC;
+    const long long nchunks = K / kc;
+    const long long cb = nchunks * split / ksplit, ce = nchunks * (split + 1) / ksplit;
 
     T acc[kTP][kTQ];
     Runner<T> run[kTP][kTQ];
@@ -351,36 +379,38 @@ __global__ void __launch_bounds__(kGroupThreads) trisum_kernel(
 #pragma unroll
         for (int b = 0; b < kTQ; b++) acc[a][b] = 0;
 
-    for (long long k0 = kb; k0 < ke; k0 += kKC) {
-        // stage q maps (transposed) and pair-source maps
-        for (int idx = threadIdx.x; idx < nq * kKC; idx += blockDim.x) {
-            const int q = idx / kKC, kk = idx % kKC;
-            const long long p = k0 + kk;
-            T v = 0;
-            if (p < ke) v = maps[(size_t)qmap[q] * mstride + (size_t)(p / N) * rs + (size_t)(p % N)];
-            sQ[(size_t)kk * qpad + q] = v;
-        }
-        for (int idx = threadIdx.x; idx < nb * kKC; idx += blockDim.x) {
-            const int a = idx / kKC, kk = idx % kKC;
-            const long long p = k0 + kk;
-            T v = 0;
-            if (p < ke) v = maps[(size_t)a * mstride + (size_t)(p / N) * rs + (size_t)(p % N)];
-            sA[idx] = v;
+    const int hv = kc / 2;  // vec2 loads per staged row
+    for (long long ch = cb; ch < ce; ch++) {
+        const long long k0 = ch * kc;
+        const size_t goff = (size_t)(k0 / N) * rs + (size_t)(k0 % N);
+        for (int idx = threadIdx.x; idx < (nq + nb) * hv; idx += blockDim.x) {
+            const int m = idx / hv, c = idx - m * hv;
+            const int map = m < nq ? qmap[m] : m - nq;
+            const V2 v = *reinterpret_cast<const V2 *>(maps + (size_t)map * mstride + goff + 2 * c);
+            if (m < nq) {
+                sQ[(size_t)(2 * c) * qrow + m] = v.x;
+                sQ[(size_t)(2 * c + 1) * qrow + m] = v.y;
+            } else {
+                T *dst = sA + (size_t)(m - nq) * ARS + 2 * c;
+                dst[0] = v.x;
+                dst[1] = v.y;
+            }
         }
         __syncthreads();
-        for (int idx = threadIdx.x; idx < npg * kKC; idx += blockDim.x) {
-            const int pp = idx / kKC, kk = idx % kKC;
+        for (int idx = threadIdx.x; idx < npg * kc; idx += blockDim.x) {
+            const int pp = idx % npg, k = idx / npg;
             const int2 pr = pairs[p0g + pp];
-            sP[(size_t)kk * gpad + pp] = sA[pr.x * kKC + kk] * sA[pr.y * kKC + kk];
+            sP[(size_t)k * prow + pp] = sA[(size_t)pr.x * ARS + k] * sA[(size_t)pr.y * ARS + k];
         }
         __syncthreads();
         if (my < ntile) {
 #pragma unroll 4
-            for (int kk = 0; kk < kKC; kk++) {
-                T av[4], qv[8];
-                load4(sP + (size_t)kk * gpad + tp, av);
-                load4(sQ + (size_t)kk * qpad + tq, qv);
-                load4(sQ + (size_t)kk * qpad + tq + 4, qv + 4);
+            for (int kk = 0; kk < kc; kk++) {
+                T av[kTP], qv[kTQ];
+                vload<T>(sP + (size_t)kk * prow + tp, av);
+                if (VecOf<T>::W == 2) vload<T>(sP + (size_t)kk * prow + tp + 2, av + 2);
+#pragma unroll
+                for (int b = 0; b < kTQ; b += VecOf<T>::W) vload<T>(sQ + (size_t)kk * qrow + tq + b, qv + b);
 #pragma unroll
                 for (int a = 0; a < kTP; a++)
 #pragma unroll
@@ -422,19 +452,25 @@ int triangle_sums(const Shells &sh, const TriPlan &tp, const T *maps, size_t mst
                   double *S, cudaStream_t st, int64_t *launches) {
     const int N = sh.N;
     const long long K = (long long)N * N * N;
-    const int qpad = ((tp.nq + kTQ - 1) / kTQ) * kTQ + 4;        // +4: fewer bank conflicts on transposed stores
-    const int gpad = ((tp.max_group_pairs + kTP - 1) / kTP) * kTP + 4;
-    const size_t smem = sizeof(T) * ((size_t)kKC * qpad + (size_t)sh.nb * kKC + (size_t)kKC * gpad);
+    int kc = kKCmax;
+    while (kc > 4 && N % kc) kc /= 2;  // chunk inside one grid row
+    if (N % kc || (rs & 1) || (mstride & 1))
+        return set_error(PBI4G_ERR_UNSUPPORTED, "triangle sums: grid %d has no even chunk width", N);
+    const int qpad = ((tp.nq + kTQ - 1) / kTQ) * kTQ;  // q tiles read up to 8 columns per tile
+    const int gpad = ((tp.max_group_pairs + kTP - 1) / kTP) * kTP;
+    const int qrow = qpad + 4, prow = gpad + 4;          // 16-B aligned rows, staggered banks
+    const int ARS = kKCmax + (sizeof(T) == 4 ? 4 : 2);
+    const size_t smem = sizeof(T) * ((size_t)kKCmax * (qrow + prow) + (size_t)sh.nb * ARS);
     if (smem > 220 * 1024) return set_error(PBI4G_ERR_UNSUPPORTED, "triangle sums: %zu B shared memory", smem);
-    const int target = 152 * 3;
+    const int target = 152 * 2;
     int ksplit = std::max(1, target / std::max(1, tp.ngroups));
-    ksplit = (int)std::min<long long>(ksplit, std::max<long long>(1, K / (kKC * 16)));
+    ksplit = (int)std::min<long long>(ksplit, std::max<long long>(1, K / kc / 8));
     PBI4G_CHECK(partial.ensure(sizeof(double) * (size_t)ksplit * tp.nslots));
     auto kern = trisum_kernel<T>;
     PBI4G_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kern<<<tp.ngroups * ksplit, kGroupThreads, smem, st>>>(
-        N, maps, mstride, rs, sh.nb, tp.nq, qpad, tp.qmap.as<int>(), tp.pairs.as<int2>(), tp.tiles.as<int4>(),
-        tp.groups.as<int4>(), tp.slots.as<int>(), tp.ngroups, ksplit, K, tp.nslots, gpad, partial.as<double>());
+        N, kc, maps, mstride, rs, sh.nb, qpad, tp.qmap.as<int>(), tp.pairs.as<int2>(), tp.tiles.as<int4>(),
+        tp.groups.as<int4>(), tp.slots.as<int>(), tp.ngroups, ksplit, K, tp.nslots, partial.as<double>(), qrow, prow);
     PBI4G_LAUNCH_CHECK();
     reduce_partial_kernel<<<(tp.nslots + 255) / 256, 256, 0, st>>>(tp.nslots, ksplit, partial.as<double>(), S);
     PBI4G_LAUNCH_CHECK();
@@ -516,7 +552,7 @@ int triangle_counts(Shells &sh, cudaStream_t st, int64_t *launches) {
     // all three factors are indicator maps of the same set (also for the cross
     // enumeration, bispectrumI4.f90:887-896), so the non-cross pair layout applies
     TriPlan tp;
-    PBI4G_CHECK(tp.build(sh, 1, 0));
+    PBI4G_CHECK(tp.build(sh, 1, 0, 128));
     PBI4G_CHECK(S.ensure(sizeof(double) * tp.nslots));
     PBI4G_CHECK(triangle_sums<double>(sh, tp, maps.as<double>(), 2 * HC, 2 * NH, partial, S.as<double>(), st, launches));
     std::vector<double> Sh(tp.nslots);

@@ -42,7 +42,7 @@ struct TriPlan {
     DevBuf groups;       // int4 [ngroups]: (tile0, tile1, pair0, pair1)
     std::vector<int> group_tiles;
     int ntiles = 0, max_group_pairs = 0;
-    int build(const Shells &sh, int nsets, int cross);
+    int build(const Shells &sh, int nsets, int cross, int max_pairs = 256);
 };
 
 // Build the half spectra of maps [m0, m0+count) into `out` (count x N*N*(N/2+1)

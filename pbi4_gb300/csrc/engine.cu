@@ -76,10 +76,11 @@ int BkEngine::run(const typename Cx<R>::T *const src[3], const int fac[3], const
     const size_t HC = half_cells(N);
     const int nm = nmaps();
     const bool fp64 = sizeof(R) == 8;
-    if (tp_nsets != nsets || tp_cross != cross) {
-        PBI4G_CHECK(tp.build(sh, cross ? 1 : nsets, cross));
+    if (tp_nsets != nsets || tp_cross != cross || tp_fp64 != (int)fp64) {
+        PBI4G_CHECK(tp.build(sh, cross ? 1 : nsets, cross, fp64 ? 128 : 256));
         tp_nsets = nsets;
         tp_cross = cross;
+        tp_fp64 = fp64;
     }
     PBI4G_CHECK(maps.ensure(sizeof(C) * HC * nm));
     PBI4G_CHECK(powsum.ensure(sizeof(double) * nb));

@@ -22,7 +22,7 @@ struct Prof {
 struct BkEngine {
     Shells sh;
     TriPlan tp;
-    int tp_nsets = -1, tp_cross = -1;
+    int tp_nsets = -1, tp_cross = -1, tp_fp64 = -1;
     int nsets = 1, cross = 0;  // cross: 1 => q maps from the second field
     DevBuf maps;               // [nmaps][N][N][N/2+1] complex = padded real maps after C2R
     cufftHandle inv = 0;

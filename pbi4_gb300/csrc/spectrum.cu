@@ -380,18 +380,27 @@ __global__ void pk_accum_kernel(int N, int nbins, const int *__restrict__ lut, P
     for (int i = threadIdx.x; i < 3 * nbins; i += blockDim.x) out[i] = i < nq * nbins ? (double)s[i] : 0.0;
 }
 
-// Deterministic reduction over blocks + the output rows of measure_pk /
-// measure_pk_multipoles (pout Fortran (5, nbins)).
+// Deterministic reduction over blocks (one warp per bin, fixed lane order and
+// shuffle tree) + the output rows of measure_pk / measure_pk_multipoles
+// (pout Fortran (5, nbins)).
 __global__ void pk_finalize_kernel(int nbins, int blocks, int mode, double kF3, const double *__restrict__ partial,
                                    const double *__restrict__ avgk_co, double *__restrict__ pout) {
-    for (int bi = blockIdx.x * blockDim.x + threadIdx.x; bi < nbins; bi += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int bi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; bi < nbins; bi += warps) {
         double s0 = 0, s2 = 0, s4 = 0;
-        for (int k = 0; k < blocks; k++) {
+        for (int k = lane; k < blocks; k += 32) {
             const double *p = partial + (size_t)k * 3 * nbins;
             s0 += p[bi];
             s2 += p[nbins + bi];
             s4 += p[2 * nbins + bi];
         }
+        for (int o = 16; o; o >>= 1) {
+            s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+            s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+            s4 += __shfl_xor_sync(0xffffffffu, s4, o);
+        }
+        if (lane) continue;
         const double co = avgk_co[nbins + bi], avgk = avgk_co[bi];
         double *o = pout + 5 * (size_t)bi;
         o[0] = avgk / co;
@@ -433,7 +442,7 @@ int pk_measure(PkBins &bins, int mode, const double los[3], const typename Cx<R>
         k<<<blocks, 256, smem, st>>>(N, nbins, bins.lut.as<int>(), e, l0, l1, l2, a, b, c, bins.partial.as<double>());
     }
     PBI4G_LAUNCH_CHECK();
-    pk_finalize_kernel<<<(nbins + 127) / 128, 128, 0, st>>>(nbins, blocks, mode == 0 ? 0 : 1, bins.kF3,
+    pk_finalize_kernel<<<(nbins * 32 + 255) / 256, 256, 0, st>>>(nbins, blocks, mode == 0 ? 0 : 1, bins.kF3,
                                                             bins.partial.as<double>(), bins.avgk_co.as<double>(),
                                                             d_pout);
     PBI4G_LAUNCH_CHECK();

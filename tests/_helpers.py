@@ -35,8 +35,10 @@ def p_errors(pout, ref, multipoles):
 
 
 def b_errors(bout, ref, rows=(6, 9, 10)):
-    """Per-triangle error of B_l: |dB| / max(|B_ref|, P1 P2 + P1 P3 + P2 P3), i.e. relative
-    error of B, or the error of the reduced bispectrum Q where B itself is near zero.
+    """Per-triangle error of B_l: |dB| / max(|B_ref|, (2l+1)(P1 P2 + P1 P3 + P2 P3)), i.e. the
+    relative error of B, or, where B itself is near zero, the error of the reduced
+    bispectrum Q = B / (P1 P2 + P1 P3 + P2 P3) (with the (2l+1) prefactor that
+    measure_bk_multipoles puts on B2 and B4, bispectrumI4.f90:499-500).
     Also returns the plain relative error of the powers of the shells."""
     P1, P2, P3 = ref[3], ref[4], ref[5]
     den = np.abs(P1 * P2) + np.abs(P1 * P3) + np.abs(P2 * P3)
@@ -44,6 +46,7 @@ def b_errors(bout, ref, rows=(6, 9, 10)):
     for r in rows:
         if r >= ref.shape[0]:
             continue
-        out.append(np.max(np.abs(bout[r] - ref[r]) / np.maximum(np.abs(ref[r]), den)))
+        ell_fac = {6: 1.0, 9: 5.0, 10: 9.0}[r]
+        out.append(np.max(np.abs(bout[r] - ref[r]) / np.maximum(np.abs(ref[r]), ell_fac * den)))
     pw = np.max(np.abs(bout[3:6] / ref[3:6] - 1))
     return out, pw

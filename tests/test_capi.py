@@ -1,0 +1,67 @@
+"""The C-ABI library: builds, loads without a GPU, exports every declared entry
+point, and its config struct has the layout the Python binding assumes."""
+import ctypes
+import os
+import re
+import subprocess
+import tempfile
+
+import pytest
+
+from pbi4_gb300 import _lib, build
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "pbi4gpu.h")
+
+
+def declared():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(pbi4g_[a-z0-9_]+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return _lib.lib()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = declared()
+    assert len(names) >= 30
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(names) == set(_lib.EXPORTS)
+
+
+def test_no_other_symbols_exported():
+    out = subprocess.run(["nm", "-D", "--defined-only", build.LIB], capture_output=True, text=True).stdout
+    funcs = {l.split()[-1] for l in out.splitlines() if " T " in l}
+    ours = {f for f in funcs if f.startswith("pbi4g_")}
+    assert ours == set(declared())
+
+
+def test_config_struct_layout(tmp_path):
+    c = tmp_path / "t.c"
+    c.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "pbi4gpu.h"\n'
+                 'int main(void){printf("%zu %zu %zu %zu\\n", sizeof(pbi4g_config), offsetof(pbi4g_config, los),'
+                 ' offsetof(pbi4g_config, precision), offsetof(pbi4g_config, reserved));return 0;}\n')
+    exe = tmp_path / "t"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(c), "-o", str(exe)], check=True)
+    got = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    C = _lib.Config
+    want = [ctypes.sizeof(C), C.los.offset, C.precision.offset, C.reserved.offset]
+    assert [int(x) for x in got] == want
+
+
+def test_errors_without_device(lib):
+    """Argument validation happens before any device work, so it answers on a CPU-only host."""
+    cfg = _lib.Config()
+    cfg.grid = 7  # odd grid: rejected
+    out = ctypes.c_int64()
+    rc = lib.pbi4g_plan_footprint(ctypes.byref(cfg), 10, ctypes.byref(out))
+    assert rc == 1
+    assert b"grid" in lib.pbi4g_last_error()
+    cfg.grid, cfg.box, cfg.nintp, cfg.nbins_ps, cfg.kbin_ps = 256, 1000.0, 4, 128, 1.0
+    assert lib.pbi4g_plan_footprint(ctypes.byref(cfg), 2 ** 21, ctypes.byref(out)) == 0
+    assert out.value > 256 ** 3 * 8

@@ -58,8 +58,8 @@ def test_assign_bit_reproducible_under_permutation(box_uniform):
     perm = np.random.default_rng(1).permutation(pos.shape[1])
     b = P.assign_double_grid(32, 4, pos.shape[1], np.ascontiguousarray(pos[:, perm]), w)
     c = P.assign_double_grid(32, 4, pos.shape[1], pos, w)
-    assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
-    assert np.array_equal(a.view(np.uint64), c.view(np.uint64))
+    assert a.tobytes() == b.tobytes()
+    assert a.tobytes() == c.tobytes()
 
 
 def test_assign_edge_positions():
