@@ -82,6 +82,24 @@ int pbi4g_measure_pk(int32_t grid, float box, float kbin, float kcenter, int32_t
 int pbi4g_measure_pk_multipoles(int32_t grid, float box, float kbin, float kcenter, int32_t nbins,
                                 const double *dcl, const double *dcl2, const double *dcl4, double *pout);
 
+/* P(k) multipoles like pbi4g_measure_pk_multipoles, but for callers that may
+ * not allocate device memory: applications that hand all device memory out
+ * through their own pool, or pipelines that forbid allocation after start-up.
+ * It has no counterpart in the reference.  Inputs are device arrays: the kx >= 0
+ * halves of dcl, dcl2, dcl4 as complex128 (N, N, N/2+1), C order [z][y][x]
+ * (x = ix-1 fastest); d_pout is a device (5, nbins) float64 array, Fortran
+ * order.  Work is queued on `stream` (a cudaStream_t, NULL = legacy default);
+ * the call returns without synchronising.  No cudaMalloc/cudaFree: its scratch
+ * is a fixed 4.3 MiB device array inside the library, held by every device that
+ * loads the library until exit, sized for grid <= 512 and nbins <= 512; larger
+ * sizes return PBI4G_ERR_RANGE.  The first call on a device looks up the
+ * array's device address; make that first call before any stream capture.
+ * All calls share the one array: calls that overlap on the GPU (other streams,
+ * other host threads) race and must be serialised by the caller. */
+int pbi4g_measure_pk_multipoles_noalloc(int32_t grid, float box, float kbin, float kcenter, int32_t nbins,
+                                        const void *d_dcl_half, const void *d_dcl2_half, const void *d_dcl4_half,
+                                        double *d_pout, void *stream);
+
 /* ---------------- 1. f2py drop-ins: bispectrumI4 ---------------- */
 
 /* replaces bispectrumI4.f90:763-915 count_triangles; counts: itot float64

@@ -14,6 +14,7 @@
 
 #include <float.h>
 #include <math.h>
+#include <mutex>
 #include <vector>
 
 namespace pbi4g {
@@ -524,4 +525,102 @@ int reduce_full(int L, const double2 *din, int N, double2 *dout, cudaStream_t st
     return PBI4G_OK;
 }
 
+
+// ------------------------------------------- allocation-free P(k) variant ---
+// Scratch of pbi4g_measure_pk_multipoles_noalloc lives in this file-scope
+// device array instead of device allocations: the |k|^2 -> bin table, the
+// per-bin mode counts and |k| sums, and the per-block partial sums.
+constexpr int kNoAllocMaxGrid = 512;
+constexpr int kNoAllocMaxBins = 512;
+constexpr int kNoAllocBlocks = 304;
+constexpr size_t kNoAllocLutBytes =
+    ((sizeof(int) * (3 * (kNoAllocMaxGrid / 2) * (kNoAllocMaxGrid / 2) + 1) + 255) / 256) * 256;
+constexpr size_t kNoAllocBinBytes = 24 * kNoAllocMaxBins;  // sum|k|, count (double), count (uint64)
+constexpr size_t kNoAllocPartialBytes = sizeof(double) * 3 * kNoAllocMaxBins * kNoAllocBlocks;
+constexpr size_t kNoAllocScratchBytes = kNoAllocLutBytes + kNoAllocBinBytes + kNoAllocPartialBytes;  // 4.3 MiB
+
+static __device__ __align__(256) unsigned char g_pk_noalloc_scratch[kNoAllocScratchBytes];
+
+// The host-side name of g_pk_noalloc_scratch is not a device address; its
+// device address is looked up once per device with that device current.
+static std::mutex g_noalloc_mutex;
+static void *g_noalloc_ptr[128];
+
+static int noalloc_scratch(void **out) {
+    int dev = -1;
+    PBI4G_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 128) return set_error(PBI4G_ERR_UNSUPPORTED, "device index %d out of range", dev);
+    std::lock_guard<std::mutex> g(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_pk_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return set_error(PBI4G_ERR_CUDA, "cudaGetSymbolAddress(scratch) failed: %s", cudaGetErrorString(e));
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return PBI4G_OK;
+}
+
+// |k|^2 -> P bin table on the device (same rule as PkBins::build on the host).
+__global__ void pk_lut_kernel(int k2max, double kbin, double kck, int nbins, int *__restrict__ lut) {
+    for (int k2 = blockIdx.x * blockDim.x + threadIdx.x; k2 <= k2max; k2 += gridDim.x * blockDim.x) {
+        const double t = sqrt((double)k2) / kbin - kck;
+        const double f = t - floor(t);
+        int b;
+        if (fabs(f - 0.5) < 1e-7) {
+            b = -1;
+        } else {
+            const long long bb = llround(t) + 1;
+            b = (bb >= 1 && bb <= nbins) ? (int)bb : 0;
+        }
+        lut[k2] = b;
+    }
+}
+
 }  // namespace pbi4g
+
+extern "C" int pbi4g_measure_pk_multipoles_noalloc(int32_t grid, float box, float kbin, float kcenter, int32_t nbins,
+                                                   const void *d_dcl_half, const void *d_dcl2_half,
+                                                   const void *d_dcl4_half, double *d_pout, void *stream) {
+    using namespace pbi4g;
+    if (grid < 4 || (grid & 1)) return set_error(PBI4G_ERR_INVALID, "noalloc P(k): grid must be even and >= 4");
+    if (grid > kNoAllocMaxGrid)
+        return set_error(PBI4G_ERR_RANGE, "noalloc P(k): grid %d exceeds the scratch limit of %d", grid,
+                         kNoAllocMaxGrid);
+    if (nbins < 1 || nbins > kNoAllocMaxBins)
+        return set_error(PBI4G_ERR_RANGE, "noalloc P(k): nbins %d outside 1..%d (scratch limit)", nbins,
+                         kNoAllocMaxBins);
+    if (!(kbin > 0) || !(box > 0)) return set_error(PBI4G_ERR_INVALID, "noalloc P(k): kbin and box must be > 0");
+    if (!d_dcl_half || !d_dcl2_half || !d_dcl4_half || !d_pout)
+        return set_error(PBI4G_ERR_INVALID, "noalloc P(k): null device pointer");
+    void *scratch = nullptr;
+    PBI4G_CHECK(noalloc_scratch(&scratch));
+    cudaStream_t st = (cudaStream_t)stream;
+    unsigned char *base = static_cast<unsigned char *>(scratch);
+    int *lut = reinterpret_cast<int *>(base);
+    double *sumk = reinterpret_cast<double *>(base + kNoAllocLutBytes);  // [2][nbins]: sum|k|, count
+    unsigned long long *co = reinterpret_cast<unsigned long long *>(sumk + 2 * nbins);
+    double *partial = reinterpret_cast<double *>(base + kNoAllocLutBytes + kNoAllocBinBytes);
+    const int k2max = 3 * (grid / 2) * (grid / 2);
+    const double kF = (double)(kTwoPiF / box);
+    PkExact e{kF, (double)kbin * kF, (double)(kcenter / kbin)};
+    // the array keeps the previous call's contents: clear the accumulators
+    PBI4G_CUDA(cudaMemsetAsync(sumk, 0, kNoAllocBinBytes, st));
+    pk_lut_kernel<<<grid_blocks((size_t)k2max + 1, 256, 152 * 4), 256, 0, st>>>(k2max, (double)kbin, e.kck, nbins,
+                                                                                 lut);
+    PBI4G_LAUNCH_CHECK();
+    pk_bins_kernel<<<grid_blocks(half_cells(grid), 256), 256, 0, st>>>(grid, nbins, e, co, sumk);
+    PBI4G_LAUNCH_CHECK();
+    pk_bins_finish_kernel<<<1, 256, 0, st>>>(nbins, co, sumk);
+    PBI4G_LAUNCH_CHECK();
+    const size_t smem = sizeof(double) * 3 * nbins;
+    pk_accum_kernel<double, 2><<<kNoAllocBlocks, 256, smem, st>>>(
+        grid, nbins, lut, e, 0.0, 0.0, 0.0, static_cast<const double2 *>(d_dcl_half),
+        static_cast<const double2 *>(d_dcl2_half), static_cast<const double2 *>(d_dcl4_half), partial);
+    PBI4G_LAUNCH_CHECK();
+    pk_finalize_kernel<<<(nbins * 32 + 255) / 256, 256, 0, st>>>(nbins, kNoAllocBlocks, 1, kF * kF * kF, partial,
+                                                                 sumk, d_pout);
+    PBI4G_LAUNCH_CHECK();
+    return PBI4G_OK;
+}
