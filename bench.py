@@ -178,57 +178,66 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------ GPU arm ---
+DTYPE = {"fp32": "f32", "fp64": "f64", "fp16split": "fp16 hi+lo (f32 accumulate)", "bf16": "bf16 (f32 accumulate)"}
+
+
+def error_report(pout, bout, p64, b64):
+    """Max per-bin error against the FP64 GPU form: P_l relative to P0, B_l relative to
+    max(|B_l|, (2l+1)(P1P2+P1P3+P2P3)); Nmodes and N_tr must be identical."""
+    ok = p64[4] > 0
+    e = {"P0": float(np.max(np.abs(pout[1][ok] / p64[1][ok] - 1))),
+         "P2": float(np.max(np.abs(pout[2][ok] - p64[2][ok]) / np.abs(p64[1][ok]))),
+         "P4": float(np.max(np.abs(pout[3][ok] - p64[3][ok]) / np.abs(p64[1][ok]))),
+         "Nmodes_equal": bool(np.array_equal(pout[4], p64[4]))}
+    den = np.abs(b64[3] * b64[4]) + np.abs(b64[3] * b64[5]) + np.abs(b64[4] * b64[5])
+    for name, r, f in (("B0", 6, 1.0), ("B2", 9, 5.0), ("B4", 10, 9.0)):
+        e[name] = float(np.max(np.abs(bout[r] - b64[r]) / np.maximum(np.abs(b64[r]), f * den)))
+    e["B0_plain_relative_median"] = float(np.median(np.abs(bout[6] / b64[6] - 1)))
+    e["Ntr_equal"] = bool(np.array_equal(bout[8], b64[8]))
+    return e
 def run_ours(args):
     import torch
     import torch.distributed as dist
 
+    from pbi4_gb300 import replicas
     from pbi4_gb300.estimator import Estimator
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
-    else:
-        torch.cuda.set_device(0)
-
-    def barrier():
-        if world > 1:
-            dist.barrier()
+    # N GPUs: independent replicas, each rank runs whole boxes; no data-path collective
+    world, rank, local = replicas.init("nccl")
+    barrier = replicas.barrier
 
     pos = make_positions(quick=args.quick, small=args.small)
     npart = pos.shape[1]
-    cfg = est_config(args.precision, grid=64 if args.quick else (128 if args.small else None))
+    grid = 64 if args.quick else (128 if args.small else None)
+    cfg = est_config(args.precision, grid=grid)
     est = Estimator(cfg)
     dpos = torch.from_numpy(pos).cuda()
     pout, bout = est.alloc_outputs()
-    # warm-up: plan tables, triangle counts, cuFFT plans
-    for _ in range(args.warmup):
-        est.run_device(npart, dpos, pout, bout)
-    torch.cuda.synchronize()
-    est.enable_timing(True)
-    est.stage_times()
-    launches0 = est.launches
-    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
-        start.record()
-        for _ in range(args.steps):
-            est.run_device(npart, dpos, pout, bout)
-        stop.record()
+
+    def timed(e, po, bo, steps, clocks=False):
+        """Device time of `steps` boxes on plan e (CUDA events on the plan's stream = torch's current)."""
+        for _ in range(args.warmup):  # plan tables, triangle counts, cuFFT plans
+            e.run_device(npart, dpos, po, bo)
         torch.cuda.synchronize()
-    barrier()
-    ms = start.elapsed_time(stop)
-    launches = est.launches - launches0
-    stages = est.stage_times()
-    est.enable_timing(False)
-    t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t.item())
-    value = world * args.steps / (ms_max / 1e3)
+        e.enable_timing(True)
+        e.stage_times()
+        l0 = e.launches
+        start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        torch.cuda.synchronize()
+        with ClockSampler(local) as clk:
+            start.record()
+            for _ in range(steps):
+                e.run_device(npart, dpos, po, bo)
+            stop.record()
+            torch.cuda.synchronize()
+        barrier()
+        st = e.stage_times()
+        e.enable_timing(False)
+        return replicas.max_over_ranks(start.elapsed_time(stop)), e.launches - l0, st, clk.summary()
+
+    ms_max, launches, stages, clocks = timed(est, pout, bout, args.steps)
+    value = replicas.throughput(world * args.steps, ms_max / 1e3)
 
     # e2e: host (pinned) positions in, host results out, through the C-ABI call
     hpos = torch.from_numpy(pos).pin_memory().numpy()
@@ -239,16 +248,44 @@ def run_ours(args):
     e2e_steps = max(2, args.steps // 2)
     for _ in range(e2e_steps):
         p_h, b_h = est.run_host(hpos)
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
-    te = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-    if world > 1:
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
-    e2e_value = world / float(te.item())
+    e2e_s = replicas.max_over_ranks(time.perf_counter() - t0)
+    e2e_value = replicas.throughput(world * e2e_steps, e2e_s)
 
-    # roofline of the dominant kernel stage
+    # the plain FP32 GPU form on the same box, and the FP64 GPU form as the error reference
+    plain = errors = None
+    if not args.no_compare and rank == 0:
+        if args.precision != "fp32":
+            e32 = Estimator(est_config("fp32", grid=grid))
+            po32, bo32 = e32.alloc_outputs()
+            ms32, _, _, _ = timed(e32, po32, bo32, max(3, args.steps // 4))
+            plain = {"value": max(3, args.steps // 4) / (ms32 / 1e3), "unit": "boxes/s",
+                     "ms_per_step": ms32 / max(3, args.steps // 4)}
+            p32, b32 = e32.run_host(pos)
+            e32.close()
+        e64 = Estimator(est_config("fp64", grid=grid))
+        p64, b64 = e64.run_host(pos)
+        e64.close()
+        errors = error_report(p_h, b_h, p64, b64)
+        if plain is not None:
+            plain["error_vs_fp64"] = error_report(p32, b32, p64, b64)
+
+    # serving: a short Poisson stream of mixed boxes through the continuous-batching loop
+    serving = None
+    if args.serve_requests > 0 and rank == 0 and not args.quick and not args.small:
+        from pbi4_gb300 import serve_workload
+        reqs = serve_workload.make_stream(n_requests=args.serve_requests, grids=(128, 192, 256), npart_min=1e5,
+                                          npart_max=2e6, rate_hz=args.serve_rate, precision=args.precision)
+        st = serve_workload.run_stream(reqs, hbm_budget_gb=120.0, slots=4)
+        serial = serve_workload.run_serial_plain(reqs)
+        serving = {"requests": st["n"], "p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
+                   "boxes_per_s": round(st["boxes_per_s"], 2), "offered_rate_hz": args.serve_rate,
+                   "serial_plain_fp32_boxes_per_s": round(serial["boxes_per_s"], 2),
+                   "workload": "Poisson arrivals; grid in {128,192,256}; npart log-uniform [1e5, 2e6]; uniform or "
+                               "Zel'dovich positions; CIC/TSC/PCS; interlacing on/off; P-only or P+B "
+                               "(dk=2kf to 0.5 kNyq); cold plan creation included"}
+
     from pbi4_gb300 import roofline
-    rl = roofline.for_stages(stages, args.steps, cfg, npart)
-    clocks = clk.summary()
+    rl = roofline.for_stages(stages, args.steps, cfg, npart, itot=est.itot)
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
@@ -256,7 +293,7 @@ def run_ours(args):
             cpu = {"value": 1.0 / sec, "unit": "boxes/s", "cores": cores, "kind": "port", "sample": sample}
         line = {"metric": METRIC, "value": value, "unit": "boxes/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else args.precision,
+                "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[args.precision],
                 "data": "synthetic (seeded Zel'dovich box, positions resident in HBM)",
                 "config": {**WORKLOAD, "precision": args.precision, "parallelism": f"replicas{world}",
                            "l2": "working set > L2 (shell maps %.1f GB per box)" % (
@@ -265,6 +302,7 @@ def run_ours(args):
                 "e2e": {"value": e2e_value, "unit": "boxes/s", "h2d_bytes_per_step": int(pos.nbytes),
                         "d2h_bytes_per_step": int(p_h.nbytes + b_h.nbytes)},
                 "gpu_launches": int(launches), "clocks": clocks, "roofline": rl, "cpu_baseline": cpu,
+                "plain_fp32": plain, "error_vs_fp64": errors, "serving": serving,
                 "stages_ms_per_box": {k: round(v[0] / max(1, args.steps), 4) for k, v in stages.items()}}
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -277,7 +315,10 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "fp16split", "bf16"])
+    ap.add_argument("--precision", default="fp16split", choices=["fp32", "fp64", "fp16split", "bf16"])
+    ap.add_argument("--no-compare", action="store_true", help="skip the plain-FP32 and FP64 comparison runs")
+    ap.add_argument("--serve-requests", type=int, default=32, help="requests in the serving leg (0: skip)")
+    ap.add_argument("--serve-rate", type=float, default=40.0, help="offered request rate of the serving leg (1/s)")
     ap.add_argument("--quick", action="store_true", help="small box (debug only)")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: 64^3 particles on a 128^3 grid (same kernels, a few hundred MB)")

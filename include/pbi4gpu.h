@@ -50,7 +50,9 @@ extern "C" {
 
 const char *pbi4g_last_error(void);
 int pbi4g_version(void);
-/* Precision used by the drop-in bispectrum entry points (default FP32). */
+/* Precision used by the drop-in bispectrum entry points (default FP32); the
+ * tensor-core forms apply to measure_bk and measure_bk_multipoles (cross
+ * spectra use the CUDA-core FP32 form). */
 int pbi4g_set_dropin_precision(int32_t precision);
 
 /* ---------------- 1. f2py drop-ins: powerI4 ---------------- */
@@ -178,6 +180,14 @@ int pbi4g_plan_run_host(pbi4g_plan *plan, int64_t npart, const double *pos, cons
 /* Copy the resident delta(k) half spectrum (N, N, N/2+1) complex128, C order
  * [z][y][x], to host memory. */
 int pbi4g_plan_get_delta_half(pbi4g_plan *plan, double *host_half);
+/* Replace the resident delta(k) half spectrum, (N, N, N/2+1) complex128 C order
+ * [z][y][x], e.g. a density read back from disk (pbi4.py:257-288); npart is the
+ * particle count the shot-noise terms use. */
+int pbi4g_plan_set_delta_half(pbi4g_plan *plan, int64_t npart, const double *host_half);
+/* Use these triangle counts (itot float64, grid^3 x count as count_triangles
+ * returns, e.g. read from a counts file, pbi4.py:466-470) instead of computing
+ * them; they are cast to float32 as the reference does (bispectrumI4.f90:8). */
+int pbi4g_plan_set_counts(pbi4g_plan *plan, const double *counts_host);
 /* Launches of this library's kernels issued by this plan since creation. */
 int64_t pbi4g_plan_kernel_launches(const pbi4g_plan *plan);
 

@@ -27,7 +27,7 @@ EXPORTS = [
     "pbi4g_plan_shape", "pbi4g_plan_triangle_counts", "pbi4g_plan_density", "pbi4g_plan_powerspectrum",
     "pbi4g_plan_bispectrum", "pbi4g_plan_run_device", "pbi4g_plan_run_host", "pbi4g_plan_get_delta_half",
     "pbi4g_plan_kernel_launches", "pbi4g_plan_enable_timing", "pbi4g_plan_stage_times",
-    "pbi4g_measure_pk_multipoles_noalloc",
+    "pbi4g_measure_pk_multipoles_noalloc", "pbi4g_plan_set_delta_half", "pbi4g_plan_set_counts",
 ]
 NSTAGES = 10
 STAGES = ["assign", "grid_convert", "fft_r2c", "fcomb", "pk_binning", "triangle_counts", "shell_spectra",
@@ -84,6 +84,8 @@ _SIGS = {
     "pbi4g_plan_enable_timing": [_P, _i32],
     "pbi4g_plan_stage_times": [_P, _P, _P],
     "pbi4g_measure_pk_multipoles_noalloc": [_i32, _f32, _f32, _f32, _i32, _P, _P, _P, _P, _P],
+    "pbi4g_plan_set_delta_half": [_P, _i64, _P],
+    "pbi4g_plan_set_counts": [_P, _P],
 }
 
 _lock = threading.Lock()

@@ -14,7 +14,7 @@ from ._lib import PRECISIONS, check, lib
 
 
 def set_precision(name: str) -> None:
-    """'fp32' (default) or 'fp64' for the drop-in bispectrum routines."""
+    """'fp32' (default), 'fp64', 'fp16split' or 'bf16' for the drop-in bispectrum routines."""
     check(lib().pbi4g_set_dropin_precision(PRECISIONS[name]))
 
 

@@ -1,0 +1,329 @@
+// assign_owner.cu -- mass assignment for the FP32 / mixed estimator plan:
+// owner-computes 16^3 tiles, 64-bit fixed-point accumulation in shared memory,
+// FP32 grids written with plain stores.
+//
+// Same indices and weights as powerI4.f90:68-249 (see assign.cu); the weights
+// are evaluated in FP32 from the FP64 cell offset.  Every contribution
+// (w_x w_y) w_z weight is rounded once to a 64-bit integer at scale 2^S and
+// summed with integer shared-memory atomics, so the grid is bit-identical for
+// any particle order and schedule.
+//
+// 1. prep: per particle, the first stencil cell of each grid (FP64 index math,
+//    once) and the FP32 offsets; the tiles its stencils touch (1 to 8) are
+//    counted.
+// 2. counting sort: one 32-byte record per (particle, touched tile).
+// 3. one CTA per tile, one warp per record: the lanes take distinct stencil
+//    cells of the record's particle (no two lanes of a warp add to the same
+//    cell), keep those inside the tile and add them into the tile's shared
+//    accumulator; the tile is then converted to FP32 and stored.  No global
+//    atomics, no int64 grid, no memset of the grids.
+#include "assign_owner.cuh"
+
+#include <math.h>
+#include <string.h>
+
+namespace pbi4g {
+
+namespace {
+
+constexpr int kT = 16;                  // tile edge
+constexpr int kTC = kT * kT * kT;       // 4096 cells
+constexpr int kThreads = 512;
+
+struct alignas(16) PRec {               // one particle, both grids (32 bytes)
+    unsigned int f[2];                  // first cell x | y << 11 | z << 22 per grid
+    float h[2][3];                      // cell offset per grid and axis
+};
+
+__device__ __forceinline__ unsigned int pack3(int x, int y, int z) {
+    return (unsigned)x | ((unsigned)y << 11) | ((unsigned)z << 22);
+}
+
+// first cell (0-based, in [0,N)) and the offset h that sets the weights
+__device__ __forceinline__ void first_and_h(double p, int N, int nintp, bool shifted, bool cic_nint, int &f, float &h) {
+    double v = (double)N * p + 1.0;
+    if (shifted) v = v - 0.5;
+    long long iv;
+    double hh;
+    if (nintp == 4) { iv = (long long)v; f = (int)((iv - 2) % N); hh = v - (double)iv; }
+    else if (nintp == 3) { iv = llround(v); f = (int)((iv - 2) % N); hh = v - (double)iv; }
+    else if (nintp == 2) { iv = (long long)v; f = (int)(iv % N); hh = cic_nint ? v - (double)llround(v) : v - (double)iv; }
+    else { iv = llround(v); f = (int)((iv - 1) % N); hh = 0.0; }
+    if (f < 0) f += N;
+    if (f < 0 || f >= N) f = 0;
+    h = (float)hh;
+}
+
+// weight j of the per-axis stencil (the reference's polynomials, FP32)
+__device__ __forceinline__ float weight1(int nintp, float h, int j) {
+    if (nintp == 4) {
+        const float h2 = h * h;
+        const float w0 = (1.f - h) * (1.f - h) * (1.f - h) / 6.f;
+        const float w1 = 4.f / 6.f + (0.5f * h - 1.f) * h2;
+        const float w3 = h2 * h / 6.f;
+        return j == 0 ? w0 : (j == 1 ? w1 : (j == 3 ? w3 : 1.f - w0 - w1 - w3));
+    }
+    if (nintp == 3) {
+        const float w0 = 0.5f * (0.5f - h) * (0.5f - h), w1 = 0.75f - h * h;
+        return j == 0 ? w0 : (j == 1 ? w1 : 1.f - w0 - w1);
+    }
+    if (nintp == 2) return j == 0 ? 1.f - h : h;
+    return 1.f;
+}
+
+// tiles touched along one axis by a stencil of width w starting at cell lo (mod N)
+__device__ __forceinline__ int axis_tiles(int lo, int w, int N, int nt, int t[2]) {
+    t[0] = lo / kT;
+    int hi = lo + w - 1;
+    hi -= (hi >= N) ? N : 0;
+    t[1] = hi / kT;
+    return t[1] == t[0] ? 1 : 2;
+}
+
+struct PrepOut {
+    int lo[3];
+    int w;
+};
+
+__device__ __forceinline__ PRec make_rec(const double *__restrict__ pos, int64_t npart, int64_t i, int N, int nintp,
+                                         int interlaced, int lo[3]) {
+    PRec r;
+    int f[2][3];
+    for (int c = 0; c < 3; c++) {
+        const double p = pos[(size_t)c * npart + i];
+        first_and_h(p, N, nintp, false, !interlaced, f[0][c], r.h[0][c]);
+        if (interlaced) first_and_h(p, N, nintp, true, false, f[1][c], r.h[1][c]);
+        else { f[1][c] = f[0][c]; r.h[1][c] = 0.f; }
+        // the shifted grid starts at the same cell or one below (circularly)
+        lo[c] = (interlaced && f[1][c] == (f[0][c] + N - 1) % N) ? f[1][c] : f[0][c];
+    }
+    r.f[0] = pack3(f[0][0], f[0][1], f[0][2]);
+    r.f[1] = pack3(f[1][0], f[1][1], f[1][2]);
+    return r;
+}
+
+__global__ void owner_count_kernel(int N, int nintp, int interlaced, int64_t npart, const double *__restrict__ pos,
+                                   int nt, PRec *__restrict__ rec, unsigned int *__restrict__ count) {
+    const int w = nintp + (interlaced ? 1 : 0);  // cells spanned from the lowest first cell
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npart; i += (int64_t)gridDim.x * blockDim.x) {
+        int lo[3];
+        const PRec r = make_rec(pos, npart, i, N, nintp, interlaced, lo);
+        rec[i] = r;
+        int tx[2], ty[2], tz[2];
+        const int nx = axis_tiles(lo[0], w, N, nt, tx), ny = axis_tiles(lo[1], w, N, nt, ty),
+                  nz = axis_tiles(lo[2], w, N, nt, tz);
+        for (int c = 0; c < nz; c++)
+            for (int b = 0; b < ny; b++)
+                for (int a = 0; a < nx; a++) atomicAdd(count + (tz[c] * nt + ty[b]) * nt + tx[a], 1u);
+    }
+}
+
+__global__ void owner_scan_kernel(int ntiles, const unsigned int *__restrict__ count, unsigned int *__restrict__ start,
+                                  unsigned int *__restrict__ cursor) {
+    __shared__ unsigned int warp_tot[32];
+    __shared__ unsigned int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int base = 0; base < ntiles; base += blockDim.x) {
+        const int i = base + threadIdx.x;
+        const unsigned v = i < ntiles ? count[i] : 0u;
+        unsigned x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_tot[wid] = x;
+        __syncthreads();
+        if (wid == 0) {
+            unsigned t = lane < (int)(blockDim.x >> 5) ? warp_tot[lane] : 0u;
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned y = __shfl_up_sync(0xffffffffu, t, o);
+                if (lane >= o) t += y;
+            }
+            warp_tot[lane] = t;
+        }
+        __syncthreads();
+        const unsigned excl = carry + x - v + (wid ? warp_tot[wid - 1] : 0u);
+        if (i < ntiles) { start[i] = excl; cursor[i] = excl; }
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry = excl + v;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) start[ntiles] = carry;
+}
+
+__global__ void owner_scatter_kernel(int N, int nintp, int interlaced, int64_t npart, int nt,
+                                     const PRec *__restrict__ rec, const double *__restrict__ weight,
+                                     unsigned int *__restrict__ cursor, PRec *__restrict__ sorted,
+                                     float *__restrict__ wsorted) {
+    const int w = nintp + (interlaced ? 1 : 0);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npart; i += (int64_t)gridDim.x * blockDim.x) {
+        const PRec r = rec[i];
+        int lo[3];
+        for (int c = 0; c < 3; c++) {
+            const unsigned f0 = (r.f[0] >> (11 * c)) & 2047, f1 = (r.f[1] >> (11 * c)) & 2047;
+            lo[c] = (interlaced && (int)f1 == ((int)f0 + N - 1) % N) ? (int)f1 : (int)f0;
+        }
+        int tx[2], ty[2], tz[2];
+        const int nx = axis_tiles(lo[0], w, N, nt, tx), ny = axis_tiles(lo[1], w, N, nt, ty),
+                  nz = axis_tiles(lo[2], w, N, nt, tz);
+        const float wt = weight ? (float)weight[i] : 1.f;
+        for (int c = 0; c < nz; c++)
+            for (int b = 0; b < ny; b++)
+                for (int a = 0; a < nx; a++) {
+                    const unsigned d = atomicAdd(cursor + (tz[c] * nt + ty[b]) * nt + tx[a], 1u);
+                    sorted[d] = r;
+                    if (wsorted) wsorted[d] = wt;
+                }
+    }
+}
+
+// 64-bit fixed-point add as two native 32-bit shared atomics: the carry of the
+// low word is detected from its old value, so the pair sums exactly (mod 2^64).
+__device__ __forceinline__ void add64_split(unsigned *lo, unsigned *hi, long long q) {
+    const unsigned long long u = (unsigned long long)q;
+    const unsigned ql = (unsigned)u, qh = (unsigned)(u >> 32);
+    const unsigned old = atomicAdd(lo, ql);
+    atomicAdd(hi, qh + ((old + ql < old) ? 1u : 0u));
+}
+
+__global__ void __launch_bounds__(kThreads) owner_tile_kernel(int N, int nintp, int interlaced, int nt,
+                                                               const unsigned int *__restrict__ start,
+                                                               const PRec *__restrict__ sorted,
+                                                               const float *__restrict__ wsorted, float scale,
+                                                               float inv_scale, float *__restrict__ out1,
+                                                               float *__restrict__ out2) {
+    extern __shared__ unsigned acc32[];  // [G][lo, hi][kTC]
+    const int G = interlaced ? 2 : 1;
+    const int ntiles = nt * nt * nt;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int ncell = nintp * nintp * nintp;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int tx = tile % nt, ty = (tile / nt) % nt, tz = tile / (nt * nt);
+        const int ox = tx * kT, oy = ty * kT, oz = tz * kT;
+        for (int c = threadIdx.x; c < 2 * G * kTC; c += blockDim.x) acc32[c] = 0u;
+        __syncthreads();
+        const unsigned b = start[tile], e = start[tile + 1];
+        for (unsigned k = b + warp; k < e; k += nwarps) {
+            const PRec r = sorted[k];
+            const float wt = wsorted ? wsorted[k] : 1.f;
+            for (int g = 0; g < G; g++) {
+                const unsigned pf = r.f[g];
+                const int fx = pf & 2047, fy = (pf >> 11) & 2047, fz = pf >> 22;
+                unsigned *alo = acc32 + 2 * g * kTC, *ahi = alo + kTC;
+                for (int c = lane; c < ncell; c += 32) {
+                    const int i = c % nintp, j = (c / nintp) % nintp, l = c / (nintp * nintp);
+                    int x = fx + i, y = fy + j, z = fz + l;
+                    x -= (x >= N) ? N : 0;
+                    y -= (y >= N) ? N : 0;
+                    z -= (z >= N) ? N : 0;
+                    const int lx = x - ox, ly = y - oy, lz = z - oz;
+                    if (lx < 0 || lx >= kT || ly < 0 || ly >= kT || lz < 0 || lz >= kT) continue;
+                    // the reference's product order: ((w_x w_y) w_z) weight
+                    const float wv = weight1(nintp, r.h[g][0], i) * weight1(nintp, r.h[g][1], j) *
+                                     weight1(nintp, r.h[g][2], l) * wt;
+                    // wv * 2^S is exact in FP32 (a power-of-two scale), so the FP32 rounding to an
+                    // integer gives the same q as the FP64 route, without FP64 arithmetic
+                    const long long q = __float2ll_rn(wv * scale);
+                    const int cell = (lz * kT + ly) * kT + lx;
+                    add64_split(alo + cell, ahi + cell, q);
+                }
+            }
+        }
+        __syncthreads();
+        for (int c = threadIdx.x; c < G * kTC; c += blockDim.x) {
+            const int g = c / kTC, cc = c % kTC;
+            const int x = cc % kT, y = (cc / kT) % kT, z = cc / (kT * kT);
+            const unsigned *alo = acc32 + 2 * g * kTC;
+            const long long v = (long long)(((unsigned long long)alo[kTC + cc] << 32) | alo[cc]);
+            float *out = g ? out2 : out1;
+            out[((size_t)(oz + z) * N + (oy + y)) * N + (ox + x)] = (float)v * inv_scale;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void owner_wmax_kernel(int64_t n, const double *__restrict__ w, unsigned long long *__restrict__ out) {
+    double m = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double a = fabs(w[i]);
+        if (!(a <= 1e300)) a = 1e308;
+        m = fmax(m, a);
+    }
+    for (int o = 16; o; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
+}  // namespace
+
+bool owner_supported(int N) { return N % kT == 0 && N >= 2 * kT && N <= 2048; }
+
+int OwnerWork::ensure(int N, int64_t npart) {
+    const int nt = N / kT;
+    const size_t ntiles = (size_t)nt * nt * nt;
+    const size_t n = (size_t)(npart > 0 ? npart : 1);
+    PBI4G_CHECK(count.ensure((ntiles + 1) * 4));
+    PBI4G_CHECK(start.ensure((ntiles + 1) * 4));
+    PBI4G_CHECK(cursor.ensure((ntiles + 1) * 4));
+    PBI4G_CHECK(rec.ensure(n * sizeof(PRec)));
+    // a record per (particle, touched tile): at most 8 per particle
+    PBI4G_CHECK(sorted.ensure(8 * n * sizeof(PRec)));
+    PBI4G_CHECK(wsorted.ensure(8 * n * 4));
+    PBI4G_CHECK(wmax.ensure(8));
+    return PBI4G_OK;
+}
+
+size_t OwnerWork::footprint(int N, int64_t npart) {
+    const size_t nt = (size_t)(N / kT);
+    return 3 * (nt * nt * nt + 1) * 4 + (size_t)npart * (sizeof(PRec) + 8 * (sizeof(PRec) + 4)) + 64;
+}
+
+int assign_owner(OwnerWork &wk, int N, int nintp, bool interlaced, int64_t npart, const double *d_pos,
+                 const double *d_weight, float *out, cudaStream_t st, int64_t *launches) {
+    if (!owner_supported(N)) return set_error(PBI4G_ERR_UNSUPPORTED, "owner assignment needs grid %% 16 == 0");
+    if (nintp < 1 || nintp > 4 || npart < 1 || !d_pos)
+        return set_error(PBI4G_ERR_INVALID, "assign: nintp=%d npart=%lld", nintp, (long long)npart);
+    if (npart >= (int64_t)0x1fffffffLL) return set_error(PBI4G_ERR_RANGE, "assign: npart >= 2^29");
+    PBI4G_CHECK(wk.ensure(N, npart));
+    double wmax = 1.0;
+    if (d_weight) {
+        PBI4G_CUDA(cudaMemsetAsync(wk.wmax.p, 0, 8, st));
+        owner_wmax_kernel<<<grid_blocks(npart, 256, 152 * 8), 256, 0, st>>>(npart, d_weight,
+                                                                            wk.wmax.as<unsigned long long>());
+        PBI4G_LAUNCH_CHECK();
+        ++*launches;
+        unsigned long long bitsw = 0;
+        PBI4G_CUDA(cudaMemcpyAsync(&bitsw, wk.wmax.p, 8, cudaMemcpyDeviceToHost, st));
+        PBI4G_CUDA(cudaStreamSynchronize(st));
+        memcpy(&wmax, &bitsw, 8);
+    }
+    int bits;
+    PBI4G_CHECK(fixed_point_bits(npart, wmax, &bits));
+    const int nt = N / kT, ntiles = nt * nt * nt;
+    PBI4G_CUDA(cudaMemsetAsync(wk.count.p, 0, (size_t)(ntiles + 1) * 4, st));
+    owner_count_kernel<<<grid_blocks(npart, 256), 256, 0, st>>>(N, nintp, interlaced, npart, d_pos, nt,
+                                                                static_cast<PRec *>(wk.rec.p),
+                                                                wk.count.as<unsigned int>());
+    PBI4G_LAUNCH_CHECK();
+    owner_scan_kernel<<<1, 1024, 0, st>>>(ntiles, wk.count.as<unsigned int>(), wk.start.as<unsigned int>(),
+                                          wk.cursor.as<unsigned int>());
+    PBI4G_LAUNCH_CHECK();
+    owner_scatter_kernel<<<grid_blocks(npart, 256), 256, 0, st>>>(
+        N, nintp, interlaced, npart, nt, static_cast<const PRec *>(wk.rec.p), d_weight, wk.cursor.as<unsigned int>(),
+        static_cast<PRec *>(wk.sorted.p), d_weight ? wk.wsorted.as<float>() : nullptr);
+    PBI4G_LAUNCH_CHECK();
+    const int G = interlaced ? 2 : 1;
+    const size_t smem = sizeof(unsigned) * 2 * G * kTC;
+    PBI4G_CUDA(cudaFuncSetAttribute(owner_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const size_t FC = full_cells(N);
+    owner_tile_kernel<<<ntiles < 152 * 3 ? ntiles : 152 * 3, kThreads, smem, st>>>(
+        N, nintp, interlaced, nt, wk.start.as<unsigned int>(), static_cast<const PRec *>(wk.sorted.p),
+        d_weight ? wk.wsorted.as<float>() : nullptr, ldexpf(1.0f, bits), ldexpf(1.0f, -bits), out,
+        interlaced ? out + FC : nullptr);
+    PBI4G_LAUNCH_CHECK();
+    *launches += 4;
+    return PBI4G_OK;
+}
+
+}  // namespace pbi4g

@@ -1,0 +1,20 @@
+// assign_owner.cuh -- owner-computes tiled assignment into FP32 grids (assign_owner.cu).
+#pragma once
+#include "assign.cuh"
+
+namespace pbi4g {
+
+struct OwnerWork {
+    DevBuf count, start, cursor, key, rec, sorted, wsorted, wmax;
+    int ensure(int N, int64_t npart);
+    static size_t footprint(int N, int64_t npart);
+};
+
+bool owner_supported(int N);
+
+// Assign npart particles (device (3, npart) float64, optional device weights)
+// into FP32 real grids out[G][N^3] (G = 2 when interlaced), fixed-point exact sums.
+int assign_owner(OwnerWork &wk, int N, int nintp, bool interlaced, int64_t npart, const double *d_pos,
+                 const double *d_weight, float *out, cudaStream_t st, int64_t *launches);
+
+}  // namespace pbi4g

@@ -18,6 +18,8 @@
 #include <math.h>
 #include <algorithm>
 #include <map>
+#include <mutex>
+#include <tuple>
 
 namespace pbi4g {
 
@@ -53,6 +55,32 @@ int Shells::build(int N_, float kbin_, float kcenter_, int nb_, int iopen_, int 
                 int m = (dx == 0 || dx == h ? 1 : 2) * (dy == 0 || dy == h ? 1 : 2) * (dz == 0 || dz == h ? 1 : 2);
                 nmodes[b - 1] += m;
             }
+    // Map grid: every shell mode has |k_axis| <= kmax, so the per-axis sum of
+    // three of them lies in [-3 kmax, 3 kmax].  On any grid Nm > 3 kmax the
+    // condition q1+q2+q3 = 0 (mod Nm) holds only for exact triangles; when
+    // 3 kmax < N the reference's N grid has no aliased triangles either, and the
+    // sum over x of three maps on the Nm grid equals the reference's sum times
+    // (Nm/N)^3.  Otherwise the maps stay on the N grid.
+    int kmax = 0;
+    for (int k2 = 0; k2 <= k2max; k2++)
+        if (lut_h[k2]) kmax = std::max(kmax, (int)floor(sqrt((double)k2)));
+    // smallest multiple of 4 above 3 kmax that cuFFT handles fast: 5-smooth,
+    // or 7-smooth when that is more than 5% smaller
+    auto smooth = [](int n, int fmax) {
+        for (int f : {2, 3, 5, 7})
+            if (f <= fmax)
+                while (n % f == 0) n /= f;
+        return n == 1;
+    };
+    int n5 = 0, n7 = 0;
+    for (int n = 4; n < N && (!n5 || !n7); n += 4) {
+        if (n <= 3 * kmax) continue;
+        if (!n7 && smooth(n, 7)) n7 = n;
+        if (!n5 && smooth(n, 5)) n5 = n;
+    }
+    Nm = N;
+    if (n5) Nm = (n7 && n7 < 0.95 * n5) ? n7 : n5;
+    else if (n7) Nm = n7;
     ishift = (int)(kcenter / kbin) + (iopen ? 1 : 0);  // bispectrumI4.f90:38-42
     tri.clear();
     for (int l = 1; l <= nb; l++)
@@ -191,45 +219,52 @@ int TriPlan::build(const Shells &sh, int nsets_, int cross_, int max_pairs) {
 // ------------------------------------------------------- map spectra ---
 template <class C> __device__ __forceinline__ C czero() { C c; c.x = 0; c.y = 0; return c; }
 
+constexpr int kMapChunk = 8;  // maps per block row: each block writes 8 contiguous map regions
+
 template <class R>
-__global__ void build_map_spectra_kernel(int N, int nb, const int *__restrict__ lut, int m0, int count,
+__global__ void build_map_spectra_kernel(int N, int Nm, int nb, int k2max, const int *__restrict__ lut, int count,
                                          const typename Cx<R>::T *__restrict__ s0,
                                          const typename Cx<R>::T *__restrict__ s1,
                                          const typename Cx<R>::T *__restrict__ s2, int f0, int f1, int f2, double l0,
                                          double l1, double l2, typename Cx<R>::T *__restrict__ out,
-                                         double *__restrict__ powsum) {
+                                         double *__restrict__ powsum, int pow_mask) {
     using C = typename Cx<R>::T;
-    extern __shared__ double spow[];
+    extern __shared__ double spow[];  // [3][nb] powers sum |H|^2 over the full grid, per set and shell
     if (powsum)
-        for (int b = threadIdx.x; b < nb; b += blockDim.x) spow[b] = 0.0;
+        for (int b = threadIdx.x; b < 3 * nb; b += blockDim.x) spow[b] = 0.0;
     __syncthreads();
-    const int NH = N / 2 + 1;
-    const size_t HC = (size_t)N * N * NH;
-    for (size_t cell = blockIdx.x * (size_t)blockDim.x + threadIdx.x; cell < HC;
+    const int NH = N / 2 + 1, NHm = Nm / 2 + 1;
+    const size_t HCm = (size_t)Nm * Nm * NHm;
+    const int j0 = blockIdx.y * kMapChunk, j1 = min(count, j0 + kMapChunk);
+    for (size_t cell = blockIdx.x * (size_t)blockDim.x + threadIdx.x; cell < HCm;
          cell += (size_t)gridDim.x * blockDim.x) {
-        const int x = (int)(cell % NH), y = (int)((cell / NH) % N), z = (int)(cell / ((size_t)NH * N));
-        const int ay = kabs0(y, N), az = kabs0(z, N);
-        const int sb = lut[x * x + ay * ay + az * az];
-        const int s_lo = m0 / nb, s_hi = (m0 + count - 1) / nb;
-        if (sb == 0) {
-            for (int j = 0; j < count; j++) out[(size_t)j * HC + cell] = czero<C>();
+        const int x = (int)(cell % NHm), y = (int)((cell / NHm) % Nm), z = (int)(cell / ((size_t)NHm * Nm));
+        const int ky = kfreq0(y, Nm), kz = kfreq0(z, Nm);
+        const int k2 = x * x + ky * ky + kz * kz;
+        const int sb = k2 <= k2max ? lut[k2] : 0;
+        bool any = false;
+        for (int j = j0; j < j1; j++) any |= (j % nb + 1 == sb);
+        if (!any) {
+            for (int j = j0; j < j1; j++) out[(size_t)j * HCm + cell] = czero<C>();
             continue;
         }
-        const bool herm = (x == 0 || x == N / 2);
-        const size_t mc = ((size_t)kneg0(z, N) * N + kneg0(y, N)) * NH + x;
-        const int ky = kfreq0(y, N), kz = kfreq0(z, N);
-        const int k2 = x * x + ky * ky + kz * kz;
+        // source cell on the N grid (same signed frequency), and its mirror -k
+        const int yN = ky < 0 ? ky + N : ky, zN = kz < 0 ? kz + N : kz;
+        const size_t sc = ((size_t)zN * N + yN) * NH + x;
+        const bool herm = (x == 0 || x == Nm / 2);
+        const size_t mc = ((size_t)kneg0(zN, N) * N + kneg0(yN, N)) * NH + x;
         const double lk = l0 * x + l1 * ky + l2 * kz;
         const R mu2 = k2 > 0 ? (R)(lk * lk / (double)k2) : (R)0;
-        // one value per set present in the chunk
-        C val[3];
-#pragma unroll
-        for (int s = 0; s < 3; s++) {
-            val[s] = czero<C>();
-            if (s < s_lo || s > s_hi) continue;
+        const double wfull = herm ? 1.0 : 2.0;
+        for (int j = j0; j < j1; j++) {
+            const int s = j / nb, b = j % nb + 1;
+            if (b != sb) {
+                out[(size_t)j * HCm + cell] = czero<C>();
+                continue;
+            }
             const C *src = s == 0 ? s0 : (s == 1 ? s1 : s2);
             const int fac = s == 0 ? f0 : (s == 1 ? f1 : f2);
-            C v = src[cell];
+            C v = src[sc];
             if (herm) {
                 const C w = src[mc];
                 v.x = (v.x + w.x) * (R)0.5;
@@ -240,45 +275,39 @@ __global__ void build_map_spectra_kernel(int N, int nb, const int *__restrict__ 
             else if (fac == 4) L = (R)0.375 + mu2 * ((R)-3.75 + (R)4.375 * mu2);
             v.x *= L;
             v.y *= L;
-            val[s] = v;
-        }
-        for (int j = 0; j < count; j++) {
-            const int m = m0 + j, s = m / nb, b = m % nb + 1;
-            out[(size_t)j * HC + cell] = (b == sb) ? val[s] : czero<C>();
-        }
-        if (powsum && s_lo == 0 && (sb - 1) >= m0 && (sb - 1) < m0 + count) {
-            const C v = val[0];
-            atomicAdd(&spow[sb - 1], (herm ? 1.0 : 2.0) * ((double)v.x * v.x + (double)v.y * v.y));
+            out[(size_t)j * HCm + cell] = v;
+            if (powsum && (pow_mask >> s & 1))
+                atomicAdd(&spow[s * nb + b - 1], wfull * ((double)v.x * v.x + (double)v.y * v.y));
         }
     }
     if (powsum) {
         __syncthreads();
-        for (int b = threadIdx.x; b < nb; b += blockDim.x)
+        for (int b = threadIdx.x; b < 3 * nb; b += blockDim.x)
             if (spow[b] != 0.0) atomicAdd(powsum + b, spow[b]);
     }
 }
 
 template <class R>
-int build_map_spectra(const Shells &sh, int m0, int count, const typename Cx<R>::T *const src[3], const int fac[3],
-                      const double los[3], typename Cx<R>::T *out, double *powsum, cudaStream_t st,
+int build_map_spectra(const Shells &sh, int count, const typename Cx<R>::T *const src[3], const int fac[3],
+                      const double los[3], typename Cx<R>::T *out, double *powsum, int pow_mask, cudaStream_t st,
                       int64_t *launches) {
-    const int N = sh.N;
-    const size_t smem = powsum ? sizeof(double) * sh.nb : 0;
-    build_map_spectra_kernel<R><<<grid_blocks(half_cells(N), 256, 152 * 8), 256, smem, st>>>(
-        N, sh.nb, sh.lut.as<int>(), m0, count, src[0], src[1], src[2], fac[0], fac[1], fac[2], los ? los[0] : 0,
-        los ? los[1] : 0, los ? los[2] : 0, out, powsum);
+    const size_t smem = powsum ? sizeof(double) * 3 * sh.nb : 0;
+    const dim3 grid(grid_blocks(half_cells(sh.Nm), 256, 152 * 2), (count + kMapChunk - 1) / kMapChunk);
+    build_map_spectra_kernel<R><<<grid, 256, smem, st>>>(
+        sh.N, sh.Nm, sh.nb, sh.k2max, sh.lut.as<int>(), count, src[0], src[1], src[2], fac[0], fac[1], fac[2],
+        los ? los[0] : 0, los ? los[1] : 0, los ? los[2] : 0, out, powsum, pow_mask);
     PBI4G_LAUNCH_CHECK();
     ++*launches;
     return PBI4G_OK;
 }
 
-template int build_map_spectra<float>(const Shells &, int, int, const float2 *const[3], const int[3], const double[3],
-                                      float2 *, double *, cudaStream_t, int64_t *);
-template int build_map_spectra<double>(const Shells &, int, int, const double2 *const[3], const int[3],
-                                       const double[3], double2 *, double *, cudaStream_t, int64_t *);
+template int build_map_spectra<float>(const Shells &, int, const float2 *const[3], const int[3], const double[3],
+                                      float2 *, double *, int, cudaStream_t, int64_t *);
+template int build_map_spectra<double>(const Shells &, int, const double2 *const[3], const int[3], const double[3],
+                                       double2 *, double *, int, cudaStream_t, int64_t *);
 
 template <class R>
-__global__ void build_indicator_kernel(int N, const int *__restrict__ lut, int m0, int count,
+__global__ void build_indicator_kernel(int N, int k2max, const int *__restrict__ lut, int m0, int count,
                                        typename Cx<R>::T *__restrict__ out) {
     using C = typename Cx<R>::T;
     const int NH = N / 2 + 1;
@@ -287,7 +316,8 @@ __global__ void build_indicator_kernel(int N, const int *__restrict__ lut, int m
          cell += (size_t)gridDim.x * blockDim.x) {
         const int x = (int)(cell % NH), ay = kabs0((int)((cell / NH) % N), N),
                   az = kabs0((int)(cell / ((size_t)NH * N)), N);
-        const int sb = lut[x * x + ay * ay + az * az];
+        const int k2 = x * x + ay * ay + az * az;
+        const int sb = k2 <= k2max ? lut[k2] : 0;
         for (int j = 0; j < count; j++) {
             C v = czero<C>();
             if (sb == m0 + j + 1) v.x = 1;
@@ -299,8 +329,8 @@ __global__ void build_indicator_kernel(int N, const int *__restrict__ lut, int m
 template <class R>
 int build_indicator_spectra(const Shells &sh, int m0, int count, typename Cx<R>::T *out, cudaStream_t st,
                             int64_t *launches) {
-    build_indicator_kernel<R><<<grid_blocks(half_cells(sh.N), 256, 152 * 8), 256, 0, st>>>(sh.N, sh.lut.as<int>(), m0,
-                                                                                         count, out);
+    build_indicator_kernel<R><<<grid_blocks(half_cells(sh.Nm), 256, 152 * 8), 256, 0, st>>>(
+        sh.Nm, sh.k2max, sh.lut.as<int>(), m0, count, out);
     PBI4G_LAUNCH_CHECK();
     ++*launches;
     return PBI4G_OK;
@@ -382,11 +412,13 @@ __global__ void __launch_bounds__(kGroupThreads) trisum_kernel(
     const int hv = kc / 2;  // vec2 loads per staged row
     for (long long ch = cb; ch < ce; ch++) {
         const long long k0 = ch * kc;
-        const size_t goff = (size_t)(k0 / N) * rs + (size_t)(k0 % N);
         for (int idx = threadIdx.x; idx < (nq + nb) * hv; idx += blockDim.x) {
             const int m = idx / hv, c = idx - m * hv;
             const int map = m < nq ? qmap[m] : m - nq;
-            const V2 v = *reinterpret_cast<const V2 *>(maps + (size_t)map * mstride + goff + 2 * c);
+            // N is even, so a pair of points never straddles a grid row
+            const long long p = k0 + 2 * c;
+            const V2 v = *reinterpret_cast<const V2 *>(maps + (size_t)map * mstride + (size_t)(p / N) * rs +
+                                                       (size_t)(p % N));
             if (m < nq) {
                 sQ[(size_t)(2 * c) * qrow + m] = v.x;
                 sQ[(size_t)(2 * c + 1) * qrow + m] = v.y;
@@ -447,14 +479,20 @@ __global__ void reduce_partial_kernel(int nslots, int ksplit, const double *__re
     }
 }
 
+int reduce_partials(int nslots, int ksplit, const double *partial, double *S, cudaStream_t st) {
+    reduce_partial_kernel<<<(nslots + 255) / 256, 256, 0, st>>>(nslots, ksplit, partial, S);
+    PBI4G_LAUNCH_CHECK();
+    return PBI4G_OK;
+}
+
 template <class T>
 int triangle_sums(const Shells &sh, const TriPlan &tp, const T *maps, size_t mstride, int rs, DevBuf &partial,
                   double *S, cudaStream_t st, int64_t *launches) {
-    const int N = sh.N;
+    const int N = sh.Nm;  // maps live on the map grid
     const long long K = (long long)N * N * N;
     int kc = kKCmax;
-    while (kc > 4 && N % kc) kc /= 2;  // chunk inside one grid row
-    if (N % kc || (rs & 1) || (mstride & 1))
+    while (kc > 4 && K % kc) kc /= 2;
+    if (K % kc || (N & 1) || (rs & 1) || (mstride & 1))
         return set_error(PBI4G_ERR_UNSUPPORTED, "triangle sums: grid %d has no even chunk width", N);
     const int qpad = ((tp.nq + kTQ - 1) / kTQ) * kTQ;  // q tiles read up to 8 columns per tile
     const int gpad = ((tp.max_group_pairs + kTP - 1) / kTP) * kTP;
@@ -488,7 +526,7 @@ __global__ void bk_finalize_kernel(int64_t itot, int nb, int nsets, int cross, c
                                    const double *__restrict__ S, const double *__restrict__ powsum,
                                    const double *__restrict__ nmodes, double kf3, double powSN, double gridD,
                                    double kcenter, double kbin, const float *__restrict__ counts,
-                                   double *__restrict__ bout) {
+                                   double *__restrict__ bout, double sfac) {
     const double powSN2 = powSN * powSN;
     for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < itot; m += (int64_t)gridDim.x * blockDim.x) {
         const int l = tri[3 * m], j = tri[3 * m + 1], i = tri[3 * m + 2];
@@ -498,7 +536,7 @@ __global__ void bk_finalize_kernel(int64_t itot, int nb, int nsets, int cross, c
         if (cross) {
             double *o = bout + 5 * m;
             o[0] = tl; o[1] = tj; o[2] = ti;
-            o[3] = kf3 * S[m * nsets] / c;
+            o[3] = kf3 * (sfac * S[m * nsets]) / c;
             o[4] = (double)(float)(c / gridD);
             continue;
         }
@@ -510,12 +548,12 @@ __global__ void bk_finalize_kernel(int64_t itot, int nb, int nsets, int cross, c
         double *o = bout + (size_t)rows * m;
         o[0] = tl; o[1] = tj; o[2] = ti;
         o[3] = pl; o[4] = pj; o[5] = pi;
-        o[6] = kf3 * S[m * nsets] / c + bispSN;
+        o[6] = kf3 * (sfac * S[m * nsets]) / c + bispSN;
         o[7] = bispSN;
         o[8] = (double)(float)(c / gridD);
         if (nsets == 3) {
-            o[9] = 5 * kf3 * S[m * nsets + 1] / c;
-            o[10] = 9 * kf3 * S[m * nsets + 2] / c;
+            o[9] = 5 * kf3 * (sfac * S[m * nsets + 1]) / c;
+            o[10] = 9 * kf3 * (sfac * S[m * nsets + 2]) / c;
         }
     }
 }
@@ -528,16 +566,41 @@ int bk_finalize(const Shells &sh, int nsets, int cross, const double *S, const d
     const double gridD = (double)sh.N * sh.N * sh.N;
     bk_finalize_kernel<<<grid_blocks(sh.itot, 128), 128, 0, st>>>(
         sh.itot, sh.nb, nsets, cross, sh.tri_d.as<int>(), S, powsum, sh.nmodes_d.as<double>(), kf3, powSN, gridD,
-        (double)sh.kcenter, (double)sh.kbin, counts_f32, bout);
+        (double)sh.kcenter, (double)sh.kbin, counts_f32, bout,
+        // the sums were taken over the Nm^3 map grid: the reference sums over N^3
+        ((double)sh.N / sh.Nm) * ((double)sh.N / sh.Nm) * ((double)sh.N / sh.Nm));
     PBI4G_LAUNCH_CHECK();
     ++*launches;
     return PBI4G_OK;
 }
 
 // ------------------------------------------------------------- counts ---
+// Counts depend only on (grid, kbin, kcenter, nbins, iopen, cross): one
+// process-wide copy per binning serves every plan that uses it.
+static std::mutex g_counts_mutex;
+static std::map<std::tuple<int, float, float, int, int, int>, std::vector<int64_t>> g_counts_cache;
+
+static int upload_counts(Shells &sh) {
+    const double gridD = (double)sh.N * sh.N * sh.N;
+    std::vector<float> c32(sh.itot);
+    for (int64_t m = 0; m < sh.itot; m++) c32[m] = (float)(gridD * (double)sh.counts[m]);
+    PBI4G_CHECK(sh.counts_f32.ensure(sizeof(float) * std::max<int64_t>(1, sh.itot)));
+    PBI4G_CUDA(cudaMemcpy(sh.counts_f32.p, c32.data(), sizeof(float) * sh.itot, cudaMemcpyHostToDevice));
+    return PBI4G_OK;
+}
+
 int triangle_counts(Shells &sh, cudaStream_t st, int64_t *launches) {
     if (!sh.counts.empty()) return PBI4G_OK;
-    const int N = sh.N, nb = sh.nb, NH = N / 2 + 1;
+    const auto ckey = std::make_tuple(sh.N, sh.kbin, sh.kcenter, sh.nb, sh.iopen, sh.cross);
+    {
+        std::lock_guard<std::mutex> g(g_counts_mutex);
+        auto it = g_counts_cache.find(ckey);
+        if (it != g_counts_cache.end()) {
+            sh.counts = it->second;
+            return upload_counts(sh);
+        }
+    }
+    const int N = sh.Nm, nb = sh.nb, NH = N / 2 + 1;  // indicator maps on the map grid
     const size_t HC = half_cells(N);
     DevBuf maps, partial, S;
     PBI4G_CHECK(maps.ensure(sizeof(double2) * HC * nb));
@@ -573,9 +636,12 @@ int triangle_counts(Shells &sh, cudaStream_t st, int64_t *launches) {
         sh.counts.clear();
         return set_error(PBI4G_ERR_RANGE, "triangle counts not resolved to integers (max deviation %g)", maxdev);
     }
-    PBI4G_CHECK(sh.counts_f32.ensure(sizeof(float) * sh.itot));
-    PBI4G_CUDA(cudaMemcpy(sh.counts_f32.p, c32.data(), sizeof(float) * sh.itot, cudaMemcpyHostToDevice));
-    return PBI4G_OK;
+    {
+        std::lock_guard<std::mutex> g(g_counts_mutex);
+        g_counts_cache[ckey] = sh.counts;
+    }
+    (void)c32;
+    return upload_counts(sh);
 }
 
 }  // namespace pbi4g

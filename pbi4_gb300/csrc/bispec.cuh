@@ -13,6 +13,7 @@ namespace pbi4g {
 // Input-independent shell binning and triangle enumeration (cached per plan).
 struct Shells {
     int N = 0, nb = 0, iopen = 0, cross = 0, ishift = 0;
+    int Nm = 0;  // grid of the shell maps (the smallest alias-free size, at most N)
     float kbin = 0, kcenter = 0;
     int k2max = 0;
     std::vector<int> lut_h;          // shell of |k|^2 (1..nb), 0 outside
@@ -45,16 +46,17 @@ struct TriPlan {
     int build(const Shells &sh, int nsets, int cross, int max_pairs = 256);
 };
 
-// Build the half spectra of maps [m0, m0+count) into `out` (count x N*N*(N/2+1)
-// complex R, the in-place C2R layout).  Map m belongs to set m / nb and shell
-// m % nb + 1.  Set s reads src[s] (a half spectrum) times the multipole factor
-// fac[s] (0: 1, 2: L2(mu), 4: L4(mu)); the kx = 0 and kx = N/2 planes are
-// Hermitian-symmetrised.  When powsum != null, sum of |H|^2 over the full grid
-// of every set-0 shell is accumulated into powsum[nb] (double).
+// Build the half spectra of all `count` maps on the map grid Nm into `out`
+// (count x Nm*Nm*(Nm/2+1) complex R, the in-place C2R layout).  Map m belongs
+// to set m / nb and shell m % nb + 1.  Set s reads src[s] (a half spectrum on the
+// N grid) times the multipole factor fac[s] (0: 1, 2: L2(mu), 4: L4(mu)); the
+// kx = 0 (and Nyquist) planes are Hermitian-symmetrised.  When powsum != null,
+// the full-grid sum of |H|^2 of every shell of each set in pow_mask is added
+// into powsum[s * nb + shell - 1] (double).
 template <class R>
-int build_map_spectra(const Shells &sh, int m0, int count, const typename Cx<R>::T *const src[3],
-                      const int fac[3], const double los[3], typename Cx<R>::T *out, double *powsum,
-                      cudaStream_t st, int64_t *launches);
+int build_map_spectra(const Shells &sh, int count, const typename Cx<R>::T *const src[3], const int fac[3],
+                      const double los[3], typename Cx<R>::T *out, double *powsum, int pow_mask, cudaStream_t st,
+                      int64_t *launches);
 
 // Indicator half spectra of shells [m0, m0+count) (count_triangles, bispectrumI4.f90:862-869).
 template <class R>

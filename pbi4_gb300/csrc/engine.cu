@@ -8,11 +8,14 @@
 //             (pbi4.py:478-553, bispectrumI4.f90)
 #include "engine.cuh"
 #include "assign.cuh"
+#include "assign_owner.cuh"
 
 #include <stdarg.h>
 #include <stdio.h>
 #include <string.h>
+#include <math.h>
 #include <algorithm>
+#include <vector>
 
 namespace pbi4g {
 
@@ -58,11 +61,11 @@ void Prof::end(cudaStream_t st) {
 }
 
 size_t BkEngine::footprint(int N, int nb, int nsets, int cross, bool fp64) {
-    const size_t HC = half_cells(N);
+    const size_t HC = half_cells(N);  // upper bound: the map grid is at most N
     const int nm = cross ? 2 * nb : nsets * nb;
     const size_t cs = fp64 ? 16 : 8;
     // maps + a cuFFT work area of about one batch of the same size (upper estimate)
-    return 2 * (size_t)nm * HC * cs + (size_t)nb * 8 + (size_t)1 << 26;
+    return 2 * (size_t)nm * HC * cs + (size_t)nb * 8 + ((size_t)1 << 26);
 }
 
 template <class R>
@@ -72,7 +75,7 @@ int BkEngine::run(const typename Cx<R>::T *const src[3], const int fac[3], const
     using C = typename Cx<R>::T;
     Prof dummy;
     Prof &pf = prof ? *prof : dummy;
-    const int N = sh.N, NH = N / 2 + 1, nb = sh.nb;
+    const int N = sh.Nm, NH = N / 2 + 1, nb = sh.nb;  // maps live on the map grid Nm
     const size_t HC = half_cells(N);
     const int nm = nmaps();
     const bool fp64 = sizeof(R) == 8;
@@ -83,11 +86,25 @@ int BkEngine::run(const typename Cx<R>::T *const src[3], const int fac[3], const
         tp_fp64 = fp64;
     }
     PBI4G_CHECK(maps.ensure(sizeof(C) * HC * nm));
-    PBI4G_CHECK(powsum.ensure(sizeof(double) * nb));
+    PBI4G_CHECK(powsum.ensure(sizeof(double) * 3 * nb));
     PBI4G_CHECK(S.ensure(sizeof(double) * std::max(1, tp.nslots)));
+    const bool tc = tc_mode != 0 && !fp64 && !cross;
+    // set 0 always (shell powers); the other sets only when the tensor-core scale
+    // bound needs their own power (explicit delta_2 / delta_4 grids)
+    int pow_mask = 1;
+    if (tc) {
+        if (tcp_nsets != nsets) {
+            PBI4G_CHECK(tcp.build(sh, nsets));
+            tcp_nsets = nsets;
+        }
+        PBI4G_CHECK(S.ensure(sizeof(double) * std::max(1, tcp.nslots)));
+        for (int s = 1; s < nsets; s++)
+            if (fac[s] == 0) pow_mask |= 1 << s;
+    }
     pf.begin(6, st);
-    PBI4G_CUDA(cudaMemsetAsync(powsum.p, 0, sizeof(double) * nb, st));
-    PBI4G_CHECK(build_map_spectra<R>(sh, 0, nm, src, fac, los, maps.as<C>(), powsum.as<double>(), st, launches));
+    PBI4G_CUDA(cudaMemsetAsync(powsum.p, 0, sizeof(double) * 3 * nb, st));
+    PBI4G_CHECK(build_map_spectra<R>(sh, nm, src, fac, los, maps.as<C>(), powsum.as<double>(), pow_mask, st,
+                                     launches));
     pf.end(st);
     if (!inv || inv_batch != nm || inv_N != N || inv_fp64 != (int)fp64) {
         if (inv) cufftDestroy(inv);
@@ -107,7 +124,26 @@ int BkEngine::run(const typename Cx<R>::T *const src[3], const int fac[3], const
         PBI4G_CUFFT(cufftExecC2R(inv, maps.as<cufftComplex>(), maps.as<cufftReal>()));
     pf.end(st);
     pf.begin(8, st);
-    PBI4G_CHECK(triangle_sums<R>(sh, tp, maps.as<R>(), 2 * HC, 2 * NH, partial, S.as<double>(), st, launches));
+    if (tc) {
+        // largest |L_l(mu)| over mu^2 in [0, |los|^2]: bounds the delta_2 / delta_4 maps by the delta map
+        double lfac[3] = {1.0, 1.0, 1.0};
+        const double l2max = los ? los[0] * los[0] + los[1] * los[1] + los[2] * los[2] : 1.0;
+        for (int s = 1; s < nsets; s++) {
+            if (fac[s] == 0) continue;
+            double mx = 0;
+            for (int k = 0; k <= 2000; k++) {
+                const double m2 = l2max * k / 2000.0;
+                const double L = fac[s] == 2 ? -0.5 + 1.5 * m2 : 0.375 + m2 * (-3.75 + 4.375 * m2);
+                mx = std::max(mx, fabs(L));
+            }
+            lfac[s] = mx * 1.01;
+        }
+        PBI4G_CHECK(triangle_sums_tc(sh, tcp, tc_mode == 1, reinterpret_cast<const float *>(maps.p), 2 * HC, 2 * NH,
+                                     powsum.as<double>(), pow_mask, lfac, mexp, partial, S.as<double>(), st,
+                                     launches));
+    } else {
+        PBI4G_CHECK(triangle_sums<R>(sh, tp, maps.as<R>(), 2 * HC, 2 * NH, partial, S.as<double>(), st, launches));
+    }
     pf.end(st);
     pf.begin(9, st);
     PBI4G_CHECK(bk_finalize(sh, cross ? 1 : nsets, cross, S.as<double>(), powsum.as<double>(), kf, npart, counts_f32,
@@ -133,10 +169,12 @@ struct pbi4g_plan {
     bool fp64 = false;
     int N = 0, G = 1;
     AssignWork aw;
+    OwnerWork ow;
     DevBuf real_grids, spec, delta;
     DevBuf pos_stage, w_stage, pout_d, bout_d;
     cufftHandle fwd = 0;
     PkBins pk;
+    WinCache win;
     BkEngine bk;
     bool have_delta = false;
     int64_t npart = 0;
@@ -173,7 +211,8 @@ int pbi4g_plan_footprint(const pbi4g_config *cfg, int64_t npart_max, int64_t *by
     const int N = cfg->grid, G = cfg->interlacing ? 2 : 1;
     const bool fp64 = cfg->precision == PBI4G_PREC_FP64;
     const size_t rs = fp64 ? 8 : 4, cs = 2 * rs, HC = half_cells(N), FC = full_cells(N);
-    size_t b = AssignWork::footprint(N, npart_max, cfg->interlacing) + G * FC * rs + G * HC * cs + HC * cs;
+    size_t b = (fp64 ? AssignWork::footprint(N, npart_max, cfg->interlacing) : OwnerWork::footprint(N, npart_max)) +
+               G * FC * rs + G * HC * cs + HC * cs;
     b += 2 * G * HC * cs;  // cuFFT work area (upper estimate)
     b += (size_t)npart_max * 32 + 5 * (size_t)cfg->nbins_ps * 8 * 1300;
     if (cfg->do_bispectrum) {
@@ -208,6 +247,7 @@ int pbi4g_plan_create(const pbi4g_config *cfg, pbi4g_plan **out) {
             if ((rc = p->bk.sh.build(N, cfg->kbin_bs, cfg->kcenter_bs, cfg->nbins_bs, cfg->iopen, 0, p->st))) break;
             p->bk.nsets = cfg->multipoles ? 3 : 1;
             p->bk.cross = 0;
+            p->bk.tc_mode = cfg->precision == PBI4G_PREC_FP16SPLIT ? 1 : (cfg->precision == PBI4G_PREC_BF16 ? 2 : 0);
         }
         cudaError_t e = cudaStreamSynchronize(p->st);
         if (e != cudaSuccess) { rc = set_error(PBI4G_ERR_CUDA, "plan create: %s", cudaGetErrorString(e)); break; }
@@ -253,13 +293,21 @@ int pbi4g_plan_density(pbi4g_plan *p, int64_t npart, const double *d_pos, const 
     if (npart < 1) return set_error(PBI4G_ERR_INVALID, "npart must be >= 1");
     const int N = p->N;
     int bits;
-    p->prof.begin(0, p->st);
-    PBI4G_CHECK(assign_fixed(p->aw, N, p->cfg.nintp, p->G == 2, p->fp64, npart, d_pos, d_weight, &bits, p->st,
-                             &p->launches));
-    p->prof.end(p->st);
-    p->prof.begin(1, p->st);
-    PBI4G_CHECK(fixed_to_real(p->aw, N, p->G == 2, bits, p->fp64, p->real_grids.p, p->st, &p->launches));
-    p->prof.end(p->st);
+    if (!p->fp64 && owner_supported(N)) {
+        // FP32 grids straight from the owner-computes tiles (fixed-point sums in shared memory)
+        p->prof.begin(0, p->st);
+        PBI4G_CHECK(assign_owner(p->ow, N, p->cfg.nintp, p->G == 2, npart, d_pos, d_weight,
+                                 p->real_grids.as<float>(), p->st, &p->launches));
+        p->prof.end(p->st);
+    } else {
+        p->prof.begin(0, p->st);
+        PBI4G_CHECK(assign_fixed(p->aw, N, p->cfg.nintp, p->G == 2, p->fp64, npart, d_pos, d_weight, &bits, p->st,
+                                 &p->launches));
+        p->prof.end(p->st);
+        p->prof.begin(1, p->st);
+        PBI4G_CHECK(fixed_to_real(p->aw, N, p->G == 2, bits, p->fp64, p->real_grids.p, p->st, &p->launches));
+        p->prof.end(p->st);
+    }
     PBI4G_CUFFT(cufftSetStream(p->fwd, p->st));
     p->prof.begin(2, p->st);
     if (p->fp64)
@@ -270,10 +318,10 @@ int pbi4g_plan_density(pbi4g_plan *p, int64_t npart, const double *d_pos, const 
     p->prof.begin(3, p->st);
     if (p->fp64)
         PBI4G_CHECK(fcomb_half<double>(N, p->cfg.nintp, p->G == 2, p->cfg.box, (double)npart, p->spec.as<double2>(),
-                                       p->delta.as<double2>(), p->st, &p->launches));
+                                       p->delta.as<double2>(), p->win, p->st, &p->launches));
     else
         PBI4G_CHECK(fcomb_half<float>(N, p->cfg.nintp, p->G == 2, p->cfg.box, (double)npart, p->spec.as<float2>(),
-                                      p->delta.as<float2>(), p->st, &p->launches));
+                                      p->delta.as<float2>(), p->win, p->st, &p->launches));
     p->prof.end(p->st);
     p->have_delta = true;
     p->npart = npart;
@@ -300,8 +348,6 @@ int pbi4g_plan_bispectrum(pbi4g_plan *p, double *d_bout) {
     if (!p || !d_bout) return set_error(PBI4G_ERR_INVALID, "null plan/output");
     if (!p->cfg.do_bispectrum) return set_error(PBI4G_ERR_INVALID, "plan has no bispectrum");
     if (!p->have_delta) return set_error(PBI4G_ERR_INVALID, "bispectrum before density");
-    if (p->cfg.precision == PBI4G_PREC_FP16SPLIT || p->cfg.precision == PBI4G_PREC_BF16)
-        return set_error(PBI4G_ERR_UNSUPPORTED, "tensor-core precision not built in this library");
     if (p->bk.sh.counts.empty()) {
         p->prof.begin(5, p->st);
         PBI4G_CHECK(triangle_counts(p->bk.sh, p->st, &p->launches));
@@ -374,6 +420,38 @@ int pbi4g_plan_stage_times(pbi4g_plan *p, double *ms, int64_t *calls) {
         p->prof.pool.push_back(r.b);
     }
     p->prof.recs.clear();
+    return PBI4G_OK;
+}
+
+int pbi4g_plan_set_delta_half(pbi4g_plan *p, int64_t npart, const double *host_half) {
+    if (!p || !host_half || npart < 1) return set_error(PBI4G_ERR_INVALID, "bad arguments");
+    const size_t HC = half_cells(p->N);
+    if (p->fp64) {
+        PBI4G_CUDA(cudaMemcpyAsync(p->delta.p, host_half, HC * 16, cudaMemcpyHostToDevice, p->st));
+    } else {
+        std::vector<float2> tmp(HC);
+        for (size_t i = 0; i < HC; i++) tmp[i] = make_float2((float)host_half[2 * i], (float)host_half[2 * i + 1]);
+        PBI4G_CUDA(cudaMemcpyAsync(p->delta.p, tmp.data(), HC * 8, cudaMemcpyHostToDevice, p->st));
+        PBI4G_CUDA(cudaStreamSynchronize(p->st));
+    }
+    p->have_delta = true;
+    p->npart = npart;
+    return PBI4G_OK;
+}
+
+int pbi4g_plan_set_counts(pbi4g_plan *p, const double *counts_host) {
+    if (!p || !counts_host) return set_error(PBI4G_ERR_INVALID, "bad arguments");
+    if (!p->cfg.do_bispectrum) return set_error(PBI4G_ERR_INVALID, "plan has no bispectrum");
+    Shells &sh = p->bk.sh;
+    const double gridD = (double)p->N * p->N * p->N;
+    sh.counts.assign(sh.itot, 0);
+    std::vector<float> c32(sh.itot);
+    for (int64_t m = 0; m < sh.itot; m++) {
+        c32[m] = (float)counts_host[m];
+        sh.counts[m] = llround(counts_host[m] / gridD);
+    }
+    PBI4G_CHECK(sh.counts_f32.ensure(sizeof(float) * std::max<int64_t>(1, sh.itot)));
+    PBI4G_CUDA(cudaMemcpy(sh.counts_f32.p, c32.data(), sizeof(float) * sh.itot, cudaMemcpyHostToDevice));
     return PBI4G_OK;
 }
 

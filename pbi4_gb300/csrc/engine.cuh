@@ -1,6 +1,7 @@
 // engine.cuh -- bispectrum engine shared by the plan and the drop-in entry points.
 #pragma once
 #include "bispec.cuh"
+#include "trisum_tc.cuh"
 
 namespace pbi4g {
 
@@ -28,6 +29,11 @@ struct BkEngine {
     cufftHandle inv = 0;
     int inv_batch = 0, inv_N = 0, inv_fp64 = -1;
     DevBuf powsum, S, partial;
+    // tensor-core form: 0 off (CUDA cores), 1 FP16 hi+lo, 2 BF16
+    int tc_mode = 0;
+    TcPlan tcp;
+    int tcp_nsets = -1;
+    DevBuf mexp;
     ~BkEngine() {
         if (inv) cufftDestroy(inv);
     }

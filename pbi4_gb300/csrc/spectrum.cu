@@ -156,21 +156,23 @@ __global__ void fcomb_plain_half_kernel(int N, const typename Cx<R>::T *__restri
 
 template <class R>
 int fcomb_half(int N, int nintp, bool interlaced, float box, double norm, const typename Cx<R>::T *spec,
-               typename Cx<R>::T *delta, cudaStream_t st, int64_t *launches) {
+               typename Cx<R>::T *delta, WinCache &wcache, cudaStream_t st, int64_t *launches) {
     const int NH = N / 2 + 1;
     std::vector<double> tW(NH);
     window_table(N, nintp, tW.data());
     std::vector<R> iW(NH);
     for (int i = 0; i < NH; i++) iW[i] = (R)(1.0 / tW[i]);
-    // iW is tiny; keep it in a per-call device buffer that lives in a static
-    // cache keyed by (N, nintp, precision) to avoid an allocation per box.
-    static thread_local DevBuf cache;
-    static thread_local int cN = -1, cn = -1, cs = -1;
-    if (cN != N || cn != nintp || cs != (int)sizeof(R) || !cache.p) {
-        PBI4G_CHECK(cache.ensure(sizeof(R) * NH));
-        PBI4G_CUDA(cudaMemcpy(cache.p, iW.data(), sizeof(R) * NH, cudaMemcpyHostToDevice));
-        cN = N; cn = nintp; cs = (int)sizeof(R);
+    // the 1/W table is tiny; it lives in the caller's buffer and is rebuilt only
+    // when (N, nintp, precision) changes
+    if (wcache.N != N || wcache.nintp != nintp || wcache.rsize != (int)sizeof(R) || !wcache.buf.p) {
+        PBI4G_CHECK(wcache.buf.ensure(sizeof(R) * NH));
+        PBI4G_CUDA(cudaMemcpyAsync(wcache.buf.p, iW.data(), sizeof(R) * NH, cudaMemcpyHostToDevice, st));
+        PBI4G_CUDA(cudaStreamSynchronize(st));
+        wcache.N = N;
+        wcache.nintp = nintp;
+        wcache.rsize = (int)sizeof(R);
     }
+    DevBuf &cache = wcache.buf;
     const double kF3 = fcomb_kF3(box);
     const double cf = (interlaced ? 1.0 / (4.0 * kF3) : 1.0 / kF3) / norm;
     if (interlaced) {
@@ -187,8 +189,10 @@ int fcomb_half(int N, int nintp, bool interlaced, float box, double norm, const 
     return PBI4G_OK;
 }
 
-template int fcomb_half<float>(int, int, bool, float, double, const float2 *, float2 *, cudaStream_t, int64_t *);
-template int fcomb_half<double>(int, int, bool, float, double, const double2 *, double2 *, cudaStream_t, int64_t *);
+template int fcomb_half<float>(int, int, bool, float, double, const float2 *, float2 *, WinCache &, cudaStream_t,
+                               int64_t *);
+template int fcomb_half<double>(int, int, bool, float, double, const double2 *, double2 *, WinCache &, cudaStream_t,
+                                int64_t *);
 
 // ------------------------------------------------ fcomb on full grids (FP64) ---
 __global__ void fcomb_interlaced_full_kernel(int N, const double2 *in, double2 *out, const double *__restrict__ tW,

@@ -22,12 +22,18 @@ struct PkBins {
     int build(int N, float box, float kbin, float kcenter, int nbins, cudaStream_t st, int64_t *launches);
 };
 
+// Device copy of the 1/W window table used by fcomb_half.
+struct WinCache {
+    DevBuf buf;
+    int N = -1, nintp = -1, rsize = -1;
+};
+
 // fcomb on the R2C half spectra of one (non-interlaced) or two (interlaced)
 // real grids: spec [G][N][N][N/2+1] -> delta [N][N][N/2+1], including the
 // 1/norm normalisation (dcl /= npart, pbi4.py:336).
 template <class R>
 int fcomb_half(int N, int nintp, bool interlaced, float box, double norm, const typename Cx<R>::T *spec,
-               typename Cx<R>::T *delta, cudaStream_t st, int64_t *launches);
+               typename Cx<R>::T *delta, WinCache &wcache, cudaStream_t st, int64_t *launches);
 
 // Full-grid fcomb (drop-in, FP64), in place allowed.
 int fcomb_full(int N, int nintp, bool interlaced, float box, const double2 *in, double2 *out, cudaStream_t st);

@@ -172,6 +172,19 @@ class Estimator:
         check(lib().pbi4g_plan_triangle_counts(self._h, out.ctypes.data))
         return out
 
+    def set_delta_half(self, npart: int, half: np.ndarray):
+        h = np.ascontiguousarray(half, dtype=np.complex128)
+        n = int(self.cfg.grid)
+        if h.shape != (n, n, n // 2 + 1):
+            raise ValueError(f"expected a ({n},{n},{n // 2 + 1}) half spectrum")
+        check(lib().pbi4g_plan_set_delta_half(self._h, int(npart), h.ctypes.data))
+
+    def set_counts(self, counts: np.ndarray):
+        c = np.ascontiguousarray(counts, dtype=np.float64)
+        if c.shape[0] < self.itot:
+            raise ValueError(f"counts has {c.shape[0]} entries, itot={self.itot}")
+        check(lib().pbi4g_plan_set_counts(self._h, c.ctypes.data))
+
     def delta_half(self) -> np.ndarray:
         n = int(self.cfg.grid)
         out = np.empty((n, n, n // 2 + 1), dtype=np.complex128)

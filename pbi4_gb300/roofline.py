@@ -55,23 +55,35 @@ def stage_work(cfg, npart):
     }
 
 
-def for_stages(stages, steps, cfg, npart, tri_flops=None):
-    """Roofline object of the dominant own-kernel HBM stage (library FFT stages excluded)."""
+def for_stages(stages, steps, cfg, npart, itot=None):
+    """Roofline object of the dominant stage among this library's kernels (the
+    cuFFT stages are library calls and are reported only in the stage times).
+    Tensor-core triangle sums count the useful flops 2 N^3 itot S against the
+    measured bf16 dense peak; HBM stages count their algorithmic bytes."""
     pk = peaks()
-    work = stage_work(cfg, npart)
+    work = dict(stage_work(cfg, npart))
+    if itot and cfg.precision in ("fp16split", "bf16"):
+        nsets = 3 if cfg.multipoles else 1
+        work["triangle_sums"] = ("tensor", 2.0 * int(cfg.grid) ** 3 * itot * nsets)
     best = None
-    for name, (bound, nbytes) in work.items():
+    for name, (bound, amount) in work.items():
         ms, calls = stages.get(name, (0.0, 0))
         if calls == 0 or ms <= 0:
             continue
         avg_ms = ms / calls
         if best is None or avg_ms > best[1]:
-            best = (name, avg_ms, nbytes)
+            best = (name, avg_ms, amount, bound)
     if best is None:
         return None
-    name, avg_ms, nbytes = best
-    achieved = nbytes / (avg_ms * 1e-3) / 1e9
+    name, avg_ms, amount, bound = best
     tt = traffic_table().get(name)
+    if bound == "tensor":
+        achieved = amount / (avg_ms * 1e-3) / 1e12
+        peak = pk["bf16_tflops"]
+        return {"kernel": "trisum_tc_kernel", "stage": name, "bound": "tensor", "achieved": round(achieved, 2),
+                "peak": peak, "unit": "TFLOP/s", "frac": round(achieved / peak, 5), "traffic": tt,
+                "algorithmic_flops": amount, "avg_ms": round(avg_ms, 4), "peak_source": pk["source"]}
+    achieved = amount / (avg_ms * 1e-3) / 1e9
     return {"kernel": name, "bound": "hbm", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
-            "frac": round(achieved / pk["hbm_gbs"], 4), "traffic": tt, "algorithmic_bytes": nbytes,
+            "frac": round(achieved / pk["hbm_gbs"], 4), "traffic": tt, "algorithmic_bytes": amount,
             "avg_ms": round(avg_ms, 4), "peak_source": pk["source"]}

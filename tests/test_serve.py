@@ -1,0 +1,69 @@
+"""Serving loop: each box's result is the same alone and in the mix.
+
+Boxes of several configurations (grid sizes, assignment orders, interlacing,
+P-only and P+B, FP32 and FP16-split) are submitted at once to a Server with
+three CUDA-stream slots; every result is compared with the same box run alone
+on a fresh plan.  Tolerance: 1e-6 relative (the only differences allowed are
+the ordering of floating-point atomics in the P bins and shell powers); mode
+and triangle counts identical.  A second run squeezes the HBM budget so plans
+are evicted and rebuilt, with the same check.
+"""
+import numpy as np
+import pytest
+
+from pbi4_gb300 import synthetic
+from pbi4_gb300.estimator import Estimator, EstimatorConfig
+from pbi4_gb300.serve import Request, Server
+
+pytestmark = pytest.mark.gpu
+
+
+def _requests():
+    cfgs = [
+        EstimatorConfig(grid=32, box=1000.0, nintp=4, interlacing=True, multipoles=True, kbin_bs=2.0, kcenter_bs=2.0),
+        EstimatorConfig(grid=48, box=800.0, nintp=2, interlacing=False, multipoles=False, do_bispectrum=False),
+        EstimatorConfig(grid=64, box=1000.0, nintp=3, interlacing=True, multipoles=False, kbin_bs=4.0,
+                        kcenter_bs=4.0, precision="fp16split"),
+    ]
+    reqs = []
+    rng = np.random.default_rng(5)
+    for k in range(9):
+        cfg = cfgs[k % 3]
+        n = int(rng.integers(5000, 40000))
+        pos = synthetic.uniform_box(n, seed=100 + k) if k % 2 else synthetic.zeldovich_box(20 + k, 1000.0, seed=k)
+        reqs.append(Request(cfg=cfg, pos=pos, rid=k))
+    return reqs
+
+
+def _check(results, reqs):
+    for r in reqs:
+        res = results[r.rid]
+        alone = Estimator(r.cfg)
+        pout, bout = alone.run_host(r.pos)
+        alone.close()
+        np.testing.assert_array_equal(res.pout[4 if r.cfg.multipoles else 2], pout[4 if r.cfg.multipoles else 2])
+        ok = pout[1] != 0
+        assert np.max(np.abs(res.pout[1][ok] / pout[1][ok] - 1)) < 1e-6
+        if bout is not None:
+            np.testing.assert_array_equal(res.bout[8], bout[8])
+            scale = np.maximum(np.abs(bout[6]), np.abs(bout[3] * bout[4]))
+            assert np.max(np.abs(res.bout[6] - bout[6]) / scale) < 1e-6
+
+
+@pytest.mark.parametrize("tight", [False, True])
+def test_serving_mix_matches_alone(tight):
+    from pbi4_gb300.estimator import footprint
+    reqs = _requests()
+    max_npart = 50000
+    fp = sorted({footprint(r.cfg, max_npart) for r in reqs})
+    # tight: room for the two largest plans only, so the loop must evict and rebuild
+    budget = int(fp[-1] + fp[-2] + 1) if tight else int(40e9)
+    srv = Server(hbm_budget_bytes=budget, slots=3, max_npart=max_npart)
+    futs = [srv.submit(r) for r in reqs]
+    results = {f.result(timeout=300).rid: f.result() for f in futs}
+    stats = srv.stats()
+    srv.close()
+    assert stats["n"] == len(reqs) and stats["p99_ms"] >= stats["p50_ms"] > 0
+    if tight:
+        assert stats["evictions"] > 0
+    _check(results, reqs)
