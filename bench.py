@@ -62,7 +62,7 @@ class ClockSampler:
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -94,74 +94,140 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------ CPU legs ---
-def cpu_reference_box_seconds(pos, budget_s=20.0):
-    """Seconds per box of the CPU restatement of the reference, from a bounded
-    sample: assignment (full), one density FFT, fcomb, one of the 21
-    multipole FFTs (x22), measure_pk_multipoles, one shell-map FFT (x63) and a
-    subset of the triangle sums (extrapolated to all 1156 x 3 sums)."""
-    import scipy.fft
+class ReferenceSampler:
+    """Seconds per box of the CPU restatement of the reference (oracle/: the
+    Fortran loops in C, serial as in the reference; FFTs through scipy on all
+    host cores), timed stage by stage on bounded samples of the workload:
+      assign          a fraction of the particles, extrapolated linearly
+      fft, fcomb, pk  one density FFT, the interlacing combine, P(k) multipole binning
+      multipoles      one of the 22 FFT passes of compute_density_multipoles (x22)
+      maps            one of the 3 x 21 shell-map FFTs (x63)
+      triangle_sums   a few triangles of the serial FP64 triple sum (x1156 / n)
+    A step times every stage (`rotate=False`) or, for long runs, the assignment,
+    the triangles and one of the three FFT groups in turn; the box time of a
+    step is the sum of the latest timing of every stage."""
 
-    from oracle import pbi4_oracle as O
-    w = WORKLOAD
-    N, cores = w["grid"], os.cpu_count() or 1
-    p = dict(grid=N, box=w["box"], interpolation=w["nintp"], interlacing=w["interlacing"], multipoles=True,
-             kbin=w["kbin_ps"], kcenter=w["kcenter_ps"], iopen=True, los=w["los"], cross=False, om=0.3, ol=0.7,
-             z=0.5)
-    p.update(O.derived_params(p))
-    t = {}
-    t0 = time.perf_counter()
-    npart, dcl = O.assign_grid(pos, p)
-    t["assign"] = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    f = scipy.fft.fftn(dcl / npart, workers=cores)
-    t["fft"] = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    d = O.fcomb(N, w["nintp"], True, w["box"], f)
-    t["fcomb"] = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    dx = scipy.fft.ifftn(d, workers=cores)
-    q = O.compute_q2k(N, w["box"], scipy.fft.fftn(dx * 1.0, workers=cores), 3, 3)
-    t["multipoles"] = (time.perf_counter() - t0) * 22  # 1 ifftn + 21 fftn/q-factor passes
-    d2 = -0.5 * d + 1.5 * q
-    t0 = time.perf_counter()
-    O.measure_pk_multipoles(N, w["box"], 1.0, 1.0, w["nbins_ps"], d, d2, d2)
-    t["pk"] = time.perf_counter() - t0
-    nb = w["nbins_bs"]
-    full = O.hermitian_full_grid(d)
-    shell = O.shell_index(N, w["kbin_bs"], w["kcenter_bs"])
-    t0 = time.perf_counter()
-    m = scipy.fft.fftn(np.where(shell == 5, full, 0.0), workers=cores).real.ravel()
-    t["maps"] = (time.perf_counter() - t0) * 3 * nb
-    # triangle sums: time a few triangles of the serial FP64 loop (bispectrumI4.f90:484-488)
-    maps = np.stack([m, m, m])
-    ntri = 0
-    t0 = time.perf_counter()
-    counts = np.ones(1, dtype=np.float32)
-    bout = np.zeros((11, 1))
-    while time.perf_counter() - t0 < min(budget_s, 6.0) and ntri < 50:
-        O.lib().or_bk_multipoles_last_sum(1, 3.0, 3.0, 1, 0.00628, int(npart), N ** 3,
-                                          counts.ctypes.data_as(O._f), O._p(maps), O._p(maps), O._p(maps),
-                                          O._p(np.zeros(1)), O._p(bout))
-        ntri += 1
-    per_tri = (time.perf_counter() - t0) / ntri
-    t["triangle_sums"] = per_tri * 1156
-    total = sum(t.values())
-    sample = (f"full assignment + 1 density FFT + fcomb + P binning; 1 of 22 multipole FFT passes (x22), 1 of 63 "
-              f"shell-map FFTs (x63), {ntri} of 1156 triangle triple-sums (x1156/{ntri}); FFTs on {cores} threads, "
-              f"Fortran loops serial as in the reference")
-    return total, t, sample, cores
+    def __init__(self, pos, assign_fraction=1.0, tri_budget_s=2.0, rotate=False):
+        import scipy.fft
+
+        from oracle import pbi4_oracle as O
+        self.O, self.fft = O, scipy.fft
+        w = WORKLOAD
+        self.N, self.cores = w["grid"], os.cpu_count() or 1
+        p = dict(grid=self.N, box=w["box"], interpolation=w["nintp"], interlacing=w["interlacing"], multipoles=True,
+                 kbin=w["kbin_ps"], kcenter=w["kcenter_ps"], iopen=True, los=w["los"], cross=False, om=0.3, ol=0.7,
+                 z=0.5)
+        p.update(O.derived_params(p))
+        self.p, self.pos = p, pos
+        self.nsub = max(1, int(round(pos.shape[1] * assign_fraction)))
+        self.sub = np.ascontiguousarray(pos[:, : self.nsub])
+        self.tri_budget, self.rotate, self.k = tri_budget_s, rotate, 0
+        # one real density (the full assignment, untimed) feeds the FFT-side stages
+        npart, dcl = O.assign_grid(pos, p)
+        self.npart, self.dcl = npart, dcl
+        d = O.compute_density(npart, dcl, p, workers=self.cores)
+        self.d = d
+        shell = O.shell_index(self.N, w["kbin_bs"], w["kcenter_bs"])
+        self.shell_in = np.where(shell == 5, O.hermitian_full_grid(d), 0.0)
+        self.latest = {}
+        self.ntri = 0
+
+    def _assign(self):
+        t0 = time.perf_counter()
+        self.O.assign_grid(self.sub, self.p)
+        self.latest["assign"] = (time.perf_counter() - t0) * self.pos.shape[1] / self.nsub
+
+    def _density(self):
+        O, N, w = self.O, self.N, WORKLOAD
+        t0 = time.perf_counter()
+        f = self.fft.fftn(self.dcl / self.npart, workers=self.cores)
+        self.latest["fft"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        d = O.fcomb(N, w["nintp"], True, w["box"], f)
+        self.latest["fcomb"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        O.measure_pk_multipoles(N, w["box"], 1.0, 1.0, w["nbins_ps"], d, d, d)
+        self.latest["pk"] = time.perf_counter() - t0
+
+    def _multipoles(self):
+        O, N, w = self.O, self.N, WORKLOAD
+        t0 = time.perf_counter()
+        dx = self.fft.ifftn(self.d, workers=self.cores)
+        O.compute_q2k(N, w["box"], self.fft.fftn(dx * 1.0, workers=self.cores), 3, 3)
+        self.latest["multipoles"] = (time.perf_counter() - t0) * 22  # 1 ifftn + 21 fftn/q-factor passes
+
+    def _maps(self):
+        t0 = time.perf_counter()
+        self.m = self.fft.fftn(self.shell_in, workers=self.cores).real.ravel()
+        self.latest["maps"] = (time.perf_counter() - t0) * 3 * WORKLOAD["nbins_bs"]
+
+    def _triangles(self):
+        O, N = self.O, self.N
+        maps = np.stack([self.m, self.m, self.m])
+        counts = np.ones(1, dtype=np.float32)
+        bout = np.zeros((11, 1))
+        ntri = 0
+        t0 = time.perf_counter()
+        while ntri < 1 or (time.perf_counter() - t0 < self.tri_budget and ntri < 50):
+            O.lib().or_bk_multipoles_last_sum(1, 3.0, 3.0, 1, 0.00628, int(self.npart), N ** 3,
+                                              counts.ctypes.data_as(O._f), O._p(maps), O._p(maps), O._p(maps),
+                                              O._p(np.zeros(1)), O._p(bout))
+            ntri += 1
+        self.ntri = ntri
+        self.latest["triangle_sums"] = (time.perf_counter() - t0) / ntri * 1156
+
+    def step(self):
+        """Time one step's sample; return the box time in seconds."""
+        groups = (self._density, self._multipoles, self._maps)
+        if self.k == 0 or not self.rotate:
+            for g in groups:
+                g()
+        else:
+            groups[self.k % 3]()
+            if self.k % 3 != 2 and "maps" not in self.latest:
+                self._maps()
+        self._assign()
+        self._triangles()
+        self.k += 1
+        return sum(self.latest.values())
+
+    def sample(self):
+        n = self.pos.shape[1]
+        return (f"assignment of {self.nsub} of {n} particles (x{n / self.nsub:.3g}) + 1 density FFT + fcomb + P "
+                f"binning; 1 of 22 multipole FFT passes (x22), 1 of 63 shell-map FFTs (x63), {self.ntri} of 1156 "
+                f"triangle triple-sums (x1156/{self.ntri}); FFTs on {self.cores} threads, Fortran loops serial as "
+                f"in the reference" + ("; FFT groups re-timed in rotation" if self.rotate else ""))
+
+
+def cpu_reference_box_seconds(pos, budget_s=20.0):
+    """One full bounded sample (every stage timed once): (seconds per box, stage
+    seconds, sample description, cores)."""
+    rs = ReferenceSampler(pos, assign_fraction=1.0, tri_budget_s=max(1.0, budget_s / 2))
+    sec = rs.step()
+    return sec, dict(rs.latest), rs.sample(), rs.cores
 
 
 def run_reference(args):
+    """The reference's CPU path (the oracle restatement) on this host's cores:
+    each of the warmup + steps iterations times one bounded sample of a box,
+    sized so that the whole run takes a few minutes."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     from oracle import pbi4_oracle as O
     O.build()
     pos = make_positions(quick=args.quick)
+    nsteps = args.warmup + args.steps
+    per_step = min(8.0, max(1.0, 150.0 / nsteps))
+    t0 = time.perf_counter()
+    O.assign_grid(np.ascontiguousarray(pos[:, : pos.shape[1] // 16]), dict(
+        grid=WORKLOAD["grid"], interpolation=WORKLOAD["nintp"], interlacing=WORKLOAD["interlacing"]))
+    t_assign = (time.perf_counter() - t0) * 16
+    frac = min(1.0, 0.25 * per_step / max(t_assign, 1e-6))
+    rs = ReferenceSampler(pos, assign_fraction=frac, tri_budget_s=0.4 * per_step, rotate=per_step < 4.0)
     vals = []
-    for k in range(args.warmup + args.steps):
-        sec, stages, sample, cores = cpu_reference_box_seconds(pos, budget_s=5.0)
+    for k in range(nsteps):
+        sec = rs.step()
         if k >= args.warmup:
             vals.append(sec)
     sec = statistics.median(vals)
@@ -171,9 +237,10 @@ def run_reference(args):
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Zel'dovich box)",
             "config": {**{k: v for k, v in WORKLOAD.items()}, "parallelism": "cpu"},
             "impl": "reference",
-            "cpu_baseline": {"value": value, "unit": "boxes/s", "cores": cores, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": value, "unit": "boxes/s", "cores": rs.cores, "kind": "port",
+                             "sample": rs.sample()},
             "e2e": {"value": value, "unit": "boxes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "stages_s": stages}
+            "stages_s": dict(rs.latest)}
     print(json.dumps(line), flush=True)
 
 
@@ -285,7 +352,8 @@ def run_ours(args):
                                "(dk=2kf to 0.5 kNyq); cold plan creation included"}
 
     from pbi4_gb300 import roofline
-    rl = roofline.for_stages(stages, args.steps, cfg, npart, itot=est.itot)
+    rl, rl_all = roofline.for_stages(stages, args.steps, cfg, npart, itot=est.itot, map_grid=est.map_grid,
+                                     nmaps=est.nmaps)
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
@@ -296,12 +364,14 @@ def run_ours(args):
                 "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[args.precision],
                 "data": "synthetic (seeded Zel'dovich box, positions resident in HBM)",
                 "config": {**WORKLOAD, "precision": args.precision, "parallelism": f"replicas{world}",
-                           "l2": "working set > L2 (shell maps %.1f GB per box)" % (
-                               3 * WORKLOAD["nbins_bs"] * 256 * 256 * 129 * 8 / 1e9),
+                           "map_grid": est.map_grid,
+                           "l2": "working set > L2 (shell maps %.1f GB per box on the %d^3 map grid)" % (
+                               est.nmaps * est.map_grid ** 2 * (est.map_grid + 2) * 4 / 1e9, est.map_grid),
                            "triangle_counts": "computed once per plan (input independent)"},
                 "e2e": {"value": e2e_value, "unit": "boxes/s", "h2d_bytes_per_step": int(pos.nbytes),
                         "d2h_bytes_per_step": int(p_h.nbytes + b_h.nbytes)},
-                "gpu_launches": int(launches), "clocks": clocks, "roofline": rl, "cpu_baseline": cpu,
+                "gpu_launches": int(launches), "clocks": clocks, "roofline": rl, "roofline_stages": rl_all,
+                "cpu_baseline": cpu,
                 "plain_fp32": plain, "error_vs_fp64": errors, "serving": serving,
                 "stages_ms_per_box": {k: round(v[0] / max(1, args.steps), 4) for k, v in stages.items()}}
         print(json.dumps(line), flush=True)
@@ -312,7 +382,7 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", default="fp16split", choices=["fp32", "fp64", "fp16split", "bf16"])

@@ -157,6 +157,11 @@ int pbi4g_plan_destroy(pbi4g_plan *plan);
 int pbi4g_plan_set_stream(pbi4g_plan *plan, void *stream);
 /* Output sizes: pout is (5, nbins_ps), bout is (brows, itot), Fortran order. */
 int pbi4g_plan_shape(const pbi4g_plan *plan, int32_t *nbins_ps, int64_t *itot, int32_t *brows);
+
+/* Grid of the bispectrum shell maps (the smallest FFT-friendly size above
+ * 3 kmax, at most `grid`; 0 without a bispectrum) and the number of maps per
+ * box (nbins_bs, x3 with multipoles).  Sums on it are scaled by (grid/map_grid)^3. */
+int pbi4g_plan_map_grid(const pbi4g_plan *plan, int32_t *map_grid, int32_t *nmaps);
 /* Exact integer triangle counts of the plan's binning (computed once, cached). */
 int pbi4g_plan_triangle_counts(pbi4g_plan *plan, int64_t *counts_host);
 

@@ -24,7 +24,8 @@ EXPORTS = [
     "pbi4g_compute_q2k", "pbi4g_compute_q4k", "pbi4g_measure_pk", "pbi4g_measure_pk_multipoles",
     "pbi4g_count_triangles", "pbi4g_measure_bk", "pbi4g_measure_bk_multipoles", "pbi4g_measure_bk_cross",
     "pbi4g_plan_footprint", "pbi4g_plan_create", "pbi4g_plan_destroy", "pbi4g_plan_set_stream",
-    "pbi4g_plan_shape", "pbi4g_plan_triangle_counts", "pbi4g_plan_density", "pbi4g_plan_powerspectrum",
+    "pbi4g_plan_shape", "pbi4g_plan_map_grid", "pbi4g_plan_triangle_counts", "pbi4g_plan_density",
+    "pbi4g_plan_powerspectrum",
     "pbi4g_plan_bispectrum", "pbi4g_plan_run_device", "pbi4g_plan_run_host", "pbi4g_plan_get_delta_half",
     "pbi4g_plan_kernel_launches", "pbi4g_plan_enable_timing", "pbi4g_plan_stage_times",
     "pbi4g_measure_pk_multipoles_noalloc", "pbi4g_plan_set_delta_half", "pbi4g_plan_set_counts",
@@ -74,6 +75,7 @@ _SIGS = {
     "pbi4g_plan_destroy": [_P],
     "pbi4g_plan_set_stream": [_P, _P],
     "pbi4g_plan_shape": [_P, ctypes.POINTER(_i32), ctypes.POINTER(_i64), ctypes.POINTER(_i32)],
+    "pbi4g_plan_map_grid": [_P, ctypes.POINTER(_i32), ctypes.POINTER(_i32)],
     "pbi4g_plan_triangle_counts": [_P, _P],
     "pbi4g_plan_density": [_P, _i64, _P, _P],
     "pbi4g_plan_powerspectrum": [_P, _P],

@@ -279,6 +279,14 @@ int pbi4g_plan_shape(const pbi4g_plan *plan, int32_t *nbins_ps, int64_t *itot, i
     return PBI4G_OK;
 }
 
+int pbi4g_plan_map_grid(const pbi4g_plan *plan, int32_t *map_grid, int32_t *nmaps) {
+    if (!plan) return set_error(PBI4G_ERR_INVALID, "null plan");
+    const bool bk = plan->cfg.do_bispectrum != 0;
+    if (map_grid) *map_grid = bk ? plan->bk.sh.Nm : 0;
+    if (nmaps) *nmaps = bk ? (plan->cfg.multipoles ? 3 : 1) * plan->bk.sh.nb : 0;
+    return PBI4G_OK;
+}
+
 int64_t pbi4g_plan_kernel_launches(const pbi4g_plan *plan) { return plan ? plan->launches : -1; }
 
 int pbi4g_plan_triangle_counts(pbi4g_plan *plan, int64_t *counts_host) {

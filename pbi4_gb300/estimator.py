@@ -99,6 +99,9 @@ class Estimator:
         nb, it, br = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int32()
         check(lib().pbi4g_plan_shape(self._h, ctypes.byref(nb), ctypes.byref(it), ctypes.byref(br)))
         self.nbins_ps, self.itot, self.brows = nb.value, it.value, br.value
+        mg, nm = ctypes.c_int32(), ctypes.c_int32()
+        check(lib().pbi4g_plan_map_grid(self._h, ctypes.byref(mg), ctypes.byref(nm)))
+        self.map_grid, self.nmaps = mg.value, nm.value
 
     # -- lifecycle
     def close(self):

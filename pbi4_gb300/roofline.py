@@ -1,13 +1,16 @@
 """Roofline bookkeeping of the per-stage timings (algorithmic bytes / flops).
 
 Algorithmic traffic per box (N grid, H = N^2 (N/2+1) half-spectrum cells,
-G = 2 grids with interlacing, M shell maps, T triangles, S q-sets):
-  assign          24 Np (float64 xyz read) + 8 G N^3 (int64 fixed-point grid write)
-  grid_convert    8 G N^3 read + 4 G N^3 write
+G = 2 grids with interlacing, Np particles; M shell maps on the map grid Nm,
+Hm = Nm^2 (Nm/2+1); T triangles, S = 3 multipole sets or 1):
+  assign          24 Np (float64 xyz read) + 4 G N^3 (FP32 grid write; 8 G N^3
+                  int64 fixed-point for the FP64 form)
+  grid_convert    8 G N^3 read + 4 G N^3 write (FP64 form only)
   fcomb           8 G H read + 8 H write
   pk_binning      8 H read
-  shell_spectra   8 H read + 8 M H write
-  triangle_sums   2 N^3 T S flops (tensor-core forms) / maps read 4 M N^3 bytes (CUDA-core FP32)
+  shell_spectra   8 H read + 8 M Hm write
+  triangle_sums   2 Nm^3 T S flops (tensor-core forms; useful sums only)
+cuFFT stages (fft_r2c, fft_c2r) are library calls: timed, not given a roofline.
 Peaks are the measured ones in MEASURED_PEAKS.json at the repository root
 (HBM copy bandwidth, cuBLAS bf16 dense), else the documented fallback.
 """
@@ -40,50 +43,62 @@ def traffic_table():
         return {}
 
 
-def stage_work(cfg, npart):
+def stage_work(cfg, npart, map_grid=None, nmaps=None):
     N = int(cfg.grid)
     G = 2 if cfg.interlacing else 1
     H = N * N * (N // 2 + 1)
     nsets = 3 if cfg.multipoles else 1
-    M = nsets * int(cfg.nbins_bs) if cfg.do_bispectrum else 0
+    M = nmaps if nmaps is not None else (nsets * int(cfg.nbins_bs) if cfg.do_bispectrum else 0)
+    Nm = map_grid or N
+    Hm = Nm * Nm * (Nm // 2 + 1)
+    gbytes = 8 if cfg.precision == "fp64" else 4
     return {
-        "assign": ("hbm", 24 * npart + 8 * G * N ** 3),
+        "assign": ("hbm", 24 * npart + gbytes * G * N ** 3),
         "grid_convert": ("hbm", 12 * G * N ** 3),
         "fcomb": ("hbm", 8 * G * H + 8 * H),
         "pk_binning": ("hbm", 8 * H),
-        "shell_spectra": ("hbm", 8 * H + 8 * M * H),
+        "shell_spectra": ("hbm", 8 * H + 8 * M * Hm),
     }
 
 
-def for_stages(stages, steps, cfg, npart, itot=None):
-    """Roofline object of the dominant stage among this library's kernels (the
-    cuFFT stages are library calls and are reported only in the stage times).
-    Tensor-core triangle sums count the useful flops 2 N^3 itot S against the
-    measured bf16 dense peak; HBM stages count their algorithmic bytes."""
+KERNEL = {"assign": "owner_tile_kernel", "grid_convert": "fixed_to_real_kernel",
+          "fcomb": "fcomb_interlaced_half_kernel",
+          "pk_binning": "pk_accum_kernel", "shell_spectra": "build_map_spectra_kernel",
+          "triangle_sums": "trisum_tc_kernel"}
+
+
+def _entry(name, bound, amount, avg_ms, pk, traffic):
+    if bound == "tensor":
+        achieved = amount / (avg_ms * 1e-3) / 1e12
+        return {"kernel": KERNEL.get(name, name), "stage": name, "bound": "tensor", "achieved": round(achieved, 2),
+                "peak": pk["bf16_tflops"], "unit": "TFLOP/s", "frac": round(achieved / pk["bf16_tflops"], 5),
+                "traffic": traffic, "algorithmic_flops": amount, "avg_ms": round(avg_ms, 4),
+                "peak_source": pk["source"]}
+    achieved = amount / (avg_ms * 1e-3) / 1e9
+    return {"kernel": KERNEL.get(name, name), "stage": name, "bound": "hbm", "achieved": round(achieved, 1),
+            "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4), "traffic": traffic,
+            "algorithmic_bytes": amount, "avg_ms": round(avg_ms, 4), "peak_source": pk["source"]}
+
+
+def for_stages(stages, steps, cfg, npart, itot=None, map_grid=None, nmaps=None):
+    """(dominant, all): the roofline object of the slowest stage among this
+    library's kernels and the list for every timed stage.  Tensor-core triangle
+    sums count the useful flops 2 Nm^3 itot S against the measured bf16 dense
+    peak; HBM stages count their algorithmic bytes.  `traffic` is the per-launch
+    DRAM bytes of the committed ncu capture for this workload, if one exists."""
     pk = peaks()
-    work = dict(stage_work(cfg, npart))
+    work = dict(stage_work(cfg, npart, map_grid, nmaps))
     if itot and cfg.precision in ("fp16split", "bf16"):
         nsets = 3 if cfg.multipoles else 1
-        work["triangle_sums"] = ("tensor", 2.0 * int(cfg.grid) ** 3 * itot * nsets)
-    best = None
+        work["triangle_sums"] = ("tensor", 2.0 * int(map_grid or cfg.grid) ** 3 * itot * nsets)
+    table = traffic_table()
+    out = []
     for name, (bound, amount) in work.items():
         ms, calls = stages.get(name, (0.0, 0))
         if calls == 0 or ms <= 0:
             continue
-        avg_ms = ms / calls
-        if best is None or avg_ms > best[1]:
-            best = (name, avg_ms, amount, bound)
-    if best is None:
-        return None
-    name, avg_ms, amount, bound = best
-    tt = traffic_table().get(name)
-    if bound == "tensor":
-        achieved = amount / (avg_ms * 1e-3) / 1e12
-        peak = pk["bf16_tflops"]
-        return {"kernel": "trisum_tc_kernel", "stage": name, "bound": "tensor", "achieved": round(achieved, 2),
-                "peak": peak, "unit": "TFLOP/s", "frac": round(achieved / peak, 5), "traffic": tt,
-                "algorithmic_flops": amount, "avg_ms": round(avg_ms, 4), "peak_source": pk["source"]}
-    achieved = amount / (avg_ms * 1e-3) / 1e9
-    return {"kernel": name, "bound": "hbm", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
-            "frac": round(achieved / pk["hbm_gbs"], 4), "traffic": tt, "algorithmic_bytes": amount,
-            "avg_ms": round(avg_ms, 4), "peak_source": pk["source"]}
+        out.append(_entry(name, bound, amount, ms / calls, pk, table.get(name)))
+    if not out:
+        return None, []
+    best = max(out, key=lambda e: e["avg_ms"])
+    return best, out
