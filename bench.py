@@ -245,7 +245,8 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------ GPU arm ---
-DTYPE = {"fp32": "f32", "fp64": "f64", "fp16split": "fp16 hi+lo (f32 accumulate)", "bf16": "bf16 (f32 accumulate)"}
+DTYPE = {"fp32": "f32", "fp64": "f64", "fp16split": "fp16 hi+lo (f32 accumulate)", "bf16": "bf16 (f32 accumulate)",
+         "tf32split": "tf32 hi+lo (f32 accumulate)"}
 
 
 def error_report(pout, bout, p64, b64):
@@ -385,7 +386,7 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--precision", default="fp16split", choices=["fp32", "fp64", "fp16split", "bf16"])
+    ap.add_argument("--precision", default="fp16split", choices=["fp32", "fp64", "fp16split", "bf16", "tf32split"])
     ap.add_argument("--no-compare", action="store_true", help="skip the plain-FP32 and FP64 comparison runs")
     ap.add_argument("--serve-requests", type=int, default=32, help="requests in the serving leg (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=40.0, help="offered request rate of the serving leg (1/s)")

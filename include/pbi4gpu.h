@@ -47,6 +47,7 @@ extern "C" {
 #define PBI4G_PREC_FP64 1      /* FP64 everywhere (GPU oracle form) */
 #define PBI4G_PREC_FP16SPLIT 2 /* mixed: maps as FP16 hi+lo, tensor-core sums, FP32 accumulate */
 #define PBI4G_PREC_BF16 3      /* mixed: maps as BF16, tensor-core sums, FP32 accumulate */
+#define PBI4G_PREC_TF32SPLIT 4 /* mixed: maps and pair products as TF32 hi+lo, tensor-core sums, FP32 accumulate */
 
 const char *pbi4g_last_error(void);
 int pbi4g_version(void);
@@ -182,6 +183,10 @@ int pbi4g_plan_run_device(pbi4g_plan *plan, int64_t npart, const double *d_pos, 
  * pout/bout back, synchronises the plan's stream. */
 int pbi4g_plan_run_host(pbi4g_plan *plan, int64_t npart, const double *pos, const double *weight,
                         double *pout, double *bout);
+/* Synchronise the plan's stream and report PBI4G_ERR_TIMEOUT if a bounded wait
+ * inside a tensor-core launch of this plan gave up (the device launches of
+ * pbi4g_plan_run_device are asynchronous; run_host checks by itself). */
+int pbi4g_plan_check(pbi4g_plan *plan);
 /* Copy the resident delta(k) half spectrum (N, N, N/2+1) complex128, C order
  * [z][y][x], to host memory. */
 int pbi4g_plan_get_delta_half(pbi4g_plan *plan, double *host_half);

@@ -14,8 +14,9 @@ import numpy as np
 from . import build as _build
 
 PBI4G_OK = 0
-PREC_FP32, PREC_FP64, PREC_FP16SPLIT, PREC_BF16 = 0, 1, 2, 3
-PRECISIONS = {"fp32": PREC_FP32, "fp64": PREC_FP64, "fp16split": PREC_FP16SPLIT, "bf16": PREC_BF16}
+PREC_FP32, PREC_FP64, PREC_FP16SPLIT, PREC_BF16, PREC_TF32SPLIT = 0, 1, 2, 3, 4
+PRECISIONS = {"fp32": PREC_FP32, "fp64": PREC_FP64, "fp16split": PREC_FP16SPLIT, "bf16": PREC_BF16,
+              "tf32split": PREC_TF32SPLIT}
 
 # every entry point the header declares (checked by tests/test_capi.py)
 EXPORTS = [
@@ -29,6 +30,7 @@ EXPORTS = [
     "pbi4g_plan_bispectrum", "pbi4g_plan_run_device", "pbi4g_plan_run_host", "pbi4g_plan_get_delta_half",
     "pbi4g_plan_kernel_launches", "pbi4g_plan_enable_timing", "pbi4g_plan_stage_times",
     "pbi4g_measure_pk_multipoles_noalloc", "pbi4g_plan_set_delta_half", "pbi4g_plan_set_counts",
+    "pbi4g_plan_check",
 ]
 NSTAGES = 10
 STAGES = ["assign", "grid_convert", "fft_r2c", "fcomb", "pk_binning", "triangle_counts", "shell_spectra",
@@ -76,6 +78,7 @@ _SIGS = {
     "pbi4g_plan_set_stream": [_P, _P],
     "pbi4g_plan_shape": [_P, ctypes.POINTER(_i32), ctypes.POINTER(_i64), ctypes.POINTER(_i32)],
     "pbi4g_plan_map_grid": [_P, ctypes.POINTER(_i32), ctypes.POINTER(_i32)],
+    "pbi4g_plan_check": [_P],
     "pbi4g_plan_triangle_counts": [_P, _P],
     "pbi4g_plan_density": [_P, _i64, _P, _P],
     "pbi4g_plan_powerspectrum": [_P, _P],

@@ -82,7 +82,7 @@ int bk_common(int32_t nbins, int32_t grid, float kbin, float kcenter, int32_t io
                          (long long)itot, (long long)bk->sh.itot);
     bk->nsets = nsets;
     bk->cross = cross;
-    bk->tc_mode = g_dropin_precision == PBI4G_PREC_FP16SPLIT ? 1 : (g_dropin_precision == PBI4G_PREC_BF16 ? 2 : 0);
+    bk->tc_mode = tc_mode_of(g_dropin_precision);
     DevBuf h[3], hf[3], dcounts, dbout;
     for (int s = 0; s < nsrc; s++) {
         if (!fulls[s]) return set_error(PBI4G_ERR_INVALID, "null grid");
@@ -110,7 +110,7 @@ int bk_common(int32_t nbins, int32_t grid, float kbin, float kcenter, int32_t io
     }
     PBI4G_CUDA(cudaMemcpyAsync(bout, dbout.p, sizeof(double) * rows * itot, cudaMemcpyDeviceToHost, st));
     PBI4G_CUDA(cudaStreamSynchronize(st));
-    return PBI4G_OK;
+    return bk->check(st);
 }
 
 }  // namespace
@@ -118,7 +118,7 @@ int bk_common(int32_t nbins, int32_t grid, float kbin, float kcenter, int32_t io
 extern "C" {
 
 int pbi4g_set_dropin_precision(int32_t precision) {
-    if (precision < PBI4G_PREC_FP32 || precision > PBI4G_PREC_BF16)
+    if (precision < PBI4G_PREC_FP32 || precision > PBI4G_PREC_TF32SPLIT)
         return set_error(PBI4G_ERR_INVALID, "unknown precision %d", precision);
     g_dropin_precision = precision;
     return PBI4G_OK;

@@ -64,8 +64,14 @@ size_t BkEngine::footprint(int N, int nb, int nsets, int cross, bool fp64) {
     const size_t HC = half_cells(N);  // upper bound: the map grid is at most N
     const int nm = cross ? 2 * nb : nsets * nb;
     const size_t cs = fp64 ? 16 : 8;
-    // maps + a cuFFT work area of about one batch of the same size (upper estimate)
-    return 2 * (size_t)nm * HC * cs + (size_t)nb * 8 + ((size_t)1 << 26);
+    // half spectra (+ dense and blocked FP32 maps for the FP32 forms) + a cuFFT work area of
+    // about one batch of the same size (upper estimate)
+    return (fp64 ? 2 : 4) * (size_t)nm * HC * cs + (size_t)nb * 8 + ((size_t)1 << 26);
+}
+
+int BkEngine::check(cudaStream_t st) {
+    if (tmp_nsets >= 0) PBI4G_CHECK(tm_check_error(tmp, st));
+    return PBI4G_OK;
 }
 
 template <class R>
@@ -89,18 +95,24 @@ int BkEngine::run(const typename Cx<R>::T *const src[3], const int fac[3], const
     PBI4G_CHECK(powsum.ensure(sizeof(double) * 3 * nb));
     PBI4G_CHECK(S.ensure(sizeof(double) * std::max(1, tp.nslots)));
     const bool tc = tc_mode != 0 && !fp64 && !cross;
-    // set 0 always (shell powers); the other sets only when the tensor-core scale
-    // bound needs their own power (explicit delta_2 / delta_4 grids)
+    const int form = tc_mode == 1 ? 1 : (tc_mode == 2 ? 2 : 0);  // trisum_tm forms
+    if (tc && !tm_supported(sh))
+        return set_error(PBI4G_ERR_UNSUPPORTED, "tensor-core triangle sums: map grid %d with %d shells", N, nb);
+    // set 0 always (shell powers); the other sets only when the FP16 scale bound
+    // needs their own power (explicit delta_2 / delta_4 grids)
     int pow_mask = 1;
     if (tc) {
-        if (tcp_nsets != nsets) {
-            PBI4G_CHECK(tcp.build(sh, nsets));
-            tcp_nsets = nsets;
+        if (tmp_nsets != nsets) {
+            PBI4G_CHECK(tmp.build(sh, nsets));
+            tmp_nsets = nsets;
         }
-        PBI4G_CHECK(S.ensure(sizeof(double) * std::max(1, tcp.nslots)));
-        for (int s = 1; s < nsets; s++)
-            if (fac[s] == 0) pow_mask |= 1 << s;
+        PBI4G_CHECK(S.ensure(sizeof(double) * std::max(1, tmp.nslots)));
+        if (form == 1)
+            for (int s = 1; s < nsets; s++)
+                if (fac[s] == 0) pow_mask |= 1 << s;
     }
+    const size_t FCm = (size_t)N * N * N;
+    if (!fp64) PBI4G_CHECK(dense.ensure(sizeof(float) * FCm * nm));
     pf.begin(6, st);
     PBI4G_CUDA(cudaMemsetAsync(powsum.p, 0, sizeof(double) * 3 * nb, st));
     PBI4G_CHECK(build_map_spectra<R>(sh, nm, src, fac, los, maps.as<C>(), powsum.as<double>(), pow_mask, st,
@@ -109,9 +121,11 @@ int BkEngine::run(const typename Cx<R>::T *const src[3], const int fac[3], const
     if (!inv || inv_batch != nm || inv_N != N || inv_fp64 != (int)fp64) {
         if (inv) cufftDestroy(inv);
         inv = 0;
-        int n[3] = {N, N, N}, inembed[3] = {N, N, NH}, onembed[3] = {N, N, 2 * NH};
-        PBI4G_CUFFT(cufftPlanMany(&inv, 3, n, inembed, 1, (int)HC, onembed, 1, (int)(2 * HC),
-                                  fp64 ? CUFFT_Z2D : CUFFT_C2R, nm));
+        // FP64: in place (padded rows); FP32: out of place into dense N^3 maps
+        int n[3] = {N, N, N}, inembed[3] = {N, N, NH}, onembed[3] = {N, N, fp64 ? 2 * NH : N};
+        const int odist = fp64 ? (int)(2 * HC) : (int)FCm;
+        PBI4G_CUFFT(cufftPlanMany(&inv, 3, n, inembed, 1, (int)HC, onembed, 1, odist, fp64 ? CUFFT_Z2D : CUFFT_C2R,
+                                  nm));
         inv_batch = nm;
         inv_N = N;
         inv_fp64 = fp64;
@@ -121,7 +135,7 @@ int BkEngine::run(const typename Cx<R>::T *const src[3], const int fac[3], const
     if (fp64)
         PBI4G_CUFFT(cufftExecZ2D(inv, maps.as<cufftDoubleComplex>(), maps.as<cufftDoubleReal>()));
     else
-        PBI4G_CUFFT(cufftExecC2R(inv, maps.as<cufftComplex>(), maps.as<cufftReal>()));
+        PBI4G_CUFFT(cufftExecC2R(inv, maps.as<cufftComplex>(), dense.as<cufftReal>()));
     pf.end(st);
     pf.begin(8, st);
     if (tc) {
@@ -138,11 +152,12 @@ int BkEngine::run(const typename Cx<R>::T *const src[3], const int fac[3], const
             }
             lfac[s] = mx * 1.01;
         }
-        PBI4G_CHECK(triangle_sums_tc(sh, tcp, tc_mode == 1, reinterpret_cast<const float *>(maps.p), 2 * HC, 2 * NH,
-                                     powsum.as<double>(), pow_mask, lfac, mexp, partial, S.as<double>(), st,
-                                     launches));
-    } else {
+        PBI4G_CHECK(triangle_sums_tm(sh, tmp, form, dense.as<float>(), nm, powsum.as<double>(), pow_mask, lfac,
+                                     partial, S.as<double>(), st, launches));
+    } else if (fp64) {
         PBI4G_CHECK(triangle_sums<R>(sh, tp, maps.as<R>(), 2 * HC, 2 * NH, partial, S.as<double>(), st, launches));
+    } else {
+        PBI4G_CHECK(triangle_sums<float>(sh, tp, dense.as<float>(), FCm, N, partial, S.as<double>(), st, launches));
     }
     pf.end(st);
     pf.begin(9, st);
@@ -193,7 +208,7 @@ static int check_config(const pbi4g_config *c) {
     if (c->nbins_ps < 1 || !(c->kbin_ps > 0)) return set_error(PBI4G_ERR_INVALID, "bad P binning");
     if (c->do_bispectrum && (c->nbins_bs < 1 || !(c->kbin_bs > 0)))
         return set_error(PBI4G_ERR_INVALID, "bad B binning");
-    if (c->precision < PBI4G_PREC_FP32 || c->precision > PBI4G_PREC_BF16)
+    if (c->precision < PBI4G_PREC_FP32 || c->precision > PBI4G_PREC_TF32SPLIT)
         return set_error(PBI4G_ERR_INVALID, "unknown precision %d", c->precision);
     for (int k = 0; k < 7; k++)
         if (c->reserved[k]) return set_error(PBI4G_ERR_INVALID, "reserved config fields must be zero");
@@ -247,7 +262,7 @@ int pbi4g_plan_create(const pbi4g_config *cfg, pbi4g_plan **out) {
             if ((rc = p->bk.sh.build(N, cfg->kbin_bs, cfg->kcenter_bs, cfg->nbins_bs, cfg->iopen, 0, p->st))) break;
             p->bk.nsets = cfg->multipoles ? 3 : 1;
             p->bk.cross = 0;
-            p->bk.tc_mode = cfg->precision == PBI4G_PREC_FP16SPLIT ? 1 : (cfg->precision == PBI4G_PREC_BF16 ? 2 : 0);
+            p->bk.tc_mode = tc_mode_of(cfg->precision);
         }
         cudaError_t e = cudaStreamSynchronize(p->st);
         if (e != cudaSuccess) { rc = set_error(PBI4G_ERR_CUDA, "plan create: %s", cudaGetErrorString(e)); break; }
@@ -403,7 +418,13 @@ int pbi4g_plan_run_host(pbi4g_plan *p, int64_t npart, const double *pos, const d
     PBI4G_CUDA(cudaMemcpyAsync(pout, p->pout_d.p, pb, cudaMemcpyDeviceToHost, p->st));
     if (bb) PBI4G_CUDA(cudaMemcpyAsync(bout, p->bout_d.p, bb, cudaMemcpyDeviceToHost, p->st));
     PBI4G_CUDA(cudaStreamSynchronize(p->st));
-    return PBI4G_OK;
+    return p->cfg.do_bispectrum ? p->bk.check(p->st) : PBI4G_OK;
+}
+
+int pbi4g_plan_check(pbi4g_plan *p) {
+    if (!p) return set_error(PBI4G_ERR_INVALID, "null plan");
+    PBI4G_CUDA(cudaStreamSynchronize(p->st));
+    return p->cfg.do_bispectrum ? p->bk.check(p->st) : PBI4G_OK;
 }
 
 int pbi4g_plan_enable_timing(pbi4g_plan *p, int32_t enable) {

@@ -1,7 +1,7 @@
 // engine.cuh -- bispectrum engine shared by the plan and the drop-in entry points.
 #pragma once
 #include "bispec.cuh"
-#include "trisum_tc.cuh"
+#include "trisum_tm.cuh"
 
 namespace pbi4g {
 
@@ -19,26 +19,39 @@ struct Prof {
     void end(cudaStream_t st);
 };
 
+// Triangle-sum form of a PBI4G_PREC_* precision: 0 CUDA cores (FP32 / FP64),
+// 1 FP16 hi+lo, 2 BF16, 3 TF32 hi+lo (tensor cores).
+inline int tc_mode_of(int precision) {
+    switch (precision) {
+        case PBI4G_PREC_FP16SPLIT: return 1;
+        case PBI4G_PREC_BF16: return 2;
+        case PBI4G_PREC_TF32SPLIT: return 3;
+        default: return 0;
+    }
+}
+
 // Resident state of the bispectrum stage for one (grid, binning, sets) layout.
 struct BkEngine {
     Shells sh;
     TriPlan tp;
     int tp_nsets = -1, tp_cross = -1, tp_fp64 = -1;
     int nsets = 1, cross = 0;  // cross: 1 => q maps from the second field
-    DevBuf maps;               // [nmaps][N][N][N/2+1] complex = padded real maps after C2R
+    DevBuf maps;               // [nmaps][N][N][N/2+1] complex half spectra (FP64: padded real maps after C2R)
+    DevBuf dense;              // FP32 forms: [nmaps][N^3] real maps (out-of-place C2R)
     cufftHandle inv = 0;
-    int inv_batch = 0, inv_N = 0, inv_fp64 = -1;
+    int inv_batch = 0, inv_N = 0, inv_fp64 = -1;  // FP32 plans are out of place
     DevBuf powsum, S, partial;
-    // tensor-core form: 0 off (CUDA cores), 1 FP16 hi+lo, 2 BF16
+    // tensor-core form: 0 off (CUDA cores), 1 FP16 hi+lo, 2 BF16, 3 TF32 hi+lo
     int tc_mode = 0;
-    TcPlan tcp;
-    int tcp_nsets = -1;
-    DevBuf mexp;
+    TmPlan tmp;
+    int tmp_nsets = -1;
     ~BkEngine() {
         if (inv) cufftDestroy(inv);
     }
     int nmaps() const { return cross ? 2 * sh.nb : nsets * sh.nb; }
     static size_t footprint(int N, int nb, int nsets, int cross, bool fp64);
+    // PBI4G_ERR_TIMEOUT if a bounded wait of a tensor-core launch gave up (synchronises st)
+    int check(cudaStream_t st);
 
     // src[s]: half spectra (N, N, N/2+1) of set s; fac[s]: 0 none, 2/4 the
     // multipole factor from `los`.  counts_f32: device float counts[itot].

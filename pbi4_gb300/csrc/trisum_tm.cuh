@@ -1,0 +1,34 @@
+// trisum_tm.cuh -- host interface of the tensor-core triangle sums (trisum_tm.cu).
+#pragma once
+#include "bispec.cuh"
+
+namespace pbi4g {
+
+// Unit layout of the tcgen05 contraction for one (shells, q sets) layout:
+// units of one 128-pair M tile and one 64-map N tile; q = map index (set-major).
+struct TmPlan {
+    int nsets = 1, npairs = 0, nslots = 0, nunits = 0, nA = 0;
+    DevBuf units, prow, slots, err;
+    DevBuf blocked;  // the maps as [Nm^3 / 32][nmaps][32] FP32 (one contiguous read per chunk)
+    DevBuf mexp;     // FP16 form: per-map power-of-two exponents
+    int build(const Shells &sh, int nsets);
+};
+
+bool tm_supported(const Shells &sh);
+
+// S[slot] for every (triangle, set) slot on the tensor cores.  form: 0 TF32
+// hi+lo, 1 FP16 hi+lo, 2 BF16.  maps: dense FP32 maps on the map grid (map m at
+// maps + m * Nm^3, 16-byte aligned).  FP16 form only: powsum[s*nb + b] is the
+// full-grid sum of |H|^2 per set and shell (sets in pow_mask), which with the
+// shell's mode count bounds max |M| and sets each map's scale; lfac[s] bounds
+// |L_l| for sets without their own power.
+int triangle_sums_tm(const Shells &sh, TmPlan &tp, int form, const float *maps, int nmaps, const double *powsum,
+                     int pow_mask, const double lfac[3], DevBuf &partial, double *S, cudaStream_t st,
+                     int64_t *launches);
+// PBI4G_ERR_TIMEOUT if a bounded wait inside the last launch gave up (synchronises st).
+int tm_check_error(TmPlan &tp, cudaStream_t st);
+
+// deterministic reduction of [ksplit][nslots] partial sums (bispec.cu)
+int reduce_partials(int nslots, int ksplit, const double *partial, double *S, cudaStream_t st);
+
+}  // namespace pbi4g

@@ -148,6 +148,10 @@ class Estimator:
     def run_device(self, npart: int, pos, pout, bout=None, weight=None):
         check(lib().pbi4g_plan_run_device(self._h, int(npart), ptr(pos), ptr(weight), ptr(pout), ptr(bout)))
 
+    def check(self):
+        """Synchronise and raise if a bounded wait inside a tensor-core launch gave up."""
+        check(lib().pbi4g_plan_check(self._h))
+
     def alloc_outputs(self, device="cuda"):
         """Device output tensors (pout (5, nbins_ps), bout (brows, itot)) in Fortran layout."""
         import torch

@@ -64,8 +64,7 @@ def stage_work(cfg, npart, map_grid=None, nmaps=None):
 KERNEL = {"assign": "owner_tile_kernel", "grid_convert": "fixed_to_real_kernel",
           "fcomb": "fcomb_interlaced_half_kernel",
           "pk_binning": "pk_accum_kernel", "shell_spectra": "build_map_spectra_kernel",
-          "triangle_sums": "trisum_tc_kernel"}
-
+          "triangle_sums": "trisum_tm_kernel"}
 
 def _entry(name, bound, amount, avg_ms, pk, traffic):
     if bound == "tensor":
@@ -88,7 +87,7 @@ def for_stages(stages, steps, cfg, npart, itot=None, map_grid=None, nmaps=None):
     DRAM bytes of the committed ncu capture for this workload, if one exists."""
     pk = peaks()
     work = dict(stage_work(cfg, npart, map_grid, nmaps))
-    if itot and cfg.precision in ("fp16split", "bf16"):
+    if itot and cfg.precision in ("fp16split", "bf16", "tf32split"):
         nsets = 3 if cfg.multipoles else 1
         work["triangle_sums"] = ("tensor", 2.0 * int(map_grid or cfg.grid) ** 3 * itot * nsets)
     table = traffic_table()
