@@ -25,7 +25,7 @@
 //   * a TMA warp loads the chunk's set-0 maps (the pair factors) and the 64
 //     maps of the N tile, FP32, 128-byte swizzled, into a ring of shared-memory
 //     stages;
-//   * two producer warpgroups take the chunks in turn (thread = TMEM lane =
+//   * three producer warpgroups take the chunks in turn (thread = TMEM lane =
 //     pair row): they form the 64 products of their pair, split them and store
 //     them straight into a tensor-memory A stage with tcgen05.st (the A operand
 //     never touches shared memory), and turn the FP32 B tile into the MMA
@@ -69,19 +69,18 @@ constexpr int kN = 64;           // maps per unit (MMA N)
 constexpr int kKB = 32;          // FP32 values per 128-byte swizzle row (one K block)
 constexpr int kBlocks = 2;       // K blocks per chunk
 constexpr int kKC = kKB * kBlocks;  // grid points per chunk
-constexpr int kMaxStages = 4;    // shared-memory stages
-constexpr int kGroups = 2;       // producer warpgroups, chunks assigned round robin
+constexpr int kMaxStages = 8;    // TMA staging slots (released by the producers)
+constexpr int kGroups = 3;       // producer warpgroups, chunks assigned round robin
 constexpr int kProdWarps = 4 * kGroups;
 constexpr int kDrainWarps = 8;   // two warpgroups, 32 accumulator columns each
 constexpr int kMmaWarp = kProdWarps + kDrainWarps;
 constexpr int kTmaWarp = kMmaWarp + 1;
-constexpr int kThreads = (kTmaWarp + 1) * 32;  // 576
+constexpr int kThreads = (kTmaWarp + 1) * 32;  // 704
 constexpr int kFold = 16;        // chunks summed in registers before a Kahan fold
 constexpr int kAcc = 4;          // TMEM accumulators (one chunk each)
 constexpr int kDone = 16;        // per-chunk MMA completion barriers (ring)
 constexpr uint32_t kColAcc = 0;  // kAcc accumulators of kN columns, then the A stages
 constexpr uint32_t kColA = kAcc * kN;
-constexpr uint32_t kKahanBytes = 2 * kN * kM * 4;  // Kahan sum and compensation in shared memory
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kBBlock = kN * 128;   // bytes of one 128-byte-row tile of the N tile
 constexpr uint32_t kTfMask = 0xFFFFE000u;
@@ -93,6 +92,7 @@ template <int F> struct Form;
 template <> struct Form<kFormTF32> {
     static constexpr uint32_t kACols = 2 * kKC;
     static constexpr int kAStages = 2;
+    static constexpr int kOpSlots = 2;
     static constexpr int kKStep = 8;
     static constexpr bool kSplit = true;
     static constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kN >> 3) << 17) |
@@ -102,6 +102,7 @@ template <> struct Form<kFormTF32> {
 template <> struct Form<kFormF16> {
     static constexpr uint32_t kACols = kKC;
     static constexpr int kAStages = 4;
+    static constexpr int kOpSlots = 4;
     static constexpr int kKStep = 16;
     static constexpr bool kSplit = true;
     static constexpr uint32_t kIdesc = (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(kN >> 3) << 17) |
@@ -111,6 +112,7 @@ template <> struct Form<kFormF16> {
 template <> struct Form<kFormBF16> {
     static constexpr uint32_t kACols = kKC / 2;
     static constexpr int kAStages = 4;
+    static constexpr int kOpSlots = 4;
     static constexpr int kKStep = 16;
     static constexpr bool kSplit = false;
     static constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kN >> 3) << 17) |
@@ -192,7 +194,8 @@ __device__ __forceinline__ void pack2(float x, float y, uint32_t &hi, uint32_t &
 struct TmArgs {
     long long nchunks;     // K / kKC
     int nunits, ksplit, nslots, nA, nstages, nmaps;
-    uint32_t stage_bytes, ablock, bar_bytes;
+    uint32_t stage_bytes, op_bytes, ablock;
+    float *kahan;          // [grid][2][kN][kM] running sum and compensation of each CTA (L2-resident)
     const int2 *units;     // (M tile, N tile) per unit
     const int2 *prow;      // [nunits][kM] staged rows (i, j) of each pair's factors, (-1, -1) for none
     const int *slots;      // [nunits][kM][kN] output slot or -1
@@ -206,21 +209,24 @@ __global__ void __launch_bounds__(kThreads, 1)
     trisum_tm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                      const TmArgs a) {
     using FM = Form<F>;
-    constexpr int AST = FM::kAStages;
+    constexpr int AST = FM::kAStages, kOpSlots = FM::kOpSlots;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *base =
         reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     const int nst = a.nstages;
     // barriers: full per smem stage (TMA -> producers), prod per A stage (producers -> MMA),
     // done per chunk ring (MMA completion -> TMA, producers, drain), accfree per accumulator (drain -> MMA)
-    uint64_t *bars = reinterpret_cast<uint64_t *>(base + (size_t)nst * a.stage_bytes);
-    uint64_t *full = bars, *prod = full + kMaxStages, *done = prod + 4, *accfree = done + kDone;
+    // smem: nst staging slots | kOpSlots operand slots | barriers and tables
+    unsigned char *opbase = base + (size_t)nst * a.stage_bytes;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(opbase + (size_t)kOpSlots * a.op_bytes);
+    uint64_t *full = bars, *sfree = full + kMaxStages, *prod = sfree + kMaxStages, *done = prod + 4;
+    uint64_t *accfree = done + kDone;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(accfree + kAcc);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
     int2 *prow_s = reinterpret_cast<int2 *>(tmem_slot + 4);
     int *qexp_s = reinterpret_cast<int *>(prow_s + kM);  // [kN] FP16 exponent of each B row
-    float *run_s = reinterpret_cast<float *>(base + (size_t)nst * a.stage_bytes + a.bar_bytes);
-    float *comp_s = run_s + kN * kM;
+    float *run_g = a.kahan + (size_t)blockIdx.x * 2 * kN * kM;  // [kN][kM], then the compensation
+    float *comp_g = run_g + kN * kM;
 
     const int unit = blockIdx.x % a.nunits, split = blockIdx.x / a.nunits;
     const int2 U = a.units[unit];
@@ -234,7 +240,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         qexp_s[r] = (F == kFormF16 && q < a.nmaps) ? a.mexp[q] : 0;
     }
     if (tid == 0) {
-        for (int s = 0; s < kMaxStages; s++) mbar_init(&full[s], 1);
+        for (int s = 0; s < kMaxStages; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&sfree[s], 128);  // the warpgroup that consumed the slot
+        }
         for (int s = 0; s < 4; s++) mbar_init(&prod[s], 128);  // one warpgroup per chunk
         for (int s = 0; s < kDone; s++) mbar_init(&done[s], 1);
         for (int s = 0; s < kAcc; s++) mbar_init(&accfree[s], kDrainWarps * 32);
@@ -250,9 +259,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
-    // stage layout: A-source blocks [kBlocks][ablock] | B FP32 blocks [kBlocks][kBBlock] |
-    //               B lo (TF32: FP32 blocks) or B 16-bit hi, lo tiles [2][kBBlock]
+    // staging slot: A-source blocks [kBlocks][ablock] | B FP32 blocks [kBlocks][kBBlock]
+    // operand slot: TF32 hi, lo blocks [2][kBlocks][kBBlock]; FP16/BF16 hi, lo tiles [2][kBBlock]
     auto stage_ptr = [&](int s) { return base + (size_t)s * a.stage_bytes; };
+    auto op_ptr = [&](int o) { return opbase + (size_t)o * a.op_bytes; };
     auto fail = [&]() {
         *abort_flag = 1;
         atomicExch(a.err, 1);
@@ -268,15 +278,23 @@ __global__ void __launch_bounds__(kThreads, 1)
         const uint32_t lane_addr = tmem + ((uint32_t)(quad * 32) << 16);
         const int gtid = tid & 127;
         for (long long i = grp; i < n; i += kGroups) {
-            const int s = (int)(i % nst), as = (int)(i % AST);
+            const int s = (int)(i % nst), as = (int)(i % AST), o = (int)(i % kOpSlots);
             if (!warp_wait(&full[s], ph(i, nst), abort_flag)) { fail(); break; }
+            // the A stage and the operand slot are free once the MMAs of chunk
+            // i - min(AST, kOpSlots) completed (MMAs complete in order)
+            constexpr int kBack = AST < kOpSlots ? AST : kOpSlots;
+            if (i >= kBack && !warp_wait(&done[(i - kBack) % kDone], ph(i - kBack, kDone), abort_flag)) {
+                fail();
+                break;
+            }
             unsigned char *stg = stage_ptr(s);
-            unsigned char *bf = stg + kBlocks * a.ablock;  // FP32 B tile (kBlocks blocks)
-            unsigned char *bx = bf + kBlocks * kBBlock;    // TF32: lo blocks; 16-bit: hi tile, lo tile
+            const unsigned char *bf = stg + kBlocks * a.ablock;  // FP32 B tile (kBlocks blocks)
+            unsigned char *bx = op_ptr(o);
             if constexpr (F == kFormTF32) {
-                // hi in place, lo copy (elementwise on the swizzled bytes)
-                float4 *bv = reinterpret_cast<float4 *>(bf);
-                float4 *lv = reinterpret_cast<float4 *>(bx);
+                // hi and lo blocks, elementwise on the swizzled bytes
+                const float4 *bv = reinterpret_cast<const float4 *>(bf);
+                float4 *hv = reinterpret_cast<float4 *>(bx);
+                float4 *lv = reinterpret_cast<float4 *>(bx + kBlocks * kBBlock);
 #pragma unroll
                 for (int e = 0; e < (int)(kBlocks * kBBlock / 16) / 128; e++) {
                     const int idx = gtid + e * 128;
@@ -286,7 +304,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                     h.y = __uint_as_float(__float_as_uint(v.y) & kTfMask); l.y = v.y - h.y;
                     h.z = __uint_as_float(__float_as_uint(v.z) & kTfMask); l.z = v.z - h.z;
                     h.w = __uint_as_float(__float_as_uint(v.w) & kTfMask); l.w = v.w - h.w;
-                    bv[idx] = h;
+                    hv[idx] = h;
                     lv[idx] = l;
                 }
             } else {
@@ -309,11 +327,6 @@ __global__ void __launch_bounds__(kThreads, 1)
                     *reinterpret_cast<uint4 *>(bx + off) = make_uint4(h[0], h[1], h[2], h[3]);
                     if (FM::kSplit) *reinterpret_cast<uint4 *>(bx + kBBlock + off) = make_uint4(l[0], l[1], l[2], l[3]);
                 }
-            }
-            // A stage `as` is free once the MMAs of chunk i - AST completed
-            if (i >= AST && !warp_wait(&done[(i - AST) % kDone], ph(i - AST, kDone), abort_flag)) {
-                fail();
-                break;
             }
             const uint32_t acol = kColA + (uint32_t)as * FM::kACols;
 #pragma unroll
@@ -369,6 +382,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                     if (FM::kSplit) tmem_st16(lane_addr + col + kKC / 2, lo);
                 }
             }
+            mbar_arrive(&sfree[s]);  // staging slot consumed (its values are in registers / TMEM / the operand slot)
             tmem_wait_st();
             fence_proxy_async();  // the B operand written by these threads is read by the tensor core
             tc_fence_before();
@@ -386,29 +400,28 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
         for (int e = 0; e < 32; e++) {
             mid[e] = 0.f;
-            run_s[(c0 + e) * kM + row] = 0.f;
-            comp_s[(c0 + e) * kM + row] = 0.f;
+            run_g[(c0 + e) * kM + row] = 0.f;
+            comp_g[(c0 + e) * kM + row] = 0.f;
         }
         bool ok = true;
         for (long long i = 0; i < n; i++) {
             const int b = (int)(i % kAcc);
             if (!warp_wait(&done[i % kDone], ph(i, kDone), abort_flag)) { fail(); ok = false; break; }
             tc_fence_after();
-            uint32_t ac0[16], ac1[16];
-            tmem_ld16(lane_addr + kColAcc + (uint32_t)b * kN + c0, ac0);
-            tmem_ld16(lane_addr + kColAcc + (uint32_t)b * kN + c0 + 16, ac1);
-            tmem_wait_ld();
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                uint32_t ac[16];
+                tmem_ld16(lane_addr + kColAcc + (uint32_t)b * kN + c0 + 16 * h, ac);
+                tmem_wait_ld();
+#pragma unroll
+                for (int e = 0; e < 16; e++) mid[16 * h + e] += __uint_as_float(ac[e]);
+            }
             tc_fence_before();
             mbar_arrive(&accfree[b]);
-#pragma unroll
-            for (int e = 0; e < 16; e++) {
-                mid[e] += __uint_as_float(ac0[e]);
-                mid[16 + e] += __uint_as_float(ac1[e]);
-            }
             if ((i + 1) % kFold == 0 || i == n - 1) {
 #pragma unroll
                 for (int e = 0; e < 32; e++) {
-                    float *pr_ = run_s + (c0 + e) * kM + row, *pc = comp_s + (c0 + e) * kM + row;
+                    float *pr_ = run_g + (c0 + e) * kM + row, *pc = comp_g + (c0 + e) * kM + row;
                     const float y = mid[e] - *pc;
                     const float sm = *pr_;
                     const float t2 = sm + y;
@@ -426,7 +439,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int e = 0; e < 32; e++) {
                 const int slot = sl[c0 + e];
                 if (slot < 0) continue;
-                const double v = (double)run_s[(c0 + e) * kM + row] - (double)comp_s[(c0 + e) * kM + row];
+                const double v = (double)run_g[(c0 + e) * kM + row] - (double)comp_g[(c0 + e) * kM + row];
                 a.partial[(size_t)split * a.nslots + slot] = F == kFormF16 ? ldexp(v, -(pe + qexp_s[c0 + e])) : v;
             }
         }
@@ -440,8 +453,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 if (i >= kAcc && !wait_or_abort(&accfree[b], ph(i - kAcc, kAcc), abort_flag)) { ok = false; break; }
                 if (!wait_or_abort(&prod[as], ph(i, AST), abort_flag)) { ok = false; break; }
                 tc_fence_after();
-                const int s = (int)(i % nst);
-                const uint32_t b0 = smem_u32(stage_ptr(s) + kBlocks * a.ablock);
+                const uint32_t b0 = smem_u32(op_ptr((int)(i % kOpSlots)));
                 const uint32_t ahi = tmem + kColA + (uint32_t)as * FM::kACols;
                 const uint32_t d = tmem + kColAcc + (uint32_t)b * kN;
 #pragma unroll
@@ -455,7 +467,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                         a_lo = a_hi + kKC;
                     } else {
                         // 16-bit rows: K-step of 16 = 32 bytes of the hi / lo tiles
-                        bh = b0 + kBlocks * kBBlock + (uint32_t)kk * 32;
+                        bh = b0 + (uint32_t)kk * 32;
                         bl = bh + kBBlock;
                         a_hi = ahi + 8 * kk;
                         a_lo = a_hi + kKC / 2;
@@ -481,8 +493,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         bool ok = true;
         for (long long j = 0; j < n; j++) {
             const int s = (int)(j % nst);
-            // stage s is free once the MMAs of chunk j - nst completed
-            if (j >= nst && !wait_or_abort(&done[(j - nst) % kDone], ph(j - nst, kDone), abort_flag)) {
+            // staging slot s is free once the producers consumed chunk j - nst
+            if (j >= nst && !wait_or_abort(&sfree[s], ph(j - nst, nst), abort_flag)) {
                 ok = false;
                 break;
             }
@@ -696,14 +708,15 @@ int triangle_sums_tm(const Shells &sh, TmPlan &tp, int form, const float *maps, 
     a.nA = tp.nA;
     a.nmaps = nmaps;
     a.ablock = (uint32_t)(((tp.nA + 7) / 8) * 8 * 128);
-    a.stage_bytes = kBlocks * (a.ablock + 2 * kBBlock);
-    // barriers, TMEM address, abort flag, pair table, B-row exponents; then the Kahan arrays
-    a.bar_bytes = (uint32_t)(((8 * (kMaxStages + 4 + kDone + kAcc) + 16 + sizeof(int2) * kM + sizeof(int) * kN) +
-                              15) / 16 * 16);
-    const size_t tail = a.bar_bytes + kKahanBytes;
+    a.stage_bytes = kBlocks * (a.ablock + kBBlock);
+    a.op_bytes = form == 0 ? 2 * kBlocks * kBBlock : 2 * kBBlock;
+    // barriers, TMEM address, abort flag, pair table, B-row exponents
+    const size_t tail = 8 * (2 * kMaxStages + 4 + kDone + kAcc) + 16 + sizeof(int2) * kM + sizeof(int) * kN;
+    const int op_slots = form == 0 ? Form<kFormTF32>::kOpSlots : Form<kFormF16>::kOpSlots;
+    const size_t fixed = 1024 + (size_t)op_slots * a.op_bytes + tail;
     a.nstages = kMaxStages;
-    while (a.nstages > 2 && 1024 + (size_t)a.nstages * a.stage_bytes + tail > 227 * 1024) a.nstages--;
-    const size_t smem = 1024 + (size_t)a.nstages * a.stage_bytes + tail;
+    while (a.nstages > 3 && fixed + (size_t)a.nstages * a.stage_bytes > 227 * 1024) a.nstages--;
+    const size_t smem = fixed + (size_t)a.nstages * a.stage_bytes;
     if (smem > 227 * 1024) return set_error(PBI4G_ERR_UNSUPPORTED, "tensor-core triangle sums: %zu B smem", smem);
     a.units = tp.units.as<int2>();
     a.prow = tp.prow.as<int2>();
@@ -714,6 +727,8 @@ int triangle_sums_tm(const Shells &sh, TmPlan &tp, int form, const float *maps, 
     a.err = tp.err.as<int>();
     PBI4G_CUDA(cudaMemsetAsync(tp.err.p, 0, sizeof(int), st));
     const int grid = tp.nunits * a.ksplit;
+    PBI4G_CHECK(tp.kahan.ensure(sizeof(float) * 2 * kN * kM * (size_t)grid));
+    a.kahan = tp.kahan.as<float>();
     if (form == 0) PBI4G_CHECK(launch_tm<kFormTF32>(tmA, tmB, a, smem, grid, st));
     else if (form == 1) PBI4G_CHECK(launch_tm<kFormF16>(tmA, tmB, a, smem, grid, st));
     else PBI4G_CHECK(launch_tm<kFormBF16>(tmA, tmB, a, smem, grid, st));

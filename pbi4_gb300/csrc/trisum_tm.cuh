@@ -11,6 +11,7 @@ struct TmPlan {
     DevBuf units, prow, slots, err;
     DevBuf blocked;  // the maps as [Nm^3 / 32][nmaps][32] FP32 (one contiguous read per chunk)
     DevBuf mexp;     // FP16 form: per-map power-of-two exponents
+    DevBuf kahan;    // per-CTA running sums of the contraction (L2-resident scratch)
     int build(const Shells &sh, int nsets);
 };
 
