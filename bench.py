@@ -279,6 +279,7 @@ def run_ours(args):
     grid = 64 if args.quick else (128 if args.small else None)
     cfg = est_config(args.precision, grid=grid)
     est = Estimator(cfg)
+    itot, map_grid, nmaps = est.itot, est.map_grid, est.nmaps
     dpos = torch.from_numpy(pos).cuda()
     pout, bout = est.alloc_outputs()
 
@@ -341,20 +342,29 @@ def run_ours(args):
     serving = None
     if args.serve_requests > 0 and rank == 0 and not args.quick and not args.small:
         from pbi4_gb300 import serve_workload
-        reqs = serve_workload.make_stream(n_requests=args.serve_requests, grids=(128, 192, 256), npart_min=1e5,
-                                          npart_max=2e6, rate_hz=args.serve_rate, precision=args.precision)
-        st = serve_workload.run_stream(reqs, hbm_budget_gb=120.0, slots=4)
+        est.close()
+        torch.cuda.empty_cache()
+        reqs = serve_workload.make_stream(n_requests=args.serve_requests, grids=(128, 192, 256, 384),
+                                          npart_min=1e5, npart_max=args.serve_npart_max, rate_hz=args.serve_rate,
+                                          precision=args.precision)
+        live = serve_workload.run_stream(reqs, hbm_budget_gb=200.0, slots=3, batch=4, realtime=True)
+        sat = serve_workload.run_stream(reqs, hbm_budget_gb=200.0, slots=3, batch=4, realtime=False)
         serial = serve_workload.run_serial_plain(reqs)
-        serving = {"requests": st["n"], "p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
-                   "boxes_per_s": round(st["boxes_per_s"], 2), "offered_rate_hz": args.serve_rate,
+        serving = {"requests": live["n"], "offered_rate_hz": args.serve_rate,
+                   "p50_ms": round(live["p50_ms"], 3), "p99_ms": round(live["p99_ms"], 3),
+                   "boxes_per_s_offered_load": round(live["boxes_per_s"], 2),
+                   "boxes_per_s_saturated": round(sat["boxes_per_s"], 2),
+                   "p50_ms_saturated": round(sat["p50_ms"], 3), "p99_ms_saturated": round(sat["p99_ms"], 3),
+                   "mean_graph_batch_saturated": round(sat["mean_batch"], 2),
                    "serial_plain_fp32_boxes_per_s": round(serial["boxes_per_s"], 2),
-                   "workload": "Poisson arrivals; grid in {128,192,256}; npart log-uniform [1e5, 2e6]; uniform or "
-                               "Zel'dovich positions; CIC/TSC/PCS; interlacing on/off; P-only or P+B "
-                               "(dk=2kf to 0.5 kNyq); cold plan creation included"}
+                   "workload": "Poisson arrivals; grid in {128,192,256,384}; npart log-uniform [1e5, %.0e]; uniform "
+                               "or Zel'dovich (P~k^n, n in [-2,-1]) positions; CIC/TSC/PCS; interlacing on/off; P-only "
+                               "or P+B (dk=2kf to 0.5 kNyq); plans warmed before the stream (resident plans); "
+                               "same-configuration boxes batched into captured CUDA graphs (up to 4), 3 stream slots; "
+                               "serial plain FP32 = the same boxes one by one on warm FP32 plans" % args.serve_npart_max}
 
     from pbi4_gb300 import roofline
-    rl, rl_all = roofline.for_stages(stages, args.steps, cfg, npart, itot=est.itot, map_grid=est.map_grid,
-                                     nmaps=est.nmaps)
+    rl, rl_all = roofline.for_stages(stages, args.steps, cfg, npart, itot=itot, map_grid=map_grid, nmaps=nmaps)
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
@@ -365,9 +375,9 @@ def run_ours(args):
                 "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[args.precision],
                 "data": "synthetic (seeded Zel'dovich box, positions resident in HBM)",
                 "config": {**WORKLOAD, "precision": args.precision, "parallelism": f"replicas{world}",
-                           "map_grid": est.map_grid,
+                           "map_grid": map_grid,
                            "l2": "working set > L2 (shell maps %.1f GB per box on the %d^3 map grid)" % (
-                               est.nmaps * est.map_grid ** 2 * (est.map_grid + 2) * 4 / 1e9, est.map_grid),
+                               nmaps * map_grid ** 2 * (map_grid + 2) * 4 / 1e9, map_grid),
                            "triangle_counts": "computed once per plan (input independent)"},
                 "e2e": {"value": e2e_value, "unit": "boxes/s", "h2d_bytes_per_step": int(pos.nbytes),
                         "d2h_bytes_per_step": int(p_h.nbytes + b_h.nbytes)},
@@ -388,8 +398,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", default="fp16split", choices=["fp32", "fp64", "fp16split", "bf16", "tf32split"])
     ap.add_argument("--no-compare", action="store_true", help="skip the plain-FP32 and FP64 comparison runs")
-    ap.add_argument("--serve-requests", type=int, default=32, help="requests in the serving leg (0: skip)")
-    ap.add_argument("--serve-rate", type=float, default=40.0, help="offered request rate of the serving leg (1/s)")
+    ap.add_argument("--serve-requests", type=int, default=48, help="requests in the serving leg (0: skip)")
+    ap.add_argument("--serve-rate", type=float, default=20.0, help="offered request rate of the serving leg (1/s)")
+    ap.add_argument("--serve-npart-max", type=float, default=1e7, help="largest particle count of a served box")
     ap.add_argument("--quick", action="store_true", help="small box (debug only)")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: 64^3 particles on a 128^3 grid (same kernels, a few hundred MB)")

@@ -183,6 +183,21 @@ int pbi4g_plan_run_device(pbi4g_plan *plan, int64_t npart, const double *d_pos, 
  * pout/bout back, synchronises the plan's stream. */
 int pbi4g_plan_run_host(pbi4g_plan *plan, int64_t npart, const double *pos, const double *weight,
                         double *pout, double *bout);
+/* Captured form (serving): `batch` box slots of at most npart_cap particles
+ * held by the plan.  Runs one direct box to size every buffer and build the
+ * lazy tables (synchronous).  Needs an FP32-family precision, grid % 16 == 0,
+ * a stream set with pbi4g_plan_set_stream (not the legacy default stream);
+ * boxes carry no weights. */
+int pbi4g_plan_graph_build(pbi4g_plan *plan, int32_t batch, int64_t npart_cap);
+/* nboxes (1..batch) boxes through one CUDA graph launch on the plan's stream:
+ * copies pos[b] ((3, npart[b]) float64 host) into the slots, launches the graph
+ * captured for nboxes boxes (captured on first use; the particle counts and
+ * their normalisation factors are read from device memory, so one graph serves
+ * any counts up to npart_cap), copies pout[b] ((5, nbins_ps)) and bout[b]
+ * ((brows, itot)) out.  Asynchronous with pinned host buffers, which must stay
+ * alive until the plan's stream completes (pbi4g_plan_check). */
+int pbi4g_plan_graph_run_host(pbi4g_plan *plan, int32_t nboxes, const int64_t *npart, const double *const *pos,
+                              double *const *pout, double *const *bout);
 /* Synchronise the plan's stream and report PBI4G_ERR_TIMEOUT if a bounded wait
  * inside a tensor-core launch of this plan gave up (the device launches of
  * pbi4g_plan_run_device are asynchronous; run_host checks by itself). */

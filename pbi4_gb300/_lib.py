@@ -30,7 +30,7 @@ EXPORTS = [
     "pbi4g_plan_bispectrum", "pbi4g_plan_run_device", "pbi4g_plan_run_host", "pbi4g_plan_get_delta_half",
     "pbi4g_plan_kernel_launches", "pbi4g_plan_enable_timing", "pbi4g_plan_stage_times",
     "pbi4g_measure_pk_multipoles_noalloc", "pbi4g_plan_set_delta_half", "pbi4g_plan_set_counts",
-    "pbi4g_plan_check",
+    "pbi4g_plan_check", "pbi4g_plan_graph_build", "pbi4g_plan_graph_run_host",
 ]
 NSTAGES = 10
 STAGES = ["assign", "grid_convert", "fft_r2c", "fcomb", "pk_binning", "triangle_counts", "shell_spectra",
@@ -79,6 +79,8 @@ _SIGS = {
     "pbi4g_plan_shape": [_P, ctypes.POINTER(_i32), ctypes.POINTER(_i64), ctypes.POINTER(_i32)],
     "pbi4g_plan_map_grid": [_P, ctypes.POINTER(_i32), ctypes.POINTER(_i32)],
     "pbi4g_plan_check": [_P],
+    "pbi4g_plan_graph_build": [_P, _i32, _i64],
+    "pbi4g_plan_graph_run_host": [_P, _i32, _P, _P, _P, _P],
     "pbi4g_plan_triangle_counts": [_P, _P],
     "pbi4g_plan_density": [_P, _i64, _P, _P],
     "pbi4g_plan_powerspectrum": [_P, _P],

@@ -85,12 +85,12 @@ struct PrepOut {
     int w;
 };
 
-__device__ __forceinline__ PRec make_rec(const double *__restrict__ pos, int64_t npart, int64_t i, int N, int nintp,
+__device__ __forceinline__ PRec make_rec(const double *__restrict__ pos, int64_t stride, int64_t i, int N, int nintp,
                                          int interlaced, int lo[3]) {
     PRec r;
     int f[2][3];
     for (int c = 0; c < 3; c++) {
-        const double p = pos[(size_t)c * npart + i];
+        const double p = pos[(size_t)c * stride + i];
         first_and_h(p, N, nintp, false, !interlaced, f[0][c], r.h[0][c]);
         if (interlaced) first_and_h(p, N, nintp, true, false, f[1][c], r.h[1][c]);
         else { f[1][c] = f[0][c]; r.h[1][c] = 0.f; }
@@ -102,12 +102,14 @@ __device__ __forceinline__ PRec make_rec(const double *__restrict__ pos, int64_t
     return r;
 }
 
-__global__ void owner_count_kernel(int N, int nintp, int interlaced, int64_t npart, const double *__restrict__ pos,
-                                   int nt, PRec *__restrict__ rec, unsigned int *__restrict__ count) {
+__global__ void owner_count_kernel(int N, int nintp, int interlaced, int64_t npart, int64_t stride,
+                                   const BoxPar *__restrict__ bp, const double *__restrict__ pos, int nt,
+                                   PRec *__restrict__ rec, unsigned int *__restrict__ count) {
     const int w = nintp + (interlaced ? 1 : 0);  // cells spanned from the lowest first cell
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npart; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t n = bp ? bp->npart : npart;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         int lo[3];
-        const PRec r = make_rec(pos, npart, i, N, nintp, interlaced, lo);
+        const PRec r = make_rec(pos, stride, i, N, nintp, interlaced, lo);
         rec[i] = r;
         int tx[2], ty[2], tz[2];
         const int nx = axis_tiles(lo[0], w, N, nt, tx), ny = axis_tiles(lo[1], w, N, nt, ty),
@@ -153,12 +155,13 @@ __global__ void owner_scan_kernel(int ntiles, const unsigned int *__restrict__ c
     if (threadIdx.x == 0) start[ntiles] = carry;
 }
 
-__global__ void owner_scatter_kernel(int N, int nintp, int interlaced, int64_t npart, int nt,
-                                     const PRec *__restrict__ rec, const double *__restrict__ weight,
+__global__ void owner_scatter_kernel(int N, int nintp, int interlaced, int64_t npart, const BoxPar *__restrict__ bp,
+                                     int nt, const PRec *__restrict__ rec, const double *__restrict__ weight,
                                      unsigned int *__restrict__ cursor, PRec *__restrict__ sorted,
                                      float *__restrict__ wsorted) {
     const int w = nintp + (interlaced ? 1 : 0);
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npart; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t n = bp ? bp->npart : npart;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const PRec r = rec[i];
         int lo[3];
         for (int c = 0; c < 3; c++) {
@@ -280,13 +283,16 @@ size_t OwnerWork::footprint(int N, int64_t npart) {
 }
 
 int assign_owner(OwnerWork &wk, int N, int nintp, bool interlaced, int64_t npart, const double *d_pos,
-                 const double *d_weight, float *out, cudaStream_t st, int64_t *launches) {
+                 const double *d_weight, float *out, cudaStream_t st, int64_t *launches, int64_t stride,
+                 const BoxPar *bp) {
+    if (stride <= 0) stride = npart;
     if (!owner_supported(N)) return set_error(PBI4G_ERR_UNSUPPORTED, "owner assignment needs grid %% 16 == 0");
     if (nintp < 1 || nintp > 4 || npart < 1 || !d_pos)
         return set_error(PBI4G_ERR_INVALID, "assign: nintp=%d npart=%lld", nintp, (long long)npart);
     if (npart >= (int64_t)0x1fffffffLL) return set_error(PBI4G_ERR_RANGE, "assign: npart >= 2^29");
     PBI4G_CHECK(wk.ensure(N, npart));
     double wmax = 1.0;
+    if (d_weight && bp) return set_error(PBI4G_ERR_UNSUPPORTED, "captured assignment takes no weights");
     if (d_weight) {
         PBI4G_CUDA(cudaMemsetAsync(wk.wmax.p, 0, 8, st));
         owner_wmax_kernel<<<grid_blocks(npart, 256, 152 * 8), 256, 0, st>>>(npart, d_weight,
@@ -302,7 +308,7 @@ int assign_owner(OwnerWork &wk, int N, int nintp, bool interlaced, int64_t npart
     PBI4G_CHECK(fixed_point_bits(npart, wmax, &bits));
     const int nt = N / kT, ntiles = nt * nt * nt;
     PBI4G_CUDA(cudaMemsetAsync(wk.count.p, 0, (size_t)(ntiles + 1) * 4, st));
-    owner_count_kernel<<<grid_blocks(npart, 256), 256, 0, st>>>(N, nintp, interlaced, npart, d_pos, nt,
+    owner_count_kernel<<<grid_blocks(npart, 256), 256, 0, st>>>(N, nintp, interlaced, npart, stride, bp, d_pos, nt,
                                                                 static_cast<PRec *>(wk.rec.p),
                                                                 wk.count.as<unsigned int>());
     PBI4G_LAUNCH_CHECK();
@@ -310,7 +316,7 @@ int assign_owner(OwnerWork &wk, int N, int nintp, bool interlaced, int64_t npart
                                           wk.cursor.as<unsigned int>());
     PBI4G_LAUNCH_CHECK();
     owner_scatter_kernel<<<grid_blocks(npart, 256), 256, 0, st>>>(
-        N, nintp, interlaced, npart, nt, static_cast<const PRec *>(wk.rec.p), d_weight, wk.cursor.as<unsigned int>(),
+        N, nintp, interlaced, npart, bp, nt, static_cast<const PRec *>(wk.rec.p), d_weight, wk.cursor.as<unsigned int>(),
         static_cast<PRec *>(wk.sorted.p), d_weight ? wk.wsorted.as<float>() : nullptr);
     PBI4G_LAUNCH_CHECK();
     const int G = interlaced ? 2 : 1;

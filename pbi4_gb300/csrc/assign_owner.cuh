@@ -14,7 +14,11 @@ bool owner_supported(int N);
 
 // Assign npart particles (device (3, npart) float64, optional device weights)
 // into FP32 real grids out[G][N^3] (G = 2 when interlaced), fixed-point exact sums.
+// stride: distance between the x, y, z rows of d_pos (npart when <= 0).  bp:
+// when set, the particle count is read from bp->npart (npart is then the
+// capacity that sizes the launches: the graph-captured form).
 int assign_owner(OwnerWork &wk, int N, int nintp, bool interlaced, int64_t npart, const double *d_pos,
-                 const double *d_weight, float *out, cudaStream_t st, int64_t *launches);
+                 const double *d_weight, float *out, cudaStream_t st, int64_t *launches, int64_t stride = 0,
+                 const BoxPar *bp = nullptr);
 
 }  // namespace pbi4g

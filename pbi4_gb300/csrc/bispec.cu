@@ -526,7 +526,8 @@ __global__ void bk_finalize_kernel(int64_t itot, int nb, int nsets, int cross, c
                                    const double *__restrict__ S, const double *__restrict__ powsum,
                                    const double *__restrict__ nmodes, double kf3, double powSN, double gridD,
                                    double kcenter, double kbin, const float *__restrict__ counts,
-                                   double *__restrict__ bout, double sfac) {
+                                   double *__restrict__ bout, double sfac, const BoxPar *__restrict__ bp) {
+    if (bp) powSN = bp->pow_sn;
     const double powSN2 = powSN * powSN;
     for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < itot; m += (int64_t)gridDim.x * blockDim.x) {
         const int l = tri[3 * m], j = tri[3 * m + 1], i = tri[3 * m + 2];
@@ -558,17 +559,23 @@ __global__ void bk_finalize_kernel(int64_t itot, int nb, int nsets, int cross, c
     }
 }
 
+double bk_pow_sn(float kf, int64_t npart) {
+    const float kf3f = kf * kf * kf;
+    return 1.0 / (double)npart / (double)kf3f;
+}
+
 int bk_finalize(const Shells &sh, int nsets, int cross, const double *S, const double *powsum, float kf,
-                int64_t npart, const float *counts_f32, double *bout, cudaStream_t st, int64_t *launches) {
+                int64_t npart, const float *counts_f32, double *bout, cudaStream_t st, int64_t *launches,
+                const BoxPar *bp) {
     const float kf3f = kf * kf * kf;
     const double kf3 = (double)kf3f;
-    const double powSN = 1.0 / (double)npart / kf3;
+    const double powSN = bk_pow_sn(kf, npart);
     const double gridD = (double)sh.N * sh.N * sh.N;
     bk_finalize_kernel<<<grid_blocks(sh.itot, 128), 128, 0, st>>>(
         sh.itot, sh.nb, nsets, cross, sh.tri_d.as<int>(), S, powsum, sh.nmodes_d.as<double>(), kf3, powSN, gridD,
         (double)sh.kcenter, (double)sh.kbin, counts_f32, bout,
         // the sums were taken over the Nm^3 map grid: the reference sums over N^3
-        ((double)sh.N / sh.Nm) * ((double)sh.N / sh.Nm) * ((double)sh.N / sh.Nm));
+        ((double)sh.N / sh.Nm) * ((double)sh.N / sh.Nm) * ((double)sh.N / sh.Nm), bp);
     PBI4G_LAUNCH_CHECK();
     ++*launches;
     return PBI4G_OK;

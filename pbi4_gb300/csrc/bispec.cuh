@@ -71,8 +71,12 @@ int triangle_sums(const Shells &sh, const TriPlan &tp, const T *maps, size_t mst
                   double *S, cudaStream_t st, int64_t *launches);
 
 // Output rows of measure_bk (9), measure_bk_multipoles (11), measure_bk_cross (5).
+// With bp the shot-noise factor is read from bp->pow_sn (graph-captured form).
 int bk_finalize(const Shells &sh, int nsets, int cross, const double *S, const double *powsum, float kf,
-                int64_t npart, const float *counts_f32, double *bout, cudaStream_t st, int64_t *launches);
+                int64_t npart, const float *counts_f32, double *bout, cudaStream_t st, int64_t *launches,
+                const BoxPar *bp = nullptr);
+// 1 / npart / kf^3 with kf^3 in real(4), as bk_finalize uses it
+double bk_pow_sn(float kf, int64_t npart);
 
 // Exact integer triangle counts (FP64 indicator maps + FP64 sums, rounded).
 int triangle_counts(Shells &sh, cudaStream_t st, int64_t *launches);

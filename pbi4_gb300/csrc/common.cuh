@@ -68,6 +68,17 @@ inline int grid_blocks(size_t n, int threads, int cap = 152 * 32) {
 inline size_t half_cells(int N) { return (size_t)N * N * (N / 2 + 1); }
 inline size_t full_cells(int N) { return (size_t)N * N * N; }
 
+// Per-box scalars the graph-captured pipeline reads from device memory (a
+// captured launch cannot carry a per-box value): the particle count and the
+// two factors derived from it, computed on the host by the same formulas the
+// direct path passes by value.
+struct BoxPar {
+    long long npart;
+    double fcomb_cf;  // interlacing / window normalisation over npart (fcomb_half)
+    double pow_sn;    // 1 / npart / kf^3 (bk_finalize)
+    double pad;
+};
+
 // RAII device buffer
 struct DevBuf {
     void* p = nullptr;

@@ -64,9 +64,9 @@ size_t BkEngine::footprint(int N, int nb, int nsets, int cross, bool fp64) {
     const size_t HC = half_cells(N);  // upper bound: the map grid is at most N
     const int nm = cross ? 2 * nb : nsets * nb;
     const size_t cs = fp64 ? 16 : 8;
-    // half spectra (+ dense and blocked FP32 maps for the FP32 forms) + a cuFFT work area of
+    // half spectra (+ real FP32 maps for the FP32 forms) + a cuFFT work area of
     // about one batch of the same size (upper estimate)
-    return (fp64 ? 2 : 4) * (size_t)nm * HC * cs + (size_t)nb * 8 + ((size_t)1 << 26);
+    return (fp64 ? 2 : 3) * (size_t)nm * HC * cs + (size_t)nb * 8 + ((size_t)1 << 26);
 }
 
 int BkEngine::check(cudaStream_t st) {
@@ -77,7 +77,7 @@ int BkEngine::check(cudaStream_t st) {
 template <class R>
 int BkEngine::run(const typename Cx<R>::T *const src[3], const int fac[3], const double los[3], float kf,
                   int64_t npart, const float *counts_f32, double *d_bout, cudaStream_t st, int64_t *launches,
-                  Prof *prof) {
+                  Prof *prof, const BoxPar *bp) {
     using C = typename Cx<R>::T;
     Prof dummy;
     Prof &pf = prof ? *prof : dummy;
@@ -112,23 +112,28 @@ int BkEngine::run(const typename Cx<R>::T *const src[3], const int fac[3], const
                 if (fac[s] == 0) pow_mask |= 1 << s;
     }
     const size_t FCm = (size_t)N * N * N;
-    if (!fp64) PBI4G_CHECK(dense.ensure(sizeof(float) * FCm * nm));
+    // FP64: in-place C2R (padded rows); plain FP32: out of place into dense maps;
+    // tensor-core forms: out of place into row-interleaved maps (the rows of all
+    // maps for one (y, z) side by side: one contiguous read per chunk of points)
+    const int layout = fp64 ? 0 : (tc ? 2 : 1);
+    if (layout) PBI4G_CHECK(dense.ensure(sizeof(float) * FCm * nm));
     pf.begin(6, st);
     PBI4G_CUDA(cudaMemsetAsync(powsum.p, 0, sizeof(double) * 3 * nb, st));
     PBI4G_CHECK(build_map_spectra<R>(sh, nm, src, fac, los, maps.as<C>(), powsum.as<double>(), pow_mask, st,
                                      launches));
     pf.end(st);
-    if (!inv || inv_batch != nm || inv_N != N || inv_fp64 != (int)fp64) {
+    if (!inv || inv_batch != nm || inv_N != N || inv_fp64 != (int)fp64 || inv_inplace != layout) {
         if (inv) cufftDestroy(inv);
         inv = 0;
-        // FP64: in place (padded rows); FP32: out of place into dense N^3 maps
-        int n[3] = {N, N, N}, inembed[3] = {N, N, NH}, onembed[3] = {N, N, fp64 ? 2 * NH : N};
-        const int odist = fp64 ? (int)(2 * HC) : (int)FCm;
+        int n[3] = {N, N, N}, inembed[3] = {N, N, NH};
+        int onembed[3] = {N, N, layout == 0 ? 2 * NH : (layout == 1 ? N : nm * N)};
+        const int odist = layout == 0 ? (int)(2 * HC) : (layout == 1 ? (int)FCm : N);
         PBI4G_CUFFT(cufftPlanMany(&inv, 3, n, inembed, 1, (int)HC, onembed, 1, odist, fp64 ? CUFFT_Z2D : CUFFT_C2R,
                                   nm));
         inv_batch = nm;
         inv_N = N;
         inv_fp64 = fp64;
+        inv_inplace = layout;
     }
     PBI4G_CUFFT(cufftSetStream(inv, st));
     pf.begin(7, st);
@@ -162,15 +167,15 @@ int BkEngine::run(const typename Cx<R>::T *const src[3], const int fac[3], const
     pf.end(st);
     pf.begin(9, st);
     PBI4G_CHECK(bk_finalize(sh, cross ? 1 : nsets, cross, S.as<double>(), powsum.as<double>(), kf, npart, counts_f32,
-                            d_bout, st, launches));
+                            d_bout, st, launches, bp));
     pf.end(st);
     return PBI4G_OK;
 }
 
 template int BkEngine::run<float>(const float2 *const[3], const int[3], const double[3], float, int64_t, const float *,
-                                  double *, cudaStream_t, int64_t *, Prof *);
+                                  double *, cudaStream_t, int64_t *, Prof *, const BoxPar *);
 template int BkEngine::run<double>(const double2 *const[3], const int[3], const double[3], float, int64_t,
-                                   const float *, double *, cudaStream_t, int64_t *, Prof *);
+                                   const float *, double *, cudaStream_t, int64_t *, Prof *, const BoxPar *);
 
 }  // namespace pbi4g
 
@@ -194,6 +199,20 @@ struct pbi4g_plan {
     bool have_delta = false;
     int64_t npart = 0;
     Prof prof;
+    // captured form (pbi4g_plan_graph_*): `batch` box slots of at most `cap` particles
+    struct Graphs {
+        int batch = 0;
+        int64_t cap = 0;
+        DevBuf pos, pout, bout, par;           // [batch][3][cap], [batch][pout], [batch][bout], [batch] BoxPar
+        std::vector<cudaGraphExec_t> exec;     // exec[b - 1] runs boxes 0..b-1
+        std::vector<int64_t> exec_launches;    // kernels of this library in exec[b - 1]
+        std::vector<BoxPar> hpar;
+        size_t pout_n = 0, bout_n = 0;         // doubles per box
+        ~Graphs() {
+            for (auto e : exec)
+                if (e) cudaGraphExecDestroy(e);
+        }
+    } g;
     ~pbi4g_plan() {
         if (fwd) cufftDestroy(fwd);
     }
@@ -311,18 +330,20 @@ int pbi4g_plan_triangle_counts(pbi4g_plan *plan, int64_t *counts_host) {
     return PBI4G_OK;
 }
 
-int pbi4g_plan_density(pbi4g_plan *p, int64_t npart, const double *d_pos, const double *d_weight) {
-    if (!p) return set_error(PBI4G_ERR_INVALID, "null plan");
-    if (npart < 1) return set_error(PBI4G_ERR_INVALID, "npart must be >= 1");
+// One box's density.  bp == nullptr: npart particles at d_pos (rows of npart).
+// bp != nullptr (captured form): npart is the slot capacity (rows of npart), the
+// particle count and the normalisation come from bp on the device.
+static int density_impl(pbi4g_plan *p, int64_t npart, const double *d_pos, const double *d_weight, const BoxPar *bp) {
     const int N = p->N;
     int bits;
     if (!p->fp64 && owner_supported(N)) {
         // FP32 grids straight from the owner-computes tiles (fixed-point sums in shared memory)
         p->prof.begin(0, p->st);
         PBI4G_CHECK(assign_owner(p->ow, N, p->cfg.nintp, p->G == 2, npart, d_pos, d_weight,
-                                 p->real_grids.as<float>(), p->st, &p->launches));
+                                 p->real_grids.as<float>(), p->st, &p->launches, npart, bp));
         p->prof.end(p->st);
     } else {
+        if (bp) return set_error(PBI4G_ERR_UNSUPPORTED, "captured form needs the owner-computes assignment");
         p->prof.begin(0, p->st);
         PBI4G_CHECK(assign_fixed(p->aw, N, p->cfg.nintp, p->G == 2, p->fp64, npart, d_pos, d_weight, &bits, p->st,
                                  &p->launches));
@@ -341,14 +362,20 @@ int pbi4g_plan_density(pbi4g_plan *p, int64_t npart, const double *d_pos, const 
     p->prof.begin(3, p->st);
     if (p->fp64)
         PBI4G_CHECK(fcomb_half<double>(N, p->cfg.nintp, p->G == 2, p->cfg.box, (double)npart, p->spec.as<double2>(),
-                                       p->delta.as<double2>(), p->win, p->st, &p->launches));
+                                       p->delta.as<double2>(), p->win, p->st, &p->launches, bp));
     else
         PBI4G_CHECK(fcomb_half<float>(N, p->cfg.nintp, p->G == 2, p->cfg.box, (double)npart, p->spec.as<float2>(),
-                                      p->delta.as<float2>(), p->win, p->st, &p->launches));
+                                      p->delta.as<float2>(), p->win, p->st, &p->launches, bp));
     p->prof.end(p->st);
     p->have_delta = true;
     p->npart = npart;
     return PBI4G_OK;
+}
+
+int pbi4g_plan_density(pbi4g_plan *p, int64_t npart, const double *d_pos, const double *d_weight) {
+    if (!p) return set_error(PBI4G_ERR_INVALID, "null plan");
+    if (npart < 1) return set_error(PBI4G_ERR_INVALID, "npart must be >= 1");
+    return density_impl(p, npart, d_pos, d_weight, nullptr);
 }
 
 int pbi4g_plan_powerspectrum(pbi4g_plan *p, double *d_pout) {
@@ -367,7 +394,11 @@ int pbi4g_plan_powerspectrum(pbi4g_plan *p, double *d_pout) {
     return rc;
 }
 
-int pbi4g_plan_bispectrum(pbi4g_plan *p, double *d_bout) {
+static int bispectrum_impl(pbi4g_plan *p, double *d_bout, const BoxPar *bp);
+
+int pbi4g_plan_bispectrum(pbi4g_plan *p, double *d_bout) { return bispectrum_impl(p, d_bout, nullptr); }
+
+static int bispectrum_impl(pbi4g_plan *p, double *d_bout, const BoxPar *bp) {
     if (!p || !d_bout) return set_error(PBI4G_ERR_INVALID, "null plan/output");
     if (!p->cfg.do_bispectrum) return set_error(PBI4G_ERR_INVALID, "plan has no bispectrum");
     if (!p->have_delta) return set_error(PBI4G_ERR_INVALID, "bispectrum before density");
@@ -382,11 +413,112 @@ int pbi4g_plan_bispectrum(pbi4g_plan *p, double *d_bout) {
     if (p->fp64) {
         const double2 *src[3] = {p->delta.as<double2>(), p->delta.as<double2>(), p->delta.as<double2>()};
         return p->bk.run<double>(src, fac, p->cfg.los, kf, p->npart, p->bk.sh.counts_f32.as<float>(), d_bout, p->st,
-                                 &p->launches, &p->prof);
+                                 &p->launches, &p->prof, bp);
     }
     const float2 *src[3] = {p->delta.as<float2>(), p->delta.as<float2>(), p->delta.as<float2>()};
     return p->bk.run<float>(src, fac, p->cfg.los, kf, p->npart, p->bk.sh.counts_f32.as<float>(), d_bout, p->st,
-                            &p->launches, &p->prof);
+                            &p->launches, &p->prof, bp);
+}
+
+// ------------------------------------------------------- captured form ---
+static float plan_kf(const pbi4g_plan *p) { return (float)(2.0 * 3.14159265358979323846 / (double)p->cfg.box); }
+
+int pbi4g_plan_graph_build(pbi4g_plan *p, int32_t batch, int64_t npart_cap) {
+    if (!p || batch < 1 || batch > 64 || npart_cap < 1) return set_error(PBI4G_ERR_INVALID, "bad graph arguments");
+    if (p->fp64 || !owner_supported(p->N))
+        return set_error(PBI4G_ERR_UNSUPPORTED, "captured form needs an FP32-family plan with grid %% 16 == 0");
+    if (p->st == 0) return set_error(PBI4G_ERR_INVALID, "captured form needs a non-default stream");
+    auto &g = p->g;
+    for (auto e : g.exec)
+        if (e) cudaGraphExecDestroy(e);
+    g.exec.assign(batch, nullptr);
+    g.exec_launches.assign(batch, 0);
+    g.batch = batch;
+    g.cap = npart_cap;
+    g.pout_n = (size_t)5 * p->cfg.nbins_ps;
+    g.bout_n = p->cfg.do_bispectrum ? (size_t)(p->cfg.multipoles ? 11 : 9) * p->bk.sh.itot : 0;
+    PBI4G_CHECK(g.pos.ensure(sizeof(double) * 3 * (size_t)npart_cap * batch));
+    PBI4G_CHECK(g.pout.ensure(sizeof(double) * g.pout_n * batch));
+    PBI4G_CHECK(g.bout.ensure(sizeof(double) * std::max<size_t>(1, g.bout_n) * batch));
+    PBI4G_CHECK(g.par.ensure(sizeof(BoxPar) * batch));
+    g.hpar.assign(batch, BoxPar{1, fcomb_cf(p->G == 2, p->cfg.box, 1.0), bk_pow_sn(plan_kf(p), 1), 0.0});
+    // positions at 0 (valid, in [0, 1)); one direct box sizes every buffer and
+    // builds the lazy tables (windows, shells, triangle counts, cuFFT plans)
+    PBI4G_CUDA(cudaMemsetAsync(g.pos.p, 0, sizeof(double) * 3 * (size_t)npart_cap * batch, p->st));
+    PBI4G_CHECK(p->ow.ensure(p->N, npart_cap));
+    PBI4G_CHECK(pbi4g_plan_run_device(p, 1, g.pos.as<double>(), nullptr, g.pout.as<double>(),
+                                      g.bout_n ? g.bout.as<double>() : nullptr));
+    PBI4G_CUDA(cudaStreamSynchronize(p->st));
+    return p->cfg.do_bispectrum ? p->bk.check(p->st) : PBI4G_OK;
+}
+
+static int graph_capture(pbi4g_plan *p, int nboxes) {
+    auto &g = p->g;
+    const bool prof_on = p->prof.on;
+    p->prof.on = false;  // no timing events inside a graph
+    cudaGraph_t graph = nullptr;
+    const int64_t l0 = p->launches;
+    PBI4G_CUDA(cudaStreamBeginCapture(p->st, cudaStreamCaptureModeRelaxed));
+    int rc = PBI4G_OK;
+    for (int b = 0; b < nboxes && rc == PBI4G_OK; b++) {
+        const BoxPar *bp = g.par.as<BoxPar>() + b;
+        const double *pos = g.pos.as<double>() + (size_t)b * 3 * g.cap;
+        double *po = g.pout.as<double>() + (size_t)b * g.pout_n;
+        double *bo = g.bout.as<double>() + (size_t)b * g.bout_n;
+        rc = density_impl(p, g.cap, pos, nullptr, bp);
+        if (rc == PBI4G_OK) rc = pbi4g_plan_powerspectrum(p, po);
+        if (rc == PBI4G_OK && p->cfg.do_bispectrum) rc = bispectrum_impl(p, bo, bp);
+    }
+    const cudaError_t e = cudaStreamEndCapture(p->st, &graph);
+    p->prof.on = prof_on;
+    const int64_t captured = p->launches - l0;
+    p->launches = l0;
+    if (rc != PBI4G_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (e != cudaSuccess) return set_error(PBI4G_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) return set_error(PBI4G_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ei));
+    g.exec[nboxes - 1] = exec;
+    g.exec_launches[nboxes - 1] = captured;
+    return PBI4G_OK;
+}
+
+int pbi4g_plan_graph_run_host(pbi4g_plan *p, int32_t nboxes, const int64_t *npart, const double *const *pos,
+                              double *const *pout, double *const *bout) {
+    if (!p || !npart || !pos || !pout) return set_error(PBI4G_ERR_INVALID, "null argument");
+    auto &g = p->g;
+    if (g.batch == 0) return set_error(PBI4G_ERR_INVALID, "pbi4g_plan_graph_build first");
+    if (nboxes < 1 || nboxes > g.batch) return set_error(PBI4G_ERR_INVALID, "nboxes %d outside 1..%d", nboxes, g.batch);
+    if (g.bout_n && !bout) return set_error(PBI4G_ERR_INVALID, "null bout");
+    const float kf = plan_kf(p);
+    for (int b = 0; b < nboxes; b++) {
+        if (npart[b] < 1 || npart[b] > g.cap)
+            return set_error(PBI4G_ERR_RANGE, "box %d: npart %lld outside 1..%lld", b, (long long)npart[b],
+                             (long long)g.cap);
+        g.hpar[b] = BoxPar{(long long)npart[b], fcomb_cf(p->G == 2, p->cfg.box, (double)npart[b]),
+                           bk_pow_sn(kf, npart[b]), 0.0};
+    }
+    if (!g.exec[nboxes - 1]) PBI4G_CHECK(graph_capture(p, nboxes));
+    for (int b = 0; b < nboxes; b++)
+        PBI4G_CUDA(cudaMemcpy2DAsync(g.pos.as<double>() + (size_t)b * 3 * g.cap, sizeof(double) * g.cap, pos[b],
+                                     sizeof(double) * npart[b], sizeof(double) * npart[b], 3, cudaMemcpyHostToDevice,
+                                     p->st));
+    PBI4G_CUDA(cudaMemcpyAsync(g.par.p, g.hpar.data(), sizeof(BoxPar) * nboxes, cudaMemcpyHostToDevice, p->st));
+    PBI4G_CUDA(cudaGraphLaunch(g.exec[nboxes - 1], p->st));
+    p->launches += g.exec_launches[nboxes - 1];
+    for (int b = 0; b < nboxes; b++) {
+        PBI4G_CUDA(cudaMemcpyAsync(pout[b], g.pout.as<double>() + (size_t)b * g.pout_n, sizeof(double) * g.pout_n,
+                                   cudaMemcpyDeviceToHost, p->st));
+        if (g.bout_n)
+            PBI4G_CUDA(cudaMemcpyAsync(bout[b], g.bout.as<double>() + (size_t)b * g.bout_n, sizeof(double) * g.bout_n,
+                                       cudaMemcpyDeviceToHost, p->st));
+    }
+    p->npart = npart[nboxes - 1];
+    return PBI4G_OK;
 }
 
 int pbi4g_plan_run_device(pbi4g_plan *p, int64_t npart, const double *d_pos, const double *d_weight, double *d_pout,

@@ -37,9 +37,9 @@ struct BkEngine {
     int tp_nsets = -1, tp_cross = -1, tp_fp64 = -1;
     int nsets = 1, cross = 0;  // cross: 1 => q maps from the second field
     DevBuf maps;               // [nmaps][N][N][N/2+1] complex half spectra (FP64: padded real maps after C2R)
-    DevBuf dense;              // FP32 forms: [nmaps][N^3] real maps (out-of-place C2R)
+    DevBuf dense;              // FP32 forms: real maps of the out-of-place C2R (dense, or row-interleaved)
     cufftHandle inv = 0;
-    int inv_batch = 0, inv_N = 0, inv_fp64 = -1;  // FP32 plans are out of place
+    int inv_batch = 0, inv_N = 0, inv_fp64 = -1, inv_inplace = -1;
     DevBuf powsum, S, partial;
     // tensor-core form: 0 off (CUDA cores), 1 FP16 hi+lo, 2 BF16, 3 TF32 hi+lo
     int tc_mode = 0;
@@ -57,7 +57,8 @@ struct BkEngine {
     // multipole factor from `los`.  counts_f32: device float counts[itot].
     template <class R>
     int run(const typename Cx<R>::T *const src[3], const int fac[3], const double los[3], float kf, int64_t npart,
-            const float *counts_f32, double *d_bout, cudaStream_t st, int64_t *launches, Prof *prof = nullptr);
+            const float *counts_f32, double *d_bout, cudaStream_t st, int64_t *launches, Prof *prof = nullptr,
+            const BoxPar *bp = nullptr);
 };
 
 }  // namespace pbi4g

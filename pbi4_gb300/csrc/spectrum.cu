@@ -114,8 +114,9 @@ __device__ __forceinline__ typename Cx<R>::T dsample(const typename Cx<R>::T *__
 template <class R>
 __global__ void fcomb_interlaced_half_kernel(int N, const typename Cx<R>::T *__restrict__ spec,
                                              typename Cx<R>::T *__restrict__ delta, const R *__restrict__ iW,
-                                             R cf, double piN) {
+                                             R cf, double piN, const BoxPar *__restrict__ bp) {
     const int NH = N / 2 + 1;
+    if (bp) cf = (R)bp->fcomb_cf;
     const size_t HC = (size_t)N * N * NH;
     const typename Cx<R>::T *F1 = spec, *F2 = spec + HC;
     const size_t total = (size_t)NH * NH * NH;
@@ -144,8 +145,10 @@ __global__ void fcomb_interlaced_half_kernel(int N, const typename Cx<R>::T *__r
 
 template <class R>
 __global__ void fcomb_plain_half_kernel(int N, const typename Cx<R>::T *__restrict__ spec,
-                                        typename Cx<R>::T *__restrict__ delta, const R *__restrict__ iW, R cf) {
+                                        typename Cx<R>::T *__restrict__ delta, const R *__restrict__ iW, R cf,
+                                        const BoxPar *__restrict__ bp) {
     const int NH = N / 2 + 1;
+    if (bp) cf = (R)bp->fcomb_cf;
     const size_t HC = (size_t)N * N * NH;
     for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < HC; c += (size_t)gridDim.x * blockDim.x) {
         const int x = (int)(c % NH), y = (int)((c / NH) % N), z = (int)(c / ((size_t)NH * N));
@@ -154,9 +157,14 @@ __global__ void fcomb_plain_half_kernel(int N, const typename Cx<R>::T *__restri
     }
 }
 
+double fcomb_cf(bool interlaced, float box, double norm) {
+    const double kF3 = fcomb_kF3(box);
+    return (interlaced ? 1.0 / (4.0 * kF3) : 1.0 / kF3) / norm;
+}
+
 template <class R>
 int fcomb_half(int N, int nintp, bool interlaced, float box, double norm, const typename Cx<R>::T *spec,
-               typename Cx<R>::T *delta, WinCache &wcache, cudaStream_t st, int64_t *launches) {
+               typename Cx<R>::T *delta, WinCache &wcache, cudaStream_t st, int64_t *launches, const BoxPar *bp) {
     const int NH = N / 2 + 1;
     std::vector<double> tW(NH);
     window_table(N, nintp, tW.data());
@@ -173,16 +181,15 @@ int fcomb_half(int N, int nintp, bool interlaced, float box, double norm, const 
         wcache.rsize = (int)sizeof(R);
     }
     DevBuf &cache = wcache.buf;
-    const double kF3 = fcomb_kF3(box);
-    const double cf = (interlaced ? 1.0 / (4.0 * kF3) : 1.0 / kF3) / norm;
+    const double cf = fcomb_cf(interlaced, box, norm);
     if (interlaced) {
         const double tpiN = (double)kTwoPiF / (double)N;
         const size_t total = (size_t)NH * NH * NH;
         fcomb_interlaced_half_kernel<R><<<grid_blocks(total, 256), 256, 0, st>>>(N, spec, delta, cache.as<R>(),
-                                                                                 (R)cf, -tpiN / 2.0);
+                                                                                 (R)cf, -tpiN / 2.0, bp);
     } else {
         fcomb_plain_half_kernel<R><<<grid_blocks(half_cells(N), 256), 256, 0, st>>>(N, spec, delta, cache.as<R>(),
-                                                                                    (R)cf);
+                                                                                    (R)cf, bp);
     }
     PBI4G_LAUNCH_CHECK();
     ++*launches;
@@ -190,9 +197,9 @@ int fcomb_half(int N, int nintp, bool interlaced, float box, double norm, const 
 }
 
 template int fcomb_half<float>(int, int, bool, float, double, const float2 *, float2 *, WinCache &, cudaStream_t,
-                               int64_t *);
+                               int64_t *, const BoxPar *);
 template int fcomb_half<double>(int, int, bool, float, double, const double2 *, double2 *, WinCache &, cudaStream_t,
-                                int64_t *);
+                                int64_t *, const BoxPar *);
 
 // ------------------------------------------------ fcomb on full grids (FP64) ---
 __global__ void fcomb_interlaced_full_kernel(int N, const double2 *in, double2 *out, const double *__restrict__ tW,

@@ -30,10 +30,14 @@ struct WinCache {
 
 // fcomb on the R2C half spectra of one (non-interlaced) or two (interlaced)
 // real grids: spec [G][N][N][N/2+1] -> delta [N][N][N/2+1], including the
-// 1/norm normalisation (dcl /= npart, pbi4.py:336).
+// 1/norm normalisation (dcl /= npart, pbi4.py:336); with bp the factor is read
+// from bp->fcomb_cf (graph-captured form).
+// normalisation factor of fcomb_half for `norm` particles
+double fcomb_cf(bool interlaced, float box, double norm);
+
 template <class R>
 int fcomb_half(int N, int nintp, bool interlaced, float box, double norm, const typename Cx<R>::T *spec,
-               typename Cx<R>::T *delta, WinCache &wcache, cudaStream_t st, int64_t *launches);
+               typename Cx<R>::T *delta, WinCache &wcache, cudaStream_t st, int64_t *launches, const BoxPar *bp = nullptr);
 
 // Full-grid fcomb (drop-in, FP64), in place allowed.
 int fcomb_full(int N, int nintp, bool interlaced, float box, const double2 *in, double2 *out, cudaStream_t st);

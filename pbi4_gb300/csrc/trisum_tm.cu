@@ -20,8 +20,10 @@
 //
 // Data path per chunk of 64 grid points (one CTA per (M tile of 128 pairs,
 // N tile of 64 maps, K range)):
-//   * the maps are first permuted into 32-point blocks, [block][map][32], so
-//     that one chunk of all maps is one contiguous read;
+//   * the C2R writes the maps row-interleaved (the x rows of all maps for one
+//     (y, z) side by side), so one chunk of all maps is one contiguous read;
+//     chunks are pairs of (row, 32-point x block), the last block of a row
+//     zero-filled past x = Nm by the TMA bounds;
 //   * a TMA warp loads the chunk's set-0 maps (the pair factors) and the 64
 //     maps of the N tile, FP32, 128-byte swizzled, into a ring of shared-memory
 //     stages;
@@ -193,7 +195,7 @@ __device__ __forceinline__ void pack2(float x, float y, uint32_t &hi, uint32_t &
 
 struct TmArgs {
     long long nchunks;     // K / kKC
-    int nunits, ksplit, nslots, nA, nstages, nmaps;
+    int nunits, ksplit, nslots, nA, nstages, nmaps, nxb;
     uint32_t stage_bytes, op_bytes, ablock;
     float *kahan;          // [grid][2][kN][kM] running sum and compensation of each CTA (L2-resident)
     const int2 *units;     // (M tile, N tile) per unit
@@ -502,9 +504,11 @@ __global__ void __launch_bounds__(kThreads, 1)
             mbar_expect_tx(&full[s], tx);
 #pragma unroll
             for (int kb = 0; kb < kBlocks; kb++) {
-                const int blk = (int)((cb + j) * kBlocks + kb);  // 32-point block of the blocked maps
-                tma_load_3d(stg + kb * a.ablock, &tmA, 0, 0, blk, &full[s]);
-                tma_load_3d(stg + kBlocks * a.ablock + kb * kBBlock, &tmB, 0, U.y * kN, blk, &full[s]);
+                // K block -> (32-point x block, map row); blocks past the last row read zeros
+                const long long blk = (cb + j) * kBlocks + kb;
+                const int row = (int)(blk / a.nxb), x0 = (int)(blk - (long long)row * a.nxb) * kKB;
+                tma_load_3d(stg + kb * a.ablock, &tmA, x0, 0, row, &full[s]);
+                tma_load_3d(stg + kBlocks * a.ablock + kb * kBBlock, &tmB, x0, U.y * kN, row, &full[s]);
             }
             issued = j + 1;
         }
@@ -559,36 +563,21 @@ EncodeTiledFn encode_fn() {
     return fn;
 }
 
-// 3D FP32 view of the blocked maps [nkb][nmaps][32]: box 32 x box_rows x 1 at
-// (0, first row, block), 128-byte swizzle, zero fill for rows past `rows`.
-int make_block_view(CUtensorMap *tm, const float *blocked, long long nkb, int nmaps, int rows, int box_rows) {
+// 3D FP32 view of the row-interleaved maps [Nm^2 rows][nmaps][Nm]: box 32 x
+// box_rows x 1 at (x0, first map, row), 128-byte swizzle, zero fill past the
+// row end (x >= Nm), past `rows` maps and past the last row.
+int make_row_view(CUtensorMap *tm, const float *maps, int Nm, int nmaps, int rows, int box_rows) {
     EncodeTiledFn enc = encode_fn();
     if (!enc) return set_error(PBI4G_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
-    const cuuint64_t gdim[3] = {(cuuint64_t)kKB, (cuuint64_t)rows, (cuuint64_t)nkb};
-    const cuuint64_t gstride[2] = {(cuuint64_t)(kKB * sizeof(float)), (cuuint64_t)nmaps * kKB * sizeof(float)};
+    const cuuint64_t gdim[3] = {(cuuint64_t)Nm, (cuuint64_t)rows, (cuuint64_t)Nm * Nm};
+    const cuuint64_t gstride[2] = {(cuuint64_t)Nm * sizeof(float), (cuuint64_t)nmaps * Nm * sizeof(float)};
     const cuuint32_t box[3] = {(cuuint32_t)kKB, (cuuint32_t)box_rows, 1};
     const cuuint32_t estr[3] = {1, 1, 1};
-    const CUresult r = enc(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(blocked), gdim, gstride, box,
+    const CUresult r = enc(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(maps), gdim, gstride, box,
                            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return set_error(PBI4G_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
     return PBI4G_OK;
-}
-
-// blocked[kb][m][0..31] = maps[m][32 kb .. 32 kb + 31]: each 32-point block of
-// every map becomes one 128-byte row, and the rows of all maps for one block
-// are contiguous, so a chunk of the contraction is one contiguous 8 KB read.
-__global__ void map_block_permute_kernel(const float4 *__restrict__ maps, float4 *__restrict__ blocked, int nmaps,
-                                         long long nkb, size_t mstride4) {
-    const long long total = (long long)nmaps * nkb * 8;
-    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
-         idx += (long long)gridDim.x * blockDim.x) {
-        const int e = (int)(idx & 7);
-        const long long seg = idx >> 3;
-        const int m = (int)(seg / nkb);
-        const long long kb = seg - (long long)m * nkb;
-        blocked[(kb * nmaps + m) * 8 + e] = __ldcs(maps + (size_t)m * mstride4 + kb * 8 + e);
-    }
 }
 
 }  // namespace
@@ -660,8 +649,8 @@ int TmPlan::build(const Shells &sh, int nsets_) {
 }
 
 bool tm_supported(const Shells &sh) {
-    const long long K = (long long)sh.Nm * sh.Nm * sh.Nm;
-    return sh.nb <= 256 && K % kKC == 0 && K / kKB < (1LL << 31);
+    const long long rows = (long long)sh.Nm * sh.Nm;
+    return sh.nb <= 256 && sh.Nm % 4 == 0 && rows * ((sh.Nm + kKB - 1) / kKB) < (1LL << 31);
 }
 
 template <int F>
@@ -677,14 +666,12 @@ int triangle_sums_tm(const Shells &sh, TmPlan &tp, int form, const float *maps, 
                      int pow_mask, const double lfac[3], DevBuf &partial, double *S, cudaStream_t st,
                      int64_t *launches) {
     const int N = sh.Nm;
-    const long long K = (long long)N * N * N;
     if (!tm_supported(sh))
         return set_error(PBI4G_ERR_UNSUPPORTED, "tensor-core triangle sums: map grid %d, %d shells", N, sh.nb);
     if (form < 0 || form > 2) return set_error(PBI4G_ERR_INVALID, "tensor-core form %d", form);
     if (tp.nunits == 0) return PBI4G_OK;
     if (reinterpret_cast<uintptr_t>(maps) % 16)
         return set_error(PBI4G_ERR_INVALID, "tensor-core triangle sums: maps must be 16-byte aligned");
-    PBI4G_CHECK(tp.blocked.ensure(sizeof(float) * (size_t)K * nmaps));
     PBI4G_CHECK(tp.mexp.ensure(sizeof(int) * std::max(1, nmaps)));
     if (form == 1) {
         map_exponents_kernel<<<1, 256, 0, st>>>(nmaps, sh.nb, powsum, pow_mask, lfac[1], lfac[2],
@@ -692,15 +679,13 @@ int triangle_sums_tm(const Shells &sh, TmPlan &tp, int form, const float *maps, 
         PBI4G_LAUNCH_CHECK();
         *launches += 1;
     }
-    const long long nkb = K / kKB;
-    map_block_permute_kernel<<<152 * 8, 256, 0, st>>>(reinterpret_cast<const float4 *>(maps),
-                                                      tp.blocked.as<float4>(), nmaps, nkb, (size_t)(K / 4));
-    PBI4G_LAUNCH_CHECK();
     CUtensorMap tmA, tmB;
-    PBI4G_CHECK(make_block_view(&tmA, tp.blocked.as<float>(), nkb, nmaps, sh.nb, tp.nA));
-    PBI4G_CHECK(make_block_view(&tmB, tp.blocked.as<float>(), nkb, nmaps, nmaps, kN));
+    PBI4G_CHECK(make_row_view(&tmA, maps, N, nmaps, sh.nb, tp.nA));
+    PBI4G_CHECK(make_row_view(&tmB, maps, N, nmaps, nmaps, kN));
     TmArgs a;
-    a.nchunks = K / kKC;
+    // K blocks: (map row, 32-point x block), the last x block of a row zero-padded
+    a.nxb = (N + kKB - 1) / kKB;
+    a.nchunks = ((long long)N * N * a.nxb + kBlocks - 1) / kBlocks;
     a.nunits = tp.nunits;
     a.ksplit = std::max(1, 152 / tp.nunits);
     a.ksplit = (int)std::min<long long>(a.ksplit, std::max<long long>(1, a.nchunks / 128));
@@ -733,7 +718,7 @@ int triangle_sums_tm(const Shells &sh, TmPlan &tp, int form, const float *maps, 
     else if (form == 1) PBI4G_CHECK(launch_tm<kFormF16>(tmA, tmB, a, smem, grid, st));
     else PBI4G_CHECK(launch_tm<kFormBF16>(tmA, tmB, a, smem, grid, st));
     PBI4G_CHECK(reduce_partials(tp.nslots, a.ksplit, partial.as<double>(), S, st));
-    *launches += 3;
+    *launches += 2;
     return PBI4G_OK;
 }
 

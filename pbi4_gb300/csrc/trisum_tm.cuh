@@ -9,7 +9,6 @@ namespace pbi4g {
 struct TmPlan {
     int nsets = 1, npairs = 0, nslots = 0, nunits = 0, nA = 0;
     DevBuf units, prow, slots, err;
-    DevBuf blocked;  // the maps as [Nm^3 / 32][nmaps][32] FP32 (one contiguous read per chunk)
     DevBuf mexp;     // FP16 form: per-map power-of-two exponents
     DevBuf kahan;    // per-CTA running sums of the contraction (L2-resident scratch)
     int build(const Shells &sh, int nsets);
@@ -18,8 +17,10 @@ struct TmPlan {
 bool tm_supported(const Shells &sh);
 
 // S[slot] for every (triangle, set) slot on the tensor cores.  form: 0 TF32
-// hi+lo, 1 FP16 hi+lo, 2 BF16.  maps: dense FP32 maps on the map grid (map m at
-// maps + m * Nm^3, 16-byte aligned).  FP16 form only: powsum[s*nb + b] is the
+// hi+lo, 1 FP16 hi+lo, 2 BF16.  maps: FP32 maps on the map grid, row-interleaved:
+// point (x, y, z) of map m at ((z Nm + y) nmaps + m) Nm + x (every map's row of
+// one (y, z) side by side), 16-byte aligned, as a batched C2R writes them with
+// an output embedding of nmaps Nm per row.  FP16 form only: powsum[s*nb + b] is the
 // full-grid sum of |H|^2 per set and shell (sets in pow_mask), which with the
 // shell's mode count bounds max |M| and sets each map's scale; lfac[s] bounds
 // |L_l| for sets without their own power.

@@ -80,6 +80,7 @@ class EstimatorConfig:
 
 
 def footprint(cfg: EstimatorConfig, npart_max: int) -> int:
+    # (the captured form adds batch x 3 x npart_max float64 position slots)
     """Device bytes a plan for cfg needs (admission control); allocates nothing."""
     c = cfg.to_c()
     out = ctypes.c_int64()
@@ -88,6 +89,8 @@ def footprint(cfg: EstimatorConfig, npart_max: int) -> int:
 
 
 class Estimator:
+    stream = None  # the stream object last given to set_stream (serving bookkeeping)
+
     def __init__(self, cfg: EstimatorConfig, stream=None):
         self.cfg = cfg
         self._c = cfg.to_c()
@@ -151,6 +154,28 @@ class Estimator:
     def check(self):
         """Synchronise and raise if a bounded wait inside a tensor-core launch gave up."""
         check(lib().pbi4g_plan_check(self._h))
+
+    # -- captured form
+    graph_ready = False
+
+    def graph_build(self, batch: int, npart_cap: int):
+        """Hold `batch` box slots of up to npart_cap particles and capture the box
+        pipeline as CUDA graphs on first use (needs a non-default stream)."""
+        check(lib().pbi4g_plan_graph_build(self._h, int(batch), int(npart_cap)))
+        self.graph_batch, self.graph_cap, self.graph_ready = int(batch), int(npart_cap), True
+
+    def graph_run_host(self, pos_list, pout_list, bout_list=None):
+        """One graph launch for len(pos_list) boxes: pos_list of (3, npart) float64
+        C-contiguous host arrays, outputs preallocated host arrays shaped like
+        alloc_outputs' ((5, nbins_ps) / (brows, itot), Fortran order, or the
+        C-order transposes' buffers).  Asynchronous with pinned outputs: read them
+        after the plan's stream completes."""
+        n = len(pos_list)
+        npart = (ctypes.c_int64 * n)(*[int(p.shape[1]) for p in pos_list])
+        pp = (ctypes.c_void_p * n)(*[p.ctypes.data for p in pos_list])
+        po = (ctypes.c_void_p * n)(*[o.ctypes.data for o in pout_list])
+        bo = (ctypes.c_void_p * n)(*[o.ctypes.data for o in bout_list]) if bout_list else None
+        check(lib().pbi4g_plan_graph_run_host(self._h, n, npart, pp, po, bo))
 
     def alloc_outputs(self, device="cuda"):
         """Device output tensors (pout (5, nbins_ps), bout (brows, itot)) in Fortran layout."""

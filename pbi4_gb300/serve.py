@@ -1,19 +1,29 @@
 """Continuous-batching request loop for estimator boxes on one GPU.
 
 Requests (a box configuration + host positions) arrive at any time.  The loop
-keeps one resident plan per (configuration, slot) -- grids, cuFFT plans, bin and
-shell tables, triangle counts -- and runs admitted boxes on `slots` CUDA streams
-so several boxes are on the device at once.  Admission is by device footprint:
-a box starts when a slot is free and the plans it needs fit under the HBM
-budget; idle plans are evicted least-recently-used to make room.  Requests of
-the same configuration reuse the same plans back to back.
+keeps resident plans per configuration -- grids, cuFFT plans, bin and shell
+tables, triangle counts, shell-map buffers, captured graphs -- and runs admitted
+work on `slots` CUDA streams so several boxes are on the device at once; an idle
+plan runs on whichever slot is free, and a second instance of a configuration
+is built only when the first is busy.
 
-Each box is issued asynchronously on its slot's stream: pinned host -> device
-copy of the positions, the plan's kernels, device -> pinned host copy of the
-outputs, then an event; the loop thread polls events, so new requests are
-admitted while others are still running (no per-box synchronisation of the
-device).  Latency = completion time - arrival time; p50/p99 are reported by
-``stats()``.
+Batching: when a slot frees up, the request at the head of the queue and up to
+`batch - 1` further queued requests of the same configuration (the same grid,
+binning and precision: same-size boxes) form one batch, and the whole batch is
+one launch of a CUDA graph the plan captured for that batch size
+(pbi4g_plan_graph_run_host): per-box particle counts and their normalisation
+factors are read from device memory, so one captured graph serves any counts
+up to the server's max_npart.  Configurations the captured form does not cover
+(FP64 plans, grids that are not a multiple of 16, weighted boxes) run box by
+box through the direct path on the same slots.
+
+Admission is by device footprint: a batch starts when a slot is free and the
+plan it needs fits under the HBM budget; idle plans are evicted least recently
+used to make room, and a request whose plan can never fit is rejected.  Each
+batch is issued asynchronously on its slot's stream (pageable positions are
+staged by the driver, outputs land in pinned buffers) followed by an event; the
+loop thread polls events, so new requests are admitted while others run.
+Latency = completion time - arrival time; p50/p99 are reported by ``stats()``.
 """
 from __future__ import annotations
 
@@ -33,6 +43,7 @@ class Request:
     cfg: EstimatorConfig
     pos: np.ndarray                   # (3, npart) float64 in [0, 1)
     rid: int = 0
+    weight: np.ndarray | None = None
     t_arrival: float = field(default_factory=time.perf_counter)
 
 
@@ -44,34 +55,45 @@ class Result:
     t_arrival: float
     t_start: float
     t_done: float
+    batch: int = 1
 
     @property
     def latency(self) -> float:
         return self.t_done - self.t_arrival
 
 
+def graph_capable(cfg: EstimatorConfig) -> bool:
+    """Configurations the captured (graph) form covers: FP32-family plans on grids % 16 == 0."""
+    return cfg.precision != "fp64" and int(cfg.grid) % 16 == 0
+
+
 class _Slot:
     def __init__(self, torch, idx):
         self.idx = idx
         self.stream = torch.cuda.Stream()
-        self.busy = None   # (request, future, plan, event, host outputs, t_start)
+        self.busy = None   # (requests, futures, plan, event, keep-alive objects, t_start)
 
 
 class Server:
-    def __init__(self, hbm_budget_bytes: int, slots: int = 4, device: int = 0, max_npart: int = 10_000_000):
+    def __init__(self, hbm_budget_bytes: int, slots: int = 4, device: int = 0, max_npart: int = 10_000_000,
+                 batch: int = 4, lookahead: int = 64):
         import torch
         self.torch = torch
         torch.cuda.set_device(device)
         self.budget = int(hbm_budget_bytes)
         self.max_npart = int(max_npart)
+        self.batch = int(batch)
+        self.lookahead = int(lookahead)
         self.slots = [_Slot(torch, k) for k in range(slots)]
-        self.plans: "collections.OrderedDict[tuple, Estimator]" = collections.OrderedDict()  # (cfg key, slot) -> plan
+        # (cfg key, instance) -> plan, least recently used first
+        self.plans: "collections.OrderedDict[tuple, Estimator]" = collections.OrderedDict()
         self.plan_bytes: dict[tuple, int] = {}
         self.queue: "collections.deque[tuple[Request, Future]]" = collections.deque()
         self.lock = threading.Condition()
         self.results: list[Result] = []
         self.rejected = 0
         self.evictions = 0
+        self.batches = 0
         self._stop = False
         self._thread = threading.Thread(target=self._loop, daemon=True)
         self._thread.start()
@@ -88,6 +110,15 @@ class Server:
             self.lock.notify()
         return fut
 
+    def warm(self, cfgs):
+        """Build the resident plans of these configurations on every slot ahead of
+        the traffic (plan creation, tables, triangle counts, graph buffers)."""
+        with self.lock:
+            for cfg in cfgs:
+                if self._plan_for(cfg, self.slots[0]) is None:
+                    break
+        self.torch.cuda.synchronize()
+
     def close(self, wait: bool = True):
         with self.lock:
             self._stop = True
@@ -102,30 +133,47 @@ class Server:
         return sum(self.plan_bytes.values())
 
     def stats(self) -> dict:
-        lat = np.array([r.latency for r in self.results]) if self.results else np.zeros(1)
         if not self.results:
             return {"n": 0}
+        lat = np.array([r.latency for r in self.results])
         t0 = min(r.t_arrival for r in self.results)
         t1 = max(r.t_done for r in self.results)
         return {"n": len(self.results), "p50_ms": float(np.percentile(lat, 50) * 1e3),
                 "p99_ms": float(np.percentile(lat, 99) * 1e3), "mean_ms": float(lat.mean() * 1e3),
                 "boxes_per_s": len(self.results) / max(t1 - t0, 1e-9), "evictions": self.evictions,
-                "rejected": self.rejected, "resident_gb": self.resident_bytes() / 1e9}
+                "rejected": self.rejected, "batches": self.batches,
+                "mean_batch": len(self.results) / max(1, self.batches), "resident_gb": self.resident_bytes() / 1e9}
 
     # --------------------------------------------------------------- loop ---
-    def _plan_for(self, cfg: EstimatorConfig, slot: _Slot, npart: int):
-        key = (cfg.key(), slot.idx)
-        if key in self.plans:
-            self.plans.move_to_end(key)
-            return self.plans[key]
+    def _footprint(self, cfg: EstimatorConfig) -> int:
         need = footprint(cfg, self.max_npart)
+        if graph_capable(cfg):
+            need += self.batch * 3 * self.max_npart * 8
+        return need
+
+    def _busy(self, plan) -> bool:
+        return any(s.busy is not None and s.busy[2] is plan for s in self.slots)
+
+    def _plan_for(self, cfg: EstimatorConfig, slot: _Slot):
+        ck = cfg.key()
+        insts = [k for k in self.plans if k[0] == ck]
+        for k in insts:
+            plan = self.plans[k]
+            if not self._busy(plan):
+                self.plans.move_to_end(k)
+                if plan.stream is not slot.stream:
+                    plan.set_stream(slot.stream)
+                    plan.stream = slot.stream
+                return plan
+        key = (ck, max((k[1] for k in insts), default=-1) + 1)
+        need = self._footprint(cfg)
         if need > self.budget:
             raise MemoryError(f"plan footprint {need / 1e9:.2f} GB exceeds the HBM budget {self.budget / 1e9:.2f} GB")
         # evict idle plans (least recently used first) until the new one fits
         while self.resident_bytes() + need > self.budget:
             victim = None
             for k in self.plans:
-                if not any(s.busy is not None and s.busy[2] is self.plans[k] for s in self.slots):
+                if not self._busy(self.plans[k]):
                     victim = k
                     break
             if victim is None:
@@ -134,42 +182,90 @@ class Server:
             self.plan_bytes.pop(victim)
             self.evictions += 1
             self.torch.cuda.empty_cache()
-        plan = Estimator(cfg)
+        plan = Estimator(cfg, stream=slot.stream)
+        plan.stream = slot.stream
+        if graph_capable(cfg):
+            plan.graph_build(self.batch, self.max_npart)
         self.plans[key] = plan
         self.plan_bytes[key] = need
         return plan
 
-    def _start(self, slot: _Slot, req: Request, fut: Future, plan: Estimator):
+    def _take_batch(self):
+        """The head request and up to batch-1 queued requests of the same configuration."""
+        req, fut = self.queue[0]
+        if not graph_capable(req.cfg) or req.weight is not None:
+            self.queue.popleft()
+            return [(req, fut)]
+        key = req.cfg.key()
+        picked = [0]
+        for k in range(1, min(len(self.queue), self.lookahead)):
+            if len(picked) == self.batch:
+                break
+            r, _ = self.queue[k]
+            if r.weight is None and r.cfg.key() == key:
+                picked.append(k)
+        items = [self.queue[k] for k in picked]
+        for k in reversed(picked):
+            del self.queue[k]
+        return items
+
+    def _start(self, slot: _Slot, items, plan: Estimator):
         torch = self.torch
-        npart = req.pos.shape[1]
-        plan.set_stream(slot.stream)
-        with torch.cuda.stream(slot.stream):
-            hpos = torch.from_numpy(np.ascontiguousarray(req.pos, dtype=np.float64))
-            if not hpos.is_pinned():
-                hpos = hpos.pin_memory()
-            dpos = torch.empty((3, npart), dtype=torch.float64, device="cuda")
-            dpos.copy_(hpos, non_blocking=True)
-            pout_d, bout_d = plan.alloc_outputs()
-            plan.run_device(npart, dpos, pout_d, bout_d)
-            pout_h = torch.empty(pout_d.shape[::-1], dtype=torch.float64, pin_memory=True)
-            pout_h.copy_(pout_d.t(), non_blocking=True)
-            bout_h = None
-            if bout_d is not None:
-                bout_h = torch.empty(bout_d.shape[::-1], dtype=torch.float64, pin_memory=True)
-                bout_h.copy_(bout_d.t(), non_blocking=True)
-            ev = torch.cuda.Event()
-            ev.record(slot.stream)
-        # keep every buffer of the in-flight box alive until its event completes
-        slot.busy = (req, fut, plan, ev, (pout_h, bout_h, hpos, dpos, pout_d, bout_d), time.perf_counter())
+        reqs = [r for r, _ in items]
+        futs = [f for _, f in items]
+        t_start = time.perf_counter()
+        keep = []
+        if plan.graph_ready and all(r.weight is None for r in reqs):
+            pos = [np.ascontiguousarray(r.pos, dtype=np.float64) for r in reqs]
+            pouts = [torch.empty((plan.nbins_ps, 5), dtype=torch.float64, pin_memory=True) for _ in reqs]
+            bouts = ([torch.empty((plan.itot, plan.brows), dtype=torch.float64, pin_memory=True) for _ in reqs]
+                     if plan.itot else None)
+            plan.graph_run_host(pos, [p.numpy() for p in pouts], [b.numpy() for b in bouts] if bouts else None)
+            outs = [(pouts[b].numpy().T, bouts[b].numpy().T if bouts else None) for b in range(len(reqs))]
+            keep = [pos, pouts, bouts]
+        else:
+            # direct path, one box: device copies on the slot stream, outputs to pinned buffers
+            r = reqs[0]
+            npart = r.pos.shape[1]
+            with torch.cuda.stream(slot.stream):
+                hpos = torch.from_numpy(np.ascontiguousarray(r.pos, dtype=np.float64))
+                dpos = torch.empty((3, npart), dtype=torch.float64, device="cuda")
+                dpos.copy_(hpos, non_blocking=True)
+                dw = None
+                if r.weight is not None:
+                    dw = torch.from_numpy(np.ascontiguousarray(r.weight, dtype=np.float64)).cuda(non_blocking=True)
+                pout_d, bout_d = plan.alloc_outputs()
+                plan.run_device(npart, dpos, pout_d, bout_d, weight=dw)
+                pout_h = torch.empty(pout_d.shape[::-1], dtype=torch.float64, pin_memory=True)
+                pout_h.copy_(pout_d.t(), non_blocking=True)
+                bout_h = None
+                if bout_d is not None:
+                    bout_h = torch.empty(bout_d.shape[::-1], dtype=torch.float64, pin_memory=True)
+                    bout_h.copy_(bout_d.t(), non_blocking=True)
+            outs = [(pout_h.numpy().T, None if bout_h is None else bout_h.numpy().T)]
+            keep = [hpos, dpos, dw, pout_d, bout_d, pout_h, bout_h]
+        ev = torch.cuda.Event()
+        ev.record(slot.stream)
+        self.batches += 1
+        # every buffer of the batch in flight stays alive until its event completes
+        slot.busy = (reqs, futs, plan, ev, (outs, keep), t_start)
 
     def _finish(self, slot: _Slot):
-        req, fut, plan, ev, (pout_h, bout_h, *_), t_start = slot.busy
-        pout = pout_h.numpy().T
-        bout = None if bout_h is None else bout_h.numpy().T
-        res = Result(req.rid, pout, bout, req.t_arrival, t_start, time.perf_counter())
-        self.results.append(res)
+        reqs, futs, plan, ev, (outs, _), t_start = slot.busy
         slot.busy = None
-        fut.set_result(res)
+        t_done = time.perf_counter()
+        err = None
+        try:
+            plan.check()  # the slot's work is complete: this only reads the launch error flags
+        except Exception as e:  # a bounded wait in a tensor-core launch gave up
+            err = e
+        for r, f, (po, bo) in zip(reqs, futs, outs):
+            if err is not None:
+                f.set_exception(err)
+                continue
+            res = Result(r.rid, po.copy(), None if bo is None else bo.copy(), r.t_arrival, t_start, t_done, len(reqs))
+            self.results.append(res)
+            f.set_result(res)
 
     def _loop(self):
         while True:
@@ -184,25 +280,27 @@ class Server:
                 free = [s for s in self.slots if s.busy is None]
                 while free and self.queue:
                     req, fut = self.queue[0]
-                    # prefer a free slot that already holds a plan for this configuration
-                    key = req.cfg.key()
-                    free.sort(key=lambda s: (key, s.idx) not in self.plans)
                     slot = free[0]
                     try:
-                        plan = self._plan_for(req.cfg, slot, req.pos.shape[1])
+                        plan = self._plan_for(req.cfg, slot)
                     except MemoryError as e:  # can never fit: reject this request
                         self.queue.popleft()
                         self.rejected += 1
                         fut.set_exception(e)
                         continue
+                    except Exception as e:  # plan creation failed: report and keep serving
+                        self.queue.popleft()
+                        fut.set_exception(e)
+                        continue
                     if plan is None:
                         break
-                    self.queue.popleft()
+                    items = self._take_batch()
                     try:
-                        self._start(slot, req, fut, plan)
+                        self._start(slot, items, plan)
                     except Exception as e:  # report per request; keep serving
                         slot.busy = None
-                        fut.set_exception(e)
+                        for _, f in items:
+                            f.set_exception(e)
                         continue
                     free.remove(slot)
                     progressed = True

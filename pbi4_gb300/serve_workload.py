@@ -5,7 +5,7 @@ count log-uniform in [npart_min, npart_max], uniform or Zel'dovich-clustered
 positions (P ~ k^n, n uniform in [-2, -1]) in L = 1000 Mpc/h, an assignment
 order from {CIC, TSC, PCS}, interlacing on/off, and P-only or P+B with
 dk = 2 kf up to 0.5 k_Nyq.  A small pool of particle sets is generated once and
-reused so that generation does not dominate the run.
+sliced per request so that generation does not dominate the run.
 """
 from __future__ import annotations
 
@@ -19,8 +19,15 @@ from .estimator import Estimator, EstimatorConfig
 from .serve import Request, Server
 
 
-def make_stream(n_requests=64, grids=(128, 192, 256), npart_min=1e5, npart_max=3e6, rate_hz=50.0, seed=3,
-                precision="fp16split", pool=6):
+def request_config(grid, nintp, interlacing, with_b, precision, box=1000.0):
+    nb = floor((0.5 * grid / 2) / 2.0)   # dk = 2 kf up to 0.5 k_Nyq
+    return EstimatorConfig(grid=grid, box=box, nintp=nintp, interlacing=interlacing, multipoles=False,
+                           kbin_ps=1.0, kcenter_ps=1.0, do_bispectrum=with_b, kbin_bs=2.0, kcenter_bs=2.0,
+                           nbins_bs=nb, iopen=True, precision=precision)
+
+
+def make_stream(n_requests=64, grids=(128, 192, 256, 384), npart_min=1e5, npart_max=1e7, rate_hz=50.0, seed=3,
+                precision="fp16split", pool=4, orders=(2, 3, 4)):
     rng = np.random.default_rng(seed)
     box = 1000.0
     # particle pool: uniform and clustered sets of the largest size, sliced per request
@@ -42,31 +49,36 @@ def make_stream(n_requests=64, grids=(128, 192, 256), npart_min=1e5, npart_max=3
         npart = min(npart, src.shape[1])
         off = int(rng.integers(0, src.shape[1] - npart + 1))
         pos = np.ascontiguousarray(src[:, off:off + npart])
-        nintp = int(rng.choice([2, 3, 4]))
-        inter = bool(rng.integers(2))
-        with_b = bool(rng.integers(2))
-        nb = floor((0.5 * grid / 2) / 2.0)   # dk = 2 kf up to 0.5 k_Nyq
-        cfg = EstimatorConfig(grid=grid, box=box, nintp=nintp, interlacing=inter, multipoles=False,
-                              kbin_ps=1.0, kcenter_ps=1.0, do_bispectrum=with_b, kbin_bs=2.0, kcenter_bs=2.0,
-                              nbins_bs=nb, iopen=True, precision=precision)
+        cfg = request_config(grid, int(rng.choice(orders)), bool(rng.integers(2)), bool(rng.integers(2)), precision)
         reqs.append((t, Request(cfg=cfg, pos=pos, rid=rid)))
     return reqs
 
 
-def run_stream(reqs, hbm_budget_gb=120.0, slots=4, max_npart=None):
-    """Replay the stream in real time through a Server; returns its stats."""
+def configs_of(reqs):
+    seen = {}
+    for _, r in reqs:
+        seen.setdefault(r.cfg.key(), r.cfg)
+    return list(seen.values())
+
+
+def run_stream(reqs, hbm_budget_gb=200.0, slots=3, batch=4, max_npart=None, warm=True, realtime=True):
+    """Replay the stream through a Server; realtime=False submits everything at
+    once (throughput under saturation).  Returns its stats."""
     max_npart = max_npart or max(r.pos.shape[1] for _, r in reqs)
-    srv = Server(hbm_budget_bytes=int(hbm_budget_gb * 1e9), slots=slots, max_npart=max_npart)
+    srv = Server(hbm_budget_bytes=int(hbm_budget_gb * 1e9), slots=slots, max_npart=max_npart, batch=batch)
+    if warm:
+        srv.warm(configs_of(reqs))
     t0 = time.perf_counter()
     futs = []
     for t, r in reqs:
-        now = time.perf_counter() - t0
-        if t > now:
-            time.sleep(t - now)
+        if realtime:
+            now = time.perf_counter() - t0
+            if t > now:
+                time.sleep(t - now)
         r.t_arrival = time.perf_counter()
         futs.append(srv.submit(r))
     for f in futs:
-        f.result(timeout=600)
+        f.result(timeout=1800)
     st = srv.stats()
     srv.close()
     return st

@@ -3,10 +3,13 @@
 Boxes of several configurations (grid sizes, assignment orders, interlacing,
 P-only and P+B, FP32 and FP16-split) are submitted at once to a Server with
 three CUDA-stream slots; every result is compared with the same box run alone
-on a fresh plan.  Tolerance: 1e-6 relative (the only differences allowed are
-the ordering of floating-point atomics in the P bins and shell powers); mode
-and triangle counts identical.  A second run squeezes the HBM budget so plans
-are evicted and rebuilt, with the same check.
+on a fresh plan through the direct path.  Same-configuration boxes on grids
+that are multiples of 16 run as batches through captured CUDA graphs; the grid
+of 48 runs box by box.  Tolerance: 1e-6 relative (the differences allowed are
+the ordering of floating-point atomics in the P bins and shell powers, and the
+fixed-point scale of the captured form, set by the server's particle capacity);
+mode and triangle counts identical.  A second run squeezes the HBM budget so
+plans are evicted and rebuilt, with the same check.
 """
 import numpy as np
 import pytest
@@ -27,7 +30,7 @@ def _requests():
     ]
     reqs = []
     rng = np.random.default_rng(5)
-    for k in range(9):
+    for k in range(15):
         cfg = cfgs[k % 3]
         n = int(rng.integers(5000, 40000))
         pos = synthetic.uniform_box(n, seed=100 + k) if k % 2 else synthetic.zeldovich_box(20 + k, 1000.0, seed=k)
@@ -64,6 +67,34 @@ def test_serving_mix_matches_alone(tight):
     stats = srv.stats()
     srv.close()
     assert stats["n"] == len(reqs) and stats["p99_ms"] >= stats["p50_ms"] > 0
+    assert stats["batches"] < len(reqs)  # same-configuration boxes shared graph launches
     if tight:
         assert stats["evictions"] > 0
     _check(results, reqs)
+
+
+def test_graph_batch_matches_direct():
+    """One plan, four boxes of different sizes in one captured graph launch."""
+    import torch
+    cfg = EstimatorConfig(grid=64, box=1000.0, nintp=4, interlacing=True, multipoles=True, kbin_bs=4.0,
+                          kcenter_bs=4.0, precision="fp16split")
+    boxes = [synthetic.zeldovich_box(12 + 4 * k, 1000.0, seed=50 + k) for k in range(4)]
+    st = torch.cuda.Stream()
+    est = Estimator(cfg, stream=st)
+    est.graph_build(4, max(b.shape[1] for b in boxes))
+    for nb in (4, 3):  # a full and a partial batch (two captured graphs)
+        pouts = [np.empty((5, est.nbins_ps), order="F") for _ in range(nb)]
+        bouts = [np.empty((est.brows, est.itot), order="F") for _ in range(nb)]
+        est.graph_run_host(boxes[:nb], pouts, bouts)
+        est.check()
+        for k in range(nb):
+            ref = Estimator(cfg)
+            p_ref, b_ref = ref.run_host(boxes[k])
+            ref.close()
+            np.testing.assert_array_equal(pouts[k][4], p_ref[4])
+            ok = p_ref[1] != 0
+            assert np.max(np.abs(pouts[k][1][ok] / p_ref[1][ok] - 1)) < 1e-6
+            np.testing.assert_array_equal(bouts[k][8], b_ref[8])
+            scale = np.maximum(np.abs(b_ref[6]), np.abs(b_ref[3] * b_ref[4]))
+            assert np.max(np.abs(bouts[k][6] - b_ref[6]) / scale) < 1e-6
+    est.close()
