@@ -28,6 +28,11 @@ namespace {
 
 constexpr int kT = 16;                  // tile edge
 constexpr int kTC = kT * kT * kT;       // 4096 cells
+// padded shared layout of a tile: cell (x, y, z) at z * kPz + y * kPy + x.  With
+// kPy = 20 and kPz = 336 (= 16 mod 32) the 32 lanes of one stencil step,
+// (i, j, l) in [0,4) x [0,4) x [0,2), hit 32 distinct banks: i + 20 j + 16 l mod 32.
+constexpr int kPy = 20, kPz = 336;
+constexpr int kTCP = kT * kPz;          // 5376 words per tile array
 constexpr int kThreads = 512;
 
 struct alignas(16) PRec {               // one particle, both grids (32 bytes)
@@ -191,46 +196,68 @@ __device__ __forceinline__ void add64_split(unsigned *lo, unsigned *hi, long lon
     atomicAdd(hi, qh + ((old + ql < old) ? 1u : 0u));
 }
 
-__global__ void __launch_bounds__(kThreads) owner_tile_kernel(int N, int nintp, int interlaced, int nt,
-                                                               const unsigned int *__restrict__ start,
+// Tile kernel, specialised on the stencil width NI (1..4) and the number of
+// grids G (2 when interlaced): a warp takes one record (particle, tile) and
+// its lanes take the G * NI^3 (grid, cell) pairs, so the cell indices and the
+// weight polynomials fold to constants and shifts.
+template <int NI, int G>
+__global__ void __launch_bounds__(kThreads) owner_tile_kernel(int N, int nt, const unsigned int *__restrict__ start,
                                                                const PRec *__restrict__ sorted,
                                                                const float *__restrict__ wsorted, float scale,
                                                                float inv_scale, float *__restrict__ out1,
                                                                float *__restrict__ out2) {
-    extern __shared__ unsigned acc32[];  // [G][lo, hi][kTC]
-    const int G = interlaced ? 2 : 1;
+    constexpr int NC = NI * NI * NI;
+    extern __shared__ unsigned acc32[];  // [G][lo, hi][kTCP]
     const int ntiles = nt * nt * nt;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    const int ncell = nintp * nintp * nintp;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int tx = tile % nt, ty = (tile / nt) % nt, tz = tile / (nt * nt);
         const int ox = tx * kT, oy = ty * kT, oz = tz * kT;
-        for (int c = threadIdx.x; c < 2 * G * kTC; c += blockDim.x) acc32[c] = 0u;
+        for (int c = threadIdx.x; c < 2 * G * kTCP; c += blockDim.x) acc32[c] = 0u;
         __syncthreads();
         const unsigned b = start[tile], e = start[tile + 1];
+        // per-lane stencil cells of one grid: NIT steps of 32 cells; the (i, j, l)
+        // of a lane are the same for every record, so they are computed once
+        constexpr int NIT = (NC + 31) / 32;
+        int ci[NIT], cj[NIT], cl[NIT];
+#pragma unroll
+        for (int it = 0; it < NIT; it++) {
+            const int c = it * 32 + lane;
+            ci[it] = c % NI;
+            cj[it] = (c / NI) % NI;
+            cl[it] = c < NC ? c / (NI * NI) : -1;  // -1: no cell for this lane at this step
+        }
         for (unsigned k = b + warp; k < e; k += nwarps) {
             const PRec r = sorted[k];
             const float wt = wsorted ? wsorted[k] : 1.f;
+#pragma unroll
             for (int g = 0; g < G; g++) {
                 const unsigned pf = r.f[g];
-                const int fx = pf & 2047, fy = (pf >> 11) & 2047, fz = pf >> 22;
-                unsigned *alo = acc32 + 2 * g * kTC, *ahi = alo + kTC;
-                for (int c = lane; c < ncell; c += 32) {
-                    const int i = c % nintp, j = (c / nintp) % nintp, l = c / (nintp * nintp);
-                    int x = fx + i, y = fy + j, z = fz + l;
+                const int fx = (int)(pf & 2047), fy = (int)((pf >> 11) & 2047), fz = (int)(pf >> 22);
+                unsigned *alo = acc32 + 2 * g * kTCP;
+                // with NI^2 dividing 32 (NI = 1, 2, 4) a lane's x and y cells are the same
+                // at every step: their weights are formed once per grid
+                const float wxy = weight1(NI, r.h[g][0], ci[0]) * weight1(NI, r.h[g][1], cj[0]);
+#pragma unroll
+                for (int it = 0; it < NIT; it++) {
+                    if (cl[it] < 0) continue;
+                    int x = fx + ci[it], y = fy + cj[it], z = fz + cl[it];
                     x -= (x >= N) ? N : 0;
                     y -= (y >= N) ? N : 0;
                     z -= (z >= N) ? N : 0;
                     const int lx = x - ox, ly = y - oy, lz = z - oz;
-                    if (lx < 0 || lx >= kT || ly < 0 || ly >= kT || lz < 0 || lz >= kT) continue;
+                    if ((unsigned)lx >= (unsigned)kT || (unsigned)ly >= (unsigned)kT || (unsigned)lz >= (unsigned)kT)
+                        continue;
                     // the reference's product order: ((w_x w_y) w_z) weight
-                    const float wv = weight1(nintp, r.h[g][0], i) * weight1(nintp, r.h[g][1], j) *
-                                     weight1(nintp, r.h[g][2], l) * wt;
+                    const float wxy_it = (32 % (NI * NI) == 0 || it == 0)
+                                             ? wxy
+                                             : weight1(NI, r.h[g][0], ci[it]) * weight1(NI, r.h[g][1], cj[it]);
+                    const float wv = wxy_it * weight1(NI, r.h[g][2], cl[it]) * wt;
                     // wv * 2^S is exact in FP32 (a power-of-two scale), so the FP32 rounding to an
                     // integer gives the same q as the FP64 route, without FP64 arithmetic
                     const long long q = __float2ll_rn(wv * scale);
-                    const int cell = (lz * kT + ly) * kT + lx;
-                    add64_split(alo + cell, ahi + cell, q);
+                    const int cell = lz * kPz + ly * kPy + lx;
+                    add64_split(alo + cell, alo + kTCP + cell, q);
                 }
             }
         }
@@ -238,13 +265,26 @@ __global__ void __launch_bounds__(kThreads) owner_tile_kernel(int N, int nintp, 
         for (int c = threadIdx.x; c < G * kTC; c += blockDim.x) {
             const int g = c / kTC, cc = c % kTC;
             const int x = cc % kT, y = (cc / kT) % kT, z = cc / (kT * kT);
-            const unsigned *alo = acc32 + 2 * g * kTC;
-            const long long v = (long long)(((unsigned long long)alo[kTC + cc] << 32) | alo[cc]);
+            const unsigned *alo = acc32 + 2 * g * kTCP;
+            const int pc = z * kPz + y * kPy + x;
+            const long long v = (long long)(((unsigned long long)alo[kTCP + pc] << 32) | alo[pc]);
             float *out = g ? out2 : out1;
             out[((size_t)(oz + z) * N + (oy + y)) * N + (ox + x)] = (float)v * inv_scale;
         }
         __syncthreads();
     }
+}
+
+template <int NI, int G>
+static int launch_tile(int N, int nt, const unsigned *start, const PRec *sorted, const float *wsorted, int bits,
+                       float *out1, float *out2, cudaStream_t st) {
+    const size_t smem = sizeof(unsigned) * 2 * G * kTCP;
+    PBI4G_CUDA(cudaFuncSetAttribute(owner_tile_kernel<NI, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int ntiles = nt * nt * nt;
+    owner_tile_kernel<NI, G><<<ntiles < 152 * 3 ? ntiles : 152 * 3, kThreads, smem, st>>>(
+        N, nt, start, sorted, wsorted, ldexpf(1.0f, bits), ldexpf(1.0f, -bits), out1, out2);
+    PBI4G_LAUNCH_CHECK();
+    return PBI4G_OK;
 }
 
 __global__ void owner_wmax_kernel(int64_t n, const double *__restrict__ w, unsigned long long *__restrict__ out) {
@@ -319,15 +359,23 @@ int assign_owner(OwnerWork &wk, int N, int nintp, bool interlaced, int64_t npart
         N, nintp, interlaced, npart, bp, nt, static_cast<const PRec *>(wk.rec.p), d_weight, wk.cursor.as<unsigned int>(),
         static_cast<PRec *>(wk.sorted.p), d_weight ? wk.wsorted.as<float>() : nullptr);
     PBI4G_LAUNCH_CHECK();
-    const int G = interlaced ? 2 : 1;
-    const size_t smem = sizeof(unsigned) * 2 * G * kTC;
-    PBI4G_CUDA(cudaFuncSetAttribute(owner_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const size_t FC = full_cells(N);
-    owner_tile_kernel<<<ntiles < 152 * 3 ? ntiles : 152 * 3, kThreads, smem, st>>>(
-        N, nintp, interlaced, nt, wk.start.as<unsigned int>(), static_cast<const PRec *>(wk.sorted.p),
-        d_weight ? wk.wsorted.as<float>() : nullptr, ldexpf(1.0f, bits), ldexpf(1.0f, -bits), out,
-        interlaced ? out + FC : nullptr);
-    PBI4G_LAUNCH_CHECK();
+    const unsigned *st_ = wk.start.as<unsigned int>();
+    const PRec *so = static_cast<const PRec *>(wk.sorted.p);
+    const float *ws = d_weight ? wk.wsorted.as<float>() : nullptr;
+    float *o2 = interlaced ? out + FC : nullptr;
+    int rc = PBI4G_OK;
+    switch (nintp * 2 + (interlaced ? 1 : 0)) {
+        case 2: rc = launch_tile<1, 1>(N, nt, st_, so, ws, bits, out, o2, st); break;
+        case 3: rc = launch_tile<1, 2>(N, nt, st_, so, ws, bits, out, o2, st); break;
+        case 4: rc = launch_tile<2, 1>(N, nt, st_, so, ws, bits, out, o2, st); break;
+        case 5: rc = launch_tile<2, 2>(N, nt, st_, so, ws, bits, out, o2, st); break;
+        case 6: rc = launch_tile<3, 1>(N, nt, st_, so, ws, bits, out, o2, st); break;
+        case 7: rc = launch_tile<3, 2>(N, nt, st_, so, ws, bits, out, o2, st); break;
+        case 8: rc = launch_tile<4, 1>(N, nt, st_, so, ws, bits, out, o2, st); break;
+        default: rc = launch_tile<4, 2>(N, nt, st_, so, ws, bits, out, o2, st); break;
+    }
+    PBI4G_CHECK(rc);
     *launches += 4;
     return PBI4G_OK;
 }
