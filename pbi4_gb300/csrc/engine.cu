@@ -119,29 +119,46 @@ int BkEngine::run(const typename Cx<R>::T *const src[3], const int fac[3], const
     if (layout) PBI4G_CHECK(dense.ensure(sizeof(float) * FCm * nm));
     pf.begin(6, st);
     PBI4G_CUDA(cudaMemsetAsync(powsum.p, 0, sizeof(double) * 3 * nb, st));
-    PBI4G_CHECK(build_map_spectra<R>(sh, nm, src, fac, los, maps.as<C>(), powsum.as<double>(), pow_mask, st,
-                                     launches));
-    pf.end(st);
-    if (!inv || inv_batch != nm || inv_N != N || inv_fp64 != (int)fp64 || inv_inplace != layout) {
-        if (inv) cufftDestroy(inv);
-        inv = 0;
-        int n[3] = {N, N, N}, inembed[3] = {N, N, NH};
-        int onembed[3] = {N, N, layout == 0 ? 2 * NH : (layout == 1 ? N : nm * N)};
-        const int odist = layout == 0 ? (int)(2 * HC) : (layout == 1 ? (int)FCm : N);
-        PBI4G_CUFFT(cufftPlanMany(&inv, 3, n, inembed, 1, (int)HC, onembed, 1, odist, fp64 ? CUFFT_Z2D : CUFFT_C2R,
-                                  nm));
-        inv_batch = nm;
-        inv_N = N;
-        inv_fp64 = fp64;
-        inv_inplace = layout;
-    }
-    PBI4G_CUFFT(cufftSetStream(inv, st));
-    pf.begin(7, st);
-    if (fp64)
+    if (fp64) {
+        PBI4G_CHECK(build_map_spectra<R>(sh, nm, src, fac, los, maps.as<C>(), powsum.as<double>(), pow_mask, st,
+                                         launches));
+        pf.end(st);
+        if (!inv || inv_batch != nm || inv_N != N || inv_fp64 != 1) {
+            if (inv) cufftDestroy(inv);
+            inv = 0;
+            int n[3] = {N, N, N}, inembed[3] = {N, N, NH}, onembed[3] = {N, N, 2 * NH};
+            PBI4G_CUFFT(cufftPlanMany(&inv, 3, n, inembed, 1, (int)HC, onembed, 1, (int)(2 * HC), CUFFT_Z2D, nm));
+            inv_batch = nm;
+            inv_N = N;
+            inv_fp64 = 1;
+        }
+        PBI4G_CUFFT(cufftSetStream(inv, st));
+        pf.begin(7, st);
         PBI4G_CUFFT(cufftExecZ2D(inv, maps.as<cufftDoubleComplex>(), maps.as<cufftDoubleReal>()));
-    else
-        PBI4G_CUFFT(cufftExecC2R(inv, maps.as<cufftComplex>(), dense.as<cufftReal>()));
-    pf.end(st);
+        pf.end(st);
+    } else {
+        // pruned inverse transform: columns kx < KX only (every shell mode has kx <= kmax)
+        const int KX = sh.kmax + 1;
+        const float2 *const *fsrc = reinterpret_cast<const float2 *const *>(src);
+        PBI4G_CHECK(build_map_cols(sh, nm, KX, fsrc, fac, los, maps.as<float2>(), powsum.as<double>(), pow_mask, st,
+                                   launches));
+        pf.end(st);
+        if (!inv || inv_batch != nm || inv_N != N || inv_fp64 != 0 || inv_kx != KX) {
+            if (inv) cufftDestroy(inv);
+            inv = 0;
+            int n[2] = {N, N};
+            PBI4G_CUFFT(cufftPlanMany(&inv, 2, n, nullptr, 1, N * N, nullptr, 1, N * N, CUFFT_C2C, nm * KX));
+            inv_batch = nm;
+            inv_N = N;
+            inv_fp64 = 0;
+            inv_kx = KX;
+        }
+        PBI4G_CUFFT(cufftSetStream(inv, st));
+        pf.begin(7, st);
+        PBI4G_CUFFT(cufftExecC2C(inv, maps.as<cufftComplex>(), maps.as<cufftComplex>(), CUFFT_INVERSE));
+        PBI4G_CHECK(c2r_rows(sh, nm, KX, maps.as<float2>(), dense.as<float>(), layout == 1, xtw, st, launches));
+        pf.end(st);
+    }
     pf.begin(8, st);
     if (tc) {
         // largest |L_l(mu)| over mu^2 in [0, |los|^2]: bounds the delta_2 / delta_4 maps by the delta map

@@ -39,7 +39,8 @@ struct BkEngine {
     DevBuf maps;               // [nmaps][N][N][N/2+1] complex half spectra (FP64: padded real maps after C2R)
     DevBuf dense;              // FP32 forms: real maps of the out-of-place C2R (dense, or row-interleaved)
     cufftHandle inv = 0;
-    int inv_batch = 0, inv_N = 0, inv_fp64 = -1, inv_inplace = -1;
+    int inv_batch = 0, inv_N = 0, inv_fp64 = -1, inv_kx = -1;
+    DevBuf xtw;                // twiddles of the x pass of the FP32 maps
     DevBuf powsum, S, partial;
     // tensor-core form: 0 off (CUDA cores), 1 FP16 hi+lo, 2 BF16, 3 TF32 hi+lo
     int tc_mode = 0;
