@@ -488,6 +488,8 @@ struct XPassPlan {
     int M = 0, nst = 0, rad[12] = {0};
 };
 
+// PF: rows of X a warp prefetches into registers for the next tile (KX <= PF * warps)
+template <int PF>
 __global__ void c2r_rows_kernel(const float2 *__restrict__ cols, float *__restrict__ out,
                                 const float2 *__restrict__ tw_g, XPassPlan xp, int Nm, int KX, int count,
                                 int dense) {
@@ -495,18 +497,35 @@ __global__ void c2r_rows_kernel(const float2 *__restrict__ cols, float *__restri
     const int M = xp.M;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const long long plane = (long long)Nm * Nm;
-    const long long tiles_per_map = (plane + kXRows - 1) / kXRows;
+    const long long tiles_per_map = (plane + kXRows - 1) / kXRows, ntiles = tiles_per_map * count;
     float2 *tw = sx, *b0 = sx + Nm, *b1 = b0 + (size_t)M * kXPitch;
     for (int t = threadIdx.x; t < Nm; t += blockDim.x) tw[t] = tw_g[t];
-    for (long long tile = blockIdx.x; tile < tiles_per_map * count; tile += gridDim.x) {
+    // the next tile's coefficients are loaded into registers while this tile computes
+    float2 pre[PF];
+    auto fetch = [&](long long tile) {
+        const int m = (int)(tile / tiles_per_map);
+        const long long row0 = (tile - (long long)m * tiles_per_map) * kXRows;
+        const bool ok = row0 + lane < plane;
+        const float2 *src = cols + (size_t)m * KX * plane + row0 + lane;
+#pragma unroll
+        for (int i = 0; i < PF; i++) {
+            const int k = warp + i * nw;
+            pre[i] = (k < KX && ok) ? __ldcs(src + (size_t)k * plane) : make_float2(0.f, 0.f);
+        }
+    };
+    if (blockIdx.x < ntiles) fetch(blockIdx.x);
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int m = (int)(tile / tiles_per_map);
         const long long row0 = (tile - (long long)m * tiles_per_map) * kXRows;
         const int nrows = (int)((plane - row0) < kXRows ? (plane - row0) : kXRows);
         __syncthreads();
-        // raw coefficients X[k][row] for k < KX into b1 (coalesced along the rows)
-        const float2 *src = cols + (size_t)m * KX * plane + row0;
-        for (int k = warp; k < KX; k += nw)
-            b1[k * kXPitch + lane] = lane < nrows ? src[(size_t)k * plane + lane] : make_float2(0.f, 0.f);
+        // raw coefficients X[k][row] for k < KX into b1, then prefetch the next tile
+#pragma unroll
+        for (int i = 0; i < PF; i++) {
+            const int k = warp + i * nw;
+            if (k < KX) b1[k * kXPitch + lane] = pre[i];
+        }
+        if (tile + gridDim.x < ntiles) fetch(tile + gridDim.x);
         __syncthreads();
         // Z = E + i O into b0
         for (int k = warp; k < M; k += nw) {
@@ -576,9 +595,21 @@ int c2r_rows(const Shells &sh, int count, int KX, const float2 *cols, float *out
         PBI4G_CUDA(cudaMemcpy(tw.p, h.data(), sizeof(float2) * Nm, cudaMemcpyHostToDevice));
     }
     const size_t smem = sizeof(float2) * (Nm + 2 * (size_t)M * kXPitch);
-    PBI4G_CUDA(cudaFuncSetAttribute(c2r_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    c2r_rows_kernel<<<152 * 4, 256, smem, st>>>(cols, out, tw.as<float2>(), xp, Nm, KX, count, dense ? 1 : 0);
-    PBI4G_LAUNCH_CHECK();
+    const int warps = 8, pf = (KX + warps - 1) / warps;
+    auto launch = [&](auto kern) -> int {
+        PBI4G_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int per_sm = 0;
+        PBI4G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * 32, smem));
+        kern<<<152 * std::max(1, per_sm), warps * 32, smem, st>>>(cols, out, tw.as<float2>(), xp, Nm, KX, count,
+                                                                   dense ? 1 : 0);
+        PBI4G_LAUNCH_CHECK();
+        return PBI4G_OK;
+    };
+    if (pf <= 4) PBI4G_CHECK(launch(c2r_rows_kernel<4>));
+    else if (pf <= 9) PBI4G_CHECK(launch(c2r_rows_kernel<9>));
+    else if (pf <= 16) PBI4G_CHECK(launch(c2r_rows_kernel<16>));
+    else if (pf <= 32) PBI4G_CHECK(launch(c2r_rows_kernel<32>));
+    else return set_error(PBI4G_ERR_UNSUPPORTED, "x pass: KX=%d", KX);
     ++*launches;
     return PBI4G_OK;
 }
