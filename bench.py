@@ -307,6 +307,7 @@ def run_ours(args):
 
     ms_max, launches, stages, clocks = timed(est, pout, bout, args.steps)
     value = replicas.throughput(world * args.steps, ms_max / 1e3)
+    map_work = est.map_work()
 
     # e2e: host (pinned) positions in, host results out, through the C-ABI call
     hpos = torch.from_numpy(pos).pin_memory().numpy()
@@ -364,7 +365,8 @@ def run_ours(args):
                                "serial plain FP32 = the same boxes one by one on warm FP32 plans" % args.serve_npart_max}
 
     from pbi4_gb300 import roofline
-    rl, rl_all = roofline.for_stages(stages, args.steps, cfg, npart, itot=itot, map_grid=map_grid, nmaps=nmaps)
+    rl, rl_all = roofline.for_stages(stages, args.steps, cfg, npart, itot=itot, map_grid=map_grid, nmaps=nmaps,
+                                     map_work=map_work)
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
@@ -377,7 +379,7 @@ def run_ours(args):
                 "config": {**WORKLOAD, "precision": args.precision, "parallelism": f"replicas{world}",
                            "map_grid": map_grid,
                            "l2": "working set > L2 (shell maps %.1f GB per box on the %d^3 map grid)" % (
-                               nmaps * map_grid ** 2 * (map_grid + 2) * 4 / 1e9, map_grid),
+                               nmaps * map_grid ** 3 * 4 / 1e9, map_grid),
                            "triangle_counts": "computed once per plan (input independent)"},
                 "e2e": {"value": e2e_value, "unit": "boxes/s", "h2d_bytes_per_step": int(pos.nbytes),
                         "d2h_bytes_per_step": int(p_h.nbytes + b_h.nbytes)},

@@ -163,6 +163,10 @@ int pbi4g_plan_shape(const pbi4g_plan *plan, int32_t *nbins_ps, int64_t *itot, i
  * 3 kmax, at most `grid`; 0 without a bispectrum) and the number of maps per
  * box (nbins_bs, x3 with multipoles).  Sums on it are scaled by (grid/map_grid)^3. */
 int pbi4g_plan_map_grid(const pbi4g_plan *plan, int32_t *map_grid, int32_t *nmaps);
+/* Complex FP32 elements of the pruned map transform's two intermediates (the
+ * z-transformed shell columns and the (z, y)-transformed kx planes) of the
+ * FP32 forms, as sized by the first bispectrum run (0 before it, and for FP64). */
+int pbi4g_plan_map_work(const pbi4g_plan *plan, int64_t *zcols, int64_t *yplanes);
 /* Exact integer triangle counts of the plan's binning (computed once, cached). */
 int pbi4g_plan_triangle_counts(pbi4g_plan *plan, int64_t *counts_host);
 
@@ -218,13 +222,21 @@ int64_t pbi4g_plan_kernel_launches(const pbi4g_plan *plan);
 
 /* Stage timing with CUDA events on the plan's stream (off by default).
  * Stages: 0 assign, 1 grid convert, 2 forward FFT, 3 fcomb, 4 P(k) binning,
- * 5 triangle counts, 6 shell spectra, 7 inverse FFT, 8 triangle sums,
- * 9 output rows.  pbi4g_plan_stage_times synchronises the stream, writes the
+ * 5 triangle counts, 6 shell maps z (shell spectra; FP32 forms with their z
+ * transform), 7 shell maps y (FP32 forms: y transform; FP64: the batched C2R),
+ * 8 triangle sums, 9 output rows, 10 shell maps x (FP32 forms: the real maps).  pbi4g_plan_stage_times synchronises the stream, writes the
  * summed milliseconds and the number of timed calls per stage since the last
  * query (arrays of PBI4G_NSTAGES) and resets them. */
-#define PBI4G_NSTAGES 10
+#define PBI4G_NSTAGES 11
 int pbi4g_plan_enable_timing(pbi4g_plan *plan, int32_t enable);
 int pbi4g_plan_stage_times(pbi4g_plan *plan, double *ms, int64_t *calls);
+
+/* Host check of the shell maps' FFT plans (no device work): `batch` inverse
+ * DFTs of n points, X[k] = sum_j x[j] e^{+2 pi i j k / n}, of interleaved
+ * complex FP32 rows in[t][n][2] -> out[t][n][2], computed on the CPU with the
+ * same plan tables and butterflies the z / y / x pass kernels run.  n must be
+ * 7-smooth (else PBI4G_ERR_UNSUPPORTED). */
+int pbi4g_fft_plan_check(int32_t n, int32_t batch, const float *in, float *out);
 
 #ifdef __cplusplus
 }

@@ -25,16 +25,16 @@ EXPORTS = [
     "pbi4g_compute_q2k", "pbi4g_compute_q4k", "pbi4g_measure_pk", "pbi4g_measure_pk_multipoles",
     "pbi4g_count_triangles", "pbi4g_measure_bk", "pbi4g_measure_bk_multipoles", "pbi4g_measure_bk_cross",
     "pbi4g_plan_footprint", "pbi4g_plan_create", "pbi4g_plan_destroy", "pbi4g_plan_set_stream",
-    "pbi4g_plan_shape", "pbi4g_plan_map_grid", "pbi4g_plan_triangle_counts", "pbi4g_plan_density",
+    "pbi4g_plan_shape", "pbi4g_plan_map_grid", "pbi4g_plan_map_work", "pbi4g_plan_triangle_counts", "pbi4g_plan_density",
     "pbi4g_plan_powerspectrum",
     "pbi4g_plan_bispectrum", "pbi4g_plan_run_device", "pbi4g_plan_run_host", "pbi4g_plan_get_delta_half",
-    "pbi4g_plan_kernel_launches", "pbi4g_plan_enable_timing", "pbi4g_plan_stage_times",
+    "pbi4g_plan_kernel_launches", "pbi4g_plan_enable_timing", "pbi4g_plan_stage_times", "pbi4g_fft_plan_check",
     "pbi4g_measure_pk_multipoles_noalloc", "pbi4g_plan_set_delta_half", "pbi4g_plan_set_counts",
     "pbi4g_plan_check", "pbi4g_plan_graph_build", "pbi4g_plan_graph_run_host",
 ]
-NSTAGES = 10
-STAGES = ["assign", "grid_convert", "fft_r2c", "fcomb", "pk_binning", "triangle_counts", "shell_spectra",
-          "fft_c2r", "triangle_sums", "bk_rows"]
+NSTAGES = 11
+STAGES = ["assign", "grid_convert", "fft_r2c", "fcomb", "pk_binning", "triangle_counts", "shell_maps_z",
+          "shell_maps_y", "triangle_sums", "bk_rows", "shell_maps_x"]
 
 
 class Pbi4GpuError(RuntimeError):
@@ -78,6 +78,7 @@ _SIGS = {
     "pbi4g_plan_set_stream": [_P, _P],
     "pbi4g_plan_shape": [_P, ctypes.POINTER(_i32), ctypes.POINTER(_i64), ctypes.POINTER(_i32)],
     "pbi4g_plan_map_grid": [_P, ctypes.POINTER(_i32), ctypes.POINTER(_i32)],
+    "pbi4g_plan_map_work": [_P, _P, _P],
     "pbi4g_plan_check": [_P],
     "pbi4g_plan_graph_build": [_P, _i32, _i64],
     "pbi4g_plan_graph_run_host": [_P, _i32, _P, _P, _P, _P],
@@ -90,6 +91,7 @@ _SIGS = {
     "pbi4g_plan_get_delta_half": [_P, _P],
     "pbi4g_plan_enable_timing": [_P, _i32],
     "pbi4g_plan_stage_times": [_P, _P, _P],
+    "pbi4g_fft_plan_check": [_i32, _i32, _P, _P],
     "pbi4g_measure_pk_multipoles_noalloc": [_i32, _f32, _f32, _f32, _i32, _P, _P, _P, _P, _P],
     "pbi4g_plan_set_delta_half": [_P, _i64, _P],
     "pbi4g_plan_set_counts": [_P, _P],

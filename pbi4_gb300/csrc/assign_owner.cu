@@ -22,6 +22,8 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
+
 namespace pbi4g {
 
 namespace {
@@ -59,21 +61,41 @@ __device__ __forceinline__ void first_and_h(double p, int N, int nintp, bool shi
     h = (float)hh;
 }
 
-// weight j of the per-axis stencil (the reference's polynomials, FP32)
-__device__ __forceinline__ float weight1(int nintp, float h, int j) {
-    if (nintp == 4) {
-        const float h2 = h * h;
-        const float w0 = (1.f - h) * (1.f - h) * (1.f - h) / 6.f;
-        const float w1 = 4.f / 6.f + (0.5f * h - 1.f) * h2;
-        const float w3 = h2 * h / 6.f;
-        return j == 0 ? w0 : (j == 1 ? w1 : (j == 3 ? w3 : 1.f - w0 - w1 - w3));
+// the NI weights of the per-axis stencil at offset h (the reference's
+// polynomials in FP32; the division by 6 as a product with the FP32 value of
+// 1/6, which stays within one rounding of the quotient and needs no division
+// sequence)
+template <int NI>
+__device__ __forceinline__ void axis_weights(float h, float (&w)[4]) {
+    if constexpr (NI == 4) {
+        const float h2 = h * h, a = 1.f - h;
+        w[0] = a * a * a * (1.f / 6.f);
+        w[1] = 4.f / 6.f + (0.5f * h - 1.f) * h2;
+        w[3] = h2 * h * (1.f / 6.f);
+        w[2] = 1.f - w[0] - w[1] - w[3];
+    } else if constexpr (NI == 3) {
+        w[0] = 0.5f * (0.5f - h) * (0.5f - h);
+        w[1] = 0.75f - h * h;
+        w[2] = 1.f - w[0] - w[1];
+        w[3] = 0.f;
+    } else if constexpr (NI == 2) {
+        w[0] = 1.f - h;
+        w[1] = h;
+        w[2] = w[3] = 0.f;
+    } else {
+        w[0] = 1.f;
+        w[1] = w[2] = w[3] = 0.f;
     }
-    if (nintp == 3) {
-        const float w0 = 0.5f * (0.5f - h) * (0.5f - h), w1 = 0.75f - h * h;
-        return j == 0 ? w0 : (j == 1 ? w1 : 1.f - w0 - w1);
-    }
-    if (nintp == 2) return j == 0 ? 1.f - h : h;
-    return 1.f;
+}
+
+// w[j] for a lane-dependent j in [0, NI) (selects, no local memory)
+template <int NI>
+__device__ __forceinline__ float pick(const float (&w)[4], int j) {
+    float v = w[0];
+    if (NI > 1) v = j == 1 ? w[1] : v;
+    if (NI > 2) v = j == 2 ? w[2] : v;
+    if (NI > 3) v = j == 3 ? w[3] : v;
+    return v;
 }
 
 // tiles touched along one axis by a stencil of width w starting at cell lo (mod N)
@@ -187,15 +209,6 @@ __global__ void owner_scatter_kernel(int N, int nintp, int interlaced, int64_t n
     }
 }
 
-// 64-bit fixed-point add as two native 32-bit shared atomics: the carry of the
-// low word is detected from its old value, so the pair sums exactly (mod 2^64).
-__device__ __forceinline__ void add64_split(unsigned *lo, unsigned *hi, long long q) {
-    const unsigned long long u = (unsigned long long)q;
-    const unsigned ql = (unsigned)u, qh = (unsigned)(u >> 32);
-    const unsigned old = atomicAdd(lo, ql);
-    atomicAdd(hi, qh + ((old + ql < old) ? 1u : 0u));
-}
-
 // Tile kernel, specialised on the stencil width NI (1..4) and the number of
 // grids G (2 when interlaced): a warp takes one record (particle, tile) and
 // its lanes take the G * NI^3 (grid, cell) pairs, so the cell indices and the
@@ -205,12 +218,20 @@ __global__ void __launch_bounds__(kThreads) owner_tile_kernel(int N, int nt, con
                                                                const PRec *__restrict__ sorted,
                                                                const float *__restrict__ wsorted, float scale,
                                                                float inv_scale, float *__restrict__ out1,
-                                                               float *__restrict__ out2) {
+                                                               float *__restrict__ out2,
+                                                               unsigned int *__restrict__ next_tile) {
     constexpr int NC = NI * NI * NI;
     extern __shared__ unsigned acc32[];  // [G][lo, hi][kTCP]
     const int ntiles = nt * nt * nt;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    __shared__ int s_tile;
+    // tiles are handed out dynamically (their particle loads differ by orders of
+    // magnitude in clustered boxes); the counter is zeroed before the launch
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = (int)atomicAdd(next_tile, 1u);
+        __syncthreads();
+        const int tile = s_tile;
+        if (tile >= ntiles) break;
         const int tx = tile % nt, ty = (tile / nt) % nt, tz = tile / (nt * nt);
         const int ox = tx * kT, oy = ty * kT, oz = tz * kT;
         for (int c = threadIdx.x; c < 2 * G * kTCP; c += blockDim.x) acc32[c] = 0u;
@@ -227,39 +248,58 @@ __global__ void __launch_bounds__(kThreads) owner_tile_kernel(int N, int nt, con
             cj[it] = (c / NI) % NI;
             cl[it] = c < NC ? c / (NI * NI) : -1;  // -1: no cell for this lane at this step
         }
+        // with NI^2 dividing 32 (NI = 1, 2, 4) a lane's x and y cells are the same at every step
+        constexpr bool kXYFixed = 32 % (NI * NI) == 0;
         for (unsigned k = b + warp; k < e; k += nwarps) {
             const PRec r = sorted[k];
             const float wt = wsorted ? wsorted[k] : 1.f;
+            int cell[G][NIT];
+            long long q[G][NIT];
+            bool ok[G][NIT];
 #pragma unroll
             for (int g = 0; g < G; g++) {
                 const unsigned pf = r.f[g];
                 const int fx = (int)(pf & 2047), fy = (int)((pf >> 11) & 2047), fz = (int)(pf >> 22);
-                unsigned *alo = acc32 + 2 * g * kTCP;
-                // with NI^2 dividing 32 (NI = 1, 2, 4) a lane's x and y cells are the same
-                // at every step: their weights are formed once per grid
-                const float wxy = weight1(NI, r.h[g][0], ci[0]) * weight1(NI, r.h[g][1], cj[0]);
+                float wx[4], wy[4], wz[4];
+                axis_weights<NI>(r.h[g][0], wx);
+                axis_weights<NI>(r.h[g][1], wy);
+                axis_weights<NI>(r.h[g][2], wz);
 #pragma unroll
                 for (int it = 0; it < NIT; it++) {
-                    if (cl[it] < 0) continue;
-                    int x = fx + ci[it], y = fy + cj[it], z = fz + cl[it];
+                    const int ii = kXYFixed ? ci[0] : ci[it], jj = kXYFixed ? cj[0] : cj[it];
+                    int x = fx + ii, y = fy + jj, z = fz + cl[it];
                     x -= (x >= N) ? N : 0;
                     y -= (y >= N) ? N : 0;
                     z -= (z >= N) ? N : 0;
                     const int lx = x - ox, ly = y - oy, lz = z - oz;
-                    if ((unsigned)lx >= (unsigned)kT || (unsigned)ly >= (unsigned)kT || (unsigned)lz >= (unsigned)kT)
-                        continue;
-                    // the reference's product order: ((w_x w_y) w_z) weight
-                    const float wxy_it = (32 % (NI * NI) == 0 || it == 0)
-                                             ? wxy
-                                             : weight1(NI, r.h[g][0], ci[it]) * weight1(NI, r.h[g][1], cj[it]);
-                    const float wv = wxy_it * weight1(NI, r.h[g][2], cl[it]) * wt;
-                    // wv * 2^S is exact in FP32 (a power-of-two scale), so the FP32 rounding to an
-                    // integer gives the same q as the FP64 route, without FP64 arithmetic
-                    const long long q = __float2ll_rn(wv * scale);
-                    const int cell = lz * kPz + ly * kPy + lx;
-                    add64_split(alo + cell, alo + kTCP + cell, q);
+                    ok[g][it] = cl[it] >= 0 && (unsigned)lx < (unsigned)kT && (unsigned)ly < (unsigned)kT &&
+                                (unsigned)lz < (unsigned)kT;
+                    // the reference's product order: ((w_x w_y) w_z) weight; wv * 2^S is exact in
+                    // FP32 (a power-of-two scale), so the FP32 rounding to an integer gives the
+                    // same q as the FP64 route, without FP64 arithmetic
+                    const float wv = pick<NI>(wx, ii) * pick<NI>(wy, jj) * pick<NI>(wz, cl[it] < 0 ? 0 : cl[it]) * wt;
+                    q[g][it] = __float2ll_rn(wv * scale);
+                    cell[g][it] = lz * kPz + ly * kPy + lx;
                 }
             }
+            // 64-bit fixed-point adds as two 32-bit shared atomics: all low words of the
+            // record first (independent), then the high words with the carries the
+            // returned low words give, so the pair sums exactly (mod 2^64)
+            unsigned old[G][NIT];
+#pragma unroll
+            for (int g = 0; g < G; g++)
+#pragma unroll
+                for (int it = 0; it < NIT; it++)
+                    if (ok[g][it]) old[g][it] = atomicAdd(acc32 + 2 * g * kTCP + cell[g][it], (unsigned)q[g][it]);
+#pragma unroll
+            for (int g = 0; g < G; g++)
+#pragma unroll
+                for (int it = 0; it < NIT; it++)
+                    if (ok[g][it]) {
+                        const unsigned ql = (unsigned)q[g][it];
+                        const unsigned qh = (unsigned)((unsigned long long)q[g][it] >> 32) + (old[g][it] + ql < old[g][it] ? 1u : 0u);
+                        if (qh) atomicAdd(acc32 + (2 * g + 1) * kTCP + cell[g][it], qh);
+                    }
         }
         __syncthreads();
         for (int c = threadIdx.x; c < G * kTC; c += blockDim.x) {
@@ -277,12 +317,15 @@ __global__ void __launch_bounds__(kThreads) owner_tile_kernel(int N, int nt, con
 
 template <int NI, int G>
 static int launch_tile(int N, int nt, const unsigned *start, const PRec *sorted, const float *wsorted, int bits,
-                       float *out1, float *out2, cudaStream_t st) {
+                       float *out1, float *out2, unsigned *next_tile, cudaStream_t st) {
     const size_t smem = sizeof(unsigned) * 2 * G * kTCP;
     PBI4G_CUDA(cudaFuncSetAttribute(owner_tile_kernel<NI, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int ntiles = nt * nt * nt;
-    owner_tile_kernel<NI, G><<<ntiles < 152 * 3 ? ntiles : 152 * 3, kThreads, smem, st>>>(
-        N, nt, start, sorted, wsorted, ldexpf(1.0f, bits), ldexpf(1.0f, -bits), out1, out2);
+    int per_sm = 0;
+    PBI4G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, owner_tile_kernel<NI, G>, kThreads, smem));
+    const int grid = std::min(ntiles, 152 * std::max(1, per_sm));
+    owner_tile_kernel<NI, G><<<grid, kThreads, smem, st>>>(N, nt, start, sorted, wsorted, ldexpf(1.0f, bits),
+                                                           ldexpf(1.0f, -bits), out1, out2, next_tile);
     PBI4G_LAUNCH_CHECK();
     return PBI4G_OK;
 }
@@ -306,7 +349,7 @@ int OwnerWork::ensure(int N, int64_t npart) {
     const int nt = N / kT;
     const size_t ntiles = (size_t)nt * nt * nt;
     const size_t n = (size_t)(npart > 0 ? npart : 1);
-    PBI4G_CHECK(count.ensure((ntiles + 1) * 4));
+    PBI4G_CHECK(count.ensure((ntiles + 2) * 4));  // + the tile kernel's work counter
     PBI4G_CHECK(start.ensure((ntiles + 1) * 4));
     PBI4G_CHECK(cursor.ensure((ntiles + 1) * 4));
     PBI4G_CHECK(rec.ensure(n * sizeof(PRec)));
@@ -319,7 +362,7 @@ int OwnerWork::ensure(int N, int64_t npart) {
 
 size_t OwnerWork::footprint(int N, int64_t npart) {
     const size_t nt = (size_t)(N / kT);
-    return 3 * (nt * nt * nt + 1) * 4 + (size_t)npart * (sizeof(PRec) + 8 * (sizeof(PRec) + 4)) + 64;
+    return 3 * (nt * nt * nt + 2) * 4 + (size_t)npart * (sizeof(PRec) + 8 * (sizeof(PRec) + 4)) + 64;
 }
 
 int assign_owner(OwnerWork &wk, int N, int nintp, bool interlaced, int64_t npart, const double *d_pos,
@@ -347,7 +390,7 @@ int assign_owner(OwnerWork &wk, int N, int nintp, bool interlaced, int64_t npart
     int bits;
     PBI4G_CHECK(fixed_point_bits(npart, wmax, &bits));
     const int nt = N / kT, ntiles = nt * nt * nt;
-    PBI4G_CUDA(cudaMemsetAsync(wk.count.p, 0, (size_t)(ntiles + 1) * 4, st));
+    PBI4G_CUDA(cudaMemsetAsync(wk.count.p, 0, (size_t)(ntiles + 2) * 4, st));  // counts and the tile counter
     owner_count_kernel<<<grid_blocks(npart, 256), 256, 0, st>>>(N, nintp, interlaced, npart, stride, bp, d_pos, nt,
                                                                 static_cast<PRec *>(wk.rec.p),
                                                                 wk.count.as<unsigned int>());
@@ -364,16 +407,17 @@ int assign_owner(OwnerWork &wk, int N, int nintp, bool interlaced, int64_t npart
     const PRec *so = static_cast<const PRec *>(wk.sorted.p);
     const float *ws = d_weight ? wk.wsorted.as<float>() : nullptr;
     float *o2 = interlaced ? out + FC : nullptr;
+    unsigned *nx = wk.count.as<unsigned int>() + ntiles + 1;
     int rc = PBI4G_OK;
     switch (nintp * 2 + (interlaced ? 1 : 0)) {
-        case 2: rc = launch_tile<1, 1>(N, nt, st_, so, ws, bits, out, o2, st); break;
-        case 3: rc = launch_tile<1, 2>(N, nt, st_, so, ws, bits, out, o2, st); break;
-        case 4: rc = launch_tile<2, 1>(N, nt, st_, so, ws, bits, out, o2, st); break;
-        case 5: rc = launch_tile<2, 2>(N, nt, st_, so, ws, bits, out, o2, st); break;
-        case 6: rc = launch_tile<3, 1>(N, nt, st_, so, ws, bits, out, o2, st); break;
-        case 7: rc = launch_tile<3, 2>(N, nt, st_, so, ws, bits, out, o2, st); break;
-        case 8: rc = launch_tile<4, 1>(N, nt, st_, so, ws, bits, out, o2, st); break;
-        default: rc = launch_tile<4, 2>(N, nt, st_, so, ws, bits, out, o2, st); break;
+        case 2: rc = launch_tile<1, 1>(N, nt, st_, so, ws, bits, out, o2, nx, st); break;
+        case 3: rc = launch_tile<1, 2>(N, nt, st_, so, ws, bits, out, o2, nx, st); break;
+        case 4: rc = launch_tile<2, 1>(N, nt, st_, so, ws, bits, out, o2, nx, st); break;
+        case 5: rc = launch_tile<2, 2>(N, nt, st_, so, ws, bits, out, o2, nx, st); break;
+        case 6: rc = launch_tile<3, 1>(N, nt, st_, so, ws, bits, out, o2, nx, st); break;
+        case 7: rc = launch_tile<3, 2>(N, nt, st_, so, ws, bits, out, o2, nx, st); break;
+        case 8: rc = launch_tile<4, 1>(N, nt, st_, so, ws, bits, out, o2, nx, st); break;
+        default: rc = launch_tile<4, 2>(N, nt, st_, so, ws, bits, out, o2, nx, st); break;
     }
     PBI4G_CHECK(rc);
     *launches += 4;

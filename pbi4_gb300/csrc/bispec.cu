@@ -305,315 +305,6 @@ int build_map_spectra(const Shells &sh, int count, const typename Cx<R>::T *cons
 template int build_map_spectra<float>(const Shells &, int, const float2 *const[3], const int[3], const double[3],
                                       float2 *, double *, int, cudaStream_t, int64_t *);
 
-// ---------------------------------------------- pruned map spectra (FP32) ---
-// The spectra of all maps as planes [m][kx][z][y] with kx < KX: every mode of
-// every shell has kx <= kmax < KX, so the planes kx >= KX (and the Nyquist
-// plane) are zero and are neither stored nor transformed.  The same mask,
-// multipole factor, Hermitian symmetrisation and shell powers as
-// build_map_spectra_kernel.  Threads run along y, so the writes are coalesced;
-// the reads of delta(k) (one N-grid half spectrum) stay in L2.
-__global__ void build_map_cols_kernel(int N, int Nm, int KX, int nb, int k2max, const int *__restrict__ lut, int count,
-                                      const float2 *__restrict__ s0, const float2 *__restrict__ s1,
-                                      const float2 *__restrict__ s2, int f0, int f1, int f2, double l0, double l1,
-                                      double l2, float2 *__restrict__ out, double *__restrict__ powsum, int pow_mask) {
-    extern __shared__ double spow[];  // [3][nb]
-    if (powsum)
-        for (int b = threadIdx.x; b < 3 * nb; b += blockDim.x) spow[b] = 0.0;
-    __syncthreads();
-    const int NH = N / 2 + 1;
-    const size_t plane = (size_t)Nm * Nm, cells = plane * KX;
-    const int j0 = blockIdx.y * kMapChunk, j1 = min(count, j0 + kMapChunk);
-    for (size_t cell = blockIdx.x * (size_t)blockDim.x + threadIdx.x; cell < cells;
-         cell += (size_t)gridDim.x * blockDim.x) {
-        const int x = (int)(cell / plane);
-        const size_t row = cell - (size_t)x * plane;  // z * Nm + y
-        const int y = (int)(row % Nm), z = (int)(row / Nm);
-        const int ky = kfreq0(y, Nm), kz = kfreq0(z, Nm);
-        const int k2 = x * x + ky * ky + kz * kz;
-        const int sb = k2 <= k2max ? lut[k2] : 0;
-        float2 *o = out + (size_t)x * plane + row;  // + j * KX * plane for map j
-        const size_t mstr = (size_t)KX * plane;
-        bool any = false;
-        for (int j = j0; j < j1; j++) any |= (j % nb + 1 == sb);
-        if (!any) {
-            for (int j = j0; j < j1; j++) o[(size_t)j * mstr] = make_float2(0.f, 0.f);
-            continue;
-        }
-        const int yN = ky < 0 ? ky + N : ky, zN = kz < 0 ? kz + N : kz;
-        const size_t sc = ((size_t)zN * N + yN) * NH + x;
-        const bool herm = x == 0;
-        const size_t mc = ((size_t)kneg0(zN, N) * N + kneg0(yN, N)) * NH + x;
-        const double lk = l0 * x + l1 * ky + l2 * kz;
-        const float mu2 = k2 > 0 ? (float)(lk * lk / (double)k2) : 0.f;
-        const double wfull = herm ? 1.0 : 2.0;
-        for (int j = j0; j < j1; j++) {
-            const int s = j / nb, b = j % nb + 1;
-            if (b != sb) {
-                o[(size_t)j * mstr] = make_float2(0.f, 0.f);
-                continue;
-            }
-            const float2 *src = s == 0 ? s0 : (s == 1 ? s1 : s2);
-            const int fac = s == 0 ? f0 : (s == 1 ? f1 : f2);
-            float2 v = src[sc];
-            if (herm) {
-                const float2 w = src[mc];
-                v.x = (v.x + w.x) * 0.5f;
-                v.y = (v.y - w.y) * 0.5f;
-            }
-            float L = 1.f;
-            if (fac == 2) L = -0.5f + 1.5f * mu2;
-            else if (fac == 4) L = 0.375f + mu2 * (-3.75f + 4.375f * mu2);
-            v.x *= L;
-            v.y *= L;
-            o[(size_t)j * mstr] = v;
-            if (powsum && (pow_mask >> s & 1))
-                atomicAdd(&spow[s * nb + b - 1], wfull * ((double)v.x * v.x + (double)v.y * v.y));
-        }
-    }
-    if (powsum) {
-        __syncthreads();
-        for (int b = threadIdx.x; b < 3 * nb; b += blockDim.x)
-            if (spow[b] != 0.0) atomicAdd(powsum + b, spow[b]);
-    }
-}
-
-int build_map_cols(const Shells &sh, int count, int KX, const float2 *const src[3], const int fac[3],
-                   const double los[3], float2 *out, double *powsum, int pow_mask, cudaStream_t st,
-                   int64_t *launches) {
-    const size_t smem = powsum ? sizeof(double) * 3 * sh.nb : 0;
-    const dim3 grid(grid_blocks((size_t)sh.Nm * sh.Nm * KX, 256, 152 * 2), (count + kMapChunk - 1) / kMapChunk);
-    build_map_cols_kernel<<<grid, 256, smem, st>>>(sh.N, sh.Nm, KX, sh.nb, sh.k2max, sh.lut.as<int>(), count, src[0],
-                                                   src[1], src[2], fac[0], fac[1], fac[2], los ? los[0] : 0,
-                                                   los ? los[1] : 0, los ? los[2] : 0, out, powsum, pow_mask);
-    PBI4G_LAUNCH_CHECK();
-    ++*launches;
-    return PBI4G_OK;
-}
-
-// The last (x) pass of the inverse 3D transform, after the (z, y) passes, on
-// planes kx < KX of Hermitian rows: x[n] = sum_k X[k] e^{+2 pi i k n / Nm} with
-// X[Nm - k] = conj X[k] (cuFFT's C2R convention).  With M = Nm / 2,
-// E[k] = X[k] + conj X[M-k] and O[k] = (X[k] - conj X[M-k]) e^{2 pi i k / Nm},
-// z = IDFT_M(E + i O) gives x[2m] = Re z[m], x[2m+1] = Im z[m].  A CTA takes 32
-// rows (one map, 32 consecutive (y, z)): it loads their KX coefficients with
-// coalesced reads along y, runs a mixed-radix Stockham FFT of the 32 rows
-// together in shared memory ([k][row], rows fastest), and writes each row with
-// one warp.
-namespace {
-__constant__ float2 c_roots[9][8];  // e^{2 pi i t / R} for R = 2..8
-constexpr int kXRows = 32;
-constexpr int kXPitch = kXRows + 1;  // padded [k][row] pitch of the shared tiles
-
-__device__ __forceinline__ float2 cadd2(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 csub2(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
-__device__ __forceinline__ float2 cmul2(float2 a, float2 b) {
-    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-__device__ __forceinline__ float2 itimes(float2 a) { return make_float2(-a.y, a.x); }  // i a
-
-// inverse (e^{+2 pi i q r / R}) DFT of R points in place
-template <int R>
-__device__ __forceinline__ void dft_small(float2 (&v)[8]) {
-    if constexpr (R == 2) {
-        const float2 a = v[0], b = v[1];
-        v[0] = cadd2(a, b);
-        v[1] = csub2(a, b);
-    } else if constexpr (R == 3) {
-        const float c = -0.5f, sn = 0.8660254037844386f;
-        const float2 b = cadd2(v[1], v[2]), d = csub2(v[1], v[2]);
-        const float2 t = make_float2(v[0].x + c * b.x, v[0].y + c * b.y);
-        const float2 u = itimes(make_float2(sn * d.x, sn * d.y));
-        v[0] = cadd2(v[0], b);
-        v[1] = cadd2(t, u);
-        v[2] = csub2(t, u);
-    } else if constexpr (R == 4) {
-        const float2 s02 = cadd2(v[0], v[2]), d02 = csub2(v[0], v[2]);
-        const float2 s13 = cadd2(v[1], v[3]), d13 = itimes(csub2(v[1], v[3]));
-        v[0] = cadd2(s02, s13);
-        v[2] = csub2(s02, s13);
-        v[1] = cadd2(d02, d13);
-        v[3] = csub2(d02, d13);
-    } else if constexpr (R == 5) {
-        const float c1 = 0.30901699437494745f, c2 = -0.8090169943749475f;
-        const float s1 = 0.9510565162951535f, s2 = 0.5877852522924731f;
-        const float2 b1 = cadd2(v[1], v[4]), b2 = cadd2(v[2], v[3]);
-        const float2 d1 = csub2(v[1], v[4]), d2 = csub2(v[2], v[3]);
-        const float2 t1 = make_float2(v[0].x + c1 * b1.x + c2 * b2.x, v[0].y + c1 * b1.y + c2 * b2.y);
-        const float2 t2 = make_float2(v[0].x + c2 * b1.x + c1 * b2.x, v[0].y + c2 * b1.y + c1 * b2.y);
-        const float2 u1 = itimes(make_float2(s1 * d1.x + s2 * d2.x, s1 * d1.y + s2 * d2.y));
-        const float2 u2 = itimes(make_float2(s2 * d1.x - s1 * d2.x, s2 * d1.y - s1 * d2.y));
-        v[0] = cadd2(v[0], cadd2(b1, b2));
-        v[1] = cadd2(t1, u1);
-        v[4] = csub2(t1, u1);
-        v[2] = cadd2(t2, u2);
-        v[3] = csub2(t2, u2);
-    } else {
-        float2 o[R];
-#pragma unroll
-        for (int q = 0; q < R; q++) {
-            float2 acc = v[0];
-#pragma unroll
-            for (int r = 1; r < R; r++) acc = cadd2(acc, cmul2(v[r], c_roots[R][(q * r) % R]));
-            o[q] = acc;
-        }
-#pragma unroll
-        for (int q = 0; q < R; q++) v[q] = o[q];
-    }
-}
-
-// one Stockham stage over the 32 rows of the tile: warp w takes butterflies
-// j = w, w + nwarps, ..., its lanes the rows (uniform j, twiddles broadcast)
-template <int R>
-__device__ __forceinline__ void stockham_stage(const float2 *__restrict__ b0, float2 *__restrict__ b1,
-                                               const float2 *__restrict__ tw, int M, int Ns, int warp, int nw,
-                                               int lane) {
-    const int nj = M / R, tstep = 2 * (M / (Ns * R));  // twiddle e^{2 pi i jn r / (Ns R)} = tw[jn r tstep]
-    for (int j = warp; j < nj; j += nw) {
-        float2 v[8];
-        const int jq = j / Ns, jn = j - jq * Ns;
-#pragma unroll
-        for (int r = 0; r < R; r++) {
-            const float2 a = b0[(j + r * nj) * kXPitch + lane];
-            v[r] = r > 0 ? cmul2(a, tw[jn * r * tstep]) : a;
-        }
-        dft_small<R>(v);
-        const int base = jq * Ns * R + jn;
-#pragma unroll
-        for (int r = 0; r < R; r++) b1[(base + r * Ns) * kXPitch + lane] = v[r];
-    }
-}
-}  // namespace
-
-struct XPassPlan {
-    int M = 0, nst = 0, rad[12] = {0};
-};
-
-// PF: rows of X a warp prefetches into registers for the next tile (KX <= PF * warps)
-template <int PF>
-__global__ void c2r_rows_kernel(const float2 *__restrict__ cols, float *__restrict__ out,
-                                const float2 *__restrict__ tw_g, XPassPlan xp, int Nm, int KX, int count,
-                                int dense) {
-    extern __shared__ float2 sx[];  // [Nm] twiddles | [M][kXPitch] x 2 buffers
-    const int M = xp.M;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const long long plane = (long long)Nm * Nm;
-    const long long tiles_per_map = (plane + kXRows - 1) / kXRows, ntiles = tiles_per_map * count;
-    float2 *tw = sx, *b0 = sx + Nm, *b1 = b0 + (size_t)M * kXPitch;
-    for (int t = threadIdx.x; t < Nm; t += blockDim.x) tw[t] = tw_g[t];
-    // the next tile's coefficients are loaded into registers while this tile computes
-    float2 pre[PF];
-    auto fetch = [&](long long tile) {
-        const int m = (int)(tile / tiles_per_map);
-        const long long row0 = (tile - (long long)m * tiles_per_map) * kXRows;
-        const bool ok = row0 + lane < plane;
-        const float2 *src = cols + (size_t)m * KX * plane + row0 + lane;
-#pragma unroll
-        for (int i = 0; i < PF; i++) {
-            const int k = warp + i * nw;
-            pre[i] = (k < KX && ok) ? __ldcs(src + (size_t)k * plane) : make_float2(0.f, 0.f);
-        }
-    };
-    if (blockIdx.x < ntiles) fetch(blockIdx.x);
-    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int m = (int)(tile / tiles_per_map);
-        const long long row0 = (tile - (long long)m * tiles_per_map) * kXRows;
-        const int nrows = (int)((plane - row0) < kXRows ? (plane - row0) : kXRows);
-        __syncthreads();
-        // raw coefficients X[k][row] for k < KX into b1, then prefetch the next tile
-#pragma unroll
-        for (int i = 0; i < PF; i++) {
-            const int k = warp + i * nw;
-            if (k < KX) b1[k * kXPitch + lane] = pre[i];
-        }
-        if (tile + gridDim.x < ntiles) fetch(tile + gridDim.x);
-        __syncthreads();
-        // Z = E + i O into b0
-        for (int k = warp; k < M; k += nw) {
-            const float2 xk = k < KX ? b1[k * kXPitch + lane] : make_float2(0.f, 0.f);
-            const int kc = M - k;
-            float2 xc = make_float2(0.f, 0.f);
-            if (kc < KX) {
-                xc = b1[kc * kXPitch + lane];
-                xc.y = -xc.y;
-            }
-            const float2 o = cmul2(csub2(xk, xc), tw[k]);
-            b0[k * kXPitch + lane] = cadd2(cadd2(xk, xc), itimes(o));
-        }
-        __syncthreads();
-        int Ns = 1;
-        float2 *in = b0, *ou = b1;
-        for (int s = 0; s < xp.nst; s++) {
-            const int R = xp.rad[s];
-            switch (R) {
-                case 2: stockham_stage<2>(in, ou, tw, M, Ns, warp, nw, lane); break;
-                case 3: stockham_stage<3>(in, ou, tw, M, Ns, warp, nw, lane); break;
-                case 4: stockham_stage<4>(in, ou, tw, M, Ns, warp, nw, lane); break;
-                case 5: stockham_stage<5>(in, ou, tw, M, Ns, warp, nw, lane); break;
-                default: stockham_stage<7>(in, ou, tw, M, Ns, warp, nw, lane); break;
-            }
-            __syncthreads();
-            float2 *t = in;
-            in = ou;
-            ou = t;
-            Ns *= R;
-        }
-        // x[2mm] = Re z[mm], x[2mm+1] = Im z[mm]; one warp per row
-        for (int l = warp; l < nrows; l += nw) {
-            const long long row = row0 + l;
-            float *o = dense ? out + (size_t)m * plane * Nm + (size_t)row * Nm
-                             : out + ((size_t)row * count + m) * Nm;
-            for (int mm = lane; mm < M; mm += 32) reinterpret_cast<float2 *>(o)[mm] = in[mm * kXPitch + l];
-        }
-    }
-}
-
-int c2r_rows(const Shells &sh, int count, int KX, const float2 *cols, float *out, bool dense, DevBuf &tw,
-             cudaStream_t st, int64_t *launches) {
-    const int Nm = sh.Nm, M = Nm / 2;
-    XPassPlan xp;
-    xp.M = M;
-    int rest = M;
-    for (int r : {4, 2, 3, 5, 7})
-        while (rest % r == 0 && xp.nst < 12) {
-            xp.rad[xp.nst++] = r;
-            rest /= r;
-        }
-    if (rest != 1 || KX > M) return set_error(PBI4G_ERR_UNSUPPORTED, "x pass: Nm=%d (KX=%d)", Nm, KX);
-    static std::once_flag roots_once;
-    static int roots_rc = 0;
-    std::call_once(roots_once, [] {
-        float2 h[9][8] = {};
-        for (int R = 2; R <= 8; R++)
-            for (int t = 0; t < R; t++) h[R][t] = make_float2((float)cos(2 * M_PI * t / R), (float)sin(2 * M_PI * t / R));
-        roots_rc = cudaMemcpyToSymbol(c_roots, h, sizeof(h)) == cudaSuccess ? 0 : 1;
-    });
-    if (roots_rc) return set_error(PBI4G_ERR_CUDA, "x pass: constant roots upload failed");
-    if (tw.bytes < sizeof(float2) * Nm) {
-        std::vector<float2> h(Nm);
-        for (int t = 0; t < Nm; t++) h[t] = make_float2((float)cos(2 * M_PI * t / Nm), (float)sin(2 * M_PI * t / Nm));
-        PBI4G_CHECK(tw.ensure(sizeof(float2) * Nm));
-        PBI4G_CUDA(cudaMemcpy(tw.p, h.data(), sizeof(float2) * Nm, cudaMemcpyHostToDevice));
-    }
-    const size_t smem = sizeof(float2) * (Nm + 2 * (size_t)M * kXPitch);
-    const int warps = 8, pf = (KX + warps - 1) / warps;
-    auto launch = [&](auto kern) -> int {
-        PBI4G_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        int per_sm = 0;
-        PBI4G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * 32, smem));
-        kern<<<152 * std::max(1, per_sm), warps * 32, smem, st>>>(cols, out, tw.as<float2>(), xp, Nm, KX, count,
-                                                                   dense ? 1 : 0);
-        PBI4G_LAUNCH_CHECK();
-        return PBI4G_OK;
-    };
-    if (pf <= 4) PBI4G_CHECK(launch(c2r_rows_kernel<4>));
-    else if (pf <= 9) PBI4G_CHECK(launch(c2r_rows_kernel<9>));
-    else if (pf <= 16) PBI4G_CHECK(launch(c2r_rows_kernel<16>));
-    else if (pf <= 32) PBI4G_CHECK(launch(c2r_rows_kernel<32>));
-    else return set_error(PBI4G_ERR_UNSUPPORTED, "x pass: KX=%d", KX);
-    ++*launches;
-    return PBI4G_OK;
-}
-
 template int build_map_spectra<double>(const Shells &, int, const double2 *const[3], const int[3], const double[3],
                                        double2 *, double *, int, cudaStream_t, int64_t *);
 

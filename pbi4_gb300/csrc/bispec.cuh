@@ -59,18 +59,6 @@ int build_map_spectra(const Shells &sh, int count, const typename Cx<R>::T *cons
                       const double los[3], typename Cx<R>::T *out, double *powsum, int pow_mask, cudaStream_t st,
                       int64_t *launches);
 
-// FP32 maps through the pruned inverse transform: build_map_cols writes the
-// spectra of `count` maps as planes [m][kx][z][y], kx < KX (KX > kmax; the
-// other planes of every map are zero); after an in-place batched 2D inverse C2C
-// over (z, y) of all count * KX planes, c2r_rows runs the last (x) pass and
-// writes the real maps, row-interleaved [z][y][m][x] (dense = false) or dense
-// [m][z][y][x] (dense = true).  tw: a per-plan twiddle table (filled on first use).
-int build_map_cols(const Shells &sh, int count, int KX, const float2 *const src[3], const int fac[3],
-                   const double los[3], float2 *out, double *powsum, int pow_mask, cudaStream_t st,
-                   int64_t *launches);
-int c2r_rows(const Shells &sh, int count, int KX, const float2 *cols, float *out, bool dense, DevBuf &tw,
-             cudaStream_t st, int64_t *launches);
-
 // Indicator half spectra of shells [m0, m0+count) (count_triangles, bispectrumI4.f90:862-869).
 template <class R>
 int build_indicator_spectra(const Shells &sh, int m0, int count, typename Cx<R>::T *out, cudaStream_t st,

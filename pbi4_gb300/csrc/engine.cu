@@ -91,7 +91,6 @@ int BkEngine::run(const typename Cx<R>::T *const src[3], const int fac[3], const
         tp_cross = cross;
         tp_fp64 = fp64;
     }
-    PBI4G_CHECK(maps.ensure(sizeof(C) * HC * nm));
     PBI4G_CHECK(powsum.ensure(sizeof(double) * 3 * nb));
     PBI4G_CHECK(S.ensure(sizeof(double) * std::max(1, tp.nslots)));
     const bool tc = tc_mode != 0 && !fp64 && !cross;
@@ -112,51 +111,47 @@ int BkEngine::run(const typename Cx<R>::T *const src[3], const int fac[3], const
                 if (fac[s] == 0) pow_mask |= 1 << s;
     }
     const size_t FCm = (size_t)N * N * N;
-    // FP64: in-place C2R (padded rows); plain FP32: out of place into dense maps;
-    // tensor-core forms: out of place into row-interleaved maps (the rows of all
-    // maps for one (y, z) side by side: one contiguous read per chunk of points)
+    // FP64: in-place C2R (padded rows); plain FP32: dense maps; tensor-core
+    // forms: row-interleaved maps (the rows of all maps for one (y, z) side by
+    // side: one contiguous read per chunk of points)
     const int layout = fp64 ? 0 : (tc ? 2 : 1);
     if (layout) PBI4G_CHECK(dense.ensure(sizeof(float) * FCm * nm));
-    pf.begin(6, st);
     PBI4G_CUDA(cudaMemsetAsync(powsum.p, 0, sizeof(double) * 3 * nb, st));
     if (fp64) {
+        PBI4G_CHECK(maps.ensure(sizeof(C) * HC * nm));
+        pf.begin(6, st);
         PBI4G_CHECK(build_map_spectra<R>(sh, nm, src, fac, los, maps.as<C>(), powsum.as<double>(), pow_mask, st,
                                          launches));
         pf.end(st);
-        if (!inv || inv_batch != nm || inv_N != N || inv_fp64 != 1) {
+        if (!inv || inv_batch != nm || inv_N != N) {
             if (inv) cufftDestroy(inv);
             inv = 0;
             int n[3] = {N, N, N}, inembed[3] = {N, N, NH}, onembed[3] = {N, N, 2 * NH};
             PBI4G_CUFFT(cufftPlanMany(&inv, 3, n, inembed, 1, (int)HC, onembed, 1, (int)(2 * HC), CUFFT_Z2D, nm));
             inv_batch = nm;
             inv_N = N;
-            inv_fp64 = 1;
         }
         PBI4G_CUFFT(cufftSetStream(inv, st));
         pf.begin(7, st);
         PBI4G_CUFFT(cufftExecZ2D(inv, maps.as<cufftDoubleComplex>(), maps.as<cufftDoubleReal>()));
         pf.end(st);
     } else {
-        // pruned inverse transform: columns kx < KX only (every shell mode has kx <= kmax)
-        const int KX = sh.kmax + 1;
-        const float2 *const *fsrc = reinterpret_cast<const float2 *const *>(src);
-        PBI4G_CHECK(build_map_cols(sh, nm, KX, fsrc, fac, los, maps.as<float2>(), powsum.as<double>(), pow_mask, st,
-                                   launches));
-        pf.end(st);
-        if (!inv || inv_batch != nm || inv_N != N || inv_fp64 != 0 || inv_kx != KX) {
-            if (inv) cufftDestroy(inv);
-            inv = 0;
-            int n[2] = {N, N};
-            PBI4G_CUFFT(cufftPlanMany(&inv, 2, n, nullptr, 1, N * N, nullptr, 1, N * N, CUFFT_C2C, nm * KX));
-            inv_batch = nm;
-            inv_N = N;
-            inv_fp64 = 0;
-            inv_kx = KX;
+        // pruned inverse transform: z pass (with the shell spectra), y pass, x pass
+        if (mt_nmaps != nm || mt.Nm != N) {
+            PBI4G_CHECK(mt.build(sh, nm));
+            mt_nmaps = nm;
         }
-        PBI4G_CUFFT(cufftSetStream(inv, st));
+        PBI4G_CHECK(maps.ensure(mt.work_bytes()));
+        const float2 *const *fsrc = reinterpret_cast<const float2 *const *>(src);
+        pf.begin(6, st);
+        PBI4G_CHECK(map_zpass(sh, mt, fsrc, fac, los, maps.as<float2>(), powsum.as<double>(), pow_mask, st,
+                              launches));
+        pf.end(st);
         pf.begin(7, st);
-        PBI4G_CUFFT(cufftExecC2C(inv, maps.as<cufftComplex>(), maps.as<cufftComplex>(), CUFFT_INVERSE));
-        PBI4G_CHECK(c2r_rows(sh, nm, KX, maps.as<float2>(), dense.as<float>(), layout == 1, xtw, st, launches));
+        PBI4G_CHECK(map_ypass(mt, maps.as<float2>(), st, launches));
+        pf.end(st);
+        pf.begin(10, st);
+        PBI4G_CHECK(map_xpass(mt, maps.as<float2>(), dense.as<float>(), layout == 1, st, launches));
         pf.end(st);
     }
     pf.begin(8, st);
@@ -254,6 +249,12 @@ static int check_config(const pbi4g_config *c) {
 extern "C" {
 
 const char *pbi4g_last_error(void) { return g_err; }
+
+int pbi4g_fft_plan_check(int32_t n, int32_t batch, const float *in, float *out) {
+    if (n < 2 || batch < 0 || (batch > 0 && (!in || !out)))
+        return set_error(PBI4G_ERR_INVALID, "fft plan check: n=%d batch=%d", n, batch);
+    return fft_plan_host_check(n, batch, in, out);
+}
 int pbi4g_version(void) { return 100; }
 
 int pbi4g_plan_footprint(const pbi4g_config *cfg, int64_t npart_max, int64_t *bytes) {
@@ -335,6 +336,14 @@ int pbi4g_plan_map_grid(const pbi4g_plan *plan, int32_t *map_grid, int32_t *nmap
     const bool bk = plan->cfg.do_bispectrum != 0;
     if (map_grid) *map_grid = bk ? plan->bk.sh.Nm : 0;
     if (nmaps) *nmaps = bk ? (plan->cfg.multipoles ? 3 : 1) * plan->bk.sh.nb : 0;
+    return PBI4G_OK;
+}
+
+int pbi4g_plan_map_work(const pbi4g_plan *plan, int64_t *zcols, int64_t *yplanes) {
+    if (!plan) return set_error(PBI4G_ERR_INVALID, "null plan");
+    const bool built = plan->cfg.do_bispectrum && plan->bk.mt_nmaps >= 0;
+    if (zcols) *zcols = built ? plan->bk.mt.tsize : 0;
+    if (yplanes) *yplanes = built ? plan->bk.mt.usize : 0;
     return PBI4G_OK;
 }
 

@@ -1,6 +1,7 @@
 // engine.cuh -- bispectrum engine shared by the plan and the drop-in entry points.
 #pragma once
 #include "bispec.cuh"
+#include "mapfft.cuh"
 #include "trisum_tm.cuh"
 
 namespace pbi4g {
@@ -36,11 +37,13 @@ struct BkEngine {
     TriPlan tp;
     int tp_nsets = -1, tp_cross = -1, tp_fp64 = -1;
     int nsets = 1, cross = 0;  // cross: 1 => q maps from the second field
-    DevBuf maps;               // [nmaps][N][N][N/2+1] complex half spectra (FP64: padded real maps after C2R)
-    DevBuf dense;              // FP32 forms: real maps of the out-of-place C2R (dense, or row-interleaved)
-    cufftHandle inv = 0;
-    int inv_batch = 0, inv_N = 0, inv_fp64 = -1, inv_kx = -1;
-    DevBuf xtw;                // twiddles of the x pass of the FP32 maps
+    DevBuf maps;               // FP64: [nmaps][N][N][N/2+1] half spectra, padded real maps after the C2R;
+                               // FP32: the pruned transform's intermediates (MapTransform T, U)
+    DevBuf dense;              // FP32 forms: real maps (dense, or row-interleaved)
+    cufftHandle inv = 0;       // FP64 maps: batched Z2D
+    int inv_batch = 0, inv_N = 0;
+    MapTransform mt;           // FP32 maps: pruned z / y / x passes
+    int mt_nmaps = -1;
     DevBuf powsum, S, partial;
     // tensor-core form: 0 off (CUDA cores), 1 FP16 hi+lo, 2 BF16, 3 TF32 hi+lo
     int tc_mode = 0;

@@ -1,0 +1,222 @@
+// fft_small.cuh -- building blocks of the shell-map inverse transforms
+// (mapfft.cu): complex helpers, inverse DFTs of 2, 3, 4, 5, 7 and 8 points, and
+// the host-side plan of an in-place mixed-radix decimation-in-frequency FFT.
+//
+// Sign convention: every transform here is an inverse DFT,
+//   X[k] = sum_n x[n] e^{+2 pi i n k / N}   (no 1/N: cuFFT's CUFFT_INVERSE / C2R).
+//
+// In-place DIF over a batch of transforms held as buf[n * pitch + t] (t the
+// transform, n the point): with N = R_1 R_2 ... R_s and L_1 = N, stage t
+// (radix R = R_t, Ls = L_t / R) runs N / R butterflies j = b Ls + n1 over the
+// points base + Ls r (base = b L_t + n1, r < R): an R-point DFT, then output q
+// times e^{2 pi i n1 q / L_t}, stored back in place; L_{t+1} = Ls.  The result
+// X[k] ends at the digit-reversed position perm[k]: for k = q + R_1 k1,
+// perm_N(k) = q N / R_1 + perm_{N/R_1}(k1).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <vector>
+
+namespace pbi4g {
+namespace fftd {
+
+__host__ __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__host__ __device__ __forceinline__ float2 itimes(float2 a) { return make_float2(-a.y, a.x); }  // i a
+__host__ __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(s * a.x, s * a.y); }
+
+// inverse DFT of R points in place: v[q] <- sum_r v[r] e^{+2 pi i q r / R}
+template <int R>
+__host__ __device__ __forceinline__ void dft_small(float2 (&v)[8]) {
+    if constexpr (R == 2) {
+        const float2 a = v[0], b = v[1];
+        v[0] = cadd(a, b);
+        v[1] = csub(a, b);
+    } else if constexpr (R == 3) {
+        const float c = -0.5f, sn = 0.8660254037844386f;
+        const float2 b = cadd(v[1], v[2]), d = csub(v[1], v[2]);
+        const float2 t = make_float2(v[0].x + c * b.x, v[0].y + c * b.y);
+        const float2 u = itimes(cscale(d, sn));
+        v[0] = cadd(v[0], b);
+        v[1] = cadd(t, u);
+        v[2] = csub(t, u);
+    } else if constexpr (R == 4) {
+        const float2 s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
+        const float2 s13 = cadd(v[1], v[3]), d13 = itimes(csub(v[1], v[3]));
+        v[0] = cadd(s02, s13);
+        v[2] = csub(s02, s13);
+        v[1] = cadd(d02, d13);
+        v[3] = csub(d02, d13);
+    } else if constexpr (R == 5) {
+        const float c1 = 0.30901699437494745f, c2 = -0.8090169943749475f;
+        const float s1 = 0.9510565162951535f, s2 = 0.5877852522924731f;
+        const float2 b1 = cadd(v[1], v[4]), b2 = cadd(v[2], v[3]);
+        const float2 d1 = csub(v[1], v[4]), d2 = csub(v[2], v[3]);
+        const float2 t1 = make_float2(v[0].x + c1 * b1.x + c2 * b2.x, v[0].y + c1 * b1.y + c2 * b2.y);
+        const float2 t2 = make_float2(v[0].x + c2 * b1.x + c1 * b2.x, v[0].y + c2 * b1.y + c1 * b2.y);
+        const float2 u1 = itimes(make_float2(s1 * d1.x + s2 * d2.x, s1 * d1.y + s2 * d2.y));
+        const float2 u2 = itimes(make_float2(s2 * d1.x - s1 * d2.x, s2 * d1.y - s1 * d2.y));
+        v[0] = cadd(v[0], cadd(b1, b2));
+        v[1] = cadd(t1, u1);
+        v[4] = csub(t1, u1);
+        v[2] = cadd(t2, u2);
+        v[3] = csub(t2, u2);
+    } else if constexpr (R == 7) {
+        // pairs (r, 7 - r): X[q] = v0 + sum_k cos(2 pi k q / 7) b_k + i sum_k sin(2 pi k q / 7) d_k
+        const float c1 = 0.6234898018587336f, c2 = -0.22252093395631434f, c3 = -0.900968867902419f;
+        const float s1 = 0.7818314824680298f, s2 = 0.9749279121818236f, s3 = 0.43388373911755823f;
+        const float2 b1 = cadd(v[1], v[6]), b2 = cadd(v[2], v[5]), b3 = cadd(v[3], v[4]);
+        const float2 d1 = csub(v[1], v[6]), d2 = csub(v[2], v[5]), d3 = csub(v[3], v[4]);
+        const float2 x0 = v[0];
+        const float2 t1 = make_float2(x0.x + c1 * b1.x + c2 * b2.x + c3 * b3.x, x0.y + c1 * b1.y + c2 * b2.y + c3 * b3.y);
+        const float2 t2 = make_float2(x0.x + c2 * b1.x + c3 * b2.x + c1 * b3.x, x0.y + c2 * b1.y + c3 * b2.y + c1 * b3.y);
+        const float2 t3 = make_float2(x0.x + c3 * b1.x + c1 * b2.x + c2 * b3.x, x0.y + c3 * b1.y + c1 * b2.y + c2 * b3.y);
+        const float2 u1 = itimes(make_float2(s1 * d1.x + s2 * d2.x + s3 * d3.x, s1 * d1.y + s2 * d2.y + s3 * d3.y));
+        const float2 u2 = itimes(make_float2(s2 * d1.x - s3 * d2.x - s1 * d3.x, s2 * d1.y - s3 * d2.y - s1 * d3.y));
+        const float2 u3 = itimes(make_float2(s3 * d1.x - s1 * d2.x + s2 * d3.x, s3 * d1.y - s1 * d2.y + s2 * d3.y));
+        v[0] = cadd(x0, cadd(b1, cadd(b2, b3)));
+        v[1] = cadd(t1, u1);
+        v[6] = csub(t1, u1);
+        v[2] = cadd(t2, u2);
+        v[5] = csub(t2, u2);
+        v[3] = cadd(t3, u3);
+        v[4] = csub(t3, u3);
+    } else {
+        static_assert(R == 8, "radix");
+        // one radix-2 step (n, n + 4) then two 4-point DFTs: even outputs from the
+        // sums, odd outputs from the differences times e^{2 pi i r / 8}
+        const float h = 0.7071067811865476f;
+        float2 a[4], b[4];
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            a[r] = cadd(v[r], v[r + 4]);
+            b[r] = csub(v[r], v[r + 4]);
+        }
+        b[1] = make_float2(h * (b[1].x - b[1].y), h * (b[1].x + b[1].y));    // (1 + i) / sqrt 2
+        b[2] = itimes(b[2]);                                                // i
+        b[3] = make_float2(-h * (b[3].x + b[3].y), h * (b[3].x - b[3].y));  // (-1 + i) / sqrt 2
+        float2 e[8], o[8];
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            e[r] = a[r];
+            o[r] = b[r];
+        }
+        dft_small<4>(e);
+        dft_small<4>(o);
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            v[2 * q] = e[q];
+            v[2 * q + 1] = o[q];
+        }
+    }
+}
+
+// One DIF butterfly of radix R for the transform in column `t` of buf (pitch
+// between points): points base + ls r, outputs times tw[q * tstep] (tw[s] =
+// e^{2 pi i s / N}), in place.
+template <int R>
+__host__ __device__ __forceinline__ void dif_butterfly(float2 *buf, int pitch, int t, int base, int ls, int tstep,
+                                                       const float2 *tw) {
+    float2 v[8];
+#pragma unroll
+    for (int r = 0; r < R; r++) v[r] = buf[(base + ls * r) * pitch + t];
+    dft_small<R>(v);
+    buf[base * pitch + t] = v[0];
+#pragma unroll
+    for (int q = 1; q < R; q++) buf[(base + ls * q) * pitch + t] = tstep ? cmul(v[q], tw[q * tstep]) : v[q];
+}
+
+constexpr int kMaxStages = 10;
+
+// Device-side description of an in-place DIF plan; its tables (stage entries,
+// perm, twiddles) live in one device buffer laid out as FftPlan::pack writes it.
+struct FftDesc {
+    int n = 0, nst = 0;
+    int rad[kMaxStages] = {0}, ls[kMaxStages] = {0}, eoff[kMaxStages] = {0};
+    int nent = 0;  // stage entries in total
+};
+
+// Host plan: radices, per-stage butterfly entries (base, tstep), output perm, twiddles.
+struct FftPlan {
+    FftDesc d;
+    std::vector<int2> ent;   // [nent]: (base, tstep) per butterfly, stage by stage
+    std::vector<int> perm;   // [n]: position of X[k]
+    std::vector<float2> tw;  // [n]: e^{2 pi i s / n}
+
+    // false when n has a prime factor above 7 (or needs too many stages)
+    bool build(int n) {
+        d = FftDesc();
+        d.n = n;
+        int rest = n;
+        for (int r : {8, 4, 2, 3, 5, 7})
+            while (rest % r == 0) {
+                if (d.nst == kMaxStages) return false;
+                d.rad[d.nst++] = r;
+                rest /= r;
+            }
+        if (rest != 1 || n < 2) return false;
+        ent.clear();
+        int L = n;
+        for (int s = 0; s < d.nst; s++) {
+            const int R = d.rad[s], Ls = L / R;
+            d.ls[s] = Ls;
+            d.eoff[s] = (int)ent.size();
+            for (int j = 0; j < n / R; j++) {
+                const int b = j / Ls, n1 = j % Ls;
+                ent.push_back(make_int2(b * L + n1, n1 * (n / L)));
+            }
+            L = Ls;
+        }
+        d.nent = (int)ent.size();
+        perm.assign(n, 0);
+        for (int k = 0; k < n; k++) {
+            int pos = 0, kk = k, len = n;
+            for (int s = 0; s < d.nst; s++) {
+                const int R = d.rad[s], sub = len / R;
+                pos += (kk % R) * sub;
+                kk /= R;
+                len = sub;
+            }
+            perm[k] = pos;
+        }
+        tw.resize(n);
+        for (int s = 0; s < n; s++)
+            tw[s] = make_float2((float)std::cos(2.0 * M_PI * s / n), (float)std::sin(2.0 * M_PI * s / n));
+        return true;
+    }
+
+    // bytes of the packed tables: twiddles, entries, perm
+    size_t bytes() const { return sizeof(float2) * tw.size() + sizeof(int2) * ent.size() + sizeof(int) * perm.size(); }
+    void pack(unsigned char *dst) const {
+        size_t o = 0;
+        for (const float2 &t : tw) { *reinterpret_cast<float2 *>(dst + o) = t; o += sizeof(float2); }
+        for (const int2 &e : ent) { *reinterpret_cast<int2 *>(dst + o) = e; o += sizeof(int2); }
+        for (int p : perm) { *reinterpret_cast<int *>(dst + o) = p; o += sizeof(int); }
+    }
+};
+
+// Run the plan over transform t of buf on one thread (the host check of the
+// plan and butterflies; the kernels run the same butterflies across warps).
+inline void run_plan_host(const FftPlan &p, float2 *buf, int pitch, int t) {
+    for (int s = 0; s < p.d.nst; s++) {
+        for (int j = 0; j < p.d.n / p.d.rad[s]; j++) {
+            const int2 e = p.ent[p.d.eoff[s] + j];
+            switch (p.d.rad[s]) {
+                case 2: dif_butterfly<2>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
+                case 3: dif_butterfly<3>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
+                case 4: dif_butterfly<4>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
+                case 5: dif_butterfly<5>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
+                case 7: dif_butterfly<7>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
+                default: dif_butterfly<8>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
+            }
+        }
+    }
+}
+
+}  // namespace fftd
+}  // namespace pbi4g

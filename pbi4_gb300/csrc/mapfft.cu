@@ -1,0 +1,489 @@
+// mapfft.cu -- pruned inverse transform of the FP32 shell maps (see mapfft.cuh).
+//
+// The maps are the "real-space shell" fields of bispectrumI4.f90 (the C2R of
+// the shell-masked delta(k), bispectrumI4.f90:120-158 and 430-474 for the
+// multipole sets); the same maps as build_map_spectra + a full C2R, with the
+// zero parts of the shell spectra never stored or transformed.
+//
+// Every pass runs tiles of 32 one-dimensional transforms (lanes = transforms,
+// warps = butterflies) through an in-place mixed-radix DIF FFT in shared memory
+// ([point][transform], pitch 33 float2): no ping-pong buffer, so four CTAs of
+// 256 threads fit on an SM for the 200-point transforms of the 256^3 workload.
+#include "mapfft.cuh"
+
+#include <math.h>
+
+#include <algorithm>
+
+namespace pbi4g {
+
+namespace {
+
+constexpr int kP = 33;        // shared pitch (float2) between the points of a tile
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ float2 czero() { return make_float2(0.f, 0.f); }
+
+// copy the packed plan tables (twiddles | entries | positions) into shared memory
+__device__ __forceinline__ void load_tables(const unsigned char *__restrict__ tab, const fftd::FftDesc &fd,
+                                            float2 *tw, int2 *ent, int *perm) {
+    const float2 *t = reinterpret_cast<const float2 *>(tab);
+    const int2 *e = reinterpret_cast<const int2 *>(t + fd.n);
+    const int *p = reinterpret_cast<const int *>(e + fd.nent);
+    for (int i = threadIdx.x; i < fd.n; i += blockDim.x) {
+        tw[i] = t[i];
+        perm[i] = p[i];
+    }
+    for (int i = threadIdx.x; i < fd.nent; i += blockDim.x) ent[i] = e[i];
+}
+
+// the plan's stages over the 32 transforms of a tile (ends with a barrier)
+__device__ __forceinline__ void run_dif(const fftd::FftDesc &fd, float2 *buf, const int2 *ent, const float2 *tw,
+                                        int warp, int nw, int lane) {
+    for (int s = 0; s < fd.nst; s++) {
+        const int R = fd.rad[s], ls = fd.ls[s], nbf = fd.n / R;
+        const int2 *e = ent + fd.eoff[s];
+        switch (R) {
+            case 8:
+                for (int j = warp; j < nbf; j += nw) fftd::dif_butterfly<8>(buf, kP, lane, e[j].x, ls, e[j].y, tw);
+                break;
+            case 4:
+                for (int j = warp; j < nbf; j += nw) fftd::dif_butterfly<4>(buf, kP, lane, e[j].x, ls, e[j].y, tw);
+                break;
+            case 2:
+                for (int j = warp; j < nbf; j += nw) fftd::dif_butterfly<2>(buf, kP, lane, e[j].x, ls, e[j].y, tw);
+                break;
+            case 3:
+                for (int j = warp; j < nbf; j += nw) fftd::dif_butterfly<3>(buf, kP, lane, e[j].x, ls, e[j].y, tw);
+                break;
+            case 5:
+                for (int j = warp; j < nbf; j += nw) fftd::dif_butterfly<5>(buf, kP, lane, e[j].x, ls, e[j].y, tw);
+                break;
+            default:
+                for (int j = warp; j < nbf; j += nw) fftd::dif_butterfly<7>(buf, kP, lane, e[j].x, ls, e[j].y, tw);
+                break;
+        }
+        __syncthreads();
+    }
+}
+
+size_t table_smem(const fftd::FftDesc &fd) {
+    return sizeof(float2) * fd.n + sizeof(int2) * fd.nent + sizeof(int) * fd.n;
+}
+
+struct ZArgs {
+    int N, NH, Nm, nb, k2max;
+    const int *lut;
+    const float2 *src[3];
+    int fac[3];
+    double los[3];
+    double *powsum;
+    int pow_mask;
+    const int2 *cols;
+    const MapInfo *info;
+    const int2 *tiles;
+    int ntiles;
+    const unsigned char *tab;
+    fftd::FftDesc fd;
+    float2 *T;
+};
+
+// z pass: tile = (map m, 32 columns (kx, ky) of its shell).  Point i of a
+// column is kz = kfreq0(i, Nm); a mode enters when lut[k^2] is the map's shell
+// (the mask, multipole factor and kx = 0 symmetrisation of build_map_spectra).
+__global__ void __launch_bounds__(kThreads) map_zpass_kernel(const ZArgs a) {
+    extern __shared__ __align__(16) unsigned char zsm[];
+    const fftd::FftDesc &fd = a.fd;
+    const int Nm = a.Nm, N = a.N, nb = a.nb;
+    float2 *tw = reinterpret_cast<float2 *>(zsm);
+    int2 *ent = reinterpret_cast<int2 *>(tw + fd.n);
+    int *perm = reinterpret_cast<int *>(ent + fd.nent);
+    float2 *buf = reinterpret_cast<float2 *>(perm + fd.n);
+    double *spow = reinterpret_cast<double *>(buf + (size_t)Nm * kP);
+    load_tables(a.tab, fd, tw, ent, perm);
+    if (a.powsum)
+        for (int b = threadIdx.x; b < 3 * nb; b += blockDim.x) spow[b] = 0.0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
+        const int2 tl = a.tiles[tile];
+        const int m = tl.x, c0 = tl.y;
+        const MapInfo mi = a.info[m];
+        const int s = m / nb, b = mi.shell + 1;
+        const int c = c0 + lane;
+        const bool valid = c < mi.ncol;
+        const int2 kk = valid ? a.cols[mi.col0 + c] : make_int2(0, 0);
+        const int kx = kk.x, ky = kk.y, kzl = mi.kxn - 1;
+        const float2 *src = a.src[s];
+        const int fac = a.fac[s];
+        const bool pw = a.powsum && (a.pow_mask >> s & 1);
+        const int yN = ky < 0 ? ky + N : ky;
+        const double lxy = a.los[0] * kx + a.los[1] * ky;
+        for (int i = warp; i < Nm; i += nw) {
+            const int kz = kfreq0(i, Nm);
+            float2 v = czero();
+            if (valid && kz >= -kzl && kz <= kzl) {
+                const int k2 = kx * kx + ky * ky + kz * kz;
+                const int sb = k2 <= a.k2max ? __ldg(a.lut + k2) : 0;
+                if (sb == b) {
+                    const int zN = kz < 0 ? kz + N : kz;
+                    v = src[((size_t)zN * N + yN) * a.NH + kx];
+                    if (kx == 0) {
+                        const float2 w = src[((size_t)kneg0(zN, N) * N + kneg0(yN, N)) * a.NH];
+                        v.x = (v.x + w.x) * 0.5f;
+                        v.y = (v.y - w.y) * 0.5f;
+                    }
+                    if (fac) {
+                        const double lk = lxy + a.los[2] * kz;
+                        const float mu2 = k2 > 0 ? (float)(lk * lk / (double)k2) : 0.f;
+                        const float L = fac == 2 ? -0.5f + 1.5f * mu2 : 0.375f + mu2 * (-3.75f + 4.375f * mu2);
+                        v.x *= L;
+                        v.y *= L;
+                    }
+                    if (pw)
+                        atomicAdd(&spow[s * nb + b - 1],
+                                  (kx == 0 ? 1.0 : 2.0) * ((double)v.x * v.x + (double)v.y * v.y));
+                }
+            }
+            buf[i * kP + lane] = v;
+        }
+        __syncthreads();
+        run_dif(fd, buf, ent, tw, warp, nw, lane);
+        // column c0 + l -> T[tbase + (c0 + l) Nm + z], z along the lanes
+        for (int l = warp; l < 32; l += nw) {
+            if (c0 + l >= mi.ncol) break;
+            float2 *o = a.T + mi.tbase + (size_t)(c0 + l) * Nm;
+            for (int z = lane; z < Nm; z += 32) o[z] = buf[perm[z] * kP + l];
+        }
+        __syncthreads();
+    }
+    if (a.powsum) {
+        for (int b = threadIdx.x; b < 3 * nb; b += blockDim.x)
+            if (spow[b] != 0.0) atomicAdd(a.powsum + b, spow[b]);
+    }
+}
+
+struct YArgs {
+    int Nm;
+    const MapInfo *info;
+    const int2 *kxr;
+    const int2 *tiles;
+    int ntiles;
+    const unsigned char *tab;
+    fftd::FftDesc fd;
+    const float2 *T;
+    float2 *U;
+};
+
+// y pass: tile = (map m, 32 consecutive transforms t = kx Nm + z); input
+// ky in [-r(kx), r(kx)] from T, output U[m][kx][z][y].
+__global__ void __launch_bounds__(kThreads) map_ypass_kernel(const YArgs a) {
+    extern __shared__ __align__(16) unsigned char ysm[];
+    const fftd::FftDesc &fd = a.fd;
+    const int Nm = a.Nm;
+    float2 *tw = reinterpret_cast<float2 *>(ysm);
+    int2 *ent = reinterpret_cast<int2 *>(tw + fd.n);
+    int *perm = reinterpret_cast<int *>(ent + fd.nent);
+    float2 *buf = reinterpret_cast<float2 *>(perm + fd.n);
+    load_tables(a.tab, fd, tw, ent, perm);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
+        const int2 tl = a.tiles[tile];
+        const int m = tl.x, t0 = tl.y;
+        const MapInfo mi = a.info[m];
+        const int ntr = mi.kxn * Nm;
+        const int t = t0 + lane;
+        const bool valid = t < ntr;
+        const int kx = valid ? t / Nm : 0, z = valid ? t - kx * Nm : 0;
+        const int2 rc = valid ? a.kxr[mi.kx0 + kx] : make_int2(-1, 0);  // (r, first column)
+        const float2 *in = a.T + mi.tbase + (size_t)(rc.y + rc.x) * Nm + z;  // column ky = 0
+        for (int i = warp; i < Nm; i += nw) {
+            const int ky = kfreq0(i, Nm);
+            buf[i * kP + lane] = (ky >= -rc.x && ky <= rc.x) ? __ldcs(in + (ptrdiff_t)ky * Nm) : czero();
+        }
+        __syncthreads();
+        run_dif(fd, buf, ent, tw, warp, nw, lane);
+        for (int l = warp; l < 32; l += nw) {
+            if (t0 + l >= ntr) break;
+            float2 *o = a.U + mi.ubase + (size_t)(t0 + l) * Nm;
+            for (int y = lane; y < Nm; y += 32) o[y] = buf[perm[y] * kP + l];
+        }
+        __syncthreads();
+    }
+}
+
+struct XArgs {
+    int Nm, count, kxmax, dense;
+    const MapInfo *info;
+    const unsigned char *tab;
+    fftd::FftDesc fd;   // M = Nm / 2 points
+    const float2 *xtw;  // e^{2 pi i k / Nm}
+    const float2 *U;
+    float *out;
+};
+
+// x pass: tile = (map m, 32 consecutive rows (z, y)).  With M = Nm / 2,
+// Z[k] = (X[k] + conj X[M-k]) + i (X[k] - conj X[M-k]) e^{2 pi i k / Nm} and
+// z = IDFT_M(Z) give the C2R output x[2j] = Re z[j], x[2j+1] = Im z[j]; the
+// pair (k, M - k) is formed in place.  PF: coefficient rows a warp prefetches
+// into registers for the next tile (kxmax <= PF * warps).
+template <int PF>
+__global__ void __launch_bounds__(kThreads, PF <= 9 ? 4 : 2) map_xpass_kernel(const XArgs a) {
+    extern __shared__ __align__(16) unsigned char xsm[];
+    const fftd::FftDesc &fd = a.fd;
+    const int Nm = a.Nm, M = fd.n, KX = a.kxmax;
+    float2 *tw = reinterpret_cast<float2 *>(xsm);
+    int2 *ent = reinterpret_cast<int2 *>(tw + fd.n);
+    int *perm = reinterpret_cast<int *>(ent + fd.nent);
+    float2 *xt = reinterpret_cast<float2 *>(perm + fd.n);  // [Nm]
+    float2 *buf = xt + Nm;                                 // [M][kP]
+    load_tables(a.tab, fd, tw, ent, perm);
+    for (int i = threadIdx.x; i < Nm; i += blockDim.x) xt[i] = a.xtw[i];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const long long plane = (long long)Nm * Nm;
+    const long long tiles_per_map = (plane + 31) / 32, ntiles = tiles_per_map * a.count;
+    float2 pre[PF];
+    auto fetch = [&](long long tile) {
+        const int m = (int)(tile / tiles_per_map);
+        const long long row0 = (tile - (long long)m * tiles_per_map) * 32;
+        const bool ok = row0 + lane < plane;
+        const MapInfo &mi = a.info[m];
+        const int kxn = mi.kxn;
+        const float2 *src = a.U + mi.ubase + row0 + lane;
+#pragma unroll
+        for (int i = 0; i < PF; i++) {
+            const int k = warp + i * nw;
+            pre[i] = (k < kxn && ok) ? __ldcs(src + (size_t)k * plane) : czero();
+        }
+    };
+    if (blockIdx.x < ntiles) fetch(blockIdx.x);
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int m = (int)(tile / tiles_per_map);
+        const long long row0 = (tile - (long long)m * tiles_per_map) * 32;
+        const int nrows = (int)((plane - row0) < 32 ? (plane - row0) : 32);
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < PF; i++) {
+            const int k = warp + i * nw;
+            if (k < KX) buf[k * kP + lane] = pre[i];
+        }
+        if (tile + gridDim.x < ntiles) fetch(tile + gridDim.x);
+        __syncthreads();
+        // (k, M - k) pairs in place; rows >= KX hold no coefficients (zero)
+        for (int k = warp; k <= M / 2; k += nw) {
+            const int kc = M - k;
+            const float2 xk = k < KX ? buf[k * kP + lane] : czero();
+            const float2 xc = (k > 0 && kc < KX) ? buf[kc * kP + lane] : czero();  // X[M - k]
+            const float2 ck = make_float2(xc.x, -xc.y), cc = make_float2(xk.x, -xk.y);
+            const float2 o1 = fftd::cmul(fftd::csub(xk, ck), xt[k]);
+            const float2 z1 = fftd::cadd(fftd::cadd(xk, ck), fftd::itimes(o1));
+            if (k > 0 && kc != k) {
+                const float2 o2 = fftd::cmul(fftd::csub(xc, cc), xt[kc]);
+                buf[kc * kP + lane] = fftd::cadd(fftd::cadd(xc, cc), fftd::itimes(o2));
+            }
+            buf[k * kP + lane] = z1;
+        }
+        __syncthreads();
+        run_dif(fd, buf, ent, tw, warp, nw, lane);
+        for (int l = warp; l < nrows; l += nw) {
+            const long long row = row0 + l;
+            float *o = a.dense ? a.out + (size_t)m * plane * Nm + (size_t)row * Nm
+                               : a.out + ((size_t)row * a.count + m) * Nm;
+            for (int j = lane; j < M; j += 32) reinterpret_cast<float2 *>(o)[j] = buf[perm[j] * kP + l];
+        }
+    }
+}
+
+int upload(DevBuf &d, const void *h, size_t bytes) {
+    PBI4G_CHECK(d.ensure(bytes > 0 ? bytes : 8));
+    if (bytes) PBI4G_CUDA(cudaMemcpy(d.p, h, bytes, cudaMemcpyHostToDevice));
+    return PBI4G_OK;
+}
+
+int upload_plan(DevBuf &d, const fftd::FftPlan &p) {
+    std::vector<unsigned char> h(p.bytes());
+    p.pack(h.data());
+    return upload(d, h.data(), h.size());
+}
+
+int grid_for(const void *kern, size_t smem, int work) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem) != cudaSuccess) per_sm = 1;
+    return std::max(1, std::min(work, 152 * std::max(1, per_sm)));
+}
+
+}  // namespace
+
+int MapTransform::build(const Shells &s, int nm) {
+    Nm = s.Nm;
+    nmaps = nm;
+    nb = s.nb;
+    if (Nm % 4 || !pz.build(Nm) || !px.build(Nm / 2))
+        return set_error(PBI4G_ERR_UNSUPPORTED, "map transform: map grid %d", Nm);
+    // per shell: largest k^2, the kx range and the (kx, ky) columns
+    std::vector<int> k2hi(nb, -1);
+    for (int k2 = 0; k2 <= s.k2max && k2 < (int)s.lut_h.size(); k2++) {
+        const int b = s.lut_h[k2];
+        if (b >= 1 && b <= nb) k2hi[b - 1] = std::max(k2hi[b - 1], k2);
+    }
+    std::vector<int2> cols_h, kxr_h;
+    std::vector<int> kxn(nb), ncol(nb), col0(nb), kx0(nb);
+    auto isqrt = [](int v) {
+        int r = (int)std::sqrt((double)v);
+        while (r * r > v) r--;
+        while ((r + 1) * (r + 1) <= v) r++;
+        return r;
+    };
+    kxmax = 0;
+    for (int b = 0; b < nb; b++) {
+        col0[b] = (int)cols_h.size();
+        kx0[b] = (int)kxr_h.size();
+        kxn[b] = k2hi[b] >= 0 ? isqrt(k2hi[b]) + 1 : 0;
+        if (kxn[b] > Nm / 2) return set_error(PBI4G_ERR_UNSUPPORTED, "map transform: shell %d above Nm/2", b + 1);
+        for (int kx = 0; kx < kxn[b]; kx++) {
+            const int r = isqrt(k2hi[b] - kx * kx);
+            kxr_h.push_back(make_int2(r, (int)cols_h.size() - col0[b]));
+            for (int ky = -r; ky <= r; ky++) cols_h.push_back(make_int2(kx, ky));
+        }
+        ncol[b] = (int)cols_h.size() - col0[b];
+        kxmax = std::max(kxmax, kxn[b]);
+    }
+    info_h.assign(nm, MapInfo{});
+    std::vector<int2> zt, yt;
+    long long tb = 0, ub = 0;
+    for (int m = 0; m < nm; m++) {
+        const int b = m % nb;
+        MapInfo &mi = info_h[m];
+        mi.shell = b;
+        mi.kxn = kxn[b];
+        mi.ncol = ncol[b];
+        mi.col0 = col0[b];
+        mi.kx0 = kx0[b];
+        mi.pad = 0;
+        mi.tbase = tb;
+        mi.ubase = ub;
+        tb += (long long)ncol[b] * Nm;
+        ub += (long long)kxn[b] * Nm * Nm;
+        for (int c = 0; c < ncol[b]; c += 32) zt.push_back(make_int2(m, c));
+        for (int t = 0; t < kxn[b] * Nm; t += 32) yt.push_back(make_int2(m, t));
+    }
+    tsize = tb;
+    usize = ub;
+    nzt = (int)zt.size();
+    nyt = (int)yt.size();
+    std::vector<float2> xt(Nm);
+    for (int k = 0; k < Nm; k++) xt[k] = make_float2((float)cos(2 * M_PI * k / Nm), (float)sin(2 * M_PI * k / Nm));
+    PBI4G_CHECK(upload_plan(tab_z, pz));
+    PBI4G_CHECK(upload_plan(tab_x, px));
+    PBI4G_CHECK(upload(xtw, xt.data(), sizeof(float2) * Nm));
+    PBI4G_CHECK(upload(cols, cols_h.data(), sizeof(int2) * cols_h.size()));
+    PBI4G_CHECK(upload(kxr, kxr_h.data(), sizeof(int2) * kxr_h.size()));
+    PBI4G_CHECK(upload(info, info_h.data(), sizeof(MapInfo) * info_h.size()));
+    PBI4G_CHECK(upload(ztiles, zt.data(), sizeof(int2) * zt.size()));
+    PBI4G_CHECK(upload(ytiles, yt.data(), sizeof(int2) * yt.size()));
+    return PBI4G_OK;
+}
+
+int map_zpass(const Shells &sh, const MapTransform &mt, const float2 *const src[3], const int fac[3],
+              const double los[3], float2 *work, double *powsum, int pow_mask, cudaStream_t st, int64_t *launches) {
+    if (mt.nzt == 0) return PBI4G_OK;
+    ZArgs a;
+    a.N = sh.N;
+    a.NH = sh.N / 2 + 1;
+    a.Nm = mt.Nm;
+    a.nb = mt.nb;
+    a.k2max = sh.k2max;
+    a.lut = sh.lut.as<int>();
+    for (int s = 0; s < 3; s++) {
+        a.src[s] = src[s];
+        a.fac[s] = fac[s];
+        a.los[s] = los ? los[s] : 0.0;
+    }
+    a.powsum = powsum;
+    a.pow_mask = pow_mask;
+    a.cols = mt.cols.as<int2>();
+    a.info = mt.info.as<MapInfo>();
+    a.tiles = mt.ztiles.as<int2>();
+    a.ntiles = mt.nzt;
+    a.tab = static_cast<const unsigned char *>(mt.tab_z.p);
+    a.fd = mt.pz.d;
+    a.T = work;
+    const size_t smem = table_smem(mt.pz.d) + sizeof(float2) * (size_t)mt.Nm * kP + sizeof(double) * 3 * mt.nb;
+    PBI4G_CUDA(cudaFuncSetAttribute(map_zpass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    map_zpass_kernel<<<grid_for((const void *)map_zpass_kernel, smem, mt.nzt), kThreads, smem, st>>>(a);
+    PBI4G_LAUNCH_CHECK();
+    ++*launches;
+    return PBI4G_OK;
+}
+
+int map_ypass(const MapTransform &mt, float2 *work, cudaStream_t st, int64_t *launches) {
+    if (mt.nyt == 0) return PBI4G_OK;
+    YArgs a;
+    a.Nm = mt.Nm;
+    a.info = mt.info.as<MapInfo>();
+    a.kxr = mt.kxr.as<int2>();
+    a.tiles = mt.ytiles.as<int2>();
+    a.ntiles = mt.nyt;
+    a.tab = static_cast<const unsigned char *>(mt.tab_z.p);
+    a.fd = mt.pz.d;
+    a.T = work;
+    a.U = work + mt.tsize;
+    const size_t smem = table_smem(mt.pz.d) + sizeof(float2) * (size_t)mt.Nm * kP;
+    PBI4G_CUDA(cudaFuncSetAttribute(map_ypass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    map_ypass_kernel<<<grid_for((const void *)map_ypass_kernel, smem, mt.nyt), kThreads, smem, st>>>(a);
+    PBI4G_LAUNCH_CHECK();
+    ++*launches;
+    return PBI4G_OK;
+}
+
+int map_xpass(const MapTransform &mt, const float2 *work, float *out, bool dense, cudaStream_t st,
+              int64_t *launches) {
+    if (mt.nmaps == 0) return PBI4G_OK;
+    XArgs a;
+    a.Nm = mt.Nm;
+    a.count = mt.nmaps;
+    a.kxmax = mt.kxmax;
+    a.dense = dense ? 1 : 0;
+    a.info = mt.info.as<MapInfo>();
+    a.tab = static_cast<const unsigned char *>(mt.tab_x.p);
+    a.fd = mt.px.d;
+    a.xtw = mt.xtw.as<float2>();
+    a.U = work + mt.tsize;
+    a.out = out;
+    const int M = mt.Nm / 2, warps = kThreads / 32, pf = (mt.kxmax + warps - 1) / warps;
+    const size_t smem = table_smem(mt.px.d) + sizeof(float2) * ((size_t)mt.Nm + (size_t)M * kP);
+    const long long ntiles = ((long long)mt.Nm * mt.Nm + 31) / 32 * mt.nmaps;
+    const int work_tiles = (int)std::min<long long>(ntiles, 1LL << 30);
+    auto launch = [&](auto kern) -> int {
+        PBI4G_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        kern<<<grid_for((const void *)kern, smem, work_tiles), kThreads, smem, st>>>(a);
+        PBI4G_LAUNCH_CHECK();
+        return PBI4G_OK;
+    };
+    if (pf <= 4) PBI4G_CHECK(launch(map_xpass_kernel<4>));
+    else if (pf <= 9) PBI4G_CHECK(launch(map_xpass_kernel<9>));
+    else if (pf <= 16) PBI4G_CHECK(launch(map_xpass_kernel<16>));
+    else if (pf <= 32) PBI4G_CHECK(launch(map_xpass_kernel<32>));
+    else return set_error(PBI4G_ERR_UNSUPPORTED, "x pass: %d coefficient rows", mt.kxmax);
+    ++*launches;
+    return PBI4G_OK;
+}
+
+int fft_plan_host_check(int n, int batch, const float *in, float *out) {
+    fftd::FftPlan p;
+    if (!p.build(n)) return set_error(PBI4G_ERR_UNSUPPORTED, "fft plan: %d points", n);
+    std::vector<float2> buf((size_t)n);
+    for (int t = 0; t < batch; t++) {
+        for (int i = 0; i < n; i++) buf[i] = make_float2(in[2 * ((size_t)t * n + i)], in[2 * ((size_t)t * n + i) + 1]);
+        fftd::run_plan_host(p, buf.data(), 1, 0);
+        for (int k = 0; k < n; k++) {
+            const float2 v = buf[p.perm[k]];
+            out[2 * ((size_t)t * n + k)] = v.x;
+            out[2 * ((size_t)t * n + k) + 1] = v.y;
+        }
+    }
+    return PBI4G_OK;
+}
+
+}  // namespace pbi4g

@@ -1,0 +1,64 @@
+// mapfft.cuh -- pruned inverse transform of the FP32 shell maps (mapfft.cu).
+//
+// The maps of the bispectrum are I_b(x) = sum over the modes k of shell b of
+// delta(k) e^{ikx} (times a multipole factor), i.e. a C2R of a half spectrum
+// that is zero outside one spherical shell.  The transform runs as three
+// passes of in-place FFTs over batches of 32 one-dimensional transforms, each
+// pass skipping what the shell leaves zero:
+//   z pass: the (kx >= 0, ky) columns with kx^2 + ky^2 <= k2hi(b) only; the
+//           spectrum is built on the fly from delta(k) (shell mask, multipole
+//           factor, Hermitian symmetrisation of the kx = 0 plane, shell power)
+//           -> T[m][column][z];
+//   y pass: per (kx < kxn(b), z), input ky in [-r(kx), r(kx)] -> U[m][kx][z][y];
+//   x pass: per (z, y) row, the Hermitian C2R from kx < kxn(b) -> the real map,
+//           written dense [m][z][y][x] or row-interleaved [z][y][m][x].
+#pragma once
+
+#include "bispec.cuh"
+#include "fft_small.cuh"
+
+namespace pbi4g {
+
+struct MapInfo {
+    int shell;        // 0-based shell of the map (map m: set m / nb, shell m % nb)
+    int kxn;          // columns kx < kxn hold modes of the shell
+    int ncol;         // (kx, ky) columns of the z pass
+    int col0;         // first column of the shell in MapTransform::cols
+    int kx0;          // first (shell, kx) entry in MapTransform::kxr
+    int pad;
+    long long tbase;  // first float2 of the map in T ([column][z])
+    long long ubase;  // first float2 of the map in U ([kx][z][y])
+};
+
+struct MapTransform {
+    int Nm = 0, nmaps = 0, nb = 0, kxmax = 0;
+    fftd::FftPlan pz;    // Nm points (z and y passes)
+    fftd::FftPlan px;    // Nm / 2 points (x pass)
+    DevBuf tab_z, tab_x;  // packed plan tables (twiddles, butterfly entries, output positions)
+    DevBuf xtw;           // e^{2 pi i k / Nm}, k < Nm (the x pass's even/odd split)
+    DevBuf cols;          // int2 [sum ncol]: (kx, ky) of every column of every shell
+    DevBuf kxr;           // int2 [sum kxn]: (r(kx), first column of kx) per shell
+    DevBuf info;          // MapInfo [nmaps]
+    DevBuf ztiles, ytiles;  // int2 (map, first column / first (kx, z) transform) per 32-wide tile
+    int nzt = 0, nyt = 0;
+    long long tsize = 0, usize = 0;  // float2 elements of T and U
+    std::vector<MapInfo> info_h;
+    int build(const Shells &sh, int nmaps);
+    size_t work_bytes() const { return sizeof(float2) * (size_t)(tsize + usize); }
+};
+
+// z pass (shell spectra + z transform) of all maps into work[0, tsize).
+// src[s] / fac[s] / los / powsum / pow_mask as for build_map_spectra.
+int map_zpass(const Shells &sh, const MapTransform &mt, const float2 *const src[3], const int fac[3],
+              const double los[3], float2 *work, double *powsum, int pow_mask, cudaStream_t st, int64_t *launches);
+// y pass: work[0, tsize) -> work[tsize, tsize + usize)
+int map_ypass(const MapTransform &mt, float2 *work, cudaStream_t st, int64_t *launches);
+// x pass: real maps from work[tsize, ...), dense [m][z][y][x] or row-interleaved [z][y][m][x]
+int map_xpass(const MapTransform &mt, const float2 *work, float *out, bool dense, cudaStream_t st,
+              int64_t *launches);
+
+// Host check of the in-place FFT plan: n-point inverse DFTs of `batch`
+// transforms in[t][n] -> out[t][k] on the CPU with the kernels' butterflies.
+int fft_plan_host_check(int n, int batch, const float *in, float *out);
+
+}  // namespace pbi4g

@@ -106,6 +106,13 @@ class Estimator:
         check(lib().pbi4g_plan_map_grid(self._h, ctypes.byref(mg), ctypes.byref(nm)))
         self.map_grid, self.nmaps = mg.value, nm.value
 
+    def map_work(self):
+        """(z columns, y planes): complex elements of the FP32 map transform's
+        intermediates, once a bispectrum has run (0, 0 before, and for FP64)."""
+        t, u = ctypes.c_int64(), ctypes.c_int64()
+        check(lib().pbi4g_plan_map_work(self._h, ctypes.byref(t), ctypes.byref(u)))
+        return t.value, u.value
+
     # -- lifecycle
     def close(self):
         if getattr(self, "_h", None):

@@ -1,16 +1,20 @@
 """Roofline bookkeeping of the per-stage timings (algorithmic bytes / flops).
 
 Algorithmic traffic per box (N grid, H = N^2 (N/2+1) half-spectrum cells,
-G = 2 grids with interlacing, Np particles; M shell maps on the map grid Nm,
-Hm = Nm^2 (Nm/2+1); T triangles, S = 3 multipole sets or 1):
+G = 2 grids with interlacing, Np particles; M shell maps on the map grid Nm;
+FP32 forms: Tz, Uy complex elements of the pruned transform's z-column and
+(z, y)-plane intermediates; T triangles, S = 3 multipole sets or 1):
   assign          24 Np (float64 xyz read) + 4 G N^3 (FP32 grid write; 8 G N^3
                   int64 fixed-point for the FP64 form)
   grid_convert    8 G N^3 read + 4 G N^3 write (FP64 form only)
   fcomb           8 G H read + 8 H write
   pk_binning      8 H read
-  shell_spectra   8 H read + 8 M Hm write
+  shell_maps_z    FP32: 8 Tz write (the shell modes it gathers stay in L2);
+                  FP64: 16 H read + 16 M Hm write (shell spectra)
+  shell_maps_y    FP32: 8 Tz read + 8 Uy write (FP64: cuFFT Z2D, a library call)
+  shell_maps_x    FP32: 8 Uy read + 4 M Nm^3 write (the real maps)
   triangle_sums   2 Nm^3 T S flops (tensor-core forms; useful sums only)
-cuFFT stages (fft_r2c, fft_c2r) are library calls: timed, not given a roofline.
+cuFFT stages (fft_r2c, the FP64 shell_maps_y) are library calls: timed, not given a roofline.
 Peaks are the measured ones in MEASURED_PEAKS.json at the repository root
 (HBM copy bandwidth, cuBLAS bf16 dense), else the documented fallback.
 """
@@ -43,7 +47,7 @@ def traffic_table():
         return {}
 
 
-def stage_work(cfg, npart, map_grid=None, nmaps=None):
+def stage_work(cfg, npart, map_grid=None, nmaps=None, map_work=None):
     N = int(cfg.grid)
     G = 2 if cfg.interlacing else 1
     H = N * N * (N // 2 + 1)
@@ -52,18 +56,25 @@ def stage_work(cfg, npart, map_grid=None, nmaps=None):
     Nm = map_grid or N
     Hm = Nm * Nm * (Nm // 2 + 1)
     gbytes = 8 if cfg.precision == "fp64" else 4
-    return {
+    work = {
         "assign": ("hbm", 24 * npart + gbytes * G * N ** 3),
         "grid_convert": ("hbm", 12 * G * N ** 3),
         "fcomb": ("hbm", 8 * G * H + 8 * H),
         "pk_binning": ("hbm", 8 * H),
-        "shell_spectra": ("hbm", 8 * H + 8 * M * Hm),
     }
+    if cfg.precision == "fp64":
+        work["shell_maps_z"] = ("hbm", 16 * H + 16 * M * Hm)
+    elif map_work and map_work[0] > 0:
+        tz, uy = map_work
+        work["shell_maps_z"] = ("hbm", 8 * tz)
+        work["shell_maps_y"] = ("hbm", 8 * tz + 8 * uy)
+        work["shell_maps_x"] = ("hbm", 8 * uy + 4 * M * Nm ** 3)
+    return work
 
 
 KERNEL = {"assign": "owner_tile_kernel", "grid_convert": "fixed_to_real_kernel",
-          "fcomb": "fcomb_interlaced_half_kernel",
-          "pk_binning": "pk_accum_kernel", "shell_spectra": "build_map_spectra_kernel",
+          "fcomb": "fcomb_interlaced_half_kernel", "pk_binning": "pk_accum_kernel",
+          "shell_maps_z": "map_zpass_kernel", "shell_maps_y": "map_ypass_kernel", "shell_maps_x": "map_xpass_kernel",
           "triangle_sums": "trisum_tm_kernel"}
 
 def _entry(name, bound, amount, avg_ms, pk, traffic):
@@ -79,14 +90,14 @@ def _entry(name, bound, amount, avg_ms, pk, traffic):
             "algorithmic_bytes": amount, "avg_ms": round(avg_ms, 4), "peak_source": pk["source"]}
 
 
-def for_stages(stages, steps, cfg, npart, itot=None, map_grid=None, nmaps=None):
+def for_stages(stages, steps, cfg, npart, itot=None, map_grid=None, nmaps=None, map_work=None):
     """(dominant, all): the roofline object of the slowest stage among this
     library's kernels and the list for every timed stage.  Tensor-core triangle
     sums count the useful flops 2 Nm^3 itot S against the measured bf16 dense
     peak; HBM stages count their algorithmic bytes.  `traffic` is the per-launch
     DRAM bytes of the committed ncu capture for this workload, if one exists."""
     pk = peaks()
-    work = dict(stage_work(cfg, npart, map_grid, nmaps))
+    work = dict(stage_work(cfg, npart, map_grid, nmaps, map_work))
     if itot and cfg.precision in ("fp16split", "bf16", "tf32split"):
         nsets = 3 if cfg.multipoles else 1
         work["triangle_sums"] = ("tensor", 2.0 * int(map_grid or cfg.grid) ** 3 * itot * nsets)
@@ -96,7 +107,10 @@ def for_stages(stages, steps, cfg, npart, itot=None, map_grid=None, nmaps=None):
         ms, calls = stages.get(name, (0.0, 0))
         if calls == 0 or ms <= 0:
             continue
-        out.append(_entry(name, bound, amount, ms / calls, pk, table.get(name)))
+        e = _entry(name, bound, amount, ms / calls, pk, table.get(name))
+        if name == "shell_maps_z" and cfg.precision == "fp64":
+            e["kernel"] = "build_map_spectra_kernel"
+        out.append(e)
     if not out:
         return None, []
     best = max(out, key=lambda e: e["avg_ms"])

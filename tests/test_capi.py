@@ -65,3 +65,26 @@ def test_errors_without_device(lib):
     cfg.grid, cfg.box, cfg.nintp, cfg.nbins_ps, cfg.kbin_ps = 256, 1000.0, 4, 128, 1.0
     assert lib.pbi4g_plan_footprint(ctypes.byref(cfg), 2 ** 21, ctypes.byref(out)) == 0
     assert out.value > 256 ** 3 * 8
+
+
+@pytest.mark.parametrize("n", [2, 3, 5, 7, 8, 12, 50, 100, 128, 150, 196, 200, 294, 320, 392, 400, 512])
+def test_fft_plan_host(lib, n):
+    """The in-place mixed-radix plans of the shell-map transforms (radices 2, 3,
+    4, 5, 7, 8; digit-reversed output positions) against numpy's inverse DFT."""
+    import numpy as np
+    rng = np.random.default_rng(n)
+    batch = 3
+    x = (rng.standard_normal((batch, n)) + 1j * rng.standard_normal((batch, n))).astype(np.complex64)
+    out = np.zeros_like(x)
+    rc = lib.pbi4g_fft_plan_check(n, batch, x.ctypes.data, out.ctypes.data)
+    assert rc == 0, lib.pbi4g_last_error()
+    ref = np.fft.ifft(x.astype(np.complex128), axis=1) * n
+    assert np.max(np.abs(out - ref)) <= 1e-6 * np.max(np.abs(ref))
+
+
+def test_fft_plan_rejects_large_primes(lib):
+    import numpy as np
+    x = np.zeros(22, dtype=np.complex64)
+    for n in (11, 22, 26):
+        assert lib.pbi4g_fft_plan_check(n, 1, x.ctypes.data, x.ctypes.data) != 0
+        assert b"fft plan" in lib.pbi4g_last_error()
