@@ -12,6 +12,14 @@
 // times e^{2 pi i n1 q / L_t}, stored back in place; L_{t+1} = Ls.  The result
 // X[k] ends at the digit-reversed position perm[k]: for k = q + R_1 k1,
 // perm_N(k) = q N / R_1 + perm_{N/R_1}(k1).
+//
+// The kernels run the transpose of that factorisation (the DFT matrix is
+// symmetric, and so is every stage's block of R-point DFTs and its diagonal of
+// twiddles): x[n] is placed at perm[n], the stages run last to first, each
+// butterfly multiplies its inputs by the twiddles before the R-point DFT, and
+// X[k] comes out at position k.  The permutation then falls on the side where
+// the lanes run over transforms (conflict-free in shared memory) and the
+// natural-order output is read along the points.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -116,19 +124,23 @@ __host__ __device__ __forceinline__ void dft_small(float2 (&v)[8]) {
     }
 }
 
-// One DIF butterfly of radix R for the transform in column `t` of buf (pitch
-// between points): points base + ls r, outputs times tw[q * tstep] (tw[s] =
-// e^{2 pi i s / N}), in place.
+// The transposed (decimation-in-time) butterfly: inputs r times tw[r * tstep],
+// then the R-point DFT, in place.
 template <int R>
-__host__ __device__ __forceinline__ void dif_butterfly(float2 *buf, int pitch, int t, int base, int ls, int tstep,
+__host__ __device__ __forceinline__ void dit_butterfly(float2 *buf, int pitch, int t, int base, int ls, int tstep,
                                                        const float2 *tw) {
     float2 v[8];
+    v[0] = buf[base * pitch + t];
+    if (tstep) {
 #pragma unroll
-    for (int r = 0; r < R; r++) v[r] = buf[(base + ls * r) * pitch + t];
+        for (int r = 1; r < R; r++) v[r] = cmul(buf[(base + ls * r) * pitch + t], tw[r * tstep]);
+    } else {
+#pragma unroll
+        for (int r = 1; r < R; r++) v[r] = buf[(base + ls * r) * pitch + t];
+    }
     dft_small<R>(v);
-    buf[base * pitch + t] = v[0];
 #pragma unroll
-    for (int q = 1; q < R; q++) buf[(base + ls * q) * pitch + t] = tstep ? cmul(v[q], tw[q * tstep]) : v[q];
+    for (int q = 0; q < R; q++) buf[(base + ls * q) * pitch + t] = v[q];
 }
 
 constexpr int kMaxStages = 10;
@@ -200,19 +212,20 @@ struct FftPlan {
     }
 };
 
-// Run the plan over transform t of buf on one thread (the host check of the
-// plan and butterflies; the kernels run the same butterflies across warps).
+// Run the transposed plan over transform t of buf on one thread, input already
+// at the permuted positions (the host check of the plan and butterflies; the
+// kernels run the same butterflies across warps).
 inline void run_plan_host(const FftPlan &p, float2 *buf, int pitch, int t) {
-    for (int s = 0; s < p.d.nst; s++) {
+    for (int s = p.d.nst - 1; s >= 0; s--) {
         for (int j = 0; j < p.d.n / p.d.rad[s]; j++) {
             const int2 e = p.ent[p.d.eoff[s] + j];
             switch (p.d.rad[s]) {
-                case 2: dif_butterfly<2>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
-                case 3: dif_butterfly<3>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
-                case 4: dif_butterfly<4>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
-                case 5: dif_butterfly<5>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
-                case 7: dif_butterfly<7>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
-                default: dif_butterfly<8>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
+                case 2: dit_butterfly<2>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
+                case 3: dit_butterfly<3>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
+                case 4: dit_butterfly<4>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
+                case 5: dit_butterfly<5>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
+                case 7: dit_butterfly<7>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
+                default: dit_butterfly<8>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
             }
         }
     }

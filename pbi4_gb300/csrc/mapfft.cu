@@ -37,30 +37,31 @@ __device__ __forceinline__ void load_tables(const unsigned char *__restrict__ ta
     for (int i = threadIdx.x; i < fd.nent; i += blockDim.x) ent[i] = e[i];
 }
 
-// the plan's stages over the 32 transforms of a tile (ends with a barrier)
-__device__ __forceinline__ void run_dif(const fftd::FftDesc &fd, float2 *buf, const int2 *ent, const float2 *tw,
+// the plan's stages, last to first, over the 32 transforms of a tile whose
+// points sit at the permuted positions (ends with a barrier); natural-order output
+__device__ __forceinline__ void run_dit(const fftd::FftDesc &fd, float2 *buf, const int2 *ent, const float2 *tw,
                                         int warp, int nw, int lane) {
-    for (int s = 0; s < fd.nst; s++) {
+    for (int s = fd.nst - 1; s >= 0; s--) {
         const int R = fd.rad[s], ls = fd.ls[s], nbf = fd.n / R;
         const int2 *e = ent + fd.eoff[s];
         switch (R) {
             case 8:
-                for (int j = warp; j < nbf; j += nw) fftd::dif_butterfly<8>(buf, kP, lane, e[j].x, ls, e[j].y, tw);
+                for (int j = warp; j < nbf; j += nw) fftd::dit_butterfly<8>(buf, kP, lane, e[j].x, ls, e[j].y, tw);
                 break;
             case 4:
-                for (int j = warp; j < nbf; j += nw) fftd::dif_butterfly<4>(buf, kP, lane, e[j].x, ls, e[j].y, tw);
+                for (int j = warp; j < nbf; j += nw) fftd::dit_butterfly<4>(buf, kP, lane, e[j].x, ls, e[j].y, tw);
                 break;
             case 2:
-                for (int j = warp; j < nbf; j += nw) fftd::dif_butterfly<2>(buf, kP, lane, e[j].x, ls, e[j].y, tw);
+                for (int j = warp; j < nbf; j += nw) fftd::dit_butterfly<2>(buf, kP, lane, e[j].x, ls, e[j].y, tw);
                 break;
             case 3:
-                for (int j = warp; j < nbf; j += nw) fftd::dif_butterfly<3>(buf, kP, lane, e[j].x, ls, e[j].y, tw);
+                for (int j = warp; j < nbf; j += nw) fftd::dit_butterfly<3>(buf, kP, lane, e[j].x, ls, e[j].y, tw);
                 break;
             case 5:
-                for (int j = warp; j < nbf; j += nw) fftd::dif_butterfly<5>(buf, kP, lane, e[j].x, ls, e[j].y, tw);
+                for (int j = warp; j < nbf; j += nw) fftd::dit_butterfly<5>(buf, kP, lane, e[j].x, ls, e[j].y, tw);
                 break;
             default:
-                for (int j = warp; j < nbf; j += nw) fftd::dif_butterfly<7>(buf, kP, lane, e[j].x, ls, e[j].y, tw);
+                for (int j = warp; j < nbf; j += nw) fftd::dit_butterfly<7>(buf, kP, lane, e[j].x, ls, e[j].y, tw);
                 break;
         }
         __syncthreads();
@@ -72,11 +73,10 @@ size_t table_smem(const fftd::FftDesc &fd) {
 }
 
 struct ZArgs {
-    int N, NH, Nm, nb, k2max;
-    const int *lut;
+    int N, NH, Nm, nb;
     const float2 *src[3];
     int fac[3];
-    double los[3];
+    float los[3];
     double *powsum;
     int pow_mask;
     const int2 *cols;
@@ -89,8 +89,9 @@ struct ZArgs {
 };
 
 // z pass: tile = (map m, 32 columns (kx, ky) of its shell).  Point i of a
-// column is kz = kfreq0(i, Nm); a mode enters when lut[k^2] is the map's shell
-// (the mask, multipole factor and kx = 0 symmetrisation of build_map_spectra).
+// column is kz = kfreq0(i, Nm); a mode is in the shell when k2lo <= |k|^2 <=
+// k2hi (the shell's |k|^2 range, contiguous).  The mask, multipole factor and
+// kx = 0 symmetrisation of build_map_spectra; the multipole factor in FP32.
 __global__ void __launch_bounds__(kThreads) map_zpass_kernel(const ZArgs a) {
     extern __shared__ __align__(16) unsigned char zsm[];
     const fftd::FftDesc &fd = a.fd;
@@ -113,47 +114,51 @@ __global__ void __launch_bounds__(kThreads) map_zpass_kernel(const ZArgs a) {
         const int c = c0 + lane;
         const bool valid = c < mi.ncol;
         const int2 kk = valid ? a.cols[mi.col0 + c] : make_int2(0, 0);
-        const int kx = kk.x, ky = kk.y, kzl = mi.kxn - 1;
+        const int kx = kk.x, ky = kk.y, r2 = kx * kx + ky * ky;
+        // kz^2 range of the shell on this column (empty for a padding lane)
+        const int lo2 = valid ? mi.k2lo - r2 : 1, hi2 = valid ? mi.k2hi - r2 : 0;
         const float2 *src = a.src[s];
         const int fac = a.fac[s];
-        const bool pw = a.powsum && (a.pow_mask >> s & 1);
         const int yN = ky < 0 ? ky + N : ky;
-        const double lxy = a.los[0] * kx + a.los[1] * ky;
+        const float lxy = a.los[0] * (float)kx + a.los[1] * (float)ky;
+        const float wpow = kx == 0 ? 1.f : 2.f;  // the kx > 0 modes stand for their mirror too
+        float pacc = 0.f;
         for (int i = warp; i < Nm; i += nw) {
-            const int kz = kfreq0(i, Nm);
+            const int kz = kfreq0(i, Nm), kz2 = kz * kz;
             float2 v = czero();
-            if (valid && kz >= -kzl && kz <= kzl) {
-                const int k2 = kx * kx + ky * ky + kz * kz;
-                const int sb = k2 <= a.k2max ? __ldg(a.lut + k2) : 0;
-                if (sb == b) {
-                    const int zN = kz < 0 ? kz + N : kz;
-                    v = src[((size_t)zN * N + yN) * a.NH + kx];
-                    if (kx == 0) {
-                        const float2 w = src[((size_t)kneg0(zN, N) * N + kneg0(yN, N)) * a.NH];
-                        v.x = (v.x + w.x) * 0.5f;
-                        v.y = (v.y - w.y) * 0.5f;
-                    }
-                    if (fac) {
-                        const double lk = lxy + a.los[2] * kz;
-                        const float mu2 = k2 > 0 ? (float)(lk * lk / (double)k2) : 0.f;
-                        const float L = fac == 2 ? -0.5f + 1.5f * mu2 : 0.375f + mu2 * (-3.75f + 4.375f * mu2);
-                        v.x *= L;
-                        v.y *= L;
-                    }
-                    if (pw)
-                        atomicAdd(&spow[s * nb + b - 1],
-                                  (kx == 0 ? 1.0 : 2.0) * ((double)v.x * v.x + (double)v.y * v.y));
+            if (kz2 >= lo2 && kz2 <= hi2) {
+                const int zN = kz < 0 ? kz + N : kz;
+                v = src[((size_t)zN * N + yN) * a.NH + kx];
+                if (kx == 0) {
+                    const float2 w = src[((size_t)kneg0(zN, N) * N + kneg0(yN, N)) * a.NH];
+                    v.x = (v.x + w.x) * 0.5f;
+                    v.y = (v.y - w.y) * 0.5f;
                 }
+                if (fac) {
+                    const float lk = lxy + a.los[2] * (float)kz;
+                    const int k2 = r2 + kz2;
+                    const float mu2 = k2 > 0 ? lk * lk / (float)k2 : 0.f;
+                    const float L = fac == 2 ? -0.5f + 1.5f * mu2 : 0.375f + mu2 * (-3.75f + 4.375f * mu2);
+                    v.x *= L;
+                    v.y *= L;
+                }
+                pacc += wpow * (v.x * v.x + v.y * v.y);
             }
-            buf[i * kP + lane] = v;
+            buf[perm[i] * kP + lane] = v;
+        }
+        if (a.powsum && (a.pow_mask >> s & 1)) {
+            double pw = (double)pacc;
+#pragma unroll
+            for (int o = 16; o; o >>= 1) pw += __shfl_xor_sync(0xffffffffu, pw, o);
+            if (lane == 0 && pw != 0.0) atomicAdd(&spow[s * nb + b - 1], pw);
         }
         __syncthreads();
-        run_dif(fd, buf, ent, tw, warp, nw, lane);
+        run_dit(fd, buf, ent, tw, warp, nw, lane);
         // column c0 + l -> T[tbase + (c0 + l) Nm + z], z along the lanes
         for (int l = warp; l < 32; l += nw) {
             if (c0 + l >= mi.ncol) break;
             float2 *o = a.T + mi.tbase + (size_t)(c0 + l) * Nm;
-            for (int z = lane; z < Nm; z += 32) o[z] = buf[perm[z] * kP + l];
+            for (int z = lane; z < Nm; z += 32) o[z] = buf[z * kP + l];
         }
         __syncthreads();
     }
@@ -200,14 +205,14 @@ __global__ void __launch_bounds__(kThreads) map_ypass_kernel(const YArgs a) {
         const float2 *in = a.T + mi.tbase + (size_t)(rc.y + rc.x) * Nm + z;  // column ky = 0
         for (int i = warp; i < Nm; i += nw) {
             const int ky = kfreq0(i, Nm);
-            buf[i * kP + lane] = (ky >= -rc.x && ky <= rc.x) ? __ldcs(in + (ptrdiff_t)ky * Nm) : czero();
+            buf[perm[i] * kP + lane] = (ky >= -rc.x && ky <= rc.x) ? __ldcs(in + (ptrdiff_t)ky * Nm) : czero();
         }
         __syncthreads();
-        run_dif(fd, buf, ent, tw, warp, nw, lane);
+        run_dit(fd, buf, ent, tw, warp, nw, lane);
         for (int l = warp; l < 32; l += nw) {
             if (t0 + l >= ntr) break;
             float2 *o = a.U + mi.ubase + (size_t)(t0 + l) * Nm;
-            for (int y = lane; y < Nm; y += 32) o[y] = buf[perm[y] * kP + l];
+            for (int y = lane; y < Nm; y += 32) o[y] = buf[y * kP + l];
         }
         __syncthreads();
     }
@@ -225,9 +230,11 @@ struct XArgs {
 
 // x pass: tile = (map m, 32 consecutive rows (z, y)).  With M = Nm / 2,
 // Z[k] = (X[k] + conj X[M-k]) + i (X[k] - conj X[M-k]) e^{2 pi i k / Nm} and
-// z = IDFT_M(Z) give the C2R output x[2j] = Re z[j], x[2j+1] = Im z[j]; the
-// pair (k, M - k) is formed in place.  PF: coefficient rows a warp prefetches
-// into registers for the next tile (kxmax <= PF * warps).
+// z = IDFT_M(Z) give the C2R output x[2j] = Re z[j], x[2j+1] = Im z[j].  The
+// raw coefficients (kx < kxmax) stay in their own buffer while the pairs
+// (k, M - k) are formed into the permuted positions of the FFT buffer.  PF:
+// coefficient rows a warp prefetches into registers for the next tile
+// (kxmax <= PF * warps).
 template <int PF>
 __global__ void __launch_bounds__(kThreads, PF <= 9 ? 4 : 2) map_xpass_kernel(const XArgs a) {
     extern __shared__ __align__(16) unsigned char xsm[];
@@ -237,16 +244,14 @@ __global__ void __launch_bounds__(kThreads, PF <= 9 ? 4 : 2) map_xpass_kernel(co
     int2 *ent = reinterpret_cast<int2 *>(tw + fd.n);
     int *perm = reinterpret_cast<int *>(ent + fd.nent);
     float2 *xt = reinterpret_cast<float2 *>(perm + fd.n);  // [Nm]
-    float2 *buf = xt + Nm;                                 // [M][kP]
+    float2 *xr = xt + Nm;                                  // [KX][kP] raw coefficients
+    float2 *buf = xr + (size_t)KX * kP;                    // [M][kP]
     load_tables(a.tab, fd, tw, ent, perm);
     for (int i = threadIdx.x; i < Nm; i += blockDim.x) xt[i] = a.xtw[i];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const long long plane = (long long)Nm * Nm;
-    const long long tiles_per_map = (plane + 31) / 32, ntiles = tiles_per_map * a.count;
+    const int plane = Nm * Nm, tpm = (plane + 31) / 32, ntiles = tpm * a.count;
     float2 pre[PF];
-    auto fetch = [&](long long tile) {
-        const int m = (int)(tile / tiles_per_map);
-        const long long row0 = (tile - (long long)m * tiles_per_map) * 32;
+    auto fetch = [&](int m, int row0) {
         const bool ok = row0 + lane < plane;
         const MapInfo &mi = a.info[m];
         const int kxn = mi.kxn;
@@ -257,41 +262,49 @@ __global__ void __launch_bounds__(kThreads, PF <= 9 ? 4 : 2) map_xpass_kernel(co
             pre[i] = (k < kxn && ok) ? __ldcs(src + (size_t)k * plane) : czero();
         }
     };
-    if (blockIdx.x < ntiles) fetch(blockIdx.x);
-    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int m = (int)(tile / tiles_per_map);
-        const long long row0 = (tile - (long long)m * tiles_per_map) * 32;
-        const int nrows = (int)((plane - row0) < 32 ? (plane - row0) : 32);
+    // (map, tile within the map) of this CTA's tiles, advanced without divisions
+    int m = blockIdx.x / tpm, r = blockIdx.x - m * tpm;
+    const int gm = gridDim.x / tpm, gr = gridDim.x - gm * tpm;
+    auto advance = [&](int &mm, int &rr) {
+        mm += gm;
+        rr += gr;
+        if (rr >= tpm) { rr -= tpm; mm++; }
+    };
+    if (blockIdx.x < ntiles) fetch(m, r * 32);
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int row0 = r * 32;
+        const int nrows = min(32, plane - row0);
+        int mn = m, rn = r;
+        advance(mn, rn);
         __syncthreads();
 #pragma unroll
         for (int i = 0; i < PF; i++) {
             const int k = warp + i * nw;
-            if (k < KX) buf[k * kP + lane] = pre[i];
+            if (k < KX) xr[k * kP + lane] = pre[i];
         }
-        if (tile + gridDim.x < ntiles) fetch(tile + gridDim.x);
+        if (tile + (int)gridDim.x < ntiles) fetch(mn, rn * 32);
         __syncthreads();
-        // (k, M - k) pairs in place; rows >= KX hold no coefficients (zero)
         for (int k = warp; k <= M / 2; k += nw) {
             const int kc = M - k;
-            const float2 xk = k < KX ? buf[k * kP + lane] : czero();
-            const float2 xc = (k > 0 && kc < KX) ? buf[kc * kP + lane] : czero();  // X[M - k]
+            const float2 xk = k < KX ? xr[k * kP + lane] : czero();
+            const float2 xc = (k > 0 && kc < KX) ? xr[kc * kP + lane] : czero();  // X[M - k]
             const float2 ck = make_float2(xc.x, -xc.y), cc = make_float2(xk.x, -xk.y);
             const float2 o1 = fftd::cmul(fftd::csub(xk, ck), xt[k]);
-            const float2 z1 = fftd::cadd(fftd::cadd(xk, ck), fftd::itimes(o1));
+            buf[perm[k] * kP + lane] = fftd::cadd(fftd::cadd(xk, ck), fftd::itimes(o1));
             if (k > 0 && kc != k) {
                 const float2 o2 = fftd::cmul(fftd::csub(xc, cc), xt[kc]);
-                buf[kc * kP + lane] = fftd::cadd(fftd::cadd(xc, cc), fftd::itimes(o2));
+                buf[perm[kc] * kP + lane] = fftd::cadd(fftd::cadd(xc, cc), fftd::itimes(o2));
             }
-            buf[k * kP + lane] = z1;
         }
         __syncthreads();
-        run_dif(fd, buf, ent, tw, warp, nw, lane);
+        run_dit(fd, buf, ent, tw, warp, nw, lane);
         for (int l = warp; l < nrows; l += nw) {
-            const long long row = row0 + l;
-            float *o = a.dense ? a.out + (size_t)m * plane * Nm + (size_t)row * Nm
-                               : a.out + ((size_t)row * a.count + m) * Nm;
-            for (int j = lane; j < M; j += 32) reinterpret_cast<float2 *>(o)[j] = buf[perm[j] * kP + l];
+            const size_t row = (size_t)row0 + l;
+            float *o = a.dense ? a.out + ((size_t)m * plane + row) * Nm : a.out + (row * a.count + m) * Nm;
+            for (int j = lane; j < M; j += 32) reinterpret_cast<float2 *>(o)[j] = buf[j * kP + l];
         }
+        m = mn;
+        r = rn;
     }
 }
 
@@ -322,11 +335,19 @@ int MapTransform::build(const Shells &s, int nm) {
     if (Nm % 4 || !pz.build(Nm) || !px.build(Nm / 2))
         return set_error(PBI4G_ERR_UNSUPPORTED, "map transform: map grid %d", Nm);
     // per shell: largest k^2, the kx range and the (kx, ky) columns
-    std::vector<int> k2hi(nb, -1);
+    std::vector<int> k2hi(nb, -1), k2lo(nb, -1);
     for (int k2 = 0; k2 <= s.k2max && k2 < (int)s.lut_h.size(); k2++) {
         const int b = s.lut_h[k2];
-        if (b >= 1 && b <= nb) k2hi[b - 1] = std::max(k2hi[b - 1], k2);
+        if (b < 1 || b > nb) continue;
+        if (k2lo[b - 1] < 0) k2lo[b - 1] = k2;
+        k2hi[b - 1] = std::max(k2hi[b - 1], k2);
     }
+    // the z pass tests shell membership as k2lo <= |k|^2 <= k2hi: every shell's
+    // |k|^2 values must form one range (they do: shells are intervals of |k|)
+    for (int b = 0; b < nb; b++)
+        for (int k2 = std::max(k2lo[b], 0); k2 <= k2hi[b]; k2++)
+            if (s.lut_h[k2] != b + 1)
+                return set_error(PBI4G_ERR_UNSUPPORTED, "map transform: shell %d is not one |k|^2 range", b + 1);
     std::vector<int2> cols_h, kxr_h;
     std::vector<int> kxn(nb), ncol(nb), col0(nb), kx0(nb);
     auto isqrt = [](int v) {
@@ -360,6 +381,8 @@ int MapTransform::build(const Shells &s, int nm) {
         mi.ncol = ncol[b];
         mi.col0 = col0[b];
         mi.kx0 = kx0[b];
+        mi.k2lo = k2lo[b];
+        mi.k2hi = k2hi[b];
         mi.pad = 0;
         mi.tbase = tb;
         mi.ubase = ub;
@@ -393,12 +416,10 @@ int map_zpass(const Shells &sh, const MapTransform &mt, const float2 *const src[
     a.NH = sh.N / 2 + 1;
     a.Nm = mt.Nm;
     a.nb = mt.nb;
-    a.k2max = sh.k2max;
-    a.lut = sh.lut.as<int>();
     for (int s = 0; s < 3; s++) {
         a.src[s] = src[s];
         a.fac[s] = fac[s];
-        a.los[s] = los ? los[s] : 0.0;
+        a.los[s] = los ? (float)los[s] : 0.f;
     }
     a.powsum = powsum;
     a.pow_mask = pow_mask;
@@ -452,9 +473,11 @@ int map_xpass(const MapTransform &mt, const float2 *work, float *out, bool dense
     a.U = work + mt.tsize;
     a.out = out;
     const int M = mt.Nm / 2, warps = kThreads / 32, pf = (mt.kxmax + warps - 1) / warps;
-    const size_t smem = table_smem(mt.px.d) + sizeof(float2) * ((size_t)mt.Nm + (size_t)M * kP);
+    const size_t smem =
+        table_smem(mt.px.d) + sizeof(float2) * ((size_t)mt.Nm + (size_t)mt.kxmax * kP + (size_t)M * kP);
     const long long ntiles = ((long long)mt.Nm * mt.Nm + 31) / 32 * mt.nmaps;
-    const int work_tiles = (int)std::min<long long>(ntiles, 1LL << 30);
+    if (ntiles >= (1LL << 31)) return set_error(PBI4G_ERR_UNSUPPORTED, "x pass: %lld tiles", ntiles);
+    const int work_tiles = (int)ntiles;
     auto launch = [&](auto kern) -> int {
         PBI4G_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         kern<<<grid_for((const void *)kern, smem, work_tiles), kThreads, smem, st>>>(a);
@@ -475,10 +498,11 @@ int fft_plan_host_check(int n, int batch, const float *in, float *out) {
     if (!p.build(n)) return set_error(PBI4G_ERR_UNSUPPORTED, "fft plan: %d points", n);
     std::vector<float2> buf((size_t)n);
     for (int t = 0; t < batch; t++) {
-        for (int i = 0; i < n; i++) buf[i] = make_float2(in[2 * ((size_t)t * n + i)], in[2 * ((size_t)t * n + i) + 1]);
+        for (int i = 0; i < n; i++)
+            buf[p.perm[i]] = make_float2(in[2 * ((size_t)t * n + i)], in[2 * ((size_t)t * n + i) + 1]);
         fftd::run_plan_host(p, buf.data(), 1, 0);
         for (int k = 0; k < n; k++) {
-            const float2 v = buf[p.perm[k]];
+            const float2 v = buf[k];
             out[2 * ((size_t)t * n + k)] = v.x;
             out[2 * ((size_t)t * n + k) + 1] = v.y;
         }

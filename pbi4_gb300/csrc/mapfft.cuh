@@ -25,6 +25,7 @@ struct MapInfo {
     int ncol;         // (kx, ky) columns of the z pass
     int col0;         // first column of the shell in MapTransform::cols
     int kx0;          // first (shell, kx) entry in MapTransform::kxr
+    int k2lo, k2hi;   // the shell's modes are exactly those with k2lo <= |k|^2 <= k2hi
     int pad;
     long long tbase;  // first float2 of the map in T ([column][z])
     long long ubase;  // first float2 of the map in U ([kx][z][y])
