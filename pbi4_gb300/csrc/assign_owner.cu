@@ -4,9 +4,10 @@
 //
 // Same indices and weights as powerI4.f90:68-249 (see assign.cu); the weights
 // are evaluated in FP32 from the FP64 cell offset.  Every contribution
-// (w_x w_y) w_z weight is rounded once to a 64-bit integer at scale 2^S and
-// summed with integer shared-memory atomics, so the grid is bit-identical for
-// any particle order and schedule.
+// (w_x w_y) w_z weight is rounded once to an integer at scale 2^S (|q| < 2^30,
+// 2^-28 resolution for unit weights: far below the FP32 grid's rounding) and
+// summed into 64-bit integers with shared-memory atomics, so the grid is
+// bit-identical for any particle order and schedule.
 //
 // 1. prep: per particle, the first stencil cell of each grid (FP64 index math,
 //    once) and the FP32 offsets; the tiles its stencils touch (1 to 8) are
@@ -254,7 +255,7 @@ __global__ void __launch_bounds__(kThreads) owner_tile_kernel(int N, int nt, con
             const PRec r = sorted[k];
             const float wt = wsorted ? wsorted[k] : 1.f;
             int cell[G][NIT];
-            long long q[G][NIT];
+            int q[G][NIT];
             bool ok[G][NIT];
 #pragma unroll
             for (int g = 0; g < G; g++) {
@@ -275,16 +276,17 @@ __global__ void __launch_bounds__(kThreads) owner_tile_kernel(int N, int nt, con
                     ok[g][it] = cl[it] >= 0 && (unsigned)lx < (unsigned)kT && (unsigned)ly < (unsigned)kT &&
                                 (unsigned)lz < (unsigned)kT;
                     // the reference's product order: ((w_x w_y) w_z) weight; wv * 2^S is exact in
-                    // FP32 (a power-of-two scale), so the FP32 rounding to an integer gives the
-                    // same q as the FP64 route, without FP64 arithmetic
+                    // FP32 (a power-of-two scale) and |wv| 2^S < 2^30, so q is one 32-bit integer
                     const float wv = pick<NI>(wx, ii) * pick<NI>(wy, jj) * pick<NI>(wz, cl[it] < 0 ? 0 : cl[it]) * wt;
-                    q[g][it] = __float2ll_rn(wv * scale);
+                    q[g][it] = __float2int_rn(wv * scale);
                     cell[g][it] = lz * kPz + ly * kPy + lx;
                 }
             }
-            // 64-bit fixed-point adds as two 32-bit shared atomics: all low words of the
-            // record first (independent), then the high words with the carries the
-            // returned low words give, so the pair sums exactly (mod 2^64)
+            // 64-bit fixed-point adds of the sign-extended q as two 32-bit shared
+            // atomics: all low words of the record first (independent), then the high
+            // word with the sign and the carry the returned low word gives, so the
+            // pair sums exactly (mod 2^64).  The high word is touched only on a carry
+            // or a negative weight.
             unsigned old[G][NIT];
 #pragma unroll
             for (int g = 0; g < G; g++)
@@ -297,7 +299,7 @@ __global__ void __launch_bounds__(kThreads) owner_tile_kernel(int N, int nt, con
                 for (int it = 0; it < NIT; it++)
                     if (ok[g][it]) {
                         const unsigned ql = (unsigned)q[g][it];
-                        const unsigned qh = (unsigned)((unsigned long long)q[g][it] >> 32) + (old[g][it] + ql < old[g][it] ? 1u : 0u);
+                        const unsigned qh = (q[g][it] < 0 ? 0xFFFFFFFFu : 0u) + (old[g][it] + ql < old[g][it] ? 1u : 0u);
                         if (qh) atomicAdd(acc32 + (2 * g + 1) * kTCP + cell[g][it], qh);
                     }
         }
@@ -389,6 +391,10 @@ int assign_owner(OwnerWork &wk, int N, int nintp, bool interlaced, int64_t npart
     }
     int bits;
     PBI4G_CHECK(fixed_point_bits(npart, wmax, &bits));
+    // each contribution is one 32-bit integer: |w_x w_y w_z weight| 2^S <= 3.375 wmax 2^S < 2^30
+    // (the 64-bit tile sums still hold the total); 2^-28 resolution for unit weights
+    bits = std::min(bits, (int)floor(30.0 - log2(4.0 * (wmax > 0 ? wmax : 1.0))));
+    if (bits < 8) return set_error(PBI4G_ERR_RANGE, "assign: particle weights up to %g", wmax);
     const int nt = N / kT, ntiles = nt * nt * nt;
     PBI4G_CUDA(cudaMemsetAsync(wk.count.p, 0, (size_t)(ntiles + 2) * 4, st));  // counts and the tile counter
     owner_count_kernel<<<grid_blocks(npart, 256), 256, 0, st>>>(N, nintp, interlaced, npart, stride, bp, d_pos, nt,

@@ -111,11 +111,10 @@ int BkEngine::run(const typename Cx<R>::T *const src[3], const int fac[3], const
                 if (fac[s] == 0) pow_mask |= 1 << s;
     }
     const size_t FCm = (size_t)N * N * N;
-    // FP64: in-place C2R (padded rows); plain FP32: dense maps; tensor-core
-    // forms: row-interleaved maps (the rows of all maps for one (y, z) side by
-    // side: one contiguous read per chunk of points)
-    const int layout = fp64 ? 0 : (tc ? 2 : 1);
-    if (layout) PBI4G_CHECK(dense.ensure(sizeof(float) * FCm * nm));
+    // FP64: in-place C2R (padded rows); plain FP32: dense FP32 maps; tensor-core
+    // forms: the operand planes of the form (MapPlanes)
+    if (!fp64)
+        PBI4G_CHECK(dense.ensure(tc ? MapPlanes::bytes(form, (long long)FCm, nm, nb) : sizeof(float) * FCm * nm));
     PBI4G_CUDA(cudaMemsetAsync(powsum.p, 0, sizeof(double) * 3 * nb, st));
     if (fp64) {
         PBI4G_CHECK(maps.ensure(sizeof(C) * HC * nm));
@@ -151,26 +150,33 @@ int BkEngine::run(const typename Cx<R>::T *const src[3], const int fac[3], const
         PBI4G_CHECK(map_ypass(mt, maps.as<float2>(), st, launches));
         pf.end(st);
         pf.begin(10, st);
-        PBI4G_CHECK(map_xpass(mt, maps.as<float2>(), dense.as<float>(), layout == 1, st, launches));
+        if (tc) {
+            if (form == 1) {
+                // largest |L_l(mu)| over mu^2 in [0, |los|^2]: bounds the delta_2 / delta_4 maps by the delta map
+                double lfac[3] = {1.0, 1.0, 1.0};
+                const double l2max = los ? los[0] * los[0] + los[1] * los[1] + los[2] * los[2] : 1.0;
+                for (int s = 1; s < nsets; s++) {
+                    if (fac[s] == 0) continue;
+                    double mx = 0;
+                    for (int k = 0; k <= 2000; k++) {
+                        const double m2 = l2max * k / 2000.0;
+                        const double L = fac[s] == 2 ? -0.5 + 1.5 * m2 : 0.375 + m2 * (-3.75 + 4.375 * m2);
+                        mx = std::max(mx, fabs(L));
+                    }
+                    lfac[s] = mx * 1.01;
+                }
+                PBI4G_CHECK(tm_map_exponents(sh, tmp, nm, powsum.as<double>(), pow_mask, lfac, st, launches));
+            }
+            planes.carve(form, (long long)FCm, nm, nb, dense.p, form == 1 ? tmp.mexp.as<int>() : nullptr);
+            PBI4G_CHECK(map_xpass(mt, maps.as<float2>(), nullptr, &planes, st, launches));
+        } else {
+            PBI4G_CHECK(map_xpass(mt, maps.as<float2>(), dense.as<float>(), nullptr, st, launches));
+        }
         pf.end(st);
     }
     pf.begin(8, st);
     if (tc) {
-        // largest |L_l(mu)| over mu^2 in [0, |los|^2]: bounds the delta_2 / delta_4 maps by the delta map
-        double lfac[3] = {1.0, 1.0, 1.0};
-        const double l2max = los ? los[0] * los[0] + los[1] * los[1] + los[2] * los[2] : 1.0;
-        for (int s = 1; s < nsets; s++) {
-            if (fac[s] == 0) continue;
-            double mx = 0;
-            for (int k = 0; k <= 2000; k++) {
-                const double m2 = l2max * k / 2000.0;
-                const double L = fac[s] == 2 ? -0.5 + 1.5 * m2 : 0.375 + m2 * (-3.75 + 4.375 * m2);
-                mx = std::max(mx, fabs(L));
-            }
-            lfac[s] = mx * 1.01;
-        }
-        PBI4G_CHECK(triangle_sums_tm(sh, tmp, form, dense.as<float>(), nm, powsum.as<double>(), pow_mask, lfac,
-                                     partial, S.as<double>(), st, launches));
+        PBI4G_CHECK(triangle_sums_tm(sh, tmp, planes, partial, S.as<double>(), st, launches));
     } else if (fp64) {
         PBI4G_CHECK(triangle_sums<R>(sh, tp, maps.as<R>(), 2 * HC, 2 * NH, partial, S.as<double>(), st, launches));
     } else {

@@ -39,7 +39,8 @@ struct BkEngine {
     int nsets = 1, cross = 0;  // cross: 1 => q maps from the second field
     DevBuf maps;               // FP64: [nmaps][N][N][N/2+1] half spectra, padded real maps after the C2R;
                                // FP32: the pruned transform's intermediates (MapTransform T, U)
-    DevBuf dense;              // FP32 forms: real maps (dense, or row-interleaved)
+    DevBuf dense;              // plain FP32: real maps [m][point]; tensor-core forms: the operand planes
+    MapPlanes planes;          // tensor-core forms: the layout of `dense`
     cufftHandle inv = 0;       // FP64 maps: batched Z2D
     int inv_batch = 0, inv_N = 0;
     MapTransform mt;           // FP32 maps: pruned z / y / x passes

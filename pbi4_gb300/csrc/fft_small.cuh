@@ -1,5 +1,5 @@
 // fft_small.cuh -- building blocks of the shell-map inverse transforms
-// (mapfft.cu): complex helpers, inverse DFTs of 2, 3, 4, 5, 7 and 8 points, and
+// (mapfft.cu): complex helpers, inverse DFTs of 2, 3, 4, 5, 7, 8 and 10 points, and
 // the host-side plan of an in-place mixed-radix decimation-in-frequency FFT.
 //
 // Sign convention: every transform here is an inverse DFT,
@@ -30,6 +30,8 @@
 namespace pbi4g {
 namespace fftd {
 
+constexpr int kMaxRadix = 10;
+
 __host__ __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __host__ __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 __host__ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
@@ -40,7 +42,7 @@ __host__ __device__ __forceinline__ float2 cscale(float2 a, float s) { return ma
 
 // inverse DFT of R points in place: v[q] <- sum_r v[r] e^{+2 pi i q r / R}
 template <int R>
-__host__ __device__ __forceinline__ void dft_small(float2 (&v)[8]) {
+__host__ __device__ __forceinline__ void dft_small(float2 (&v)[kMaxRadix]) {
     if constexpr (R == 2) {
         const float2 a = v[0], b = v[1];
         v[0] = cadd(a, b);
@@ -94,6 +96,25 @@ __host__ __device__ __forceinline__ void dft_small(float2 (&v)[8]) {
         v[5] = csub(t2, u2);
         v[3] = cadd(t3, u3);
         v[4] = csub(t3, u3);
+    } else if constexpr (R == 10) {
+        // prime-factor split 10 = 2 x 5 (no twiddles): n = (5 n1 + 2 n2) mod 10,
+        // X[k] with k = k1 (mod 2), k = k2 (mod 5): 2-point DFTs over n1, then
+        // 5-point DFTs over n2; X[k2 even/odd partner] read back by the CRT map
+        float2 a[kMaxRadix], b[kMaxRadix];
+#pragma unroll
+        for (int n2 = 0; n2 < 5; n2++) {
+            const float2 x0 = v[(2 * n2) % 10], x1 = v[(5 + 2 * n2) % 10];
+            a[n2] = cadd(x0, x1);  // k1 = 0
+            b[n2] = csub(x0, x1);  // k1 = 1
+        }
+        dft_small<5>(a);
+        dft_small<5>(b);
+        // k = 5 k1 + 6 k2 (mod 10): k mod 2 = k1, k mod 5 = k2
+#pragma unroll
+        for (int k2 = 0; k2 < 5; k2++) {
+            v[(6 * k2) % 10] = a[k2];
+            v[(5 + 6 * k2) % 10] = b[k2];
+        }
     } else {
         static_assert(R == 8, "radix");
         // one radix-2 step (n, n + 4) then two 4-point DFTs: even outputs from the
@@ -108,7 +129,7 @@ __host__ __device__ __forceinline__ void dft_small(float2 (&v)[8]) {
         b[1] = make_float2(h * (b[1].x - b[1].y), h * (b[1].x + b[1].y));    // (1 + i) / sqrt 2
         b[2] = itimes(b[2]);                                                // i
         b[3] = make_float2(-h * (b[3].x + b[3].y), h * (b[3].x - b[3].y));  // (-1 + i) / sqrt 2
-        float2 e[8], o[8];
+        float2 e[kMaxRadix], o[kMaxRadix];
 #pragma unroll
         for (int r = 0; r < 4; r++) {
             e[r] = a[r];
@@ -129,7 +150,7 @@ __host__ __device__ __forceinline__ void dft_small(float2 (&v)[8]) {
 template <int R>
 __host__ __device__ __forceinline__ void dit_butterfly(float2 *buf, int pitch, int t, int base, int ls, int tstep,
                                                        const float2 *tw) {
-    float2 v[8];
+    float2 v[kMaxRadix];
     v[0] = buf[base * pitch + t];
     if (tstep) {
 #pragma unroll
@@ -165,7 +186,7 @@ struct FftPlan {
         d = FftDesc();
         d.n = n;
         int rest = n;
-        for (int r : {8, 4, 2, 3, 5, 7})
+        for (int r : {10, 8, 4, 2, 3, 5, 7})
             while (rest % r == 0) {
                 if (d.nst == kMaxStages) return false;
                 d.rad[d.nst++] = r;
@@ -225,7 +246,8 @@ inline void run_plan_host(const FftPlan &p, float2 *buf, int pitch, int t) {
                 case 4: dit_butterfly<4>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
                 case 5: dit_butterfly<5>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
                 case 7: dit_butterfly<7>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
-                default: dit_butterfly<8>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
+                case 8: dit_butterfly<8>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
+                default: dit_butterfly<10>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
             }
         }
     }

@@ -11,6 +11,8 @@
 // 256 threads fit on an SM for the 200-point transforms of the 256^3 workload.
 #include "mapfft.cuh"
 
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <math.h>
 
 #include <algorithm>
@@ -45,6 +47,9 @@ __device__ __forceinline__ void run_dit(const fftd::FftDesc &fd, float2 *buf, co
         const int R = fd.rad[s], ls = fd.ls[s], nbf = fd.n / R;
         const int2 *e = ent + fd.eoff[s];
         switch (R) {
+            case 10:
+                for (int j = warp; j < nbf; j += nw) fftd::dit_butterfly<10>(buf, kP, lane, e[j].x, ls, e[j].y, tw);
+                break;
             case 8:
                 for (int j = warp; j < nbf; j += nw) fftd::dit_butterfly<8>(buf, kP, lane, e[j].x, ls, e[j].y, tw);
                 break;
@@ -219,13 +224,17 @@ __global__ void __launch_bounds__(kThreads) map_ypass_kernel(const YArgs a) {
 }
 
 struct XArgs {
-    int Nm, count, kxmax, dense;
+    int Nm, count, kxmax, oform, nb;
     const MapInfo *info;
     const unsigned char *tab;
     fftd::FftDesc fd;   // M = Nm / 2 points
     const float2 *xtw;  // e^{2 pi i k / Nm}
     const float2 *U;
-    float *out;
+    float *out;         // oform -1: dense FP32 maps
+    void *bhi, *blo;    // oform 0 / 1 / 2: operand planes (MapPlanes)
+    float2 *a32;
+    const int *mexp;
+    long long npts;
 };
 
 // x pass: tile = (map m, 32 consecutive rows (z, y)).  With M = Nm / 2,
@@ -298,10 +307,42 @@ __global__ void __launch_bounds__(kThreads, PF <= 9 ? 4 : 2) map_xpass_kernel(co
         }
         __syncthreads();
         run_dit(fd, buf, ent, tw, warp, nw, lane);
+        // pairs of outputs (x[2j], x[2j+1]) at point index 2 p2 + 2j of the map's row
+        const float sc = a.oform == 1 ? exp2f((float)a.mexp[m]) : 1.f;
         for (int l = warp; l < nrows; l += nw) {
-            const size_t row = (size_t)row0 + l;
-            float *o = a.dense ? a.out + ((size_t)m * plane + row) * Nm : a.out + (row * a.count + m) * Nm;
-            for (int j = lane; j < M; j += 32) reinterpret_cast<float2 *>(o)[j] = buf[j * kP + l];
+            const size_t p2 = ((size_t)m * a.npts + ((size_t)row0 + l) * Nm) / 2;
+            switch (a.oform) {
+                case 1:
+                    for (int j = lane; j < M; j += 32) {
+                        const float2 v = fftd::cscale(buf[j * kP + l], sc);
+                        const __half2 h = __floats2half2_rn(v.x, v.y);
+                        const float2 hb = __half22float2(h);
+                        reinterpret_cast<__half2 *>(a.bhi)[p2 + j] = h;
+                        reinterpret_cast<__half2 *>(a.blo)[p2 + j] = __floats2half2_rn(v.x - hb.x, v.y - hb.y);
+                        if (m < a.nb) a.a32[p2 + j] = v;
+                    }
+                    break;
+                case 2:
+                    for (int j = lane; j < M; j += 32) {
+                        const float2 v = buf[j * kP + l];
+                        reinterpret_cast<__nv_bfloat162 *>(a.bhi)[p2 + j] = __floats2bfloat162_rn(v.x, v.y);
+                        if (m < a.nb) a.a32[p2 + j] = v;
+                    }
+                    break;
+                case 0:
+                    for (int j = lane; j < M; j += 32) {
+                        const float2 v = buf[j * kP + l];
+                        const float2 h = make_float2(__uint_as_float(__float_as_uint(v.x) & 0xFFFFE000u),
+                                                     __uint_as_float(__float_as_uint(v.y) & 0xFFFFE000u));
+                        reinterpret_cast<float2 *>(a.bhi)[p2 + j] = h;
+                        reinterpret_cast<float2 *>(a.blo)[p2 + j] = make_float2(v.x - h.x, v.y - h.y);
+                        if (m < a.nb) a.a32[p2 + j] = v;
+                    }
+                    break;
+                default:
+                    for (int j = lane; j < M; j += 32) reinterpret_cast<float2 *>(a.out)[p2 + j] = buf[j * kP + l];
+                    break;
+            }
         }
         m = mn;
         r = rn;
@@ -458,20 +499,29 @@ int map_ypass(const MapTransform &mt, float2 *work, cudaStream_t st, int64_t *la
     return PBI4G_OK;
 }
 
-int map_xpass(const MapTransform &mt, const float2 *work, float *out, bool dense, cudaStream_t st,
+int map_xpass(const MapTransform &mt, const float2 *work, float *out, const MapPlanes *planes, cudaStream_t st,
               int64_t *launches) {
     if (mt.nmaps == 0) return PBI4G_OK;
     XArgs a;
     a.Nm = mt.Nm;
     a.count = mt.nmaps;
     a.kxmax = mt.kxmax;
-    a.dense = dense ? 1 : 0;
+    a.oform = planes ? planes->form : -1;
+    a.nb = mt.nb;
     a.info = mt.info.as<MapInfo>();
     a.tab = static_cast<const unsigned char *>(mt.tab_x.p);
     a.fd = mt.px.d;
     a.xtw = mt.xtw.as<float2>();
     a.U = work + mt.tsize;
     a.out = out;
+    a.bhi = planes ? planes->bhi : nullptr;
+    a.blo = planes ? planes->blo : nullptr;
+    a.a32 = planes ? reinterpret_cast<float2 *>(planes->a32) : nullptr;
+    a.mexp = planes ? planes->mexp : nullptr;
+    a.npts = (long long)mt.Nm * mt.Nm * mt.Nm;
+    if (planes && (planes->form < 0 || planes->form > 2 || (planes->form == 1 && !planes->mexp) ||
+                   planes->npts != a.npts || planes->nmaps != mt.nmaps))
+        return set_error(PBI4G_ERR_INVALID, "x pass: operand planes do not match the maps");
     const int M = mt.Nm / 2, warps = kThreads / 32, pf = (mt.kxmax + warps - 1) / warps;
     const size_t smem =
         table_smem(mt.px.d) + sizeof(float2) * ((size_t)mt.Nm + (size_t)mt.kxmax * kP + (size_t)M * kP);

@@ -11,7 +11,7 @@
 //           -> T[m][column][z];
 //   y pass: per (kx < kxn(b), z), input ky in [-r(kx), r(kx)] -> U[m][kx][z][y];
 //   x pass: per (z, y) row, the Hermitian C2R from kx < kxn(b) -> the real map,
-//           written dense [m][z][y][x] or row-interleaved [z][y][m][x].
+//           written dense FP32 [m][z][y][x] or as the tensor-core operand planes.
 #pragma once
 
 #include "bispec.cuh"
@@ -29,6 +29,38 @@ struct MapInfo {
     int pad;
     long long tbase;  // first float2 of the map in T ([column][z])
     long long ubase;  // first float2 of the map in U ([kx][z][y])
+};
+
+// Tensor-core operands of the maps ("planes"), written by the x pass for the
+// tensor-core forms; every array is [map][point], point = (z Nm + y) Nm + x:
+//   form 1 (FP16 hi+lo): bhi, blo FP16 with v 2^mexp[m] = hi + lo (|v 2^mexp| <= 2^14);
+//   form 2 (BF16):       bhi BF16 of v;
+//   form 0 (TF32 hi+lo): bhi FP32 = v with the 13 low mantissa bits cleared, blo = v - bhi;
+// and a32 = the set-0 maps (m < nb) in FP32, times 2^mexp[m] for form 1 (the
+// pair factors the tensor-core kernel multiplies).
+struct MapPlanes {
+    int form = -1;
+    long long npts = 0;
+    int nmaps = 0, nb = 0;
+    void *bhi = nullptr, *blo = nullptr;
+    float *a32 = nullptr;
+    const int *mexp = nullptr;
+    static size_t bytes(int form, long long npts, int nmaps, int nb) {
+        const size_t b = form == 0 ? 8 : (form == 1 ? 4 : 2);  // B bytes per point and map
+        return b * (size_t)npts * nmaps + 4 * (size_t)npts * nb;
+    }
+    void carve(int form_, long long npts_, int nmaps_, int nb_, void *base, const int *mexp_) {
+        form = form_;
+        npts = npts_;
+        nmaps = nmaps_;
+        nb = nb_;
+        mexp = mexp_;
+        const size_t half = (form == 0 ? 4 : 2) * (size_t)npts * nmaps;  // bytes of one of hi / lo
+        unsigned char *p = static_cast<unsigned char *>(base);
+        bhi = p;
+        blo = form == 2 ? nullptr : p + half;
+        a32 = reinterpret_cast<float *>(p + (form == 2 ? half : 2 * half));
+    }
 };
 
 struct MapTransform {
@@ -54,8 +86,9 @@ int map_zpass(const Shells &sh, const MapTransform &mt, const float2 *const src[
               const double los[3], float2 *work, double *powsum, int pow_mask, cudaStream_t st, int64_t *launches);
 // y pass: work[0, tsize) -> work[tsize, tsize + usize)
 int map_ypass(const MapTransform &mt, float2 *work, cudaStream_t st, int64_t *launches);
-// x pass: real maps from work[tsize, ...), dense [m][z][y][x] or row-interleaved [z][y][m][x]
-int map_xpass(const MapTransform &mt, const float2 *work, float *out, bool dense, cudaStream_t st,
+// x pass: real maps from work[tsize, ...): dense FP32 [m][z][y][x] into `out`
+// when planes is null, else the tensor-core operand planes.
+int map_xpass(const MapTransform &mt, const float2 *work, float *out, const MapPlanes *planes, cudaStream_t st,
               int64_t *launches);
 
 // Host check of the in-place FFT plan: n-point inverse DFTs of `batch`

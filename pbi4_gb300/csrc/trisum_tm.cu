@@ -20,29 +20,26 @@
 //
 // Data path per chunk of 64 grid points (one CTA per (M tile of 128 pairs,
 // N tile of 64 maps, K range)):
-//   * the C2R writes the maps row-interleaved (the x rows of all maps for one
-//     (y, z) side by side), so one chunk of all maps is one contiguous read;
-//     chunks are pairs of (row, 32-point x block), the last block of a row
-//     zero-filled past x = Nm by the TMA bounds;
-//   * a TMA warp loads the chunk's set-0 maps (the pair factors) and the 64
-//     maps of the N tile, FP32, 128-byte swizzled, into a ring of shared-memory
-//     stages;
+//   * the x pass of the map transform writes the maps as operand planes
+//     [map][point] (FP16 hi / lo, BF16, or TF32 hi / lo) plus the set-0 maps in
+//     FP32 (the pair factors), so the B tiles need no conversion here;
+//   * a TMA warp loads each chunk's B tile(s) (64 maps x 64 points, 128-byte
+//     swizzled: the K-major operand layout itself) and the FP32 set-0 maps of
+//     the chunk into a ring of shared-memory stages;
 //   * three producer warpgroups take the chunks in turn (thread = TMEM lane =
 //     pair row): they form the 64 products of their pair, split them and store
 //     them straight into a tensor-memory A stage with tcgen05.st (the A operand
-//     never touches shared memory), and turn the FP32 B tile into the MMA
-//     operand(s): in place for TF32 (hi) plus a lo copy; 16-bit hi / lo tiles
-//     in the 128-byte swizzled K-major layout for FP16 / BF16;
-//   * an MMA warp issues the MMAs (A in TMEM, B in shared memory) into one of
+//     never touches shared memory);
+//   * an MMA warp issues the MMAs (A in TMEM, B from the stage) into one of
 //     four TMEM accumulators, a fresh one per chunk, and commits them to a
-//     per-chunk completion barrier that frees the shared-memory stage, the A
-//     stage and the accumulator.  The tensor core adds the products of one
-//     instruction to the accumulator with truncation, so keeping each
-//     accumulation to one chunk keeps that error near 1e-6;
+//     per-chunk completion barrier that frees the A stage, the accumulator and
+//     (with the producers' release) the shared-memory stage.  The tensor core
+//     adds the products of one instruction to the accumulator with truncation,
+//     so keeping each accumulation to one chunk keeps that error near 1e-6;
 //   * two drain warpgroups (32 accumulator columns each) add each chunk's
 //     accumulator into FP32 registers (round to nearest) and fold those into a
-//     Kahan-compensated sum in shared memory every 16 chunks, then write the
-//     final sums (FP64, scaled back by the FP16 exponents) of the triangle slots.
+//     Kahan-compensated sum every 16 chunks, then write the final sums (FP64,
+//     scaled back by the FP16 exponents) of the triangle slots.
 // Every wait is bounded: a wait that runs out sets an abort flag that ends all
 // roles, records the error for the host, and the CTA waits (bounded) for its
 // own MMAs and copies in flight before it frees its tensor memory.
@@ -71,7 +68,7 @@ constexpr int kN = 64;           // maps per unit (MMA N)
 constexpr int kKB = 32;          // FP32 values per 128-byte swizzle row (one K block)
 constexpr int kBlocks = 2;       // K blocks per chunk
 constexpr int kKC = kKB * kBlocks;  // grid points per chunk
-constexpr int kMaxStages = 8;    // TMA staging slots (released by the producers)
+constexpr int kMaxStages = 10;   // TMA staging slots (released by the producers and the MMAs)
 constexpr int kGroups = 3;       // producer warpgroups, chunks assigned round robin
 constexpr int kProdWarps = 4 * kGroups;
 constexpr int kDrainWarps = 8;   // two warpgroups, 32 accumulator columns each
@@ -84,7 +81,8 @@ constexpr int kDone = 16;        // per-chunk MMA completion barriers (ring)
 constexpr uint32_t kColAcc = 0;  // kAcc accumulators of kN columns, then the A stages
 constexpr uint32_t kColA = kAcc * kN;
 constexpr uint32_t kTmemCols = 512;
-constexpr uint32_t kBBlock = kN * 128;   // bytes of one 128-byte-row tile of the N tile
+constexpr uint32_t kBTile = kN * 128;    // one B tile: 64 maps x 128 bytes
+static_assert(kMaxStages <= kDone, "a stage's MMA barrier must not have cycled when the stage is reused");
 constexpr uint32_t kTfMask = 0xFFFFE000u;
 
 enum : int { kFormTF32 = 0, kFormF16 = 1, kFormBF16 = 2 };
@@ -94,7 +92,7 @@ template <int F> struct Form;
 template <> struct Form<kFormTF32> {
     static constexpr uint32_t kACols = 2 * kKC;
     static constexpr int kAStages = 2;
-    static constexpr int kOpSlots = 2;
+    static constexpr int kBTiles = 4;  // hi, hi, lo, lo: 32 FP32 points per 128-byte row
     static constexpr int kKStep = 8;
     static constexpr bool kSplit = true;
     static constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kN >> 3) << 17) |
@@ -104,7 +102,7 @@ template <> struct Form<kFormTF32> {
 template <> struct Form<kFormF16> {
     static constexpr uint32_t kACols = kKC;
     static constexpr int kAStages = 4;
-    static constexpr int kOpSlots = 4;
+    static constexpr int kBTiles = 2;  // hi, lo: 64 FP16 points per 128-byte row
     static constexpr int kKStep = 16;
     static constexpr bool kSplit = true;
     static constexpr uint32_t kIdesc = (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(kN >> 3) << 17) |
@@ -114,7 +112,7 @@ template <> struct Form<kFormF16> {
 template <> struct Form<kFormBF16> {
     static constexpr uint32_t kACols = kKC / 2;
     static constexpr int kAStages = 4;
-    static constexpr int kOpSlots = 4;
+    static constexpr int kBTiles = 1;
     static constexpr int kKStep = 16;
     static constexpr bool kSplit = false;
     static constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kN >> 3) << 17) |
@@ -151,11 +149,11 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
                  : "memory");
 }
 
-__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *tm, int x, int y, int z, uint64_t *bar) {
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *tm, int x, int y, uint64_t *bar) {
     asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
-        "[%5];" ::"r"(smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+        "[%4];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar))
         : "memory");
 }
 
@@ -194,33 +192,34 @@ __device__ __forceinline__ void pack2(float x, float y, uint32_t &hi, uint32_t &
 }
 
 struct TmArgs {
-    long long nchunks;     // K / kKC
-    int nunits, ksplit, nslots, nA, nstages, nmaps, nxb;
-    uint32_t stage_bytes, op_bytes, ablock;
+    long long nchunks;     // points / kKC, rounded up
+    int nunits, ksplit, nslots, nA, nstages, nmaps;
+    uint32_t stage_bytes, ablock;
+    float apre;            // factor of every pair product: 2^-14 for the FP16 form (maps stored x 2^e), else 1
     float *kahan;          // [grid][2][kN][kM] running sum and compensation of each CTA (L2-resident)
     const int2 *units;     // (M tile, N tile) per unit
     const int2 *prow;      // [nunits][kM] staged rows (i, j) of each pair's factors, (-1, -1) for none
     const int *slots;      // [nunits][kM][kN] output slot or -1
-    const int *mexp;       // FP16 form: per-map exponent e with |M| 2^e <= 2^14
+    const int *mexp;       // FP16 form: per-map exponent e, map stored times 2^e (|M| 2^e <= 2^14)
     double *partial;       // [ksplit][nslots]
     int *err;              // set to 1 when a bounded wait gives up
 };
 
 template <int F>
 __global__ void __launch_bounds__(kThreads, 1)
-    trisum_tm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                     const TmArgs a) {
+    trisum_tm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmBh,
+                     const __grid_constant__ CUtensorMap tmBl, const TmArgs a) {
     using FM = Form<F>;
-    constexpr int AST = FM::kAStages, kOpSlots = FM::kOpSlots;
+    constexpr int AST = FM::kAStages;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *base =
         reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     const int nst = a.nstages;
-    // barriers: full per smem stage (TMA -> producers), prod per A stage (producers -> MMA),
-    // done per chunk ring (MMA completion -> TMA, producers, drain), accfree per accumulator (drain -> MMA)
-    // smem: nst staging slots | kOpSlots operand slots | barriers and tables
-    unsigned char *opbase = base + (size_t)nst * a.stage_bytes;
-    uint64_t *bars = reinterpret_cast<uint64_t *>(opbase + (size_t)kOpSlots * a.op_bytes);
+    // barriers: full per stage (TMA -> producers, MMA), sfree per stage (producers -> TMA),
+    // prod per A stage (producers -> MMA), done per chunk ring (MMA completion -> TMA,
+    // producers, drain), accfree per accumulator (drain -> MMA)
+    // smem: nst stages | barriers and tables
+    uint64_t *bars = reinterpret_cast<uint64_t *>(base + (size_t)nst * a.stage_bytes);
     uint64_t *full = bars, *sfree = full + kMaxStages, *prod = sfree + kMaxStages, *done = prod + 4;
     uint64_t *accfree = done + kDone;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(accfree + kAcc);
@@ -244,7 +243,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (tid == 0) {
         for (int s = 0; s < kMaxStages; s++) {
             mbar_init(&full[s], 1);
-            mbar_init(&sfree[s], 128);  // the warpgroup that consumed the slot
+            mbar_init(&sfree[s], 128);  // the warpgroup that consumed the stage's pair factors
         }
         for (int s = 0; s < 4; s++) mbar_init(&prod[s], 128);  // one warpgroup per chunk
         for (int s = 0; s < kDone; s++) mbar_init(&done[s], 1);
@@ -261,10 +260,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
-    // staging slot: A-source blocks [kBlocks][ablock] | B FP32 blocks [kBlocks][kBBlock]
-    // operand slot: TF32 hi, lo blocks [2][kBlocks][kBBlock]; FP16/BF16 hi, lo tiles [2][kBBlock]
+    // stage: pair-factor blocks [kBlocks][ablock] (FP32, 32 points a row) | B tiles [kBTiles][kBTile]
     auto stage_ptr = [&](int s) { return base + (size_t)s * a.stage_bytes; };
-    auto op_ptr = [&](int o) { return opbase + (size_t)o * a.op_bytes; };
     auto fail = [&]() {
         *abort_flag = 1;
         atomicExch(a.err, 1);
@@ -275,61 +272,17 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int quad = warp & 3, grp = warp >> 2;
         const int row = quad * 32 + lane;
         const int2 pr = prow_s[row];
-        const float pscale =
-            (F == kFormF16 && pr.x >= 0) ? exp2f((float)(a.mexp[pr.x] + a.mexp[pr.y] - 14)) : 1.0f;
+        const float pscale = a.apre;
         const uint32_t lane_addr = tmem + ((uint32_t)(quad * 32) << 16);
-        const int gtid = tid & 127;
         for (long long i = grp; i < n; i += kGroups) {
-            const int s = (int)(i % nst), as = (int)(i % AST), o = (int)(i % kOpSlots);
+            const int s = (int)(i % nst), as = (int)(i % AST);
             if (!warp_wait(&full[s], ph(i, nst), abort_flag)) { fail(); break; }
-            // the A stage and the operand slot are free once the MMAs of chunk
-            // i - min(AST, kOpSlots) completed (MMAs complete in order)
-            constexpr int kBack = AST < kOpSlots ? AST : kOpSlots;
-            if (i >= kBack && !warp_wait(&done[(i - kBack) % kDone], ph(i - kBack, kDone), abort_flag)) {
+            // the A stage is free once the MMAs of chunk i - AST completed (MMAs complete in order)
+            if (i >= AST && !warp_wait(&done[(i - AST) % kDone], ph(i - AST, kDone), abort_flag)) {
                 fail();
                 break;
             }
-            unsigned char *stg = stage_ptr(s);
-            const unsigned char *bf = stg + kBlocks * a.ablock;  // FP32 B tile (kBlocks blocks)
-            unsigned char *bx = op_ptr(o);
-            if constexpr (F == kFormTF32) {
-                // hi and lo blocks, elementwise on the swizzled bytes
-                const float4 *bv = reinterpret_cast<const float4 *>(bf);
-                float4 *hv = reinterpret_cast<float4 *>(bx);
-                float4 *lv = reinterpret_cast<float4 *>(bx + kBlocks * kBBlock);
-#pragma unroll
-                for (int e = 0; e < (int)(kBlocks * kBBlock / 16) / 128; e++) {
-                    const int idx = gtid + e * 128;
-                    const float4 v = bv[idx];
-                    float4 h, l;
-                    h.x = __uint_as_float(__float_as_uint(v.x) & kTfMask); l.x = v.x - h.x;
-                    h.y = __uint_as_float(__float_as_uint(v.y) & kTfMask); l.y = v.y - h.y;
-                    h.z = __uint_as_float(__float_as_uint(v.z) & kTfMask); l.z = v.z - h.z;
-                    h.w = __uint_as_float(__float_as_uint(v.w) & kTfMask); l.w = v.w - h.w;
-                    hv[idx] = h;
-                    lv[idx] = l;
-                }
-            } else {
-                // 16-bit tiles: row r, 16-byte group g (points 8g..8g+7) at r*128 + ((g ^ (r&7)) << 4);
-                // in the FP32 blocks those points are groups c, c+1 (c = 2 (g % 4)) of block g / 4
-#pragma unroll
-                for (int e = 0; e < 4; e++) {
-                    const int t = gtid + e * 128, r = t >> 3, g = t & 7;
-                    const unsigned char *blk = bf + (g >> 2) * kBBlock + r * 128;
-                    const int c = 2 * (g & 3);
-                    const float4 x0 = *reinterpret_cast<const float4 *>(blk + ((c ^ (r & 7)) << 4));
-                    const float4 x1 = *reinterpret_cast<const float4 *>(blk + (((c + 1) ^ (r & 7)) << 4));
-                    const float sc = F == kFormF16 ? exp2f((float)qexp_s[r]) : 1.0f;
-                    uint32_t h[4], l[4];
-                    pack2<F>(x0.x * sc, x0.y * sc, h[0], l[0]);
-                    pack2<F>(x0.z * sc, x0.w * sc, h[1], l[1]);
-                    pack2<F>(x1.x * sc, x1.y * sc, h[2], l[2]);
-                    pack2<F>(x1.z * sc, x1.w * sc, h[3], l[3]);
-                    const uint32_t off = (uint32_t)(r * 128 + ((g ^ (r & 7)) << 4));
-                    *reinterpret_cast<uint4 *>(bx + off) = make_uint4(h[0], h[1], h[2], h[3]);
-                    if (FM::kSplit) *reinterpret_cast<uint4 *>(bx + kBBlock + off) = make_uint4(l[0], l[1], l[2], l[3]);
-                }
-            }
+            const unsigned char *stg = stage_ptr(s);
             const uint32_t acol = kColA + (uint32_t)as * FM::kACols;
 #pragma unroll
             for (int kb = 0; kb < kBlocks; kb++) {
@@ -384,9 +337,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                     if (FM::kSplit) tmem_st16(lane_addr + col + kKC / 2, lo);
                 }
             }
-            mbar_arrive(&sfree[s]);  // staging slot consumed (its values are in registers / TMEM / the operand slot)
+            mbar_arrive(&sfree[s]);  // the stage's pair factors are consumed
             tmem_wait_st();
-            fence_proxy_async();  // the B operand written by these threads is read by the tensor core
             tc_fence_before();
             mbar_arrive(&prod[as]);
         }
@@ -394,7 +346,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         // ---------------------------------------------------------------- drain
         // each chunk's accumulator is added into FP32 registers (round to nearest);
         // every kFold chunks those are folded into a Kahan-compensated sum kept in
-        // shared memory ([column][row], conflict-free), written out at the end
+        // an L2-resident scratch ([column][row]), written out at the end
         const int quad = warp & 3, cgrp = (warp - kProdWarps) >> 2;
         const int row = quad * 32 + lane, c0 = 32 * cgrp;
         const uint32_t lane_addr = tmem + ((uint32_t)(quad * 32) << 16);
@@ -421,15 +373,29 @@ __global__ void __launch_bounds__(kThreads, 1)
             tc_fence_before();
             mbar_arrive(&accfree[b]);
             if ((i + 1) % kFold == 0 || i == n - 1) {
+                // each group's scratch loads are issued before its first store, so the
+                // fold costs a few L2 round trips
 #pragma unroll
-                for (int e = 0; e < 32; e++) {
-                    float *pr_ = run_g + (c0 + e) * kM + row, *pc = comp_g + (c0 + e) * kM + row;
-                    const float y = mid[e] - *pc;
-                    const float sm = *pr_;
-                    const float t2 = sm + y;
-                    *pc = (t2 - sm) - y;
-                    *pr_ = t2;
-                    mid[e] = 0.f;
+                for (int h = 0; h < 32; h += 8) {
+                    float rv[8], cv[8];
+#pragma unroll
+                    for (int e = 0; e < 8; e++) {
+                        rv[e] = __ldcg(run_g + (c0 + h + e) * kM + row);
+                        cv[e] = __ldcg(comp_g + (c0 + h + e) * kM + row);
+                    }
+#pragma unroll
+                    for (int e = 0; e < 8; e++) {
+                        const float y = mid[h + e] - cv[e];
+                        const float t2 = rv[e] + y;
+                        cv[e] = (t2 - rv[e]) - y;
+                        rv[e] = t2;
+                        mid[h + e] = 0.f;
+                    }
+#pragma unroll
+                    for (int e = 0; e < 8; e++) {
+                        __stcg(run_g + (c0 + h + e) * kM + row, rv[e]);
+                        __stcg(comp_g + (c0 + h + e) * kM + row, cv[e]);
+                    }
                 }
             }
         }
@@ -451,26 +417,27 @@ __global__ void __launch_bounds__(kThreads, 1)
             long long last_commit = -1;
             bool ok = true;
             for (long long i = 0; i < n; i++) {
-                const int b = (int)(i % kAcc), as = (int)(i % AST);
+                const int b = (int)(i % kAcc), as = (int)(i % AST), s = (int)(i % nst);
                 if (i >= kAcc && !wait_or_abort(&accfree[b], ph(i - kAcc, kAcc), abort_flag)) { ok = false; break; }
-                if (!wait_or_abort(&prod[as], ph(i, AST), abort_flag)) { ok = false; break; }
+                if (!wait_or_abort(&full[s], ph(i, nst), abort_flag)) { ok = false; break; }  // B tiles
+                if (!wait_or_abort(&prod[as], ph(i, AST), abort_flag)) { ok = false; break; }  // A stage
                 tc_fence_after();
-                const uint32_t b0 = smem_u32(op_ptr((int)(i % kOpSlots)));
+                const uint32_t b0 = smem_u32(stage_ptr(s)) + kBlocks * a.ablock;
                 const uint32_t ahi = tmem + kColA + (uint32_t)as * FM::kACols;
                 const uint32_t d = tmem + kColAcc + (uint32_t)b * kN;
 #pragma unroll
                 for (int kk = 0; kk < kKC / FM::kKStep; kk++) {
                     uint32_t bh, bl, a_hi, a_lo;
                     if constexpr (F == kFormTF32) {
-                        // FP32 rows: K-step of 8 = 32 bytes; block kk / 4
-                        bh = b0 + (uint32_t)(kk / 4) * kBBlock + (uint32_t)(kk % 4) * 32;
-                        bl = bh + kBlocks * kBBlock;
+                        // FP32 rows: K-step of 8 = 32 bytes; tiles hi0, hi1, lo0, lo1
+                        bh = b0 + (uint32_t)(kk / 4) * kBTile + (uint32_t)(kk % 4) * 32;
+                        bl = bh + 2 * kBTile;
                         a_hi = ahi + 8 * kk;
                         a_lo = a_hi + kKC;
                     } else {
-                        // 16-bit rows: K-step of 16 = 32 bytes of the hi / lo tiles
+                        // 16-bit rows: K-step of 16 = 32 bytes; tiles hi, lo
                         bh = b0 + (uint32_t)kk * 32;
-                        bl = bh + kBBlock;
+                        bl = bh + kBTile;
                         a_hi = ahi + 8 * kk;
                         a_lo = a_hi + kKC / 2;
                     }
@@ -490,25 +457,34 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
     } else if (lane == 0) {
         // --------------------------------------------------------- TMA issue (one thread)
-        const uint32_t tx = kBlocks * ((uint32_t)a.nA * 128 + kBBlock);
+        const uint32_t tx = kBlocks * (uint32_t)a.nA * 128 + FM::kBTiles * kBTile;
+        const int q0 = U.y * kN;
         long long issued = 0;
         bool ok = true;
         for (long long j = 0; j < n; j++) {
             const int s = (int)(j % nst);
-            // staging slot s is free once the producers consumed chunk j - nst
-            if (j >= nst && !wait_or_abort(&sfree[s], ph(j - nst, nst), abort_flag)) {
+            // stage s is free once the producers took the pair factors of chunk j - nst
+            // and the MMAs of that chunk (which read its B tiles) completed
+            if (j >= nst && (!wait_or_abort(&sfree[s], ph(j - nst, nst), abort_flag) ||
+                             !wait_or_abort(&done[(j - nst) % kDone], ph(j - nst, kDone), abort_flag))) {
                 ok = false;
                 break;
             }
             unsigned char *stg = stage_ptr(s);
+            unsigned char *bt = stg + kBlocks * a.ablock;
             mbar_expect_tx(&full[s], tx);
+            const int x0 = (int)((cb + j) * kKC);  // first point of the chunk (past the end: zero fill)
 #pragma unroll
-            for (int kb = 0; kb < kBlocks; kb++) {
-                // K block -> (32-point x block, map row); blocks past the last row read zeros
-                const long long blk = (cb + j) * kBlocks + kb;
-                const int row = (int)(blk / a.nxb), x0 = (int)(blk - (long long)row * a.nxb) * kKB;
-                tma_load_3d(stg + kb * a.ablock, &tmA, x0, 0, row, &full[s]);
-                tma_load_3d(stg + kBlocks * a.ablock + kb * kBBlock, &tmB, x0, U.y * kN, row, &full[s]);
+            for (int kb = 0; kb < kBlocks; kb++) tma_load_2d(stg + kb * a.ablock, &tmA, x0 + kb * kKB, 0, &full[s]);
+            if constexpr (F == kFormTF32) {
+#pragma unroll
+                for (int kb = 0; kb < kBlocks; kb++) {
+                    tma_load_2d(bt + kb * kBTile, &tmBh, x0 + kb * kKB, q0, &full[s]);
+                    tma_load_2d(bt + (2 + kb) * kBTile, &tmBl, x0 + kb * kKB, q0, &full[s]);
+                }
+            } else {
+                tma_load_2d(bt, &tmBh, x0, q0, &full[s]);
+                if (FM::kSplit) tma_load_2d(bt + kBTile, &tmBl, x0, q0, &full[s]);
             }
             issued = j + 1;
         }
@@ -563,18 +539,22 @@ EncodeTiledFn encode_fn() {
     return fn;
 }
 
-// 3D FP32 view of the row-interleaved maps [Nm^2 rows][nmaps][Nm]: box 32 x
-// box_rows x 1 at (x0, first map, row), 128-byte swizzle, zero fill past the
-// row end (x >= Nm), past `rows` maps and past the last row.
-int make_row_view(CUtensorMap *tm, const float *maps, int Nm, int nmaps, int rows, int box_rows) {
+// 2D view of an operand plane array [rows][npts] (element size esize): box
+// box_pts x box_rows at (first point, first row), 128-byte swizzle (box_pts
+// esize = 128 bytes: the K-major operand layout), zero fill past the last
+// point and the last row.
+int make_plane_view(CUtensorMap *tm, const void *base, CUtensorMapDataType dt, int esize, long long npts, int rows,
+                    int box_pts, int box_rows) {
     EncodeTiledFn enc = encode_fn();
     if (!enc) return set_error(PBI4G_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
-    const cuuint64_t gdim[3] = {(cuuint64_t)Nm, (cuuint64_t)rows, (cuuint64_t)Nm * Nm};
-    const cuuint64_t gstride[2] = {(cuuint64_t)Nm * sizeof(float), (cuuint64_t)nmaps * Nm * sizeof(float)};
-    const cuuint32_t box[3] = {(cuuint32_t)kKB, (cuuint32_t)box_rows, 1};
-    const cuuint32_t estr[3] = {1, 1, 1};
-    const CUresult r = enc(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(maps), gdim, gstride, box,
-                           estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+    if (box_pts * esize != 128 || reinterpret_cast<uintptr_t>(base) % 16 || (npts * esize) % 16)
+        return set_error(PBI4G_ERR_INVALID, "operand plane view: alignment");
+    const cuuint64_t gdim[2] = {(cuuint64_t)npts, (cuuint64_t)rows};
+    const cuuint64_t gstride[1] = {(cuuint64_t)npts * esize};
+    const cuuint32_t box[2] = {(cuuint32_t)box_pts, (cuuint32_t)box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = enc(tm, dt, 2, const_cast<void *>(base), gdim, gstride, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return set_error(PBI4G_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
     return PBI4G_OK;
@@ -649,56 +629,67 @@ int TmPlan::build(const Shells &sh, int nsets_) {
 }
 
 bool tm_supported(const Shells &sh) {
-    const long long rows = (long long)sh.Nm * sh.Nm;
-    return sh.nb <= 256 && sh.Nm % 4 == 0 && rows * ((sh.Nm + kKB - 1) / kKB) < (1LL << 31);
+    const long long npts = (long long)sh.Nm * sh.Nm * sh.Nm;
+    return sh.nb <= 256 && sh.Nm % 4 == 0 && npts + kKC < (1LL << 31);
 }
 
 template <int F>
-static int launch_tm(const CUtensorMap &tmA, const CUtensorMap &tmB, const TmArgs &a, size_t smem, int grid,
-                     cudaStream_t st) {
+static int launch_tm(const CUtensorMap &tmA, const CUtensorMap &tmBh, const CUtensorMap &tmBl, const TmArgs &a,
+                     size_t smem, int grid, cudaStream_t st) {
     PBI4G_CUDA(cudaFuncSetAttribute(trisum_tm_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    trisum_tm_kernel<F><<<grid, kThreads, smem, st>>>(tmA, tmB, a);
+    trisum_tm_kernel<F><<<grid, kThreads, smem, st>>>(tmA, tmBh, tmBl, a);
     PBI4G_LAUNCH_CHECK();
     return PBI4G_OK;
 }
 
-int triangle_sums_tm(const Shells &sh, TmPlan &tp, int form, const float *maps, int nmaps, const double *powsum,
-                     int pow_mask, const double lfac[3], DevBuf &partial, double *S, cudaStream_t st,
-                     int64_t *launches) {
-    const int N = sh.Nm;
+int tm_map_exponents(const Shells &sh, TmPlan &tp, int nmaps, const double *powsum, int pow_mask,
+                     const double lfac[3], cudaStream_t st, int64_t *launches) {
+    PBI4G_CHECK(tp.mexp.ensure(sizeof(int) * std::max(1, nmaps)));
+    map_exponents_kernel<<<1, 256, 0, st>>>(nmaps, sh.nb, powsum, pow_mask, lfac[1], lfac[2],
+                                            sh.nmodes_d.as<double>(), tp.mexp.as<int>());
+    PBI4G_LAUNCH_CHECK();
+    *launches += 1;
+    return PBI4G_OK;
+}
+
+int triangle_sums_tm(const Shells &sh, TmPlan &tp, const MapPlanes &pl, DevBuf &partial, double *S,
+                     cudaStream_t st, int64_t *launches) {
+    const int form = pl.form;
     if (!tm_supported(sh))
-        return set_error(PBI4G_ERR_UNSUPPORTED, "tensor-core triangle sums: map grid %d, %d shells", N, sh.nb);
+        return set_error(PBI4G_ERR_UNSUPPORTED, "tensor-core triangle sums: map grid %d, %d shells", sh.Nm, sh.nb);
     if (form < 0 || form > 2) return set_error(PBI4G_ERR_INVALID, "tensor-core form %d", form);
     if (tp.nunits == 0) return PBI4G_OK;
-    if (reinterpret_cast<uintptr_t>(maps) % 16)
-        return set_error(PBI4G_ERR_INVALID, "tensor-core triangle sums: maps must be 16-byte aligned");
-    PBI4G_CHECK(tp.mexp.ensure(sizeof(int) * std::max(1, nmaps)));
-    if (form == 1) {
-        map_exponents_kernel<<<1, 256, 0, st>>>(nmaps, sh.nb, powsum, pow_mask, lfac[1], lfac[2],
-                                                sh.nmodes_d.as<double>(), tp.mexp.as<int>());
-        PBI4G_LAUNCH_CHECK();
-        *launches += 1;
+    if (form == 1 && (!pl.mexp || pl.mexp != tp.mexp.as<int>()))
+        return set_error(PBI4G_ERR_INVALID, "tensor-core triangle sums: FP16 planes without the plan's exponents");
+    if (pl.nb != sh.nb || pl.npts != (long long)sh.Nm * sh.Nm * sh.Nm)
+        return set_error(PBI4G_ERR_INVALID, "tensor-core triangle sums: operand planes do not match the shells");
+    CUtensorMap tmA, tmBh, tmBl;
+    PBI4G_CHECK(make_plane_view(&tmA, pl.a32, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pl.npts, sh.nb, kKB, tp.nA));
+    if (form == 0) {
+        PBI4G_CHECK(make_plane_view(&tmBh, pl.bhi, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pl.npts, pl.nmaps, kKB, kN));
+        PBI4G_CHECK(make_plane_view(&tmBl, pl.blo, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pl.npts, pl.nmaps, kKB, kN));
+    } else if (form == 1) {
+        PBI4G_CHECK(make_plane_view(&tmBh, pl.bhi, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, pl.npts, pl.nmaps, kKC, kN));
+        PBI4G_CHECK(make_plane_view(&tmBl, pl.blo, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, pl.npts, pl.nmaps, kKC, kN));
+    } else {
+        PBI4G_CHECK(make_plane_view(&tmBh, pl.bhi, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, pl.npts, pl.nmaps, kKC, kN));
+        tmBl = tmBh;  // unused: one product
     }
-    CUtensorMap tmA, tmB;
-    PBI4G_CHECK(make_row_view(&tmA, maps, N, nmaps, sh.nb, tp.nA));
-    PBI4G_CHECK(make_row_view(&tmB, maps, N, nmaps, nmaps, kN));
     TmArgs a;
-    // K blocks: (map row, 32-point x block), the last x block of a row zero-padded
-    a.nxb = (N + kKB - 1) / kKB;
-    a.nchunks = ((long long)N * N * a.nxb + kBlocks - 1) / kBlocks;
+    a.nchunks = (pl.npts + kKC - 1) / kKC;
     a.nunits = tp.nunits;
     a.ksplit = std::max(1, 152 / tp.nunits);
     a.ksplit = (int)std::min<long long>(a.ksplit, std::max<long long>(1, a.nchunks / 128));
     a.nslots = tp.nslots;
     a.nA = tp.nA;
-    a.nmaps = nmaps;
+    a.nmaps = pl.nmaps;
+    a.apre = form == 1 ? ldexpf(1.0f, -14) : 1.0f;
     a.ablock = (uint32_t)(((tp.nA + 7) / 8) * 8 * 128);
-    a.stage_bytes = kBlocks * (a.ablock + kBBlock);
-    a.op_bytes = form == 0 ? 2 * kBlocks * kBBlock : 2 * kBBlock;
+    const int btiles = form == 0 ? Form<kFormTF32>::kBTiles : (form == 1 ? Form<kFormF16>::kBTiles : 1);
+    a.stage_bytes = kBlocks * a.ablock + (uint32_t)btiles * kBTile;
     // barriers, TMEM address, abort flag, pair table, B-row exponents
     const size_t tail = 8 * (2 * kMaxStages + 4 + kDone + kAcc) + 16 + sizeof(int2) * kM + sizeof(int) * kN;
-    const int op_slots = form == 0 ? Form<kFormTF32>::kOpSlots : Form<kFormF16>::kOpSlots;
-    const size_t fixed = 1024 + (size_t)op_slots * a.op_bytes + tail;
+    const size_t fixed = 1024 + tail;
     a.nstages = kMaxStages;
     while (a.nstages > 3 && fixed + (size_t)a.nstages * a.stage_bytes > 227 * 1024) a.nstages--;
     const size_t smem = fixed + (size_t)a.nstages * a.stage_bytes;
@@ -706,6 +697,7 @@ int triangle_sums_tm(const Shells &sh, TmPlan &tp, int form, const float *maps, 
     a.units = tp.units.as<int2>();
     a.prow = tp.prow.as<int2>();
     a.slots = tp.slots.as<int>();
+    PBI4G_CHECK(tp.mexp.ensure(sizeof(int) * std::max(1, pl.nmaps)));
     a.mexp = tp.mexp.as<int>();
     PBI4G_CHECK(partial.ensure(sizeof(double) * (size_t)a.ksplit * tp.nslots));
     a.partial = partial.as<double>();
@@ -714,9 +706,9 @@ int triangle_sums_tm(const Shells &sh, TmPlan &tp, int form, const float *maps, 
     const int grid = tp.nunits * a.ksplit;
     PBI4G_CHECK(tp.kahan.ensure(sizeof(float) * 2 * kN * kM * (size_t)grid));
     a.kahan = tp.kahan.as<float>();
-    if (form == 0) PBI4G_CHECK(launch_tm<kFormTF32>(tmA, tmB, a, smem, grid, st));
-    else if (form == 1) PBI4G_CHECK(launch_tm<kFormF16>(tmA, tmB, a, smem, grid, st));
-    else PBI4G_CHECK(launch_tm<kFormBF16>(tmA, tmB, a, smem, grid, st));
+    if (form == 0) PBI4G_CHECK(launch_tm<kFormTF32>(tmA, tmBh, tmBl, a, smem, grid, st));
+    else if (form == 1) PBI4G_CHECK(launch_tm<kFormF16>(tmA, tmBh, tmBl, a, smem, grid, st));
+    else PBI4G_CHECK(launch_tm<kFormBF16>(tmA, tmBh, tmBl, a, smem, grid, st));
     PBI4G_CHECK(reduce_partials(tp.nslots, a.ksplit, partial.as<double>(), S, st));
     *launches += 2;
     return PBI4G_OK;

@@ -1,6 +1,7 @@
 // trisum_tm.cuh -- host interface of the tensor-core triangle sums (trisum_tm.cu).
 #pragma once
 #include "bispec.cuh"
+#include "mapfft.cuh"
 
 namespace pbi4g {
 
@@ -16,17 +17,18 @@ struct TmPlan {
 
 bool tm_supported(const Shells &sh);
 
-// S[slot] for every (triangle, set) slot on the tensor cores.  form: 0 TF32
-// hi+lo, 1 FP16 hi+lo, 2 BF16.  maps: FP32 maps on the map grid, row-interleaved:
-// point (x, y, z) of map m at ((z Nm + y) nmaps + m) Nm + x (every map's row of
-// one (y, z) side by side), 16-byte aligned, as a batched C2R writes them with
-// an output embedding of nmaps Nm per row.  FP16 form only: powsum[s*nb + b] is the
-// full-grid sum of |H|^2 per set and shell (sets in pow_mask), which with the
-// shell's mode count bounds max |M| and sets each map's scale; lfac[s] bounds
-// |L_l| for sets without their own power.
-int triangle_sums_tm(const Shells &sh, TmPlan &tp, int form, const float *maps, int nmaps, const double *powsum,
-                     int pow_mask, const double lfac[3], DevBuf &partial, double *S, cudaStream_t st,
-                     int64_t *launches);
+// FP16 form: the per-map power-of-two exponents into tp.mexp, before the x
+// pass writes the scaled operand planes.  powsum[s*nb + b] is the full-grid sum
+// of |H|^2 per set and shell (sets in pow_mask), which with the shell's mode
+// count bounds max |M|; lfac[s] bounds |L_l| for sets without their own power.
+int tm_map_exponents(const Shells &sh, TmPlan &tp, int nmaps, const double *powsum, int pow_mask,
+                     const double lfac[3], cudaStream_t st, int64_t *launches);
+
+// S[slot] for every (triangle, set) slot on the tensor cores, from the operand
+// planes the x pass wrote (pl.form: 0 TF32 hi+lo, 1 FP16 hi+lo with pl.mexp ==
+// tp.mexp, 2 BF16).
+int triangle_sums_tm(const Shells &sh, TmPlan &tp, const MapPlanes &pl, DevBuf &partial, double *S,
+                     cudaStream_t st, int64_t *launches);
 // PBI4G_ERR_TIMEOUT if a bounded wait inside the last launch gave up (synchronises st).
 int tm_check_error(TmPlan &tp, cudaStream_t st);
 

@@ -12,7 +12,9 @@ FP32 forms: Tz, Uy complex elements of the pruned transform's z-column and
   shell_maps_z    FP32: 8 Tz write (the shell modes it gathers stay in L2);
                   FP64: 16 H read + 16 M Hm write (shell spectra)
   shell_maps_y    FP32: 8 Tz read + 8 Uy write (FP64: cuFFT Z2D, a library call)
-  shell_maps_x    FP32: 8 Uy read + 4 M Nm^3 write (the real maps)
+  shell_maps_x    FP32: 8 Uy read + 4 M Nm^3 write (the real maps; the tensor-core forms
+                  write their operand planes: 4 / 8 / 2 B per map and point for FP16 hi+lo /
+                  TF32 hi+lo / BF16, plus 4 nb Nm^3 for the FP32 pair factors)
   triangle_sums   2 Nm^3 T S flops (tensor-core forms; useful sums only)
 cuFFT stages (fft_r2c, the FP64 shell_maps_y) are library calls: timed, not given a roofline.
 Peaks are the measured ones in MEASURED_PEAKS.json at the repository root
@@ -68,7 +70,11 @@ def stage_work(cfg, npart, map_grid=None, nmaps=None, map_work=None):
         tz, uy = map_work
         work["shell_maps_z"] = ("hbm", 8 * tz)
         work["shell_maps_y"] = ("hbm", 8 * tz + 8 * uy)
-        work["shell_maps_x"] = ("hbm", 8 * uy + 4 * M * Nm ** 3)
+        # the x pass writes 4 B per map and point (FP32 maps, or FP16 hi + lo), 8 B (TF32 hi + lo) or
+        # 2 B (BF16), plus the FP32 set-0 maps (the pair factors) for the tensor-core forms
+        per_map = {"fp16split": 4, "tf32split": 8, "bf16": 2}.get(cfg.precision, 4)
+        extra = 4 * int(cfg.nbins_bs or 0) * Nm ** 3 if cfg.precision in ("fp16split", "tf32split", "bf16") else 0
+        work["shell_maps_x"] = ("hbm", 8 * uy + per_map * M * Nm ** 3 + extra)
     return work
 
 
