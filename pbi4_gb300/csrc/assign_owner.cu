@@ -62,41 +62,38 @@ __device__ __forceinline__ void first_and_h(double p, int N, int nintp, bool shi
     h = (float)hh;
 }
 
-// the NI weights of the per-axis stencil at offset h (the reference's
-// polynomials in FP32; the division by 6 as a product with the FP32 value of
-// 1/6, which stays within one rounding of the quotient and needs no division
-// sequence)
+// Weight i of the per-axis stencil at offset h as a cubic in h,
+// w_i(h) = c0 + h (c1 + h (c2 + h c3)): the reference's polynomials
+// (powerI4.f90) expanded, e.g. PCS w0 = (1-h)^3/6, w1 = 4/6 + (h/2 - 1) h^2,
+// w3 = h^3/6 and w2 = 1 - w0 - w1 - w3; TSC w0 = (1/2 - h)^2 / 2, w1 = 3/4 - h^2,
+// w2 = 1 - w0 - w1; CIC 1 - h, h.  Each lane's stencil indices are fixed, so it
+// picks its coefficients once and evaluates three FMAs per weight.
 template <int NI>
-__device__ __forceinline__ void axis_weights(float h, float (&w)[4]) {
+__device__ __forceinline__ float4 axis_poly(int i) {
     if constexpr (NI == 4) {
-        const float h2 = h * h, a = 1.f - h;
-        w[0] = a * a * a * (1.f / 6.f);
-        w[1] = 4.f / 6.f + (0.5f * h - 1.f) * h2;
-        w[3] = h2 * h * (1.f / 6.f);
-        w[2] = 1.f - w[0] - w[1] - w[3];
+        return i == 0 ? make_float4(1.f / 6.f, -0.5f, 0.5f, -1.f / 6.f)
+             : i == 1 ? make_float4(2.f / 3.f, 0.f, -1.f, 0.5f)
+             : i == 2 ? make_float4(1.f / 6.f, 0.5f, 0.5f, -0.5f)
+                      : make_float4(0.f, 0.f, 0.f, 1.f / 6.f);
     } else if constexpr (NI == 3) {
-        w[0] = 0.5f * (0.5f - h) * (0.5f - h);
-        w[1] = 0.75f - h * h;
-        w[2] = 1.f - w[0] - w[1];
-        w[3] = 0.f;
+        return i == 0 ? make_float4(0.125f, -0.5f, 0.5f, 0.f)
+             : i == 1 ? make_float4(0.75f, 0.f, -1.f, 0.f)
+                      : make_float4(0.125f, 0.5f, 0.5f, 0.f);
     } else if constexpr (NI == 2) {
-        w[0] = 1.f - h;
-        w[1] = h;
-        w[2] = w[3] = 0.f;
+        return i == 0 ? make_float4(1.f, -1.f, 0.f, 0.f) : make_float4(0.f, 1.f, 0.f, 0.f);
     } else {
-        w[0] = 1.f;
-        w[1] = w[2] = w[3] = 0.f;
+        return make_float4(1.f, 0.f, 0.f, 0.f);
     }
 }
 
-// w[j] for a lane-dependent j in [0, NI) (selects, no local memory)
-template <int NI>
-__device__ __forceinline__ float pick(const float (&w)[4], int j) {
-    float v = w[0];
-    if (NI > 1) v = j == 1 ? w[1] : v;
-    if (NI > 2) v = j == 2 ? w[2] : v;
-    if (NI > 3) v = j == 3 ? w[3] : v;
-    return v;
+__device__ __forceinline__ float horner(float4 c, float h) { return fmaf(h, fmaf(h, fmaf(h, c.w, c.z), c.y), c.x); }
+
+// offset of a stencil's first cell from the tile origin, with the stencils that
+// wrap past the upper grid edge into tile 0 shifted down by N: the lanes'
+// cells are then d + c, inside the tile iff 0 <= d + c < 16 (N >= 32)
+__device__ __forceinline__ int tile_offset(int f, int o, int N) {
+    const int d = f - o;
+    return d >= N - 4 ? d - N : d;
 }
 
 // tiles touched along one axis by a stencil of width w starting at cell lo (mod N)
@@ -239,18 +236,22 @@ __global__ void __launch_bounds__(kThreads) owner_tile_kernel(int N, int nt, con
         __syncthreads();
         const unsigned b = start[tile], e = start[tile + 1];
         // per-lane stencil cells of one grid: NIT steps of 32 cells; the (i, j, l)
-        // of a lane are the same for every record, so they are computed once
+        // of a lane and its weight polynomials are the same for every record
         constexpr int NIT = (NC + 31) / 32;
+        // with NI^2 dividing 32 (NI = 1, 2, 4) a lane's x and y cells are the same at every step
+        constexpr bool kXYFixed = 32 % (NI * NI) == 0;
         int ci[NIT], cj[NIT], cl[NIT];
+        float4 px[NIT], py[NIT], pz[NIT];
 #pragma unroll
         for (int it = 0; it < NIT; it++) {
             const int c = it * 32 + lane;
             ci[it] = c % NI;
             cj[it] = (c / NI) % NI;
             cl[it] = c < NC ? c / (NI * NI) : -1;  // -1: no cell for this lane at this step
+            px[it] = axis_poly<NI>(ci[it]);
+            py[it] = axis_poly<NI>(cj[it]);
+            pz[it] = axis_poly<NI>(cl[it] < 0 ? 0 : cl[it]);
         }
-        // with NI^2 dividing 32 (NI = 1, 2, 4) a lane's x and y cells are the same at every step
-        constexpr bool kXYFixed = 32 % (NI * NI) == 0;
         for (unsigned k = b + warp; k < e; k += nwarps) {
             const PRec r = sorted[k];
             const float wt = wsorted ? wsorted[k] : 1.f;
@@ -260,24 +261,18 @@ __global__ void __launch_bounds__(kThreads) owner_tile_kernel(int N, int nt, con
 #pragma unroll
             for (int g = 0; g < G; g++) {
                 const unsigned pf = r.f[g];
-                const int fx = (int)(pf & 2047), fy = (int)((pf >> 11) & 2047), fz = (int)(pf >> 22);
-                float wx[4], wy[4], wz[4];
-                axis_weights<NI>(r.h[g][0], wx);
-                axis_weights<NI>(r.h[g][1], wy);
-                axis_weights<NI>(r.h[g][2], wz);
+                const int dx = tile_offset((int)(pf & 2047), ox, N), dy = tile_offset((int)((pf >> 11) & 2047), oy, N),
+                          dz = tile_offset((int)(pf >> 22), oz, N);
+                const float hx = r.h[g][0], hy = r.h[g][1], hz = r.h[g][2];
 #pragma unroll
                 for (int it = 0; it < NIT; it++) {
-                    const int ii = kXYFixed ? ci[0] : ci[it], jj = kXYFixed ? cj[0] : cj[it];
-                    int x = fx + ii, y = fy + jj, z = fz + cl[it];
-                    x -= (x >= N) ? N : 0;
-                    y -= (y >= N) ? N : 0;
-                    z -= (z >= N) ? N : 0;
-                    const int lx = x - ox, ly = y - oy, lz = z - oz;
+                    const int xi = kXYFixed ? 0 : it;  // folds to one evaluation per record when fixed
+                    const int lx = dx + ci[xi], ly = dy + cj[xi], lz = dz + cl[it];
                     ok[g][it] = cl[it] >= 0 && (unsigned)lx < (unsigned)kT && (unsigned)ly < (unsigned)kT &&
                                 (unsigned)lz < (unsigned)kT;
                     // the reference's product order: ((w_x w_y) w_z) weight; wv * 2^S is exact in
                     // FP32 (a power-of-two scale) and |wv| 2^S < 2^30, so q is one 32-bit integer
-                    const float wv = pick<NI>(wx, ii) * pick<NI>(wy, jj) * pick<NI>(wz, cl[it] < 0 ? 0 : cl[it]) * wt;
+                    const float wv = horner(px[xi], hx) * horner(py[xi], hy) * horner(pz[it], hz) * wt;
                     q[g][it] = __float2int_rn(wv * scale);
                     cell[g][it] = lz * kPz + ly * kPy + lx;
                 }

@@ -235,6 +235,7 @@ struct XArgs {
     float2 *a32;
     const int *mexp;
     long long npts;
+    float inv_nm;
 };
 
 // x pass: tile = (map m, 32 consecutive rows (z, y)).  With M = Nm / 2,
@@ -307,41 +308,43 @@ __global__ void __launch_bounds__(kThreads, PF <= 9 ? 4 : 2) map_xpass_kernel(co
         }
         __syncthreads();
         run_dit(fd, buf, ent, tw, warp, nw, lane);
-        // pairs of outputs (x[2j], x[2j+1]) at point index 2 p2 + 2j of the map's row
-        const float sc = a.oform == 1 ? exp2f((float)a.mexp[m]) : 1.f;
-        for (int l = warp; l < nrows; l += nw) {
-            const size_t p2 = ((size_t)m * a.npts + ((size_t)row0 + l) * Nm) / 2;
-            switch (a.oform) {
-                case 1:
-                    for (int j = lane; j < M; j += 32) {
-                        const float2 v = fftd::cscale(buf[j * kP + l], sc);
-                        const __half2 h = __floats2half2_rn(v.x, v.y);
-                        const float2 hb = __half22float2(h);
-                        reinterpret_cast<__half2 *>(a.bhi)[p2 + j] = h;
-                        reinterpret_cast<__half2 *>(a.blo)[p2 + j] = __floats2half2_rn(v.x - hb.x, v.y - hb.y);
-                        if (m < a.nb) a.a32[p2 + j] = v;
-                    }
-                    break;
-                case 2:
-                    for (int j = lane; j < M; j += 32) {
-                        const float2 v = buf[j * kP + l];
-                        reinterpret_cast<__nv_bfloat162 *>(a.bhi)[p2 + j] = __floats2bfloat162_rn(v.x, v.y);
-                        if (m < a.nb) a.a32[p2 + j] = v;
-                    }
-                    break;
-                case 0:
-                    for (int j = lane; j < M; j += 32) {
-                        const float2 v = buf[j * kP + l];
-                        const float2 h = make_float2(__uint_as_float(__float_as_uint(v.x) & 0xFFFFE000u),
-                                                     __uint_as_float(__float_as_uint(v.y) & 0xFFFFE000u));
-                        reinterpret_cast<float2 *>(a.bhi)[p2 + j] = h;
-                        reinterpret_cast<float2 *>(a.blo)[p2 + j] = make_float2(v.x - h.x, v.y - h.y);
-                        if (m < a.nb) a.a32[p2 + j] = v;
-                    }
-                    break;
-                default:
-                    for (int j = lane; j < M; j += 32) reinterpret_cast<float2 *>(a.out)[p2 + j] = buf[j * kP + l];
-                    break;
+        if (a.oform < 0) {
+            // dense FP32 maps: one warp per row, x[2j], x[2j+1] = z[j]
+            for (int l = warp; l < nrows; l += nw) {
+                float2 *o = reinterpret_cast<float2 *>(a.out + (size_t)m * a.npts + ((size_t)row0 + l) * Nm);
+                for (int j = lane; j < M; j += 32) o[j] = buf[j * kP + l];
+            }
+        } else {
+            // operand planes, chunk-major: the tile's rows are whole chunks of 64 points
+            // (32 Nm or 16 Nm points, Nm % 4 == 0), so a warp writes one chunk row of a
+            // plane per instruction; lane = points 2 lane, 2 lane + 1 of the chunk
+            const float sb = a.oform == 1 ? exp2f((float)a.mexp[m]) : 1.f;  // B planes: x 2^e
+            const float sa = sb * (a.oform == 1 ? 1.f / 128.f : 1.f);       // pair factors: x 2^(e-7)
+            const int nck = (nrows * Nm) >> 6;
+            const size_t c0 = ((size_t)row0 * Nm) >> 6;
+            for (int cc = warp; cc < nck; cc += nw) {
+                const int pl = cc * 64 + 2 * lane;  // point within the tile (even: both in one row)
+                int l = (int)(((float)pl + 0.5f) * a.inv_nm);
+                l -= l * Nm > pl ? 1 : 0;
+                l += (l + 1) * Nm <= pl ? 1 : 0;
+                const float2 z = buf[((pl - l * Nm) >> 1) * kP + l];
+                const size_t ck = c0 + cc;
+                const size_t ib = ((ck * a.count + m) << 5) + lane;  // pair index in the B planes
+                const float2 v = fftd::cscale(z, sb);
+                if (a.oform == 1) {
+                    const __half2 h = __floats2half2_rn(v.x, v.y);
+                    const float2 hb = __half22float2(h);
+                    reinterpret_cast<__half2 *>(a.bhi)[ib] = h;
+                    reinterpret_cast<__half2 *>(a.blo)[ib] = __floats2half2_rn(v.x - hb.x, v.y - hb.y);
+                } else if (a.oform == 2) {
+                    reinterpret_cast<__nv_bfloat162 *>(a.bhi)[ib] = __floats2bfloat162_rn(v.x, v.y);
+                } else {
+                    const float2 h = make_float2(__uint_as_float(__float_as_uint(v.x) & 0xFFFFE000u),
+                                                 __uint_as_float(__float_as_uint(v.y) & 0xFFFFE000u));
+                    reinterpret_cast<float2 *>(a.bhi)[ib] = h;
+                    reinterpret_cast<float2 *>(a.blo)[ib] = make_float2(v.x - h.x, v.y - h.y);
+                }
+                if (m < a.nb) a.a32[((ck * a.nb + m) << 5) + lane] = fftd::cscale(z, sa);
             }
         }
         m = mn;
@@ -361,9 +364,9 @@ int upload_plan(DevBuf &d, const fftd::FftPlan &p) {
     return upload(d, h.data(), h.size());
 }
 
-int grid_for(const void *kern, size_t smem, int work) {
+int grid_for(const void *kern, int threads, size_t smem, int work) {
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem) != cudaSuccess) per_sm = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem) != cudaSuccess) per_sm = 1;
     return std::max(1, std::min(work, 152 * std::max(1, per_sm)));
 }
 
@@ -473,7 +476,7 @@ int map_zpass(const Shells &sh, const MapTransform &mt, const float2 *const src[
     a.T = work;
     const size_t smem = table_smem(mt.pz.d) + sizeof(float2) * (size_t)mt.Nm * kP + sizeof(double) * 3 * mt.nb;
     PBI4G_CUDA(cudaFuncSetAttribute(map_zpass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    map_zpass_kernel<<<grid_for((const void *)map_zpass_kernel, smem, mt.nzt), kThreads, smem, st>>>(a);
+    map_zpass_kernel<<<grid_for((const void *)map_zpass_kernel, kThreads, smem, mt.nzt), kThreads, smem, st>>>(a);
     PBI4G_LAUNCH_CHECK();
     ++*launches;
     return PBI4G_OK;
@@ -493,7 +496,7 @@ int map_ypass(const MapTransform &mt, float2 *work, cudaStream_t st, int64_t *la
     a.U = work + mt.tsize;
     const size_t smem = table_smem(mt.pz.d) + sizeof(float2) * (size_t)mt.Nm * kP;
     PBI4G_CUDA(cudaFuncSetAttribute(map_ypass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    map_ypass_kernel<<<grid_for((const void *)map_ypass_kernel, smem, mt.nyt), kThreads, smem, st>>>(a);
+    map_ypass_kernel<<<grid_for((const void *)map_ypass_kernel, kThreads, smem, mt.nyt), kThreads, smem, st>>>(a);
     PBI4G_LAUNCH_CHECK();
     ++*launches;
     return PBI4G_OK;
@@ -519,6 +522,7 @@ int map_xpass(const MapTransform &mt, const float2 *work, float *out, const MapP
     a.a32 = planes ? reinterpret_cast<float2 *>(planes->a32) : nullptr;
     a.mexp = planes ? planes->mexp : nullptr;
     a.npts = (long long)mt.Nm * mt.Nm * mt.Nm;
+    a.inv_nm = 1.0f / (float)mt.Nm;
     if (planes && (planes->form < 0 || planes->form > 2 || (planes->form == 1 && !planes->mexp) ||
                    planes->npts != a.npts || planes->nmaps != mt.nmaps))
         return set_error(PBI4G_ERR_INVALID, "x pass: operand planes do not match the maps");
@@ -530,7 +534,7 @@ int map_xpass(const MapTransform &mt, const float2 *work, float *out, const MapP
     const int work_tiles = (int)ntiles;
     auto launch = [&](auto kern) -> int {
         PBI4G_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        kern<<<grid_for((const void *)kern, smem, work_tiles), kThreads, smem, st>>>(a);
+        kern<<<grid_for((const void *)kern, kThreads, smem, work_tiles), kThreads, smem, st>>>(a);
         PBI4G_LAUNCH_CHECK();
         return PBI4G_OK;
     };

@@ -32,15 +32,20 @@ struct MapInfo {
 };
 
 // Tensor-core operands of the maps ("planes"), written by the x pass for the
-// tensor-core forms; every array is [map][point], point = (z Nm + y) Nm + x:
+// tensor-core forms.  Points are grouped in chunks of 64 consecutive points
+// (point = (z Nm + y) Nm + x; Nm^3 is a multiple of 64), and every array is
+// chunk-major, [chunk][map][64 points], so the operand tile of a chunk (64 maps
+// x 64 points) is one contiguous block:
 //   form 1 (FP16 hi+lo): bhi, blo FP16 with v 2^mexp[m] = hi + lo (|v 2^mexp| <= 2^14);
 //   form 2 (BF16):       bhi BF16 of v;
 //   form 0 (TF32 hi+lo): bhi FP32 = v with the 13 low mantissa bits cleared, blo = v - bhi;
-// and a32 = the set-0 maps (m < nb) in FP32, times 2^mexp[m] for form 1 (the
-// pair factors the tensor-core kernel multiplies).
+// and a32 [chunk][nb][64] = the set-0 maps in FP32, times 2^(mexp[m] - 7) for
+// form 1 (the pair factors: their products are the A operand, |A| <= 2^14, with
+// no further scaling).
 struct MapPlanes {
+    static constexpr int kChunk = 64;
     int form = -1;
-    long long npts = 0;
+    long long npts = 0, nchunks = 0;
     int nmaps = 0, nb = 0;
     void *bhi = nullptr, *blo = nullptr;
     float *a32 = nullptr;
@@ -52,6 +57,7 @@ struct MapPlanes {
     void carve(int form_, long long npts_, int nmaps_, int nb_, void *base, const int *mexp_) {
         form = form_;
         npts = npts_;
+        nchunks = npts / kChunk;
         nmaps = nmaps_;
         nb = nb_;
         mexp = mexp_;

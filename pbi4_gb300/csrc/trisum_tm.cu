@@ -26,7 +26,7 @@
 //   * a TMA warp loads each chunk's B tile(s) (64 maps x 64 points, 128-byte
 //     swizzled: the K-major operand layout itself) and the FP32 set-0 maps of
 //     the chunk into a ring of shared-memory stages;
-//   * three producer warpgroups take the chunks in turn (thread = TMEM lane =
+//   * two producer warpgroups take the chunks in turn (thread = TMEM lane =
 //     pair row): they form the 64 products of their pair, split them and store
 //     them straight into a tensor-memory A stage with tcgen05.st (the A operand
 //     never touches shared memory);
@@ -69,13 +69,15 @@ constexpr int kKB = 32;          // FP32 values per 128-byte swizzle row (one K 
 constexpr int kBlocks = 2;       // K blocks per chunk
 constexpr int kKC = kKB * kBlocks;  // grid points per chunk
 constexpr int kMaxStages = 10;   // TMA staging slots (released by the producers and the MMAs)
-constexpr int kGroups = 3;       // producer warpgroups, chunks assigned round robin
+constexpr int kGroups = 2;       // producer warpgroups, chunks assigned round robin
 constexpr int kProdWarps = 4 * kGroups;
 constexpr int kDrainWarps = 8;   // two warpgroups, 32 accumulator columns each
 constexpr int kMmaWarp = kProdWarps + kDrainWarps;
-constexpr int kTmaWarp = kMmaWarp + 1;
-constexpr int kThreads = (kTmaWarp + 1) * 32;  // 704
+constexpr int kMmaWarps = 2;     // MMA issuers, chunks alternating (a thread's MMAs of a chunk stay in order)
+constexpr int kTmaWarp = kMmaWarp + kMmaWarps;
+constexpr int kThreads = (kTmaWarp + 1) * 32;  // 608
 constexpr int kFold = 16;        // chunks summed in registers before a Kahan fold
+constexpr int kFoldGroup = 8;    // scratch values a drain thread folds per batch of loads
 constexpr int kAcc = 4;          // TMEM accumulators (one chunk each)
 constexpr int kDone = 16;        // per-chunk MMA completion barriers (ring)
 constexpr uint32_t kColAcc = 0;  // kAcc accumulators of kN columns, then the A stages
@@ -149,11 +151,11 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
                  : "memory");
 }
 
-__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *tm, int x, int y, uint64_t *bar) {
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *tm, int x, int y, int z, uint64_t *bar) {
     asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
-        "[%4];" ::"r"(smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
         : "memory");
 }
 
@@ -173,19 +175,35 @@ __device__ __forceinline__ bool warp_wait(uint64_t *bar, uint32_t parity, volati
 }
 
 // Barrier parity of the completion, for chunk i, of a barrier used every `every` chunks.
-__device__ __forceinline__ uint32_t ph(long long i, int every) { return (uint32_t)((i / every) & 1); }
+__device__ __forceinline__ uint32_t ph(int i, int every) { return (uint32_t)((i / every) & 1); }
 
-// two FP32 values -> packed 16-bit hi (and lo = v - hi for the split forms)
+// Slot and phase of a ring of `size` barriers, advanced by additions: the roles'
+// loops run on a single thread or warp per chunk, where a division by the
+// runtime stage count is a long dependent chain.
+struct Ring {
+    int idx, phase;
+    __device__ __forceinline__ Ring(int start, int size) : idx(start % size), phase((start / size) & 1) {}
+    __device__ __forceinline__ void step(int k, int size) {  // k <= size
+        idx += k;
+        if (idx >= size) {
+            idx -= size;
+            phase ^= 1;
+        }
+    }
+};
+
+// two products u0 v0, u1 v1 -> packed 16-bit hi, and for the FP16 split lo =
+// u v - hi (the FMA keeps the product's own rounding error out of lo)
 template <int F>
-__device__ __forceinline__ void pack2(float x, float y, uint32_t &hi, uint32_t &lo) {
+__device__ __forceinline__ void pack_prod2(float u0, float v0, float u1, float v1, uint32_t &hi, uint32_t &lo) {
     if constexpr (F == kFormF16) {
-        const __half2 h = __floats2half2_rn(x, y);
+        const __half2 h = __floats2half2_rn(u0 * v0, u1 * v1);
         const float2 back = __half22float2(h);
-        const __half2 l = __floats2half2_rn(x - back.x, y - back.y);
+        const __half2 l = __floats2half2_rn(fmaf(u0, v0, -back.x), fmaf(u1, v1, -back.y));
         hi = *reinterpret_cast<const uint32_t *>(&h);
         lo = *reinterpret_cast<const uint32_t *>(&l);
     } else {
-        const __nv_bfloat162 h = __floats2bfloat162_rn(x, y);
+        const __nv_bfloat162 h = __floats2bfloat162_rn(u0 * v0, u1 * v1);
         hi = *reinterpret_cast<const uint32_t *>(&h);
         lo = 0u;
     }
@@ -195,7 +213,6 @@ struct TmArgs {
     long long nchunks;     // points / kKC, rounded up
     int nunits, ksplit, nslots, nA, nstages, nmaps;
     uint32_t stage_bytes, ablock;
-    float apre;            // factor of every pair product: 2^-14 for the FP16 form (maps stored x 2^e), else 1
     float *kahan;          // [grid][2][kN][kM] running sum and compensation of each CTA (L2-resident)
     const int2 *units;     // (M tile, N tile) per unit
     const int2 *prow;      // [nunits][kM] staged rows (i, j) of each pair's factors, (-1, -1) for none
@@ -233,7 +250,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int2 U = a.units[unit];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const long long cb = a.nchunks * split / a.ksplit, ce = a.nchunks * (split + 1) / a.ksplit;
-    const long long n = ce - cb;
+    const int n = (int)(ce - cb);
 
     for (int r = tid; r < kM; r += kThreads) prow_s[r] = a.prow[(size_t)unit * kM + r];
     for (int r = tid; r < kN; r += kThreads) {
@@ -272,11 +289,11 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int quad = warp & 3, grp = warp >> 2;
         const int row = quad * 32 + lane;
         const int2 pr = prow_s[row];
-        const float pscale = a.apre;
         const uint32_t lane_addr = tmem + ((uint32_t)(quad * 32) << 16);
-        for (long long i = grp; i < n; i += kGroups) {
-            const int s = (int)(i % nst), as = (int)(i % AST);
-            if (!warp_wait(&full[s], ph(i, nst), abort_flag)) { fail(); break; }
+        Ring rs(grp, nst);  // stage and full-barrier phase of chunk i
+        for (int i = grp; i < n; i += kGroups, rs.step(kGroups, nst)) {
+            const int s = rs.idx, as = i % AST;
+            if (!warp_wait(&full[s], (uint32_t)rs.phase, abort_flag)) { fail(); break; }
             // the A stage is free once the MMAs of chunk i - AST completed (MMAs complete in order)
             if (i >= AST && !warp_wait(&done[(i - AST) % kDone], ph(i - AST, kDone), abort_flag)) {
                 fail();
@@ -325,8 +342,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                                 *reinterpret_cast<const float4 *>(blk + pr.x * 128 + ((c ^ (pr.x & 7)) << 4));
                             const float4 v =
                                 *reinterpret_cast<const float4 *>(blk + pr.y * 128 + ((c ^ (pr.y & 7)) << 4));
-                            pack2<F>(u.x * v.x * pscale, u.y * v.y * pscale, hi[2 * c], lo[2 * c]);
-                            pack2<F>(u.z * v.z * pscale, u.w * v.w * pscale, hi[2 * c + 1], lo[2 * c + 1]);
+                            pack_prod2<F>(u.x, v.x, u.y, v.y, hi[2 * c], lo[2 * c]);
+                            pack_prod2<F>(u.z, v.z, u.w, v.w, hi[2 * c + 1], lo[2 * c + 1]);
                         }
                     } else {
 #pragma unroll
@@ -358,8 +375,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             comp_g[(c0 + e) * kM + row] = 0.f;
         }
         bool ok = true;
-        for (long long i = 0; i < n; i++) {
-            const int b = (int)(i % kAcc);
+        for (int i = 0; i < n; i++) {
+            const int b = i % kAcc;
             if (!warp_wait(&done[i % kDone], ph(i, kDone), abort_flag)) { fail(); ok = false; break; }
             tc_fence_after();
 #pragma unroll
@@ -376,15 +393,15 @@ __global__ void __launch_bounds__(kThreads, 1)
                 // each group's scratch loads are issued before its first store, so the
                 // fold costs a few L2 round trips
 #pragma unroll
-                for (int h = 0; h < 32; h += 8) {
-                    float rv[8], cv[8];
+                for (int h = 0; h < 32; h += kFoldGroup) {
+                    float rv[kFoldGroup], cv[kFoldGroup];
 #pragma unroll
-                    for (int e = 0; e < 8; e++) {
+                    for (int e = 0; e < kFoldGroup; e++) {
                         rv[e] = __ldcg(run_g + (c0 + h + e) * kM + row);
                         cv[e] = __ldcg(comp_g + (c0 + h + e) * kM + row);
                     }
 #pragma unroll
-                    for (int e = 0; e < 8; e++) {
+                    for (int e = 0; e < kFoldGroup; e++) {
                         const float y = mid[h + e] - cv[e];
                         const float t2 = rv[e] + y;
                         cv[e] = (t2 - rv[e]) - y;
@@ -392,7 +409,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                         mid[h + e] = 0.f;
                     }
 #pragma unroll
-                    for (int e = 0; e < 8; e++) {
+                    for (int e = 0; e < kFoldGroup; e++) {
                         __stcg(run_g + (c0 + h + e) * kM + row, rv[e]);
                         __stcg(comp_g + (c0 + h + e) * kM + row, cv[e]);
                     }
@@ -411,40 +428,46 @@ __global__ void __launch_bounds__(kThreads, 1)
                 a.partial[(size_t)split * a.nslots + slot] = F == kFormF16 ? ldexp(v, -(pe + qexp_s[c0 + e])) : v;
             }
         }
-    } else if (warp == kMmaWarp) {
-        // --------------------------------------------------------- MMA issue (one thread)
+    } else if (warp < kTmaWarp) {
+        // ------------------------------------------ MMA issue (one thread per MMA warp)
+        // issuer w takes chunks w, w + kMmaWarps, ...: each chunk has its own
+        // accumulator, A stage and completion barrier, and tcgen05.commit tracks the
+        // issuing thread's own MMAs, so the two streams need no ordering between them
         if (lane == 0) {
-            long long last_commit = -1;
+            const int mw = warp - kMmaWarp;
+            int last_commit = -1;
             bool ok = true;
-            for (long long i = 0; i < n; i++) {
-                const int b = (int)(i % kAcc), as = (int)(i % AST), s = (int)(i % nst);
+            Ring rs(mw, nst);
+            for (int i = mw; i < n; i += kMmaWarps, rs.step(kMmaWarps, nst)) {
+                const int b = i % kAcc, as = i % AST, s = rs.idx;
                 if (i >= kAcc && !wait_or_abort(&accfree[b], ph(i - kAcc, kAcc), abort_flag)) { ok = false; break; }
-                if (!wait_or_abort(&full[s], ph(i, nst), abort_flag)) { ok = false; break; }  // B tiles
+                if (!wait_or_abort(&full[s], (uint32_t)rs.phase, abort_flag)) { ok = false; break; }  // B tiles
                 if (!wait_or_abort(&prod[as], ph(i, AST), abort_flag)) { ok = false; break; }  // A stage
                 tc_fence_after();
-                const uint32_t b0 = smem_u32(stage_ptr(s)) + kBlocks * a.ablock;
+                // descriptors advance by 16-byte units within the stage (no carry out of the address field)
+                const uint64_t db = sw128_desc(smem_u32(stage_ptr(s)) + kBlocks * a.ablock);
                 const uint32_t ahi = tmem + kColA + (uint32_t)as * FM::kACols;
                 const uint32_t d = tmem + kColAcc + (uint32_t)b * kN;
 #pragma unroll
                 for (int kk = 0; kk < kKC / FM::kKStep; kk++) {
-                    uint32_t bh, bl, a_hi, a_lo;
+                    uint64_t dh, dl;
+                    uint32_t a_hi, a_lo;
                     if constexpr (F == kFormTF32) {
                         // FP32 rows: K-step of 8 = 32 bytes; tiles hi0, hi1, lo0, lo1
-                        bh = b0 + (uint32_t)(kk / 4) * kBTile + (uint32_t)(kk % 4) * 32;
-                        bl = bh + 2 * kBTile;
+                        dh = db + (((uint32_t)(kk / 4) * kBTile + (uint32_t)(kk % 4) * 32) >> 4);
+                        dl = dh + ((2 * kBTile) >> 4);
                         a_hi = ahi + 8 * kk;
                         a_lo = a_hi + kKC;
                     } else {
                         // 16-bit rows: K-step of 16 = 32 bytes; tiles hi, lo
-                        bh = b0 + (uint32_t)kk * 32;
-                        bl = bh + kBTile;
+                        dh = db + (uint32_t)kk * 2;
+                        dl = dh + (kBTile >> 4);
                         a_hi = ahi + 8 * kk;
                         a_lo = a_hi + kKC / 2;
                     }
-                    const uint64_t dh = sw128_desc(bh);
                     umma_ta<F>(d, a_hi, dh, kk == 0 ? 0u : 1u);
                     if (FM::kSplit) {
-                        umma_ta<F>(d, a_hi, sw128_desc(bl), 1u);
+                        umma_ta<F>(d, a_hi, dl, 1u);
                         umma_ta<F>(d, a_lo, dh, 1u);
                     }
                 }
@@ -452,20 +475,22 @@ __global__ void __launch_bounds__(kThreads, 1)
                 last_commit = i;
             }
             if (!ok) fail();
-            // the MMAs still in flight (and their barrier arrival) land before TMEM goes away
+            // this thread's MMAs still in flight (and their barrier arrival) land before TMEM goes away
             if (last_commit >= 0) mbar_wait(&done[last_commit % kDone], ph(last_commit, kDone));
         }
     } else if (lane == 0) {
         // --------------------------------------------------------- TMA issue (one thread)
         const uint32_t tx = kBlocks * (uint32_t)a.nA * 128 + FM::kBTiles * kBTile;
         const int q0 = U.y * kN;
-        long long issued = 0;
+        int issued = 0;
         bool ok = true;
-        for (long long j = 0; j < n; j++) {
-            const int s = (int)(j % nst);
+        Ring rs(0, nst);
+        for (int j = 0; j < n; j++, rs.step(1, nst)) {
+            const int s = rs.idx;
             // stage s is free once the producers took the pair factors of chunk j - nst
-            // and the MMAs of that chunk (which read its B tiles) completed
-            if (j >= nst && (!wait_or_abort(&sfree[s], ph(j - nst, nst), abort_flag) ||
+            // (the ring's previous phase) and the MMAs of that chunk (which read its B
+            // tiles) completed
+            if (j >= nst && (!wait_or_abort(&sfree[s], (uint32_t)(rs.phase ^ 1), abort_flag) ||
                              !wait_or_abort(&done[(j - nst) % kDone], ph(j - nst, kDone), abort_flag))) {
                 ok = false;
                 break;
@@ -473,26 +498,25 @@ __global__ void __launch_bounds__(kThreads, 1)
             unsigned char *stg = stage_ptr(s);
             unsigned char *bt = stg + kBlocks * a.ablock;
             mbar_expect_tx(&full[s], tx);
-            const int x0 = (int)((cb + j) * kKC);  // first point of the chunk (past the end: zero fill)
+            const int c = (int)(cb + j);  // chunk: 64 consecutive points, one block of every plane
 #pragma unroll
-            for (int kb = 0; kb < kBlocks; kb++) tma_load_2d(stg + kb * a.ablock, &tmA, x0 + kb * kKB, 0, &full[s]);
+            for (int kb = 0; kb < kBlocks; kb++) tma_load_3d(stg + kb * a.ablock, &tmA, kb * kKB, 0, c, &full[s]);
             if constexpr (F == kFormTF32) {
 #pragma unroll
                 for (int kb = 0; kb < kBlocks; kb++) {
-                    tma_load_2d(bt + kb * kBTile, &tmBh, x0 + kb * kKB, q0, &full[s]);
-                    tma_load_2d(bt + (2 + kb) * kBTile, &tmBl, x0 + kb * kKB, q0, &full[s]);
+                    tma_load_3d(bt + kb * kBTile, &tmBh, kb * kKB, q0, c, &full[s]);
+                    tma_load_3d(bt + (2 + kb) * kBTile, &tmBl, kb * kKB, q0, c, &full[s]);
                 }
             } else {
-                tma_load_2d(bt, &tmBh, x0, q0, &full[s]);
-                if (FM::kSplit) tma_load_2d(bt + kBTile, &tmBl, x0, q0, &full[s]);
+                tma_load_3d(bt, &tmBh, 0, q0, c, &full[s]);
+                if (FM::kSplit) tma_load_3d(bt + kBTile, &tmBl, 0, q0, c, &full[s]);
             }
             issued = j + 1;
         }
         if (!ok) {
             fail();
             // copies in flight land (bounded) before the shared memory goes away
-            for (long long j = std::max(0LL, issued - nst); j < issued; j++)
-                mbar_wait(&full[j % nst], ph(j, nst));
+            for (int j = std::max(0, issued - nst); j < issued; j++) mbar_wait(&full[j % nst], ph(j, nst));
         }
     }
     tc_fence_before();
@@ -539,21 +563,21 @@ EncodeTiledFn encode_fn() {
     return fn;
 }
 
-// 2D view of an operand plane array [rows][npts] (element size esize): box
-// box_pts x box_rows at (first point, first row), 128-byte swizzle (box_pts
-// esize = 128 bytes: the K-major operand layout), zero fill past the last
-// point and the last row.
-int make_plane_view(CUtensorMap *tm, const void *base, CUtensorMapDataType dt, int esize, long long npts, int rows,
-                    int box_pts, int box_rows) {
+// 3D view of a chunk-major operand array [nchunks][rows][64 points] (element
+// size esize): box box_pts x box_rows x 1 at (point within the chunk, first
+// row, chunk), 128-byte swizzle (box_pts esize = 128 bytes: the K-major operand
+// layout), zero fill past the last row.
+int make_chunk_view(CUtensorMap *tm, const void *base, CUtensorMapDataType dt, int esize, long long nchunks,
+                    int rows, int box_pts, int box_rows) {
     EncodeTiledFn enc = encode_fn();
     if (!enc) return set_error(PBI4G_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
-    if (box_pts * esize != 128 || reinterpret_cast<uintptr_t>(base) % 16 || (npts * esize) % 16)
-        return set_error(PBI4G_ERR_INVALID, "operand plane view: alignment");
-    const cuuint64_t gdim[2] = {(cuuint64_t)npts, (cuuint64_t)rows};
-    const cuuint64_t gstride[1] = {(cuuint64_t)npts * esize};
-    const cuuint32_t box[2] = {(cuuint32_t)box_pts, (cuuint32_t)box_rows};
-    const cuuint32_t estr[2] = {1, 1};
-    const CUresult r = enc(tm, dt, 2, const_cast<void *>(base), gdim, gstride, box, estr,
+    if (box_pts * esize != 128 || reinterpret_cast<uintptr_t>(base) % 16)
+        return set_error(PBI4G_ERR_INVALID, "operand chunk view: alignment");
+    const cuuint64_t gdim[3] = {(cuuint64_t)MapPlanes::kChunk, (cuuint64_t)rows, (cuuint64_t)nchunks};
+    const cuuint64_t gstride[2] = {(cuuint64_t)MapPlanes::kChunk * esize, (cuuint64_t)rows * MapPlanes::kChunk * esize};
+    const cuuint32_t box[3] = {(cuuint32_t)box_pts, (cuuint32_t)box_rows, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    const CUresult r = enc(tm, dt, 3, const_cast<void *>(base), gdim, gstride, box, estr,
                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return set_error(PBI4G_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
@@ -661,29 +685,30 @@ int triangle_sums_tm(const Shells &sh, TmPlan &tp, const MapPlanes &pl, DevBuf &
     if (tp.nunits == 0) return PBI4G_OK;
     if (form == 1 && (!pl.mexp || pl.mexp != tp.mexp.as<int>()))
         return set_error(PBI4G_ERR_INVALID, "tensor-core triangle sums: FP16 planes without the plan's exponents");
-    if (pl.nb != sh.nb || pl.npts != (long long)sh.Nm * sh.Nm * sh.Nm)
+    if (pl.nb != sh.nb || pl.npts != (long long)sh.Nm * sh.Nm * sh.Nm || pl.nchunks * kKC != pl.npts)
         return set_error(PBI4G_ERR_INVALID, "tensor-core triangle sums: operand planes do not match the shells");
+    static_assert(MapPlanes::kChunk == kKC, "a planes chunk is a contraction chunk");
     CUtensorMap tmA, tmBh, tmBl;
-    PBI4G_CHECK(make_plane_view(&tmA, pl.a32, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pl.npts, sh.nb, kKB, tp.nA));
+    const long long nc = pl.nchunks;
+    PBI4G_CHECK(make_chunk_view(&tmA, pl.a32, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, nc, sh.nb, kKB, tp.nA));
     if (form == 0) {
-        PBI4G_CHECK(make_plane_view(&tmBh, pl.bhi, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pl.npts, pl.nmaps, kKB, kN));
-        PBI4G_CHECK(make_plane_view(&tmBl, pl.blo, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pl.npts, pl.nmaps, kKB, kN));
+        PBI4G_CHECK(make_chunk_view(&tmBh, pl.bhi, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, nc, pl.nmaps, kKB, kN));
+        PBI4G_CHECK(make_chunk_view(&tmBl, pl.blo, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, nc, pl.nmaps, kKB, kN));
     } else if (form == 1) {
-        PBI4G_CHECK(make_plane_view(&tmBh, pl.bhi, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, pl.npts, pl.nmaps, kKC, kN));
-        PBI4G_CHECK(make_plane_view(&tmBl, pl.blo, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, pl.npts, pl.nmaps, kKC, kN));
+        PBI4G_CHECK(make_chunk_view(&tmBh, pl.bhi, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, nc, pl.nmaps, kKC, kN));
+        PBI4G_CHECK(make_chunk_view(&tmBl, pl.blo, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, nc, pl.nmaps, kKC, kN));
     } else {
-        PBI4G_CHECK(make_plane_view(&tmBh, pl.bhi, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, pl.npts, pl.nmaps, kKC, kN));
+        PBI4G_CHECK(make_chunk_view(&tmBh, pl.bhi, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, nc, pl.nmaps, kKC, kN));
         tmBl = tmBh;  // unused: one product
     }
     TmArgs a;
-    a.nchunks = (pl.npts + kKC - 1) / kKC;
+    a.nchunks = nc;
     a.nunits = tp.nunits;
     a.ksplit = std::max(1, 152 / tp.nunits);
     a.ksplit = (int)std::min<long long>(a.ksplit, std::max<long long>(1, a.nchunks / 128));
     a.nslots = tp.nslots;
     a.nA = tp.nA;
     a.nmaps = pl.nmaps;
-    a.apre = form == 1 ? ldexpf(1.0f, -14) : 1.0f;
     a.ablock = (uint32_t)(((tp.nA + 7) / 8) * 8 * 128);
     const int btiles = form == 0 ? Form<kFormTF32>::kBTiles : (form == 1 ? Form<kFormF16>::kBTiles : 1);
     a.stage_bytes = kBlocks * a.ablock + (uint32_t)btiles * kBTile;
