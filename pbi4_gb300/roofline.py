@@ -40,7 +40,8 @@ def peaks():
 
 
 def traffic_table():
-    """Per-launch DRAM bytes of each stage from the committed ncu summary, if present."""
+    """Per-launch DRAM bytes of each stage from the committed ncu summary, if present,
+    keyed by "grid<N>_<precision>" of the workload it was measured (and scaled) for."""
     p = os.path.join(ROOT, "profiles", "dram_bytes.json")
     try:
         with open(p) as f:
@@ -107,7 +108,7 @@ def for_stages(stages, steps, cfg, npart, itot=None, map_grid=None, nmaps=None, 
     if itot and cfg.precision in ("fp16split", "bf16", "tf32split"):
         nsets = 3 if cfg.multipoles else 1
         work["triangle_sums"] = ("tensor", 2.0 * int(map_grid or cfg.grid) ** 3 * itot * nsets)
-    table = traffic_table()
+    table = traffic_table().get("grid%d_%s" % (int(cfg.grid), cfg.precision), {})
     out = []
     for name, (bound, amount) in work.items():
         ms, calls = stages.get(name, (0.0, 0))
