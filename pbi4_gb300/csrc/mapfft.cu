@@ -316,35 +316,52 @@ __global__ void __launch_bounds__(kThreads, PF <= 9 ? 4 : 2) map_xpass_kernel(co
             }
         } else {
             // operand planes, chunk-major: the tile's rows are whole chunks of 64 points
-            // (32 Nm or 16 Nm points, Nm % 4 == 0), so a warp writes one chunk row of a
-            // plane per instruction; lane = points 2 lane, 2 lane + 1 of the chunk
+            // (32 Nm or 16 Nm points, Nm % 4 == 0), so a warp writes two chunk rows of a
+            // plane per instruction
             const float sb = a.oform == 1 ? exp2f((float)a.mexp[m]) : 1.f;  // B planes: x 2^e
             const float sa = sb * (a.oform == 1 ? 1.f / 128.f : 1.f);       // pair factors: x 2^(e-7)
-            const int nck = (nrows * Nm) >> 6;
+            const int npt = nrows * Nm;
             const size_t c0 = ((size_t)row0 * Nm) >> 6;
-            for (int cc = warp; cc < nck; cc += nw) {
-                const int pl = cc * 64 + 2 * lane;  // point within the tile (even: both in one row)
+            // a lane takes 4 consecutive points (one row: Nm % 4 == 0), 16 lanes a chunk row
+            for (int pl = 128 * warp + 4 * lane; pl < npt; pl += 128 * nw) {
                 int l = (int)(((float)pl + 0.5f) * a.inv_nm);
                 l -= l * Nm > pl ? 1 : 0;
                 l += (l + 1) * Nm <= pl ? 1 : 0;
-                const float2 z = buf[((pl - l * Nm) >> 1) * kP + l];
-                const size_t ck = c0 + cc;
-                const size_t ib = ((ck * a.count + m) << 5) + lane;  // pair index in the B planes
-                const float2 v = fftd::cscale(z, sb);
+                const int j = (pl - l * Nm) >> 1;
+                const float2 z0 = buf[j * kP + l], z1 = buf[(j + 1) * kP + l];
+                const size_t ck = c0 + (pl >> 6), t = pl & 63;
+                const size_t ib = (ck * a.count + m) * 64 + t;  // element index in the B planes
+                const float2 v0 = fftd::cscale(z0, sb), v1 = fftd::cscale(z1, sb);
                 if (a.oform == 1) {
-                    const __half2 h = __floats2half2_rn(v.x, v.y);
-                    const float2 hb = __half22float2(h);
-                    reinterpret_cast<__half2 *>(a.bhi)[ib] = h;
-                    reinterpret_cast<__half2 *>(a.blo)[ib] = __floats2half2_rn(v.x - hb.x, v.y - hb.y);
+                    const __half2 h0 = __floats2half2_rn(v0.x, v0.y), h1 = __floats2half2_rn(v1.x, v1.y);
+                    const float2 b0 = __half22float2(h0), b1 = __half22float2(h1);
+                    const __half2 g0 = __floats2half2_rn(v0.x - b0.x, v0.y - b0.y);
+                    const __half2 g1 = __floats2half2_rn(v1.x - b1.x, v1.y - b1.y);
+                    uint2 hw, lw;
+                    hw.x = *reinterpret_cast<const unsigned *>(&h0);
+                    hw.y = *reinterpret_cast<const unsigned *>(&h1);
+                    lw.x = *reinterpret_cast<const unsigned *>(&g0);
+                    lw.y = *reinterpret_cast<const unsigned *>(&g1);
+                    *reinterpret_cast<uint2 *>(reinterpret_cast<__half *>(a.bhi) + ib) = hw;
+                    *reinterpret_cast<uint2 *>(reinterpret_cast<__half *>(a.blo) + ib) = lw;
                 } else if (a.oform == 2) {
-                    reinterpret_cast<__nv_bfloat162 *>(a.bhi)[ib] = __floats2bfloat162_rn(v.x, v.y);
+                    const __nv_bfloat162 h0 = __floats2bfloat162_rn(v0.x, v0.y), h1 = __floats2bfloat162_rn(v1.x, v1.y);
+                    uint2 hw;
+                    hw.x = *reinterpret_cast<const unsigned *>(&h0);
+                    hw.y = *reinterpret_cast<const unsigned *>(&h1);
+                    *reinterpret_cast<uint2 *>(reinterpret_cast<__nv_bfloat16 *>(a.bhi) + ib) = hw;
                 } else {
-                    const float2 h = make_float2(__uint_as_float(__float_as_uint(v.x) & 0xFFFFE000u),
-                                                 __uint_as_float(__float_as_uint(v.y) & 0xFFFFE000u));
-                    reinterpret_cast<float2 *>(a.bhi)[ib] = h;
-                    reinterpret_cast<float2 *>(a.blo)[ib] = make_float2(v.x - h.x, v.y - h.y);
+                    const float4 h = make_float4(__uint_as_float(__float_as_uint(v0.x) & 0xFFFFE000u),
+                                                 __uint_as_float(__float_as_uint(v0.y) & 0xFFFFE000u),
+                                                 __uint_as_float(__float_as_uint(v1.x) & 0xFFFFE000u),
+                                                 __uint_as_float(__float_as_uint(v1.y) & 0xFFFFE000u));
+                    *reinterpret_cast<float4 *>(reinterpret_cast<float *>(a.bhi) + ib) = h;
+                    *reinterpret_cast<float4 *>(reinterpret_cast<float *>(a.blo) + ib) =
+                        make_float4(v0.x - h.x, v0.y - h.y, v1.x - h.z, v1.y - h.w);
                 }
-                if (m < a.nb) a.a32[((ck * a.nb + m) << 5) + lane] = fftd::cscale(z, sa);
+                if (m < a.nb)
+                    *reinterpret_cast<float4 *>(reinterpret_cast<float *>(a.a32) + (ck * a.nb + m) * 64 + t) =
+                        make_float4(z0.x * sa, z0.y * sa, z1.x * sa, z1.y * sa);
             }
         }
         m = mn;

@@ -357,35 +357,59 @@ __global__ void pk_accum_kernel(int N, int nbins, const int *__restrict__ lut, P
     for (int i = threadIdx.x; i < nq * nbins; i += blockDim.x) s[i] = 0;
     __syncthreads();
     const int NH = N / 2 + 1;
-    const size_t HC = (size_t)N * N * NH;
-    for (size_t cell = blockIdx.x * (size_t)blockDim.x + threadIdx.x; cell < HC;
-         cell += (size_t)gridDim.x * blockDim.x) {
-        const int x = (int)(cell % NH), ky = kfreq0((int)((cell / NH) % N), N),
-                  kz = kfreq0((int)(cell / ((size_t)NH * N)), N);
-        if (!pk_keep(x, ky, kz)) continue;
-        const int k2 = x * x + ky * ky + kz * kz;
-        int bin = lut[k2];
-        if (bin < 0) bin = pk_bin_exact(e, x, ky, kz);
-        if (bin < 1 || bin > nbins) continue;
-        const typename Cx<R>::T va = a[cell];
-        if (MODE == 0) {
-            const typename Cx<R>::T vb = b[cell];
-            atomicAdd(&s[bin - 1], (A)(va.x * vb.x + va.y * vb.y));
-        } else if (MODE == 1) {
-            const A p = (A)(va.x * va.x + va.y * va.y);
-            const A lk = (A)(l0 * x + l1 * ky + l2 * kz);
-            const A mu2 = lk * lk / (A)k2;
-            const A L2 = (A)-0.5 + (A)1.5 * mu2;
-            const A L4 = (A)0.375 + mu2 * ((A)-3.75 + (A)4.375 * mu2);
-            atomicAdd(&s[bin - 1], p);
-            atomicAdd(&s[nbins + bin - 1], p * L2);
-            atomicAdd(&s[2 * nbins + bin - 1], p * L4);
-        } else {
-            const typename Cx<R>::T vb = b[cell], vc = c[cell];
-            atomicAdd(&s[bin - 1], (A)(va.x * va.x + va.y * va.y));
-            atomicAdd(&s[nbins + bin - 1], (A)(va.x * vb.x + va.y * vb.y));
-            atomicAdd(&s[2 * nbins + bin - 1], (A)(va.x * vc.x + va.y * vc.y));
+    const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+    const int nwarps = gridDim.x * wpb;
+    const A lf0 = (A)l0, lf1 = (A)l1, lf2 = (A)l2;
+    // one warp per (y, z) row; a lane takes 4 consecutive x, along which |k| and so
+    // the bin never decrease: the sums stay in registers until the bin changes
+    for (int row = blockIdx.x * wpb + (threadIdx.x >> 5); row < N * N; row += nwarps) {
+        const int ky = kfreq0(row % N, N), kz = kfreq0(row / N, N);
+        const int r2 = ky * ky + kz * kz;
+        const size_t off = (size_t)row * NH;
+        int cur = 0;
+        A s0 = 0, s1 = 0, s2 = 0;
+        auto flush = [&]() {
+            if (cur < 1) return;
+            atomicAdd(&s[cur - 1], s0);
+            if (MODE != 0) {
+                atomicAdd(&s[nbins + cur - 1], s1);
+                atomicAdd(&s[2 * nbins + cur - 1], s2);
+            }
+        };
+        for (int x0 = 4 * lane; x0 < NH; x0 += 128) {
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+                const int x = x0 + t;
+                if (x >= NH || !pk_keep(x, ky, kz)) continue;
+                const int k2 = x * x + r2;
+                int bin = lut[k2];
+                if (bin < 0) bin = pk_bin_exact(e, x, ky, kz);
+                if (bin < 1 || bin > nbins) continue;
+                if (bin != cur) {
+                    flush();
+                    cur = bin;
+                    s0 = s1 = s2 = 0;
+                }
+                const typename Cx<R>::T va = a[off + x];
+                if (MODE == 0) {
+                    const typename Cx<R>::T vb = b[off + x];
+                    s0 += (A)(va.x * vb.x + va.y * vb.y);
+                } else if (MODE == 1) {
+                    const A p = (A)(va.x * va.x + va.y * va.y);
+                    const A lk = lf0 * (A)x + lf1 * (A)ky + lf2 * (A)kz;
+                    const A mu2 = lk * lk / (A)k2;
+                    s0 += p;
+                    s1 += p * ((A)-0.5 + (A)1.5 * mu2);
+                    s2 += p * ((A)0.375 + mu2 * ((A)-3.75 + (A)4.375 * mu2));
+                } else {
+                    const typename Cx<R>::T vb = b[off + x], vc = c[off + x];
+                    s0 += (A)(va.x * va.x + va.y * va.y);
+                    s1 += (A)(va.x * vb.x + va.y * vb.y);
+                    s2 += (A)(va.x * vc.x + va.y * vc.y);
+                }
+            }
         }
+        flush();
     }
     __syncthreads();
     double *out = partial + (size_t)blockIdx.x * 3 * nbins;
