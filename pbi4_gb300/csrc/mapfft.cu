@@ -238,6 +238,79 @@ struct XArgs {
     float inv_nm;
 };
 
+template <int P>
+__device__ __forceinline__ void store_words(void *dst, const unsigned (&w)[P]) {
+    if constexpr (P == 2) *reinterpret_cast<uint2 *>(dst) = make_uint2(w[0], w[1]);
+    else *reinterpret_cast<uint4 *>(dst) = make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+template <int P>
+__device__ __forceinline__ void store_floats(float *dst, const float2 (&v)[P]) {
+#pragma unroll
+    for (int i = 0; i < P; i += 2)
+        *reinterpret_cast<float4 *>(dst + 2 * i) = make_float4(v[i].x, v[i].y, v[i + 1].x, v[i + 1].y);
+}
+
+// The x pass's operand-plane stores of one tile of map m: lane = W consecutive
+// points of a row (the z values z[j] .. z[j + W/2 - 1] of row l), written as one
+// W-element store per plane at ((chunk maps + m) 64 + point % 64).
+template <int W>
+__device__ __forceinline__ void store_planes(const XArgs &a, const float2 *buf, int m, int nrows, int npt, size_t c0,
+                                             float sb, float sa, int warp, int nw, int lane) {
+    constexpr int P = W / 2;
+    const int Nm = a.Nm;
+    for (int pl = 32 * W * warp + W * lane; pl < npt; pl += 32 * W * nw) {
+        int l = (int)(((float)pl + 0.5f) * a.inv_nm);
+        l -= l * Nm > pl ? 1 : 0;
+        l += (l + 1) * Nm <= pl ? 1 : 0;
+        const int j = (pl - l * Nm) >> 1;
+        float2 z[P], v[P];
+#pragma unroll
+        for (int i = 0; i < P; i++) {
+            z[i] = buf[(j + i) * kP + l];
+            v[i] = fftd::cscale(z[i], sb);
+        }
+        const size_t ck = c0 + (pl >> 6), t = pl & 63;
+        const size_t ib = (ck * a.count + m) * 64 + t;  // element index in the B planes
+        if (a.oform == 1) {
+            unsigned hw[P], lw[P];
+#pragma unroll
+            for (int i = 0; i < P; i++) {
+                const __half2 h = __floats2half2_rn(v[i].x, v[i].y);
+                const float2 hb = __half22float2(h);
+                const __half2 g = __floats2half2_rn(v[i].x - hb.x, v[i].y - hb.y);
+                hw[i] = *reinterpret_cast<const unsigned *>(&h);
+                lw[i] = *reinterpret_cast<const unsigned *>(&g);
+            }
+            store_words<P>(reinterpret_cast<__half *>(a.bhi) + ib, hw);
+            store_words<P>(reinterpret_cast<__half *>(a.blo) + ib, lw);
+        } else if (a.oform == 2) {
+            unsigned hw[P];
+#pragma unroll
+            for (int i = 0; i < P; i++) {
+                const __nv_bfloat162 h = __floats2bfloat162_rn(v[i].x, v[i].y);
+                hw[i] = *reinterpret_cast<const unsigned *>(&h);
+            }
+            store_words<P>(reinterpret_cast<__nv_bfloat16 *>(a.bhi) + ib, hw);
+        } else {
+            float2 h[P], lo[P];
+#pragma unroll
+            for (int i = 0; i < P; i++) {
+                h[i] = make_float2(__uint_as_float(__float_as_uint(v[i].x) & 0xFFFFE000u),
+                                   __uint_as_float(__float_as_uint(v[i].y) & 0xFFFFE000u));
+                lo[i] = make_float2(v[i].x - h[i].x, v[i].y - h[i].y);
+            }
+            store_floats<P>(reinterpret_cast<float *>(a.bhi) + ib, h);
+            store_floats<P>(reinterpret_cast<float *>(a.blo) + ib, lo);
+        }
+        if (m < a.nb) {
+#pragma unroll
+            for (int i = 0; i < P; i++) z[i] = fftd::cscale(z[i], sa);
+            store_floats<P>(reinterpret_cast<float *>(a.a32) + (ck * a.nb + m) * 64 + t, z);
+        }
+    }
+}
+
 // x pass: tile = (map m, 32 consecutive rows (z, y)).  With M = Nm / 2,
 // Z[k] = (X[k] + conj X[M-k]) + i (X[k] - conj X[M-k]) e^{2 pi i k / Nm} and
 // z = IDFT_M(Z) give the C2R output x[2j] = Re z[j], x[2j+1] = Im z[j].  The
@@ -322,47 +395,11 @@ __global__ void __launch_bounds__(kThreads, PF <= 9 ? 4 : 2) map_xpass_kernel(co
             const float sa = sb * (a.oform == 1 ? 1.f / 128.f : 1.f);       // pair factors: x 2^(e-7)
             const int npt = nrows * Nm;
             const size_t c0 = ((size_t)row0 * Nm) >> 6;
-            // a lane takes 4 consecutive points (one row: Nm % 4 == 0), 16 lanes a chunk row
-            for (int pl = 128 * warp + 4 * lane; pl < npt; pl += 128 * nw) {
-                int l = (int)(((float)pl + 0.5f) * a.inv_nm);
-                l -= l * Nm > pl ? 1 : 0;
-                l += (l + 1) * Nm <= pl ? 1 : 0;
-                const int j = (pl - l * Nm) >> 1;
-                const float2 z0 = buf[j * kP + l], z1 = buf[(j + 1) * kP + l];
-                const size_t ck = c0 + (pl >> 6), t = pl & 63;
-                const size_t ib = (ck * a.count + m) * 64 + t;  // element index in the B planes
-                const float2 v0 = fftd::cscale(z0, sb), v1 = fftd::cscale(z1, sb);
-                if (a.oform == 1) {
-                    const __half2 h0 = __floats2half2_rn(v0.x, v0.y), h1 = __floats2half2_rn(v1.x, v1.y);
-                    const float2 b0 = __half22float2(h0), b1 = __half22float2(h1);
-                    const __half2 g0 = __floats2half2_rn(v0.x - b0.x, v0.y - b0.y);
-                    const __half2 g1 = __floats2half2_rn(v1.x - b1.x, v1.y - b1.y);
-                    uint2 hw, lw;
-                    hw.x = *reinterpret_cast<const unsigned *>(&h0);
-                    hw.y = *reinterpret_cast<const unsigned *>(&h1);
-                    lw.x = *reinterpret_cast<const unsigned *>(&g0);
-                    lw.y = *reinterpret_cast<const unsigned *>(&g1);
-                    *reinterpret_cast<uint2 *>(reinterpret_cast<__half *>(a.bhi) + ib) = hw;
-                    *reinterpret_cast<uint2 *>(reinterpret_cast<__half *>(a.blo) + ib) = lw;
-                } else if (a.oform == 2) {
-                    const __nv_bfloat162 h0 = __floats2bfloat162_rn(v0.x, v0.y), h1 = __floats2bfloat162_rn(v1.x, v1.y);
-                    uint2 hw;
-                    hw.x = *reinterpret_cast<const unsigned *>(&h0);
-                    hw.y = *reinterpret_cast<const unsigned *>(&h1);
-                    *reinterpret_cast<uint2 *>(reinterpret_cast<__nv_bfloat16 *>(a.bhi) + ib) = hw;
-                } else {
-                    const float4 h = make_float4(__uint_as_float(__float_as_uint(v0.x) & 0xFFFFE000u),
-                                                 __uint_as_float(__float_as_uint(v0.y) & 0xFFFFE000u),
-                                                 __uint_as_float(__float_as_uint(v1.x) & 0xFFFFE000u),
-                                                 __uint_as_float(__float_as_uint(v1.y) & 0xFFFFE000u));
-                    *reinterpret_cast<float4 *>(reinterpret_cast<float *>(a.bhi) + ib) = h;
-                    *reinterpret_cast<float4 *>(reinterpret_cast<float *>(a.blo) + ib) =
-                        make_float4(v0.x - h.x, v0.y - h.y, v1.x - h.z, v1.y - h.w);
-                }
-                if (m < a.nb)
-                    *reinterpret_cast<float4 *>(reinterpret_cast<float *>(a.a32) + (ck * a.nb + m) * 64 + t) =
-                        make_float4(z0.x * sa, z0.y * sa, z1.x * sa, z1.y * sa);
-            }
+            // a lane takes W consecutive points of one row (Nm % W == 0), 64 / W lanes a chunk row
+            if (Nm % 8 == 0)
+                store_planes<8>(a, buf, m, nrows, npt, c0, sb, sa, warp, nw, lane);
+            else
+                store_planes<4>(a, buf, m, nrows, npt, c0, sb, sa, warp, nw, lane);
         }
         m = mn;
         r = rn;
