@@ -48,15 +48,22 @@ __device__ __forceinline__ unsigned int pack3(int x, int y, int z) {
 }
 
 // first cell (0-based, in [0,N)) and the offset h that sets the weights
+// t mod N for the cell indices: t is in [-2, 2N) for positions in [0, 1]
+// (two compares), any other t takes the division
+__device__ __forceinline__ int wrap_cell(long long t, int N) {
+    if (t >= 0 && t < 2LL * N) return (int)(t >= N ? t - N : t);
+    return (int)(t % N);
+}
+
 __device__ __forceinline__ void first_and_h(double p, int N, int nintp, bool shifted, bool cic_nint, int &f, float &h) {
     double v = (double)N * p + 1.0;
     if (shifted) v = v - 0.5;
     long long iv;
     double hh;
-    if (nintp == 4) { iv = (long long)v; f = (int)((iv - 2) % N); hh = v - (double)iv; }
-    else if (nintp == 3) { iv = llround(v); f = (int)((iv - 2) % N); hh = v - (double)iv; }
-    else if (nintp == 2) { iv = (long long)v; f = (int)(iv % N); hh = cic_nint ? v - (double)llround(v) : v - (double)iv; }
-    else { iv = llround(v); f = (int)((iv - 1) % N); hh = 0.0; }
+    if (nintp == 4) { iv = (long long)v; f = wrap_cell(iv - 2, N); hh = v - (double)iv; }
+    else if (nintp == 3) { iv = llround(v); f = wrap_cell(iv - 2, N); hh = v - (double)iv; }
+    else if (nintp == 2) { iv = (long long)v; f = wrap_cell(iv, N); hh = cic_nint ? v - (double)llround(v) : v - (double)iv; }
+    else { iv = llround(v); f = wrap_cell(iv - 1, N); hh = 0.0; }
     if (f < 0) f += N;
     if (f < 0 || f >= N) f = 0;
     h = (float)hh;
@@ -120,7 +127,7 @@ __device__ __forceinline__ PRec make_rec(const double *__restrict__ pos, int64_t
         if (interlaced) first_and_h(p, N, nintp, true, false, f[1][c], r.h[1][c]);
         else { f[1][c] = f[0][c]; r.h[1][c] = 0.f; }
         // the shifted grid starts at the same cell or one below (circularly)
-        lo[c] = (interlaced && f[1][c] == (f[0][c] + N - 1) % N) ? f[1][c] : f[0][c];
+        lo[c] = (interlaced && f[1][c] == (f[0][c] == 0 ? N - 1 : f[0][c] - 1)) ? f[1][c] : f[0][c];
     }
     r.f[0] = pack3(f[0][0], f[0][1], f[0][2]);
     r.f[1] = pack3(f[1][0], f[1][1], f[1][2]);
@@ -191,7 +198,7 @@ __global__ void owner_scatter_kernel(int N, int nintp, int interlaced, int64_t n
         int lo[3];
         for (int c = 0; c < 3; c++) {
             const unsigned f0 = (r.f[0] >> (11 * c)) & 2047, f1 = (r.f[1] >> (11 * c)) & 2047;
-            lo[c] = (interlaced && (int)f1 == ((int)f0 + N - 1) % N) ? (int)f1 : (int)f0;
+            lo[c] = (interlaced && (int)f1 == ((int)f0 == 0 ? N - 1 : (int)f0 - 1)) ? (int)f1 : (int)f0;
         }
         int tx[2], ty[2], tz[2];
         const int nx = axis_tiles(lo[0], w, N, nt, tx), ny = axis_tiles(lo[1], w, N, nt, ty),
