@@ -392,6 +392,60 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+PRECISION_FORM = dict(workload="zeldovich_512_pcs_interlaced_P024_B024_76shells", lattice=256, box=2000.0, grid=512,
+                      kbin_bs=2.0, kcenter_bs=2.0, nbins_bs=76)
+
+
+def run_precision_form(args):
+    """The 512^3 precision form: a 256^3-lattice Zel'dovich box in L = 2000 Mpc/h,
+    grid 512^3, PCS interlaced, P l=0,2,4 (dk = kf), B l=0,2,4 with dk = 2 kf up to
+    0.6 k_Nyq (76 shells, 228 maps on the 480^3 map grid).  The FP16 hi+lo and BF16
+    tensor-core forms run beside the plain FP32 form; errors are reported against
+    the plain FP32 form (an FP64 run of this box would need ~200 GB of FP64 maps and
+    a minute of FP64 triangle sums)."""
+    import torch
+    from pbi4_gb300 import synthetic
+    from pbi4_gb300.estimator import Estimator, EstimatorConfig
+    w = PRECISION_FORM
+    pos = synthetic.zeldovich_box(w["lattice"], w["box"], n_s=-1.5, rms_disp=5.0, f_growth=0.7, seed=2)
+    npart = pos.shape[1]
+    dpos = torch.from_numpy(pos).cuda()
+    out, res = {}, {}
+    for prec, steps in (("fp16split", 2), ("bf16", 2), ("fp32", 1)):
+        cfg = EstimatorConfig(grid=w["grid"], box=w["box"], nintp=4, interlacing=True, multipoles=True,
+                              los=(0.0, 0.0, 1.0), kbin_ps=1.0, kcenter_ps=1.0, do_bispectrum=True,
+                              kbin_bs=w["kbin_bs"], kcenter_bs=w["kcenter_bs"], nbins_bs=w["nbins_bs"], iopen=True,
+                              precision=prec)
+        est = Estimator(cfg)
+        po, bo = est.alloc_outputs()
+        est.run_device(npart, dpos, po, bo)  # tables, triangle counts (cached), buffers
+        torch.cuda.synchronize()
+        est.enable_timing(True)
+        est.stage_times()
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record()
+        for _ in range(steps):
+            est.run_device(npart, dpos, po, bo)
+        t1.record()
+        torch.cuda.synchronize()
+        est.check()
+        ms = t0.elapsed_time(t1) / steps
+        st = est.stage_times()
+        res[prec] = est.run_host(pos)
+        out[prec] = {"boxes_per_s": round(1e3 / ms, 3), "ms_per_box": round(ms, 2),
+                     "map_grid": est.map_grid, "maps": est.nmaps, "triangles": est.itot,
+                     "stages_ms_per_box": {k: round(v[0] / steps, 2) for k, v in st.items() if v[1]}}
+        est.close()
+        del po, bo
+        torch.cuda.empty_cache()
+    p32, b32 = res["fp32"]
+    errs = {prec: error_report(res[prec][0], res[prec][1], p32, b32) for prec in ("fp16split", "bf16")}
+    print(json.dumps({"metric": "P+B boxes/s @512^3 PCS interlaced, 76 shells (precision form)", "unit": "boxes/s",
+                      "data": "synthetic (seeded Zel'dovich box, positions resident in HBM)",
+                      "config": {**w, "particles": npart, "nintp": 4, "interlacing": True, "multipoles": True},
+                      "forms": out, "error_vs_plain_fp32": errs}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -407,10 +461,14 @@ def main():
     ap.add_argument("--small", action="store_true",
                     help="profiling case: 64^3 particles on a 128^3 grid (same kernels, a few hundred MB)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision-form", action="store_true",
+                    help="only the 512^3 precision form (FP16 split, BF16, plain FP32; ~1 min)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.precision_form:
+        run_precision_form(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

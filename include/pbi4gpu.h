@@ -224,10 +224,12 @@ int64_t pbi4g_plan_kernel_launches(const pbi4g_plan *plan);
  * Stages: 0 assign, 1 grid convert, 2 forward FFT, 3 fcomb, 4 P(k) binning,
  * 5 triangle counts, 6 shell maps z (shell spectra; FP32 forms with their z
  * transform), 7 shell maps y (FP32 forms: y transform; FP64: the batched C2R),
- * 8 triangle sums, 9 output rows, 10 shell maps x (FP32 forms: the real maps).  pbi4g_plan_stage_times synchronises the stream, writes the
+ * 8 triangle sums, 9 output rows, 10 shell maps x (FP32 forms: the real maps),
+ * 11 the FP32 forms' counting sort of the particles into owner tiles (stage 0
+ * is then the tile accumulation alone).  pbi4g_plan_stage_times synchronises the stream, writes the
  * summed milliseconds and the number of timed calls per stage since the last
  * query (arrays of PBI4G_NSTAGES) and resets them. */
-#define PBI4G_NSTAGES 11
+#define PBI4G_NSTAGES 12
 int pbi4g_plan_enable_timing(pbi4g_plan *plan, int32_t enable);
 int pbi4g_plan_stage_times(pbi4g_plan *plan, double *ms, int64_t *calls);
 

@@ -32,9 +32,9 @@ EXPORTS = [
     "pbi4g_measure_pk_multipoles_noalloc", "pbi4g_plan_set_delta_half", "pbi4g_plan_set_counts",
     "pbi4g_plan_check", "pbi4g_plan_graph_build", "pbi4g_plan_graph_run_host",
 ]
-NSTAGES = 11
+NSTAGES = 12
 STAGES = ["assign", "grid_convert", "fft_r2c", "fcomb", "pk_binning", "triangle_counts", "shell_maps_z",
-          "shell_maps_y", "triangle_sums", "bk_rows", "shell_maps_x"]
+          "shell_maps_y", "triangle_sums", "bk_rows", "shell_maps_x", "assign_sort"]
 
 
 class Pbi4GpuError(RuntimeError):

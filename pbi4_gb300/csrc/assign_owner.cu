@@ -371,7 +371,9 @@ size_t OwnerWork::footprint(int N, int64_t npart) {
 
 int assign_owner(OwnerWork &wk, int N, int nintp, bool interlaced, int64_t npart, const double *d_pos,
                  const double *d_weight, float *out, cudaStream_t st, int64_t *launches, int64_t stride,
-                 const BoxPar *bp) {
+                 const BoxPar *bp, Prof *prof, int tile_stage, int sort_stage) {
+    Prof none;
+    Prof &pf = prof ? *prof : none;
     if (stride <= 0) stride = npart;
     if (!owner_supported(N)) return set_error(PBI4G_ERR_UNSUPPORTED, "owner assignment needs grid %% 16 == 0");
     if (nintp < 1 || nintp > 4 || npart < 1 || !d_pos)
@@ -398,6 +400,7 @@ int assign_owner(OwnerWork &wk, int N, int nintp, bool interlaced, int64_t npart
     bits = std::min(bits, (int)floor(30.0 - log2(4.0 * (wmax > 0 ? wmax : 1.0))));
     if (bits < 8) return set_error(PBI4G_ERR_RANGE, "assign: particle weights up to %g", wmax);
     const int nt = N / kT, ntiles = nt * nt * nt;
+    pf.begin(sort_stage, st);
     PBI4G_CUDA(cudaMemsetAsync(wk.count.p, 0, (size_t)(ntiles + 2) * 4, st));  // counts and the tile counter
     owner_count_kernel<<<grid_blocks(npart, 256), 256, 0, st>>>(N, nintp, interlaced, npart, stride, bp, d_pos, nt,
                                                                 static_cast<PRec *>(wk.rec.p),
@@ -416,6 +419,8 @@ int assign_owner(OwnerWork &wk, int N, int nintp, bool interlaced, int64_t npart
     const float *ws = d_weight ? wk.wsorted.as<float>() : nullptr;
     float *o2 = interlaced ? out + FC : nullptr;
     unsigned *nx = wk.count.as<unsigned int>() + ntiles + 1;
+    pf.end(st);
+    pf.begin(tile_stage, st);
     int rc = PBI4G_OK;
     switch (nintp * 2 + (interlaced ? 1 : 0)) {
         case 2: rc = launch_tile<1, 1>(N, nt, st_, so, ws, bits, out, o2, nx, st); break;
@@ -427,6 +432,7 @@ int assign_owner(OwnerWork &wk, int N, int nintp, bool interlaced, int64_t npart
         case 8: rc = launch_tile<4, 1>(N, nt, st_, so, ws, bits, out, o2, nx, st); break;
         default: rc = launch_tile<4, 2>(N, nt, st_, so, ws, bits, out, o2, nx, st); break;
     }
+    pf.end(st);
     PBI4G_CHECK(rc);
     *launches += 4;
     return PBI4G_OK;

@@ -17,8 +17,10 @@ bool owner_supported(int N);
 // stride: distance between the x, y, z rows of d_pos (npart when <= 0).  bp:
 // when set, the particle count is read from bp->npart (npart is then the
 // capacity that sizes the launches: the graph-captured form).
+// prof: when set, the counting sort is timed as stage sort_stage and the tile
+// kernel as stage tile_stage.
 int assign_owner(OwnerWork &wk, int N, int nintp, bool interlaced, int64_t npart, const double *d_pos,
                  const double *d_weight, float *out, cudaStream_t st, int64_t *launches, int64_t stride = 0,
-                 const BoxPar *bp = nullptr);
+                 const BoxPar *bp = nullptr, Prof *prof = nullptr, int tile_stage = 0, int sort_stage = 0);
 
 }  // namespace pbi4g

@@ -14,6 +14,8 @@
 #include <stdint.h>
 #include <stddef.h>
 
+#include <vector>
+
 #include "../../include/pbi4gpu.h"
 
 namespace pbi4g {
@@ -105,6 +107,20 @@ struct DevBuf {
         return PBI4G_OK;
     }
     template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+// Per-stage CUDA-event timing on a stream (see pbi4g_plan_enable_timing).
+struct Prof {
+    bool on = false;
+    struct Rec { int stage; cudaEvent_t a, b; };
+    std::vector<cudaEvent_t> pool;
+    std::vector<Rec> recs;
+    cudaEvent_t cur_a = nullptr;
+    int cur_stage = -1;
+    ~Prof();
+    cudaEvent_t get();
+    void begin(int stage, cudaStream_t st);
+    void end(cudaStream_t st);
 };
 
 }  // namespace pbi4g

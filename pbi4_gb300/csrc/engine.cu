@@ -370,10 +370,8 @@ static int density_impl(pbi4g_plan *p, int64_t npart, const double *d_pos, const
     int bits;
     if (!p->fp64 && owner_supported(N)) {
         // FP32 grids straight from the owner-computes tiles (fixed-point sums in shared memory)
-        p->prof.begin(0, p->st);
         PBI4G_CHECK(assign_owner(p->ow, N, p->cfg.nintp, p->G == 2, npart, d_pos, d_weight,
-                                 p->real_grids.as<float>(), p->st, &p->launches, npart, bp));
-        p->prof.end(p->st);
+                                 p->real_grids.as<float>(), p->st, &p->launches, npart, bp, &p->prof, 0, 11));
     } else {
         if (bp) return set_error(PBI4G_ERR_UNSUPPORTED, "captured form needs the owner-computes assignment");
         p->prof.begin(0, p->st);

@@ -6,20 +6,6 @@
 
 namespace pbi4g {
 
-// Per-stage CUDA-event timing on a stream (see pbi4g_plan_enable_timing).
-struct Prof {
-    bool on = false;
-    struct Rec { int stage; cudaEvent_t a, b; };
-    std::vector<cudaEvent_t> pool;
-    std::vector<Rec> recs;
-    cudaEvent_t cur_a = nullptr;
-    int cur_stage = -1;
-    ~Prof();
-    cudaEvent_t get();
-    void begin(int stage, cudaStream_t st);
-    void end(cudaStream_t st);
-};
-
 // Triangle-sum form of a PBI4G_PREC_* precision: 0 CUDA cores (FP32 / FP64),
 // 1 FP16 hi+lo, 2 BF16, 3 TF32 hi+lo (tensor cores).
 inline int tc_mode_of(int precision) {

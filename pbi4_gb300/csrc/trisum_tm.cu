@@ -704,8 +704,21 @@ int triangle_sums_tm(const Shells &sh, TmPlan &tp, const MapPlanes &pl, DevBuf &
     TmArgs a;
     a.nchunks = nc;
     a.nunits = tp.nunits;
-    a.ksplit = std::max(1, 152 / tp.nunits);
-    a.ksplit = (int)std::min<long long>(a.ksplit, std::max<long long>(1, a.nchunks / 128));
+    // K split: one CTA per SM (152 SMs) in waves; the split minimising waves x
+    // (chunks a CTA + a CTA's fixed cost of about 64 chunks), at least 128 chunks a CTA
+    {
+        long long best_cost = -1;
+        a.ksplit = 1;
+        for (int k = 1; k <= 152; k++) {
+            if (k > 1 && a.nchunks / k < 128) break;
+            const long long waves = ((long long)tp.nunits * k + 151) / 152;
+            const long long cost = waves * ((a.nchunks + k - 1) / k + 64);
+            if (best_cost < 0 || cost < best_cost) {
+                best_cost = cost;
+                a.ksplit = k;
+            }
+        }
+    }
     a.nslots = tp.nslots;
     a.nA = tp.nA;
     a.nmaps = pl.nmaps;

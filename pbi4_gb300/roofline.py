@@ -4,8 +4,10 @@ Algorithmic traffic per box (N grid, H = N^2 (N/2+1) half-spectrum cells,
 G = 2 grids with interlacing, Np particles; M shell maps on the map grid Nm;
 FP32 forms: Tz, Uy complex elements of the pruned transform's z-column and
 (z, y)-plane intermediates; T triangles, S = 3 multipole sets or 1):
-  assign          24 Np (float64 xyz read) + 4 G N^3 (FP32 grid write; 8 G N^3
-                  int64 fixed-point for the FP64 form)
+  assign          FP32 forms (the owner-tile kernel): 32 R Np (R = records per particle,
+                  (1 + (w-1)/16)^3 for a stencil w = nintp (+1 interlaced) wide) read + 4 G N^3
+                  (FP32 grid write); FP64 form: 24 Np (float64 xyz read) + 8 G N^3 (int64)
+  assign_sort     FP32 forms' counting sort: 24 Np (xyz) + 64 Np (record write, read) + 32 R Np
   grid_convert    8 G N^3 read + 4 G N^3 write (FP64 form only)
   fcomb           8 G H read + 8 H write
   pk_binning      8 H read
@@ -59,8 +61,12 @@ def stage_work(cfg, npart, map_grid=None, nmaps=None, map_work=None):
     Nm = map_grid or N
     Hm = Nm * Nm * (Nm // 2 + 1)
     gbytes = 8 if cfg.precision == "fp64" else 4
+    w = int(cfg.nintp) + (1 if cfg.interlacing else 0)
+    R = (1.0 + (w - 1) / 16.0) ** 3
     work = {
-        "assign": ("hbm", 24 * npart + gbytes * G * N ** 3),
+        "assign": ("hbm", (24 * npart + gbytes * G * N ** 3) if cfg.precision == "fp64"
+                   else (32 * R * npart + 4 * G * N ** 3)),
+        "assign_sort": ("hbm", 24 * npart + 64 * npart + 32 * R * npart),
         "grid_convert": ("hbm", 12 * G * N ** 3),
         "fcomb": ("hbm", 8 * G * H + 8 * H),
         "pk_binning": ("hbm", 8 * H),
@@ -79,7 +85,8 @@ def stage_work(cfg, npart, map_grid=None, nmaps=None, map_work=None):
     return work
 
 
-KERNEL = {"assign": "owner_tile_kernel", "grid_convert": "fixed_to_real_kernel",
+KERNEL = {"assign": "owner_tile_kernel", "assign_sort": "owner_count/scan/scatter_kernel",
+          "grid_convert": "fixed_to_real_kernel",
           "fcomb": "fcomb_interlaced_half_kernel", "pk_binning": "pk_accum_kernel",
           "shell_maps_z": "map_zpass_kernel", "shell_maps_y": "map_ypass_kernel", "shell_maps_x": "map_xpass_kernel",
           "triangle_sums": "trisum_tm_kernel"}
