@@ -233,6 +233,18 @@ int64_t pbi4g_plan_kernel_launches(const pbi4g_plan *plan);
 int pbi4g_plan_enable_timing(pbi4g_plan *plan, int32_t enable);
 int pbi4g_plan_stage_times(pbi4g_plan *plan, double *ms, int64_t *calls);
 
+/* Catalogue step of IO.read_catalogues (pbi4.py:121-245) on the device: d_pos
+ * (npart, 3) row-major catalogue positions in Mpc/h, float32 (is_double = 0) or
+ * float64, optional d_vel (npart, 3) of the same type with the RSD shift along
+ * los[3]: rsd_mode 1 pos += vel * los / hz * (1 + z) (Gadget, Rockstar, Quijote),
+ * rsd_mode 0 pos += vel * los (Minerva), the shift in float64 and rounded to the
+ * catalogue type as numpy does; then the wrap (pos + box) % box and pos / box in
+ * the catalogue type, clipped at 1.0, into d_out (3, npart) float64: the
+ * positions the assignment reads.  Asynchronous on `stream` (a cudaStream_t). */
+int pbi4g_catalog_positions(int64_t npart, const void *d_pos, const void *d_vel, int32_t is_double,
+                            const double *los, int32_t rsd_mode, double hz, double z, double box, double *d_out,
+                            void *stream);
+
 /* Host check of the shell maps' FFT plans (no device work): `batch` inverse
  * DFTs of n points, X[k] = sum_j x[j] e^{+2 pi i j k / n}, of interleaved
  * complex FP32 rows in[t][n][2] -> out[t][n][2], computed on the CPU with the

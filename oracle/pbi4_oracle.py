@@ -403,3 +403,20 @@ def bispectrum(npart, counts, dcl, params, dcl2=None, dcl4=None, workers=None):
     for r, (name, _) in enumerate(dt):
         out[name] = bout[r]
     return out
+
+
+def catalogue_positions(pos, vel=None, los=None, hz=None, z=None, box=1000.0, rsd_mode=1):
+    """The catalogue step of IO.read_catalogues (pbi4.py:121-245) in numpy, with the
+    reference's own operations and dtypes: pos, vel (N, 3) of the catalogue's dtype;
+    RSD shift pos[:] += Vel[:] * los / Hz * (1 + z) (pbi4.py:158, 170, 214; rsd_mode 1)
+    or pos[:] += Vel[:] * los (Minerva, pbi4.py:184; rsd_mode 0); then the wrap and the
+    normalisation of pbi4.py:241-243.  Returns (3, N) float64."""
+    pos = np.array(pos, copy=True)
+    if vel is not None:
+        if rsd_mode == 1:
+            pos[:] += vel[:] * np.asarray(los) / hz * (1. + z)
+        else:
+            pos[:] += vel[:] * np.asarray(los)
+    pos = pos.T
+    pos = (pos + box) % box
+    return np.minimum(1. - np.nextafter(0, 1), pos / box)

@@ -29,6 +29,7 @@ EXPORTS = [
     "pbi4g_plan_powerspectrum",
     "pbi4g_plan_bispectrum", "pbi4g_plan_run_device", "pbi4g_plan_run_host", "pbi4g_plan_get_delta_half",
     "pbi4g_plan_kernel_launches", "pbi4g_plan_enable_timing", "pbi4g_plan_stage_times", "pbi4g_fft_plan_check",
+    "pbi4g_catalog_positions",
     "pbi4g_measure_pk_multipoles_noalloc", "pbi4g_plan_set_delta_half", "pbi4g_plan_set_counts",
     "pbi4g_plan_check", "pbi4g_plan_graph_build", "pbi4g_plan_graph_run_host",
 ]
@@ -92,6 +93,8 @@ _SIGS = {
     "pbi4g_plan_enable_timing": [_P, _i32],
     "pbi4g_plan_stage_times": [_P, _P, _P],
     "pbi4g_fft_plan_check": [_i32, _i32, _P, _P],
+    "pbi4g_catalog_positions": [_i64, _P, _P, _i32, _P, _i32, ctypes.c_double, ctypes.c_double, ctypes.c_double, _P,
+                                _P],
     "pbi4g_measure_pk_multipoles_noalloc": [_i32, _f32, _f32, _f32, _i32, _P, _P, _P, _P, _P],
     "pbi4g_plan_set_delta_half": [_P, _i64, _P],
     "pbi4g_plan_set_counts": [_P, _P],

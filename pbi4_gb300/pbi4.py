@@ -103,15 +103,24 @@ class IO:
         d.update({"itot": itot})
         return d
 
-    def read_catalogues(self, params=None):
+    def read_catalogues(self, params=None, device=False):
         """Positions of a numpy catalogue with a 'pos' field (N, 3) in Mpc/h (the
-        npz layout of pbi4.py:235-240), wrapped and normalised as pbi4.py:241-243."""
+        npz layout of pbi4.py:235-240) and, optionally, a 'vel' field (N, 3) in km/s
+        for the RSD shift along params['los'] when params['multipoles'] is set
+        (pos += vel los / Hz (1 + z), pbi4.py:158-159).  The shift, the wrap and the
+        normalisation of pbi4.py:241-243 run on the device (pbi4_gb300.catalog);
+        returns (3, N) float64 positions, a CUDA tensor with device=True."""
+        from .catalog import positions
         if params is None:
             params = self.params
         cat = np.load(params["ifile"])
-        pos = np.asarray(cat["pos"], dtype=np.float64).T
-        pos = (pos + params["box"]) % params["box"]
-        return np.minimum(1.0 - np.nextafter(0, 1), pos / params["box"])
+        pos = np.asarray(cat["pos"])
+        vel = None
+        if params.get("multipoles") and "vel" in cat.files:
+            vel = np.asarray(cat["vel"], dtype=pos.dtype)
+        out = positions(pos, vel=vel, los=params.get("los"), hz=params.get("Hz"), z=params.get("z"),
+                        box=params["box"], rsd_mode=1)
+        return out if device else out.cpu().numpy()
 
 
 class Density:

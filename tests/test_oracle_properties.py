@@ -104,3 +104,22 @@ def test_uniform_lattice_has_no_power():
     d = O.compute_density(npart, dtl, p)
     pk = O.measure_pk(N, 100.0, 1.0, 1.0, 4, d, d)
     assert np.all(np.abs(pk[1]) < 1e-20)
+
+
+def test_catalogue_positions_oracle_wraps_and_clips():
+    """The reference's catalogue normalisation (pbi4.py:241-243): periodic wrap into
+    [0, box), division by box, and the clip that leaves an exact 1.0 when float
+    rounding of (pos + box) % box returns box itself."""
+    box = 1000.0
+    pos = np.array([[0.0, box, -box], [2 * box, 250.0, -250.0]], dtype=np.float64)
+    got = O.catalogue_positions(pos, box=box)
+    np.testing.assert_array_equal(got, np.array([[0.0, 0.0], [0.0, 0.25], [0.0, 0.75]]))
+    # a float32 position just below zero: (p + box) rounds to box, % box gives 0
+    p32 = np.array([[-1e-6, 0.5, 999.9999]], dtype=np.float32)
+    g32 = O.catalogue_positions(p32, box=box)
+    assert g32.dtype == np.float64 and g32.min() >= 0.0 and g32.max() <= 1.0
+    # the RSD shift is float64 arithmetic rounded once to the catalogue dtype
+    vel = np.array([[0.0, 0.0, 100.0]], dtype=np.float32)
+    shifted = O.catalogue_positions(np.array([[10.0, 10.0, 10.0]], dtype=np.float32), vel, [0.0, 0.0, 1.0], 100.0,
+                                    0.0, box=box)
+    np.testing.assert_allclose(shifted[:, 0], [0.01, 0.01, 0.011], rtol=1e-6)
