@@ -393,33 +393,33 @@ def run_ours(args):
 
 
 PRECISION_FORM = dict(workload="zeldovich_512_pcs_interlaced_P024_B024_76shells", lattice=256, box=2000.0, grid=512,
-                      kbin_bs=2.0, kcenter_bs=2.0, nbins_bs=76)
+                      kbin_bs=2.0, kcenter_bs=2.0, nbins_bs=76, map_budget_mb=0)
+# the 1024^3 single box: B with dk = 4 kf up to 0.4 k_Nyq (51 shells); the P multipoles
+# switch on B2 and B4 as in the reference's multipole run (153 maps on the 640^3 map
+# grid); the maps stream over z-slabs so the plan's working set stays under 150 GB
+LARGE_BOX = dict(workload="zeldovich_1024_pcs_interlaced_P024_B024_51shells", lattice=512, box=3000.0, grid=1024,
+                 kbin_bs=4.0, kcenter_bs=4.0, nbins_bs=51, map_budget_mb=24576)
 
 
-def run_precision_form(args):
-    """The 512^3 precision form: a 256^3-lattice Zel'dovich box in L = 2000 Mpc/h,
-    grid 512^3, PCS interlaced, P l=0,2,4 (dk = kf), B l=0,2,4 with dk = 2 kf up to
-    0.6 k_Nyq (76 shells, 228 maps on the 480^3 map grid).  The FP16 hi+lo and BF16
-    tensor-core forms run beside the plain FP32 form; errors are reported against
-    the plain FP32 form (an FP64 run of this box would need ~200 GB of FP64 maps and
-    a minute of FP64 triangle sums)."""
+def _forms_leg(w, dpos, forms, metric, data):
+    """Time each (precision, steps) of `forms` on the device-resident box dpos
+    (after one untimed run that builds tables, counts and buffers) and report
+    errors of the mixed forms against the plain FP32 form."""
     import torch
-    from pbi4_gb300 import synthetic
     from pbi4_gb300.estimator import Estimator, EstimatorConfig
-    w = PRECISION_FORM
-    pos = synthetic.zeldovich_box(w["lattice"], w["box"], n_s=-1.5, rms_disp=5.0, f_growth=0.7, seed=2)
-    npart = pos.shape[1]
-    dpos = torch.from_numpy(pos).cuda()
+    npart = int(dpos.shape[1])
     out, res = {}, {}
-    for prec, steps in (("fp16split", 2), ("bf16", 2), ("fp32", 1)):
+    for prec, steps in forms:
         cfg = EstimatorConfig(grid=w["grid"], box=w["box"], nintp=4, interlacing=True, multipoles=True,
                               los=(0.0, 0.0, 1.0), kbin_ps=1.0, kcenter_ps=1.0, do_bispectrum=True,
                               kbin_bs=w["kbin_bs"], kcenter_bs=w["kcenter_bs"], nbins_bs=w["nbins_bs"], iopen=True,
-                              precision=prec)
+                              precision=prec, map_budget_mb=w["map_budget_mb"])
         est = Estimator(cfg)
         po, bo = est.alloc_outputs()
+        t_setup = time.perf_counter()
         est.run_device(npart, dpos, po, bo)  # tables, triangle counts (cached), buffers
         torch.cuda.synchronize()
+        t_setup = time.perf_counter() - t_setup
         est.enable_timing(True)
         est.stage_times()
         t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -431,19 +431,56 @@ def run_precision_form(args):
         est.check()
         ms = t0.elapsed_time(t1) / steps
         st = est.stage_times()
-        res[prec] = est.run_host(pos)
-        out[prec] = {"boxes_per_s": round(1e3 / ms, 3), "ms_per_box": round(ms, 2),
-                     "map_grid": est.map_grid, "maps": est.nmaps, "triangles": est.itot,
+        free, total = torch.cuda.mem_get_info()
+        res[prec] = (po.cpu().numpy(), bo.cpu().numpy())
+        zs, ns = est.map_slabs()
+        out[prec] = {"boxes_per_s": round(1e3 / ms, 4), "ms_per_box": round(ms, 2), "steps": steps,
+                     "first_run_s": round(t_setup, 2), "map_grid": est.map_grid, "maps": est.nmaps,
+                     "triangles": est.itot, "map_slabs": ns, "slab_z_planes": zs,
+                     "device_used_gb": round((total - free) / 1e9, 1),
                      "stages_ms_per_box": {k: round(v[0] / steps, 2) for k, v in st.items() if v[1]}}
         est.close()
         del po, bo
         torch.cuda.empty_cache()
     p32, b32 = res["fp32"]
-    errs = {prec: error_report(res[prec][0], res[prec][1], p32, b32) for prec in ("fp16split", "bf16")}
-    print(json.dumps({"metric": "P+B boxes/s @512^3 PCS interlaced, 76 shells (precision form)", "unit": "boxes/s",
-                      "data": "synthetic (seeded Zel'dovich box, positions resident in HBM)",
+    errs = {prec: error_report(res[prec][0], res[prec][1], p32, b32) for prec, _ in forms if prec != "fp32"}
+    print(json.dumps({"metric": metric, "unit": "boxes/s", "data": data,
                       "config": {**w, "particles": npart, "nintp": 4, "interlacing": True, "multipoles": True},
                       "forms": out, "error_vs_plain_fp32": errs}), flush=True)
+
+
+def run_precision_form(args):
+    """The 512^3 precision form: a 256^3-lattice Zel'dovich box in L = 2000 Mpc/h,
+    grid 512^3, PCS interlaced, P l=0,2,4 (dk = kf), B l=0,2,4 with dk = 2 kf up to
+    0.6 k_Nyq (76 shells, 228 maps on the 480^3 map grid).  The FP16 hi+lo and BF16
+    tensor-core forms run beside the plain FP32 form; errors are reported against
+    the plain FP32 form (an FP64 run of this box would need ~200 GB of FP64 maps and
+    a minute of FP64 triangle sums)."""
+    import torch
+    from pbi4_gb300 import synthetic
+    w = PRECISION_FORM
+    pos = synthetic.zeldovich_box(w["lattice"], w["box"], n_s=-1.5, rms_disp=5.0, f_growth=0.7, seed=2)
+    dpos = torch.from_numpy(pos).cuda()
+    _forms_leg(w, dpos, (("fp16split", 2), ("bf16", 2), ("fp32", 1)),
+               "P+B boxes/s @512^3 PCS interlaced, 76 shells (precision form)",
+               "synthetic (seeded Zel'dovich box, positions resident in HBM)")
+
+
+def run_large_box(args):
+    """The 1024^3 single box: a 512^3-lattice Zel'dovich box (134,217,728 particles,
+    generated on the device) in L = 3000 Mpc/h, grid 1024^3, PCS interlaced, P
+    l=0,2,4 (dk = kf), B l=0,2,4 with dk = 4 kf up to 0.4 k_Nyq (51 shells).  The
+    FP16 hi+lo form runs beside the plain FP32 form with a 24 GiB budget for the
+    slab-sized map buffers; errors against the plain FP32 form."""
+    import torch
+    from pbi4_gb300 import synthetic
+    w = LARGE_BOX
+    dpos = synthetic.zeldovich_box_device(w["lattice"], w["box"], n_s=-1.5, rms_disp=5.0, f_growth=0.7, seed=4)
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    _forms_leg(w, dpos, (("fp16split", 2), ("fp32", 1)),
+               "P+B boxes/s @1024^3 PCS interlaced, 51 shells (large single box)",
+               "synthetic (seeded Zel'dovich box generated on the device, positions resident in HBM)")
 
 
 def main():
@@ -463,11 +500,15 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precision-form", action="store_true",
                     help="only the 512^3 precision form (FP16 split, BF16, plain FP32; ~1 min)")
+    ap.add_argument("--large-box", action="store_true",
+                    help="only the 1024^3 single box (FP16 split and plain FP32, maps in z-slabs; ~1 min)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.precision_form:
         run_precision_form(args)
+    elif args.large_box:
+        run_large_box(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -142,7 +142,11 @@ typedef struct pbi4g_config {
     int32_t nbins_bs;
     int32_t iopen;
     int32_t precision;   /* PBI4G_PREC_* of the shell maps / triangle sums */
-    int32_t reserved[7]; /* must be zero */
+    int32_t map_budget_mb; /* FP32 forms: MiB the real-space shell maps may hold at
+                            * once (0: no bound).  Above it the maps are made and
+                            * contracted z-slab by z-slab (same results up to the
+                            * order of the FP64 slab additions). */
+    int32_t reserved[6]; /* must be zero */
 } pbi4g_config;
 
 typedef struct pbi4g_plan pbi4g_plan;
@@ -167,6 +171,9 @@ int pbi4g_plan_map_grid(const pbi4g_plan *plan, int32_t *map_grid, int32_t *nmap
  * z-transformed shell columns and the (z, y)-transformed kx planes) of the
  * FP32 forms, as sized by the first bispectrum run (0 before it, and for FP64). */
 int pbi4g_plan_map_work(const pbi4g_plan *plan, int64_t *zcols, int64_t *yplanes);
+/* z-planes per slab of the map grid and slabs per box of the last bispectrum
+ * run (one slab of map_grid planes without a map budget; 0, 0 before a run). */
+int pbi4g_plan_map_slabs(const pbi4g_plan *plan, int32_t *slab_planes, int32_t *nslabs);
 /* Exact integer triangle counts of the plan's binning (computed once, cached). */
 int pbi4g_plan_triangle_counts(pbi4g_plan *plan, int64_t *counts_host);
 

@@ -110,7 +110,7 @@ int Shells::build(int N_, float kbin_, float kcenter_, int nb_, int iopen_, int 
 // Output slot (m, s) = m * nsets + s.  Non-cross: S = sum M_i M_j Q_{s,l}, pair
 // (i, j) of set-0 maps, q = map s*nb + l-1.  Cross: S = sum Q_i M_j M_l, pair
 // (j, l) of set-0 maps, q = map qset*nb + i-1.
-int TriPlan::build(const Shells &sh, int nsets_, int cross_, int max_pairs) {
+int TriPlan::build(const Shells &sh, int nsets_, int cross_, int max_pairs, int qoff) {
     nsets = nsets_;
     cross = cross_;
     const int nb = sh.nb;
@@ -124,7 +124,7 @@ int TriPlan::build(const Shells &sh, int nsets_, int cross_, int max_pairs) {
         const int l = sh.tri[3 * m], j = sh.tri[3 * m + 1], i = sh.tri[3 * m + 2];
         for (int s = 0; s < nsets; s++) {
             int pa, pb, qm;
-            if (!cross) { pa = i - 1; pb = j - 1; qm = s * nb + l - 1; }
+            if (!cross) { pa = i - 1; pb = j - 1; qm = qoff + s * nb + l - 1; }
             else { pa = j - 1; pb = l - 1; qm = cross * nb + i - 1; }  // cross = set index of the q field
             auto pk = std::make_pair(pb, pa);
             auto it = pidx.find(pk);
@@ -473,29 +473,29 @@ __global__ void __launch_bounds__(kGroupThreads) trisum_kernel(
 }
 
 __global__ void reduce_partial_kernel(int nslots, int ksplit, const double *__restrict__ partial,
-                                      double *__restrict__ S) {
+                                      double *__restrict__ S, int accumulate) {
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nslots; s += gridDim.x * blockDim.x) {
         double v = 0;
         for (int k = 0; k < ksplit; k++) v += partial[(size_t)k * nslots + s];
-        S[s] = v;
+        S[s] = accumulate ? S[s] + v : v;
     }
 }
 
-int reduce_partials(int nslots, int ksplit, const double *partial, double *S, cudaStream_t st) {
-    reduce_partial_kernel<<<(nslots + 255) / 256, 256, 0, st>>>(nslots, ksplit, partial, S);
+int reduce_partials(int nslots, int ksplit, const double *partial, double *S, bool accumulate, cudaStream_t st) {
+    reduce_partial_kernel<<<(nslots + 255) / 256, 256, 0, st>>>(nslots, ksplit, partial, S, accumulate ? 1 : 0);
     PBI4G_LAUNCH_CHECK();
     return PBI4G_OK;
 }
 
 template <class T>
-int triangle_sums(const Shells &sh, const TriPlan &tp, const T *maps, size_t mstride, int rs, DevBuf &partial,
-                  double *S, cudaStream_t st, int64_t *launches) {
-    const int N = sh.Nm;  // maps live on the map grid
-    const long long K = (long long)N * N * N;
+int triangle_sums(const Shells &sh, const TriPlan &tp, const T *maps, size_t mstride, int rowlen, int rs,
+                  long long K, DevBuf &partial, double *S, bool accumulate, cudaStream_t st, int64_t *launches) {
+    const int N = rowlen;
     int kc = kKCmax;
     while (kc > 4 && K % kc) kc /= 2;
-    if (K % kc || (N & 1) || (rs & 1) || (mstride & 1))
-        return set_error(PBI4G_ERR_UNSUPPORTED, "triangle sums: grid %d has no even chunk width", N);
+    if (K < 1 || K % kc || (N & 1) || (rs & 1) || (mstride & 1))
+        return set_error(PBI4G_ERR_UNSUPPORTED, "triangle sums: %lld points in rows of %d have no even chunk width",
+                         K, N);
     const int qpad = ((tp.nq + kTQ - 1) / kTQ) * kTQ;  // q tiles read up to 8 columns per tile
     const int gpad = ((tp.max_group_pairs + kTP - 1) / kTP) * kTP;
     const int qrow = qpad + 4, prow = gpad + 4;          // 16-B aligned rows, staggered banks
@@ -512,16 +512,15 @@ int triangle_sums(const Shells &sh, const TriPlan &tp, const T *maps, size_t mst
         N, kc, maps, mstride, rs, sh.nb, qpad, tp.qmap.as<int>(), tp.pairs.as<int2>(), tp.tiles.as<int4>(),
         tp.groups.as<int4>(), tp.slots.as<int>(), tp.ngroups, ksplit, K, tp.nslots, partial.as<double>(), qrow, prow);
     PBI4G_LAUNCH_CHECK();
-    reduce_partial_kernel<<<(tp.nslots + 255) / 256, 256, 0, st>>>(tp.nslots, ksplit, partial.as<double>(), S);
-    PBI4G_LAUNCH_CHECK();
+    PBI4G_CHECK(reduce_partials(tp.nslots, ksplit, partial.as<double>(), S, accumulate, st));
     *launches += 2;
     return PBI4G_OK;
 }
 
-template int triangle_sums<float>(const Shells &, const TriPlan &, const float *, size_t, int, DevBuf &, double *,
-                                  cudaStream_t, int64_t *);
-template int triangle_sums<double>(const Shells &, const TriPlan &, const double *, size_t, int, DevBuf &, double *,
-                                   cudaStream_t, int64_t *);
+template int triangle_sums<float>(const Shells &, const TriPlan &, const float *, size_t, int, int, long long,
+                                  DevBuf &, double *, bool, cudaStream_t, int64_t *);
+template int triangle_sums<double>(const Shells &, const TriPlan &, const double *, size_t, int, int, long long,
+                                   DevBuf &, double *, bool, cudaStream_t, int64_t *);
 
 // ------------------------------------------------------------ outputs ---
 __global__ void bk_finalize_kernel(int64_t itot, int nb, int nsets, int cross, const int *__restrict__ tri,
@@ -598,6 +597,63 @@ static int upload_counts(Shells &sh) {
     return PBI4G_OK;
 }
 
+// Orbit representatives of the map grid under the cube group (the 48 axis
+// permutations and sign flips, x_a -> -x_a mod Nm).  A shell indicator map
+// I_b(x) = sum over the shell's modes of e^{2 pi i k.x / Nm} is invariant under
+// the group (the shell is a set of |k|, and Nm / 2 is no shell frequency since
+// Nm > 3 kmax), so sum_x I_l I_j I_i = sum over representatives (a <= b <= c,
+// each in [0, Nm/2]) of |orbit| I_l I_j I_i, with |orbit| = 2 per coordinate
+// outside {0, Nm/2} times the distinct permutations of (a, b, c) (6, 3 or 1).
+// Representatives are packed a | b << 11 | c << 22 and padded with weight-0
+// points to a multiple of 64.
+static int orbit_points(int Nm, std::vector<unsigned> &pts, long long &nrep) {
+    const int h = Nm / 2;
+    pts.clear();
+    long long wsum = 0;
+    for (int a = 0; a <= h; a++)
+        for (int b = a; b <= h; b++)
+            for (int c = b; c <= h; c++) {
+                pts.push_back((unsigned)a | ((unsigned)b << 11) | ((unsigned)c << 22));
+                const int sg = (a == 0 || a == h ? 1 : 2) * (b == 0 || b == h ? 1 : 2) * (c == 0 || c == h ? 1 : 2);
+                const int pm = (a == b && b == c) ? 1 : ((a == b || b == c) ? 3 : 6);
+                wsum += (long long)sg * pm;
+            }
+    nrep = (long long)pts.size();
+    if (wsum != (long long)Nm * Nm * Nm)
+        return set_error(PBI4G_ERR_UNSUPPORTED, "orbit weights of grid %d sum to %lld", Nm, wsum);
+    while (pts.size() % 64) pts.push_back(0u);
+    return PBI4G_OK;
+}
+
+__device__ __forceinline__ double orbit_weight(unsigned pk, int h) {
+    const int a = pk & 2047, b = (pk >> 11) & 2047, c = pk >> 22;
+    const int sg = (a == 0 || a == h ? 1 : 2) * (b == 0 || b == h ? 1 : 2) * (c == 0 || c == h ? 1 : 2);
+    const int pm = (a == b && b == c) ? 1 : ((a == b || b == c) ? 3 : 6);
+    return (double)(sg * pm);
+}
+
+// maps [m0, m0 + count) of the in-place C2R output (map j at real + j * 2 HC,
+// point (a, b, c) at (a Nm + b) (2 NH) + c) at the representatives:
+// out[m][p] = I_m(rep p), out[nb + m][p] = |orbit p| I_m(rep p)
+__global__ void orbit_gather_kernel(int Nm, int nb, int m0, int count, long long nrep, long long npad,
+                                    const unsigned *__restrict__ pts, const double *__restrict__ real,
+                                    double *__restrict__ out) {
+    const int NH = Nm / 2 + 1;
+    const size_t HC2 = 2 * (size_t)Nm * Nm * NH;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npad;
+         p += (long long)gridDim.x * blockDim.x) {
+        const unsigned pk = pts[p];
+        const bool real_pt = p < nrep;
+        const double w = real_pt ? orbit_weight(pk, Nm / 2) : 0.0;
+        const size_t off = ((size_t)(pk & 2047) * Nm + ((pk >> 11) & 2047)) * (2 * NH) + (pk >> 22);
+        for (int j = 0; j < count; j++) {
+            const double v = real_pt ? real[(size_t)j * HC2 + off] : 0.0;
+            out[(size_t)(m0 + j) * npad + p] = v;
+            out[(size_t)(nb + m0 + j) * npad + p] = w * v;
+        }
+    }
+}
+
 int triangle_counts(Shells &sh, cudaStream_t st, int64_t *launches) {
     if (!sh.counts.empty()) return PBI4G_OK;
     const auto ckey = std::make_tuple(sh.N, sh.kbin, sh.kcenter, sh.nb, sh.iopen, sh.cross);
@@ -610,36 +666,76 @@ int triangle_counts(Shells &sh, cudaStream_t st, int64_t *launches) {
         }
     }
     const int N = sh.Nm, nb = sh.nb, NH = N / 2 + 1;  // indicator maps on the map grid
+    if (N > 2046) return set_error(PBI4G_ERR_UNSUPPORTED, "counts: map grid %d", N);
     const size_t HC = half_cells(N);
-    DevBuf maps, partial, S;
-    PBI4G_CHECK(maps.ensure(sizeof(double2) * HC * nb));
-    PBI4G_CHECK(build_indicator_spectra<double>(sh, 0, nb, maps.as<double2>(), st, launches));
-    cufftHandle plan;
+    std::vector<unsigned> hpts;
+    long long nrep = 0;
+    PBI4G_CHECK(orbit_points(N, hpts, nrep));
+    const long long npad = (long long)hpts.size();
+    DevBuf pts, rep, spec, partial, S;
+    PBI4G_CHECK(pts.ensure(sizeof(unsigned) * hpts.size()));
+    PBI4G_CUDA(cudaMemcpyAsync(pts.p, hpts.data(), sizeof(unsigned) * hpts.size(), cudaMemcpyHostToDevice, st));
+    PBI4G_CHECK(rep.ensure(sizeof(double) * 2 * (size_t)nb * npad));
+    // indicator spectra and their FP64 C2R in batches of at most 4 GiB
+    const int bsz = (int)std::max<size_t>(1, std::min<size_t>((size_t)nb, ((size_t)4 << 30) / (sizeof(double2) * HC)));
+    PBI4G_CHECK(spec.ensure(sizeof(double2) * HC * bsz));
     int n[3] = {N, N, N}, inembed[3] = {N, N, NH}, onembed[3] = {N, N, 2 * NH};
-    PBI4G_CUFFT(cufftPlanMany(&plan, 3, n, inembed, 1, (int)HC, onembed, 1, (int)(2 * HC), CUFFT_Z2D, nb));
-    cufftSetStream(plan, st);
-    cufftResult r = cufftExecZ2D(plan, maps.as<cufftDoubleComplex>(), maps.as<cufftDoubleReal>());
-    cufftDestroy(plan);
-    if (r != CUFFT_SUCCESS) return set_error(PBI4G_ERR_CUFFT, "counts: cufftExecZ2D failed (%d)", (int)r);
+    cufftHandle plan = 0;
+    int plan_batch = 0;
+    int rc = PBI4G_OK;
+    for (int m0 = 0; m0 < nb && rc == PBI4G_OK; m0 += bsz) {
+        const int cnt = std::min(bsz, nb - m0);
+        if ((rc = build_indicator_spectra<double>(sh, m0, cnt, spec.as<double2>(), st, launches))) break;
+        if (plan_batch != cnt) {
+            if (plan) cufftDestroy(plan);
+            plan = 0;
+            if (cufftPlanMany(&plan, 3, n, inembed, 1, (int)HC, onembed, 1, (int)(2 * HC), CUFFT_Z2D, cnt) !=
+                CUFFT_SUCCESS) {
+                plan = 0;
+                rc = set_error(PBI4G_ERR_CUFFT, "counts: cufftPlanMany (%d maps of grid %d)", cnt, N);
+                break;
+            }
+            plan_batch = cnt;
+        }
+        cufftSetStream(plan, st);
+        const cufftResult r = cufftExecZ2D(plan, spec.as<cufftDoubleComplex>(), spec.as<cufftDoubleReal>());
+        if (r != CUFFT_SUCCESS) {
+            rc = set_error(PBI4G_ERR_CUFFT, "counts: cufftExecZ2D failed (%d)", (int)r);
+            break;
+        }
+        orbit_gather_kernel<<<grid_blocks((size_t)npad, 256, 152 * 8), 256, 0, st>>>(
+            N, nb, m0, cnt, nrep, npad, pts.as<unsigned>(), spec.as<double>(), rep.as<double>());
+        if (cudaPeekAtLastError() != cudaSuccess) {
+            rc = set_error(PBI4G_ERR_CUDA, "counts: gather launch: %s", cudaGetErrorString(cudaGetLastError()));
+            break;
+        }
+        ++*launches;
+    }
+    if (plan) {
+        cudaStreamSynchronize(st);
+        cufftDestroy(plan);
+    }
+    PBI4G_CHECK(rc);
+    spec.release();
     // all three factors are indicator maps of the same set (also for the cross
-    // enumeration, bispectrumI4.f90:887-896), so the non-cross pair layout applies
+    // enumeration, bispectrumI4.f90:887-896), so the non-cross pair layout
+    // applies: pairs from the plain copies [0, nb), q from the weighted copies
     TriPlan tp;
-    PBI4G_CHECK(tp.build(sh, 1, 0, 128));
+    PBI4G_CHECK(tp.build(sh, 1, 0, 128, nb));
     PBI4G_CHECK(S.ensure(sizeof(double) * tp.nslots));
-    PBI4G_CHECK(triangle_sums<double>(sh, tp, maps.as<double>(), 2 * HC, 2 * NH, partial, S.as<double>(), st, launches));
+    PBI4G_CHECK(triangle_sums<double>(sh, tp, rep.as<double>(), (size_t)npad, 64, 64, npad, partial, S.as<double>(),
+                                      false, st, launches));
     std::vector<double> Sh(tp.nslots);
     PBI4G_CUDA(cudaMemcpyAsync(Sh.data(), S.p, sizeof(double) * tp.nslots, cudaMemcpyDeviceToHost, st));
     PBI4G_CUDA(cudaStreamSynchronize(st));
     const double gridD = (double)N * N * N;
     sh.counts.resize(sh.itot);
-    std::vector<float> c32(sh.itot);
     double maxdev = 0;
     for (int64_t m = 0; m < sh.itot; m++) {
         double v = Sh[m] / gridD;
         long long c = llround(v);
         maxdev = std::max(maxdev, fabs(v - (double)c));
         sh.counts[m] = c;
-        c32[m] = (float)(gridD * (double)c);
     }
     if (maxdev > 0.25) {
         sh.counts.clear();
@@ -649,7 +745,6 @@ int triangle_counts(Shells &sh, cudaStream_t st, int64_t *launches) {
         std::lock_guard<std::mutex> g(g_counts_mutex);
         g_counts_cache[ckey] = sh.counts;
     }
-    (void)c32;
     return upload_counts(sh);
 }
 

@@ -44,7 +44,8 @@ struct TriPlan {
     DevBuf groups;       // int4 [ngroups]: (tile0, tile1, pair0, pair1)
     std::vector<int> group_tiles;
     int ntiles = 0, max_group_pairs = 0;
-    int build(const Shells &sh, int nsets, int cross, int max_pairs = 256);
+    // qoff: added to the map index of every non-cross q (a second copy of the maps)
+    int build(const Shells &sh, int nsets, int cross, int max_pairs = 256, int qoff = 0);
 };
 
 // Build the half spectra of all `count` maps on the map grid Nm into `out`
@@ -64,12 +65,14 @@ template <class R>
 int build_indicator_spectra(const Shells &sh, int m0, int count, typename Cx<R>::T *out, cudaStream_t st,
                             int64_t *launches);
 
-// Triangle sums on CUDA cores: S[slot] for all slots of tp, maps FP32/FP64 with
-// row stride rs (N+2 for padded C2R output).  maps: base of all maps, map m at
-// maps + m * mstride.  Result S (double, nslots) on device.
+// Triangle sums on CUDA cores: S[slot] for all slots of tp over K points,
+// maps FP32/FP64 laid out as rows of `rowlen` points with row stride rs
+// (rowlen + 2 for padded C2R output).  maps: base of all maps, map m at
+// maps + m * mstride.  Result S (double, nslots) on device; with accumulate the
+// sums are added to S (a contraction streamed in point ranges).
 template <class T>
-int triangle_sums(const Shells &sh, const TriPlan &tp, const T *maps, size_t mstride, int rs, DevBuf &partial,
-                  double *S, cudaStream_t st, int64_t *launches);
+int triangle_sums(const Shells &sh, const TriPlan &tp, const T *maps, size_t mstride, int rowlen, int rs,
+                  long long K, DevBuf &partial, double *S, bool accumulate, cudaStream_t st, int64_t *launches);
 
 // Output rows of measure_bk (9), measure_bk_multipoles (11), measure_bk_cross (5).
 // With bp the shot-noise factor is read from bp->pow_sn (graph-captured form).
@@ -79,7 +82,8 @@ int bk_finalize(const Shells &sh, int nsets, int cross, const double *S, const d
 // 1 / npart / kf^3 with kf^3 in real(4), as bk_finalize uses it
 double bk_pow_sn(float kf, int64_t npart);
 
-// Exact integer triangle counts (FP64 indicator maps + FP64 sums, rounded).
+// Exact integer triangle counts (FP64 indicator maps + FP64 sums over the
+// cube-group orbit representatives of the map grid, rounded).
 int triangle_counts(Shells &sh, cudaStream_t st, int64_t *launches);
 
 }  // namespace pbi4g

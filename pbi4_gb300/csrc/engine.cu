@@ -60,13 +60,26 @@ void Prof::end(cudaStream_t st) {
     cur_stage = -1;
 }
 
-size_t BkEngine::footprint(int N, int nb, int nsets, int cross, bool fp64) {
+size_t BkEngine::footprint(int N, int nb, int nsets, int cross, bool fp64, size_t budget) {
     const size_t HC = half_cells(N);  // upper bound: the map grid is at most N
     const int nm = cross ? 2 * nb : nsets * nb;
     const size_t cs = fp64 ? 16 : 8;
-    // half spectra (+ real FP32 maps for the FP32 forms) + a cuFFT work area of
-    // about one batch of the same size (upper estimate)
-    return (fp64 ? 2 : 3) * (size_t)nm * HC * cs + (size_t)nb * 8 + ((size_t)1 << 26);
+    // FP64: half spectra + a cuFFT work area of about one batch of the same size;
+    // FP32: the pruned transform's intermediates (at most two half-spectrum sets)
+    // + the real maps of one slab (upper estimates)
+    const size_t maps = (size_t)nm * HC * cs;
+    return 2 * maps + (fp64 ? 0 : (budget ? std::min(maps, budget) : maps)) + (size_t)nb * 8 + ((size_t)1 << 26);
+}
+
+int BkEngine::slab_planes(int Nm, size_t per_plane, size_t budget) {
+    // a slab holds whole 64-point chunks: q z-planes with q Nm^2 a multiple of 64
+    const long long plane = (long long)Nm * Nm;
+    int q = 1;
+    while ((q * plane) % 64) q *= 2;
+    if (!budget) return Nm;
+    long long zs = (long long)(budget / per_plane);
+    zs = std::max<long long>(q, zs / q * q);
+    return (int)std::min<long long>(Nm, zs);
 }
 
 int BkEngine::check(cudaStream_t st) {
@@ -112,9 +125,7 @@ int BkEngine::run(const typename Cx<R>::T *const src[3], const int fac[3], const
     }
     const size_t FCm = (size_t)N * N * N;
     // FP64: in-place C2R (padded rows); plain FP32: dense FP32 maps; tensor-core
-    // forms: the operand planes of the form (MapPlanes)
-    if (!fp64)
-        PBI4G_CHECK(dense.ensure(tc ? MapPlanes::bytes(form, (long long)FCm, nm, nb) : sizeof(float) * FCm * nm));
+    // forms: the operand planes of the form (MapPlanes), of one z-slab of the grid
     PBI4G_CUDA(cudaMemsetAsync(powsum.p, 0, sizeof(double) * 3 * nb, st));
     if (fp64) {
         PBI4G_CHECK(maps.ensure(sizeof(C) * HC * nm));
@@ -140,49 +151,66 @@ int BkEngine::run(const typename Cx<R>::T *const src[3], const int fac[3], const
             PBI4G_CHECK(mt.build(sh, nm));
             mt_nmaps = nm;
         }
-        PBI4G_CHECK(maps.ensure(mt.work_bytes()));
+        // per z-plane of a slab: the y pass's output U and the real maps (dense
+        // FP32 or the operand planes of the form)
+        const size_t per_point = tc ? MapPlanes::bytes(form, 1, nm, nb) : sizeof(float) * nm;
+        const size_t per_plane = per_point * (size_t)N * N + sizeof(float2) * (size_t)mt.kxtot * N;
+        const int zs = slab_planes(N, per_plane, map_budget);
+        slab_z = zs;
+        nslabs = (N + zs - 1) / zs;
+        PBI4G_CHECK(dense.ensure(per_point * (size_t)zs * N * N));
+        PBI4G_CHECK(maps.ensure(mt.work_bytes(zs)));
         const float2 *const *fsrc = reinterpret_cast<const float2 *const *>(src);
         pf.begin(6, st);
         PBI4G_CHECK(map_zpass(sh, mt, fsrc, fac, los, maps.as<float2>(), powsum.as<double>(), pow_mask, st,
                               launches));
         pf.end(st);
-        pf.begin(7, st);
-        PBI4G_CHECK(map_ypass(mt, maps.as<float2>(), st, launches));
-        pf.end(st);
-        pf.begin(10, st);
-        if (tc) {
-            if (form == 1) {
-                // largest |L_l(mu)| over mu^2 in [0, |los|^2]: bounds the delta_2 / delta_4 maps by the delta map
-                double lfac[3] = {1.0, 1.0, 1.0};
-                const double l2max = los ? los[0] * los[0] + los[1] * los[1] + los[2] * los[2] : 1.0;
-                for (int s = 1; s < nsets; s++) {
-                    if (fac[s] == 0) continue;
-                    double mx = 0;
-                    for (int k = 0; k <= 2000; k++) {
-                        const double m2 = l2max * k / 2000.0;
-                        const double L = fac[s] == 2 ? -0.5 + 1.5 * m2 : 0.375 + m2 * (-3.75 + 4.375 * m2);
-                        mx = std::max(mx, fabs(L));
-                    }
-                    lfac[s] = mx * 1.01;
+        if (tc && form == 1) {
+            // largest |L_l(mu)| over mu^2 in [0, |los|^2]: bounds the delta_2 / delta_4 maps by the delta map
+            double lfac[3] = {1.0, 1.0, 1.0};
+            const double l2max = los ? los[0] * los[0] + los[1] * los[1] + los[2] * los[2] : 1.0;
+            for (int s = 1; s < nsets; s++) {
+                if (fac[s] == 0) continue;
+                double mx = 0;
+                for (int k = 0; k <= 2000; k++) {
+                    const double m2 = l2max * k / 2000.0;
+                    const double L = fac[s] == 2 ? -0.5 + 1.5 * m2 : 0.375 + m2 * (-3.75 + 4.375 * m2);
+                    mx = std::max(mx, fabs(L));
                 }
-                PBI4G_CHECK(tm_map_exponents(sh, tmp, nm, powsum.as<double>(), pow_mask, lfac, st, launches));
+                lfac[s] = mx * 1.01;
             }
-            planes.carve(form, (long long)FCm, nm, nb, dense.p, form == 1 ? tmp.mexp.as<int>() : nullptr);
-            PBI4G_CHECK(map_xpass(mt, maps.as<float2>(), nullptr, &planes, st, launches));
-        } else {
-            PBI4G_CHECK(map_xpass(mt, maps.as<float2>(), dense.as<float>(), nullptr, st, launches));
+            PBI4G_CHECK(tm_map_exponents(sh, tmp, nm, powsum.as<double>(), pow_mask, lfac, st, launches));
         }
+        // y pass, x pass and triangle sums slab by slab (one slab: the whole grid)
+        for (int z0 = 0; z0 < N; z0 += zs) {
+            const int z1 = std::min(N, z0 + zs);
+            const long long spts = (long long)(z1 - z0) * N * N;
+            pf.begin(7, st);
+            PBI4G_CHECK(map_ypass(mt, maps.as<float2>(), st, launches, z0, z1));
+            pf.end(st);
+            pf.begin(10, st);
+            if (tc) {
+                planes.carve(form, spts, nm, nb, dense.p, form == 1 ? tmp.mexp.as<int>() : nullptr);
+                PBI4G_CHECK(map_xpass(mt, maps.as<float2>(), nullptr, &planes, st, launches, z0, z1));
+            } else {
+                PBI4G_CHECK(map_xpass(mt, maps.as<float2>(), dense.as<float>(), nullptr, st, launches, z0, z1));
+            }
+            pf.end(st);
+            pf.begin(8, st);
+            if (tc)
+                PBI4G_CHECK(triangle_sums_tm(sh, tmp, planes, partial, S.as<double>(), z0 > 0, st, launches));
+            else
+                PBI4G_CHECK(triangle_sums<float>(sh, tp, dense.as<float>(), (size_t)spts, N, N, spts, partial,
+                                                 S.as<double>(), z0 > 0, st, launches));
+            pf.end(st);
+        }
+    }
+    if (fp64) {
+        pf.begin(8, st);
+        PBI4G_CHECK(triangle_sums<R>(sh, tp, maps.as<R>(), 2 * HC, N, 2 * NH, (long long)FCm, partial,
+                                     S.as<double>(), false, st, launches));
         pf.end(st);
     }
-    pf.begin(8, st);
-    if (tc) {
-        PBI4G_CHECK(triangle_sums_tm(sh, tmp, planes, partial, S.as<double>(), st, launches));
-    } else if (fp64) {
-        PBI4G_CHECK(triangle_sums<R>(sh, tp, maps.as<R>(), 2 * HC, 2 * NH, partial, S.as<double>(), st, launches));
-    } else {
-        PBI4G_CHECK(triangle_sums<float>(sh, tp, dense.as<float>(), FCm, N, partial, S.as<double>(), st, launches));
-    }
-    pf.end(st);
     pf.begin(9, st);
     PBI4G_CHECK(bk_finalize(sh, cross ? 1 : nsets, cross, S.as<double>(), powsum.as<double>(), kf, npart, counts_f32,
                             d_bout, st, launches, bp));
@@ -247,7 +275,8 @@ static int check_config(const pbi4g_config *c) {
         return set_error(PBI4G_ERR_INVALID, "bad B binning");
     if (c->precision < PBI4G_PREC_FP32 || c->precision > PBI4G_PREC_TF32SPLIT)
         return set_error(PBI4G_ERR_INVALID, "unknown precision %d", c->precision);
-    for (int k = 0; k < 7; k++)
+    if (c->map_budget_mb < 0) return set_error(PBI4G_ERR_INVALID, "map budget must be >= 0");
+    for (int k = 0; k < 6; k++)
         if (c->reserved[k]) return set_error(PBI4G_ERR_INVALID, "reserved config fields must be zero");
     return PBI4G_OK;
 }
@@ -274,7 +303,7 @@ int pbi4g_plan_footprint(const pbi4g_config *cfg, int64_t npart_max, int64_t *by
     b += 2 * G * HC * cs;  // cuFFT work area (upper estimate)
     b += (size_t)npart_max * 32 + 5 * (size_t)cfg->nbins_ps * 8 * 1300;
     if (cfg->do_bispectrum) {
-        b += BkEngine::footprint(N, cfg->nbins_bs, cfg->multipoles ? 3 : 1, 0, fp64);
+        b += BkEngine::footprint(N, cfg->nbins_bs, cfg->multipoles ? 3 : 1, 0, fp64, (size_t)cfg->map_budget_mb << 20);
         b += (size_t)FC * 8 * (size_t)0;  // counts use a temporary FP64 map set, freed after the first box
     }
     *bytes = (int64_t)b;
@@ -306,6 +335,7 @@ int pbi4g_plan_create(const pbi4g_config *cfg, pbi4g_plan **out) {
             p->bk.nsets = cfg->multipoles ? 3 : 1;
             p->bk.cross = 0;
             p->bk.tc_mode = tc_mode_of(cfg->precision);
+            p->bk.map_budget = (size_t)cfg->map_budget_mb << 20;
         }
         cudaError_t e = cudaStreamSynchronize(p->st);
         if (e != cudaSuccess) { rc = set_error(PBI4G_ERR_CUDA, "plan create: %s", cudaGetErrorString(e)); break; }
@@ -350,6 +380,14 @@ int pbi4g_plan_map_work(const pbi4g_plan *plan, int64_t *zcols, int64_t *yplanes
     const bool built = plan->cfg.do_bispectrum && plan->bk.mt_nmaps >= 0;
     if (zcols) *zcols = built ? plan->bk.mt.tsize : 0;
     if (yplanes) *yplanes = built ? plan->bk.mt.usize : 0;
+    return PBI4G_OK;
+}
+
+int pbi4g_plan_map_slabs(const pbi4g_plan *plan, int32_t *slab_planes, int32_t *nslabs) {
+    if (!plan) return set_error(PBI4G_ERR_INVALID, "null plan");
+    const bool bk = plan->cfg.do_bispectrum != 0;
+    if (slab_planes) *slab_planes = bk ? plan->bk.slab_z : 0;
+    if (nslabs) *nslabs = bk ? plan->bk.nslabs : 0;
     return PBI4G_OK;
 }
 

@@ -24,9 +24,15 @@ struct BkEngine {
     int tp_nsets = -1, tp_cross = -1, tp_fp64 = -1;
     int nsets = 1, cross = 0;  // cross: 1 => q maps from the second field
     DevBuf maps;               // FP64: [nmaps][N][N][N/2+1] half spectra, padded real maps after the C2R;
-                               // FP32: the pruned transform's intermediates (MapTransform T, U)
+                               // FP32: the pruned transform's intermediates (T, and U of one slab)
     DevBuf dense;              // plain FP32: real maps [m][point]; tensor-core forms: the operand planes
     MapPlanes planes;          // tensor-core forms: the layout of `dense`
+    // FP32 forms: upper bound on the bytes of the slab-sized map buffers (the y
+    // pass's output in `maps` and the real maps in `dense`; 0: none).  When the
+    // whole grid's exceed it, the y pass, the x pass and the triangle sums stream
+    // over z-slabs of slab_z planes, the sums of each slab added to the last.
+    size_t map_budget = 0;
+    int slab_z = 0, nslabs = 0;  // of the last run
     cufftHandle inv = 0;       // FP64 maps: batched Z2D
     int inv_batch = 0, inv_N = 0;
     MapTransform mt;           // FP32 maps: pruned z / y / x passes
@@ -40,7 +46,9 @@ struct BkEngine {
         if (inv) cufftDestroy(inv);
     }
     int nmaps() const { return cross ? 2 * sh.nb : nsets * sh.nb; }
-    static size_t footprint(int N, int nb, int nsets, int cross, bool fp64);
+    static size_t footprint(int N, int nb, int nsets, int cross, bool fp64, size_t map_budget = 0);
+    // z-planes per slab on map grid Nm for `per_plane` bytes of slab buffers a z-plane
+    static int slab_planes(int Nm, size_t per_plane, size_t budget);
     // PBI4G_ERR_TIMEOUT if a bounded wait of a tensor-core launch gave up (synchronises st)
     int check(cudaStream_t st);
 

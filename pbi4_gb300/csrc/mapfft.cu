@@ -177,16 +177,19 @@ struct YArgs {
     int Nm;
     const MapInfo *info;
     const int2 *kxr;
-    const int2 *tiles;
-    int ntiles;
+    const int *gmap;
+    int z0, nz;        // the z-slab [z0, z0 + nz)
+    int nflat;         // transforms: kxtot nz
     const unsigned char *tab;
     fftd::FftDesc fd;
     const float2 *T;
     float2 *U;
 };
 
-// y pass: tile = (map m, 32 consecutive transforms t = kx Nm + z); input
-// ky in [-r(kx), r(kx)] from T, output U[m][kx][z][y].
+// y pass of one z-slab: tile = 32 consecutive flat transforms f = g nz + z - z0
+// (g = kxc + kx: the flat kx index over all maps, so a tile may span maps); a
+// lane reads column kx of its map, ky in [-r(kx), r(kx)], from T and the
+// transform lands in U[f][y].
 __global__ void __launch_bounds__(kThreads) map_ypass_kernel(const YArgs a) {
     extern __shared__ __align__(16) unsigned char ysm[];
     const fftd::FftDesc &fd = a.fd;
@@ -198,14 +201,15 @@ __global__ void __launch_bounds__(kThreads) map_ypass_kernel(const YArgs a) {
     load_tables(a.tab, fd, tw, ent, perm);
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
-        const int2 tl = a.tiles[tile];
-        const int m = tl.x, t0 = tl.y;
-        const MapInfo mi = a.info[m];
-        const int ntr = mi.kxn * Nm;
-        const int t = t0 + lane;
-        const bool valid = t < ntr;
-        const int kx = valid ? t / Nm : 0, z = valid ? t - kx * Nm : 0;
+    const int ntiles = (a.nflat + 31) / 32;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int t0 = tile * 32;
+        const int f = t0 + lane;
+        const bool valid = f < a.nflat;
+        const int g = valid ? f / a.nz : 0, z = a.z0 + (valid ? f - g * a.nz : 0);
+        const int m = a.gmap[g];
+        const MapInfo &mi = a.info[m];
+        const int kx = g - mi.kxc;
         const int2 rc = valid ? a.kxr[mi.kx0 + kx] : make_int2(-1, 0);  // (r, first column)
         const float2 *in = a.T + mi.tbase + (size_t)(rc.y + rc.x) * Nm + z;  // column ky = 0
         for (int i = warp; i < Nm; i += nw) {
@@ -215,8 +219,8 @@ __global__ void __launch_bounds__(kThreads) map_ypass_kernel(const YArgs a) {
         __syncthreads();
         run_dit(fd, buf, ent, tw, warp, nw, lane);
         for (int l = warp; l < 32; l += nw) {
-            if (t0 + l >= ntr) break;
-            float2 *o = a.U + mi.ubase + (size_t)(t0 + l) * Nm;
+            if (t0 + l >= a.nflat) break;
+            float2 *o = a.U + (size_t)(t0 + l) * Nm;
             for (int y = lane; y < Nm; y += 32) o[y] = buf[y * kP + l];
         }
         __syncthreads();
@@ -234,7 +238,8 @@ struct XArgs {
     void *bhi, *blo;    // oform 0 / 1 / 2: operand planes (MapPlanes)
     float2 *a32;
     const int *mexp;
-    long long npts;
+    long long npts;     // points of the slab (the per-map stride of the dense maps)
+    int row_lo, nrows;  // the slab's (z, y) rows: [row_lo, row_lo + nrows), row = z Nm + y
     float inv_nm;
 };
 
@@ -332,17 +337,18 @@ __global__ void __launch_bounds__(kThreads, PF <= 9 ? 4 : 2) map_xpass_kernel(co
     load_tables(a.tab, fd, tw, ent, perm);
     for (int i = threadIdx.x; i < Nm; i += blockDim.x) xt[i] = a.xtw[i];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int plane = Nm * Nm, tpm = (plane + 31) / 32, ntiles = tpm * a.count;
+    const int row_hi = a.row_lo + a.nrows, tpm = (a.nrows + 31) / 32, ntiles = tpm * a.count;
     float2 pre[PF];
+    // U holds the slab: column kx of map m, row (z, y) at ((kxc + kx) nrows + row - row_lo)
     auto fetch = [&](int m, int row0) {
-        const bool ok = row0 + lane < plane;
+        const bool ok = row0 + lane < row_hi;
         const MapInfo &mi = a.info[m];
         const int kxn = mi.kxn;
-        const float2 *src = a.U + mi.ubase + row0 + lane;
+        const float2 *src = a.U + (size_t)mi.kxc * a.nrows + (row0 - a.row_lo) + lane;
 #pragma unroll
         for (int i = 0; i < PF; i++) {
             const int k = warp + i * nw;
-            pre[i] = (k < kxn && ok) ? __ldcs(src + (size_t)k * plane) : czero();
+            pre[i] = (k < kxn && ok) ? __ldcs(src + (size_t)k * a.nrows) : czero();
         }
     };
     // (map, tile within the map) of this CTA's tiles, advanced without divisions
@@ -353,10 +359,10 @@ __global__ void __launch_bounds__(kThreads, PF <= 9 ? 4 : 2) map_xpass_kernel(co
         rr += gr;
         if (rr >= tpm) { rr -= tpm; mm++; }
     };
-    if (blockIdx.x < ntiles) fetch(m, r * 32);
+    if (blockIdx.x < ntiles) fetch(m, a.row_lo + r * 32);
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int row0 = r * 32;
-        const int nrows = min(32, plane - row0);
+        const int row0 = a.row_lo + r * 32;
+        const int nrows = min(32, row_hi - row0);
         int mn = m, rn = r;
         advance(mn, rn);
         __syncthreads();
@@ -365,7 +371,7 @@ __global__ void __launch_bounds__(kThreads, PF <= 9 ? 4 : 2) map_xpass_kernel(co
             const int k = warp + i * nw;
             if (k < KX) xr[k * kP + lane] = pre[i];
         }
-        if (tile + (int)gridDim.x < ntiles) fetch(mn, rn * 32);
+        if (tile + (int)gridDim.x < ntiles) fetch(mn, a.row_lo + rn * 32);
         __syncthreads();
         for (int k = warp; k <= M / 2; k += nw) {
             const int kc = M - k;
@@ -384,7 +390,8 @@ __global__ void __launch_bounds__(kThreads, PF <= 9 ? 4 : 2) map_xpass_kernel(co
         if (a.oform < 0) {
             // dense FP32 maps: one warp per row, x[2j], x[2j+1] = z[j]
             for (int l = warp; l < nrows; l += nw) {
-                float2 *o = reinterpret_cast<float2 *>(a.out + (size_t)m * a.npts + ((size_t)row0 + l) * Nm);
+                float2 *o =
+                    reinterpret_cast<float2 *>(a.out + (size_t)m * a.npts + ((size_t)(row0 - a.row_lo) + l) * Nm);
                 for (int j = lane; j < M; j += 32) o[j] = buf[j * kP + l];
             }
         } else {
@@ -394,7 +401,7 @@ __global__ void __launch_bounds__(kThreads, PF <= 9 ? 4 : 2) map_xpass_kernel(co
             const float sb = a.oform == 1 ? exp2f((float)a.mexp[m]) : 1.f;  // B planes: x 2^e
             const float sa = sb * (a.oform == 1 ? 1.f / 128.f : 1.f);       // pair factors: x 2^(e-7)
             const int npt = nrows * Nm;
-            const size_t c0 = ((size_t)row0 * Nm) >> 6;
+            const size_t c0 = ((size_t)(row0 - a.row_lo) * Nm) >> 6;
             // a lane takes W consecutive points of one row (Nm % W == 0), 64 / W lanes a chunk row
             if (Nm % 8 == 0)
                 store_planes<8>(a, buf, m, nrows, npt, c0, sb, sa, warp, nw, lane);
@@ -469,7 +476,8 @@ int MapTransform::build(const Shells &s, int nm) {
         kxmax = std::max(kxmax, kxn[b]);
     }
     info_h.assign(nm, MapInfo{});
-    std::vector<int2> zt, yt;
+    std::vector<int2> zt;
+    std::vector<int> gm;
     long long tb = 0, ub = 0;
     for (int m = 0; m < nm; m++) {
         const int b = m % nb;
@@ -481,18 +489,20 @@ int MapTransform::build(const Shells &s, int nm) {
         mi.kx0 = kx0[b];
         mi.k2lo = k2lo[b];
         mi.k2hi = k2hi[b];
-        mi.pad = 0;
+        mi.kxc = (int)gm.size();
         mi.tbase = tb;
         mi.ubase = ub;
         tb += (long long)ncol[b] * Nm;
         ub += (long long)kxn[b] * Nm * Nm;
         for (int c = 0; c < ncol[b]; c += 32) zt.push_back(make_int2(m, c));
-        for (int t = 0; t < kxn[b] * Nm; t += 32) yt.push_back(make_int2(m, t));
+        for (int kx = 0; kx < kxn[b]; kx++) gm.push_back(m);
     }
     tsize = tb;
     usize = ub;
     nzt = (int)zt.size();
-    nyt = (int)yt.size();
+    kxtot = (int)gm.size();
+    if ((long long)kxtot * Nm >= (1LL << 31))
+        return set_error(PBI4G_ERR_UNSUPPORTED, "map transform: %d kx columns of grid %d", kxtot, Nm);
     std::vector<float2> xt(Nm);
     for (int k = 0; k < Nm; k++) xt[k] = make_float2((float)cos(2 * M_PI * k / Nm), (float)sin(2 * M_PI * k / Nm));
     PBI4G_CHECK(upload_plan(tab_z, pz));
@@ -502,7 +512,7 @@ int MapTransform::build(const Shells &s, int nm) {
     PBI4G_CHECK(upload(kxr, kxr_h.data(), sizeof(int2) * kxr_h.size()));
     PBI4G_CHECK(upload(info, info_h.data(), sizeof(MapInfo) * info_h.size()));
     PBI4G_CHECK(upload(ztiles, zt.data(), sizeof(int2) * zt.size()));
-    PBI4G_CHECK(upload(ytiles, yt.data(), sizeof(int2) * yt.size()));
+    PBI4G_CHECK(upload(gmap, gm.data(), sizeof(int) * gm.size()));
     return PBI4G_OK;
 }
 
@@ -536,29 +546,38 @@ int map_zpass(const Shells &sh, const MapTransform &mt, const float2 *const src[
     return PBI4G_OK;
 }
 
-int map_ypass(const MapTransform &mt, float2 *work, cudaStream_t st, int64_t *launches) {
-    if (mt.nyt == 0) return PBI4G_OK;
+int map_ypass(const MapTransform &mt, float2 *work, cudaStream_t st, int64_t *launches, int z0, int z1) {
+    if (z1 < 0) z1 = mt.Nm;
+    if (z0 < 0 || z1 > mt.Nm || z0 >= z1)
+        return set_error(PBI4G_ERR_INVALID, "y pass: slab [%d, %d) of grid %d", z0, z1, mt.Nm);
+    if (mt.kxtot == 0) return PBI4G_OK;
     YArgs a;
     a.Nm = mt.Nm;
     a.info = mt.info.as<MapInfo>();
     a.kxr = mt.kxr.as<int2>();
-    a.tiles = mt.ytiles.as<int2>();
-    a.ntiles = mt.nyt;
+    a.gmap = mt.gmap.as<int>();
+    a.z0 = z0;
+    a.nz = z1 - z0;
+    a.nflat = mt.kxtot * a.nz;
     a.tab = static_cast<const unsigned char *>(mt.tab_z.p);
     a.fd = mt.pz.d;
     a.T = work;
     a.U = work + mt.tsize;
+    const int ntiles = (a.nflat + 31) / 32;
     const size_t smem = table_smem(mt.pz.d) + sizeof(float2) * (size_t)mt.Nm * kP;
     PBI4G_CUDA(cudaFuncSetAttribute(map_ypass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    map_ypass_kernel<<<grid_for((const void *)map_ypass_kernel, kThreads, smem, mt.nyt), kThreads, smem, st>>>(a);
+    map_ypass_kernel<<<grid_for((const void *)map_ypass_kernel, kThreads, smem, ntiles), kThreads, smem, st>>>(a);
     PBI4G_LAUNCH_CHECK();
     ++*launches;
     return PBI4G_OK;
 }
 
 int map_xpass(const MapTransform &mt, const float2 *work, float *out, const MapPlanes *planes, cudaStream_t st,
-              int64_t *launches) {
+              int64_t *launches, int z0, int z1) {
     if (mt.nmaps == 0) return PBI4G_OK;
+    if (z1 < 0) z1 = mt.Nm;
+    if (z0 < 0 || z1 > mt.Nm || z0 >= z1)
+        return set_error(PBI4G_ERR_INVALID, "x pass: slab [%d, %d) of grid %d", z0, z1, mt.Nm);
     XArgs a;
     a.Nm = mt.Nm;
     a.count = mt.nmaps;
@@ -575,15 +594,18 @@ int map_xpass(const MapTransform &mt, const float2 *work, float *out, const MapP
     a.blo = planes ? planes->blo : nullptr;
     a.a32 = planes ? reinterpret_cast<float2 *>(planes->a32) : nullptr;
     a.mexp = planes ? planes->mexp : nullptr;
-    a.npts = (long long)mt.Nm * mt.Nm * mt.Nm;
+    a.npts = (long long)(z1 - z0) * mt.Nm * mt.Nm;
+    a.row_lo = z0 * mt.Nm;
+    a.nrows = (z1 - z0) * mt.Nm;
     a.inv_nm = 1.0f / (float)mt.Nm;
+    // planes: whole 64-point chunks per slab
     if (planes && (planes->form < 0 || planes->form > 2 || (planes->form == 1 && !planes->mexp) ||
-                   planes->npts != a.npts || planes->nmaps != mt.nmaps))
+                   planes->npts != a.npts || planes->nmaps != mt.nmaps || a.npts % MapPlanes::kChunk))
         return set_error(PBI4G_ERR_INVALID, "x pass: operand planes do not match the maps");
     const int M = mt.Nm / 2, warps = kThreads / 32, pf = (mt.kxmax + warps - 1) / warps;
     const size_t smem =
         table_smem(mt.px.d) + sizeof(float2) * ((size_t)mt.Nm + (size_t)mt.kxmax * kP + (size_t)M * kP);
-    const long long ntiles = ((long long)mt.Nm * mt.Nm + 31) / 32 * mt.nmaps;
+    const long long ntiles = ((long long)a.nrows + 31) / 32 * mt.nmaps;
     if (ntiles >= (1LL << 31)) return set_error(PBI4G_ERR_UNSUPPORTED, "x pass: %lld tiles", ntiles);
     const int work_tiles = (int)ntiles;
     auto launch = [&](auto kern) -> int {

@@ -26,14 +26,15 @@ struct MapInfo {
     int col0;         // first column of the shell in MapTransform::cols
     int kx0;          // first (shell, kx) entry in MapTransform::kxr
     int k2lo, k2hi;   // the shell's modes are exactly those with k2lo <= |k|^2 <= k2hi
-    int pad;
+    int kxc;          // first flat kx index of the map (sum of kxn over the maps before it)
     long long tbase;  // first float2 of the map in T ([column][z])
-    long long ubase;  // first float2 of the map in U ([kx][z][y])
+    long long ubase;  // first float2 of the map in U of the whole grid ([kx][z][y]) = kxc Nm^2
 };
 
 // Tensor-core operands of the maps ("planes"), written by the x pass for the
 // tensor-core forms.  Points are grouped in chunks of 64 consecutive points
-// (point = (z Nm + y) Nm + x; Nm^3 is a multiple of 64), and every array is
+// (point = (z Nm + y) Nm + x, counted from the first point of the z-slab the
+// planes hold; the slab's point count is a multiple of 64), and every array is
 // chunk-major, [chunk][map][64 points], so the operand tile of a chunk (64 maps
 // x 64 points) is one contiguous block:
 //   form 1 (FP16 hi+lo): bhi, blo FP16 with v 2^mexp[m] = hi + lo (|v 2^mexp| <= 2^14);
@@ -78,24 +79,32 @@ struct MapTransform {
     DevBuf cols;          // int2 [sum ncol]: (kx, ky) of every column of every shell
     DevBuf kxr;           // int2 [sum kxn]: (r(kx), first column of kx) per shell
     DevBuf info;          // MapInfo [nmaps]
-    DevBuf ztiles, ytiles;  // int2 (map, first column / first (kx, z) transform) per 32-wide tile
-    int nzt = 0, nyt = 0;
-    long long tsize = 0, usize = 0;  // float2 elements of T and U
+    DevBuf ztiles;        // int2 (map, first column) per 32-wide z-pass tile
+    DevBuf gmap;          // int [kxtot]: map of each flat kx index
+    int nzt = 0, kxtot = 0;
+    long long tsize = 0, usize = 0;  // float2 elements of T and of U for the whole grid (kxtot Nm^2)
     std::vector<MapInfo> info_h;
     int build(const Shells &sh, int nmaps);
-    size_t work_bytes() const { return sizeof(float2) * (size_t)(tsize + usize); }
+    // T + U for z-slabs of zs planes (U holds one slab: kxtot zs Nm elements)
+    size_t work_bytes(int zs) const { return sizeof(float2) * (size_t)(tsize + (long long)kxtot * zs * Nm); }
+    size_t work_bytes() const { return work_bytes(Nm); }
 };
 
 // z pass (shell spectra + z transform) of all maps into work[0, tsize).
 // src[s] / fac[s] / los / powsum / pow_mask as for build_map_spectra.
 int map_zpass(const Shells &sh, const MapTransform &mt, const float2 *const src[3], const int fac[3],
               const double los[3], float2 *work, double *powsum, int pow_mask, cudaStream_t st, int64_t *launches);
-// y pass: work[0, tsize) -> work[tsize, tsize + usize)
-int map_ypass(const MapTransform &mt, float2 *work, cudaStream_t st, int64_t *launches);
-// x pass: real maps from work[tsize, ...): dense FP32 [m][z][y][x] into `out`
-// when planes is null, else the tensor-core operand planes.
+// y pass of the z-slab [z0, z1) (z1 < 0: Nm): work[0, tsize) -> U at
+// work[tsize, ...) = [kx flat][z - z0][y], i.e. float2 index
+// ((kxc + kx) (z1 - z0) + z - z0) Nm + y for map m, column kx of it.
+int map_ypass(const MapTransform &mt, float2 *work, cudaStream_t st, int64_t *launches, int z0 = 0, int z1 = -1);
+// x pass: real maps from the U that map_ypass wrote for the same z-slab
+// [z0, z1) (z1 < 0: Nm): dense FP32 [m][z][y][x] into `out` when planes is
+// null, else the tensor-core operand planes, as if the grid held the slab's
+// points alone (map stride (z1 - z0) Nm^2 for the dense maps; planes->npts =
+// that count, a multiple of 64).
 int map_xpass(const MapTransform &mt, const float2 *work, float *out, const MapPlanes *planes, cudaStream_t st,
-              int64_t *launches);
+              int64_t *launches, int z0 = 0, int z1 = -1);
 
 // Host check of the in-place FFT plan: n-point inverse DFTs of `batch`
 // transforms in[t][n] -> out[t][k] on the CPU with the kernels' butterflies.

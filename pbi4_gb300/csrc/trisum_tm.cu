@@ -677,7 +677,7 @@ int tm_map_exponents(const Shells &sh, TmPlan &tp, int nmaps, const double *pows
 }
 
 int triangle_sums_tm(const Shells &sh, TmPlan &tp, const MapPlanes &pl, DevBuf &partial, double *S,
-                     cudaStream_t st, int64_t *launches) {
+                     bool accumulate, cudaStream_t st, int64_t *launches) {
     const int form = pl.form;
     if (!tm_supported(sh))
         return set_error(PBI4G_ERR_UNSUPPORTED, "tensor-core triangle sums: map grid %d, %d shells", sh.Nm, sh.nb);
@@ -685,7 +685,7 @@ int triangle_sums_tm(const Shells &sh, TmPlan &tp, const MapPlanes &pl, DevBuf &
     if (tp.nunits == 0) return PBI4G_OK;
     if (form == 1 && (!pl.mexp || pl.mexp != tp.mexp.as<int>()))
         return set_error(PBI4G_ERR_INVALID, "tensor-core triangle sums: FP16 planes without the plan's exponents");
-    if (pl.nb != sh.nb || pl.npts != (long long)sh.Nm * sh.Nm * sh.Nm || pl.nchunks * kKC != pl.npts)
+    if (pl.nb != sh.nb || pl.npts < kKC || pl.npts > (long long)sh.Nm * sh.Nm * sh.Nm || pl.nchunks * kKC != pl.npts)
         return set_error(PBI4G_ERR_INVALID, "tensor-core triangle sums: operand planes do not match the shells");
     static_assert(MapPlanes::kChunk == kKC, "a planes chunk is a contraction chunk");
     CUtensorMap tmA, tmBh, tmBl;
@@ -747,7 +747,7 @@ int triangle_sums_tm(const Shells &sh, TmPlan &tp, const MapPlanes &pl, DevBuf &
     if (form == 0) PBI4G_CHECK(launch_tm<kFormTF32>(tmA, tmBh, tmBl, a, smem, grid, st));
     else if (form == 1) PBI4G_CHECK(launch_tm<kFormF16>(tmA, tmBh, tmBl, a, smem, grid, st));
     else PBI4G_CHECK(launch_tm<kFormBF16>(tmA, tmBh, tmBl, a, smem, grid, st));
-    PBI4G_CHECK(reduce_partials(tp.nslots, a.ksplit, partial.as<double>(), S, st));
+    PBI4G_CHECK(reduce_partials(tp.nslots, a.ksplit, partial.as<double>(), S, accumulate, st));
     *launches += 2;
     return PBI4G_OK;
 }

@@ -26,13 +26,15 @@ int tm_map_exponents(const Shells &sh, TmPlan &tp, int nmaps, const double *pows
 
 // S[slot] for every (triangle, set) slot on the tensor cores, from the operand
 // planes the x pass wrote (pl.form: 0 TF32 hi+lo, 1 FP16 hi+lo with pl.mexp ==
-// tp.mexp, 2 BF16).
+// tp.mexp, 2 BF16).  The planes may hold one slab of the map grid's points
+// (pl.npts <= Nm^3); with accumulate the slab's sums are added to S.
 int triangle_sums_tm(const Shells &sh, TmPlan &tp, const MapPlanes &pl, DevBuf &partial, double *S,
-                     cudaStream_t st, int64_t *launches);
+                     bool accumulate, cudaStream_t st, int64_t *launches);
 // PBI4G_ERR_TIMEOUT if a bounded wait inside the last launch gave up (synchronises st).
 int tm_check_error(TmPlan &tp, cudaStream_t st);
 
-// deterministic reduction of [ksplit][nslots] partial sums (bispec.cu)
-int reduce_partials(int nslots, int ksplit, const double *partial, double *S, cudaStream_t st);
+// deterministic reduction of [ksplit][nslots] partial sums into S (added to S
+// with accumulate) (bispec.cu)
+int reduce_partials(int nslots, int ksplit, const double *partial, double *S, bool accumulate, cudaStream_t st);
 
 }  // namespace pbi4g

@@ -37,6 +37,9 @@ class EstimatorConfig:
     nbins_bs: int | None = None
     iopen: bool = True
     precision: str = "fp32"
+    # FP32 forms: MiB the real-space shell maps may hold at once (0: no bound);
+    # above it the maps are made and contracted z-slab by z-slab
+    map_budget_mb: int = 0
     extra: dict = field(default_factory=dict)
 
     def __post_init__(self):
@@ -70,13 +73,14 @@ class EstimatorConfig:
         c.kbin_bs, c.kcenter_bs, c.nbins_bs = float(self.kbin_bs), float(self.kcenter_bs), int(self.nbins_bs)
         c.iopen = int(bool(self.iopen))
         c.precision = PRECISIONS[self.precision]
+        c.map_budget_mb = int(self.map_budget_mb)
         return c
 
     def key(self):
         return (int(self.grid), float(self.box), int(self.nintp), bool(self.interlacing), bool(self.multipoles),
                 tuple(self.los), float(self.kbin_ps), float(self.kcenter_ps), int(self.nbins_ps),
                 bool(self.do_bispectrum), float(self.kbin_bs), float(self.kcenter_bs), int(self.nbins_bs),
-                bool(self.iopen), self.precision)
+                bool(self.iopen), self.precision, int(self.map_budget_mb))
 
 
 def footprint(cfg: EstimatorConfig, npart_max: int) -> int:
@@ -112,6 +116,12 @@ class Estimator:
         t, u = ctypes.c_int64(), ctypes.c_int64()
         check(lib().pbi4g_plan_map_work(self._h, ctypes.byref(t), ctypes.byref(u)))
         return t.value, u.value
+
+    def map_slabs(self):
+        """(z-planes per slab, slabs per box) of the last bispectrum run."""
+        z, n = ctypes.c_int32(), ctypes.c_int32()
+        check(lib().pbi4g_plan_map_slabs(self._h, ctypes.byref(z), ctypes.byref(n)))
+        return z.value, n.value
 
     # -- lifecycle
     def close(self):

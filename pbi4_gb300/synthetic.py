@@ -53,3 +53,43 @@ def zeldovich_box(nside: int, box: float, n_s: float = -1.5, rms_disp: float = 5
     Q = np.stack(np.meshgrid(q, q, q, indexing="ij"))
     pos = (Q + psi).reshape(3, -1)
     return normalise(pos, box)
+
+
+def zeldovich_box_device(nside: int, box: float, n_s: float = -1.5, rms_disp: float = 5.0, f_growth: float = 0.7,
+                         los: int = 2, seed: int = 2, rsd: bool = True, device: str = "cuda"):
+    """zeldovich_box generated with torch on `device` (for lattices whose numpy
+    FFTs would take minutes): the same field statistics and construction from a
+    torch random stream, so not the same particles as zeldovich_box(seed).
+    Returns a (3, nside^3) float64 tensor on the device."""
+    import torch
+
+    n = nside
+    f64 = torch.float64
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    kf = 2 * np.pi / box
+    kx = torch.fft.fftfreq(n, 1.0 / n, dtype=f64, device=device) * kf
+    kz = torch.fft.rfftfreq(n, 1.0 / n, dtype=f64, device=device) * kf
+    k2 = kx[:, None, None] ** 2 + kx[None, :, None] ** 2 + kz[None, None, :] ** 2
+    k2[0, 0, 0] = 1.0
+    amp = k2 ** (n_s / 4.0)
+    amp[0, 0, 0] = 0.0
+    dk = torch.fft.rfftn(torch.randn((n, n, n), generator=g, dtype=f64, device=device)) * amp
+    del amp
+    dk /= k2
+    del k2
+    pos = torch.empty((3, n, n, n), dtype=f64, device=device)
+    for a, K in enumerate((kx[:, None, None], kx[None, :, None], kz[None, None, :])):
+        pos[a] = torch.fft.irfftn(1j * K * dk, s=(n, n, n))
+    del dk
+    pos *= rms_disp / torch.sqrt(torch.mean(torch.sum(pos ** 2, dim=0)))
+    if rsd:
+        pos[los] *= 1.0 + f_growth
+    q = (torch.arange(n, dtype=f64, device=device) + 0.5) * (box / n)
+    pos[0] += q[:, None, None]
+    pos[1] += q[None, :, None]
+    pos[2] += q[None, None, :]
+    pos = pos.reshape(3, -1)
+    # pbi4.py:242-243
+    pos = torch.remainder(pos + box, box) / box
+    return torch.clamp_max(pos, 1.0 - float(np.nextafter(0, 1)))

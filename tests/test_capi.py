@@ -45,12 +45,13 @@ def test_config_struct_layout(tmp_path):
     c = tmp_path / "t.c"
     c.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "pbi4gpu.h"\n'
                  'int main(void){printf("%zu %zu %zu %zu\\n", sizeof(pbi4g_config), offsetof(pbi4g_config, los),'
-                 ' offsetof(pbi4g_config, precision), offsetof(pbi4g_config, reserved));return 0;}\n')
+                 ' offsetof(pbi4g_config, precision), offsetof(pbi4g_config, reserved));'
+                 'printf("%zu\\n", offsetof(pbi4g_config, map_budget_mb));return 0;}\n')
     exe = tmp_path / "t"
     subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(c), "-o", str(exe)], check=True)
     got = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
     C = _lib.Config
-    want = [ctypes.sizeof(C), C.los.offset, C.precision.offset, C.reserved.offset]
+    want = [ctypes.sizeof(C), C.los.offset, C.precision.offset, C.reserved.offset, C.map_budget_mb.offset]
     assert [int(x) for x in got] == want
 
 

@@ -77,3 +77,33 @@ def test_tensor_core_forms_repeatable(box_za, precision):
     _, b2 = est.run_host(box_za)
     np.testing.assert_array_equal(b1[[0, 1, 2, 8]], b2[[0, 1, 2, 8]])
     assert np.max(np.abs(b1 - b2) / np.maximum(np.abs(b1), 1e-300)) < 1e-12
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp16split", "tf32split", "bf16"])
+def test_map_slabs_match_whole_grid(box_za, precision):
+    """A map budget below the whole grid's slab buffers streams the y pass, the
+    x pass and the triangle sums over z-slabs (here with an uneven last slab);
+    the results equal the one-slab run up to the order of the FP64 slab
+    additions, and the counts and k columns are exact."""
+    p = ref_params(64, 1000.0, 4, True, True, kbin=2.0, kcenter=2.0)
+    p["nbins_bisp"] = 10
+    whole = Estimator(EstimatorConfig.from_params(p, precision=precision))
+    pw, bw = whole.run_host(box_za)
+    nm_grid, nmaps = whole.map_grid, whole.nmaps
+    assert whole.map_slabs() == (nm_grid, 1)
+    # slab buffers per z-plane: the y pass's output (kxtot Nm complex) + the real maps
+    kxtot = whole.map_work()[1] // nm_grid ** 2
+    per_point = {"fp32": 4 * nmaps, "fp16split": 4 * nmaps + 4 * 10, "tf32split": 8 * nmaps + 4 * 10,
+                 "bf16": 2 * nmaps + 4 * 10}[precision]
+    per_plane = per_point * nm_grid ** 2 + 8 * kxtot * nm_grid
+    mb = next(m for m in range(1, 64) if (m << 20) // per_plane >= 2 and nm_grid % ((m << 20) // per_plane))
+    zs = (mb << 20) // per_plane
+    sl = Estimator(EstimatorConfig.from_params(p, precision=precision, map_budget_mb=mb))
+    ps, bs = sl.run_host(box_za)
+    assert sl.map_slabs() == (zs, -(-nm_grid // zs)), (sl.map_slabs(), zs)
+    # P does not depend on the slabs; its FP32 per-block bin sums are added in
+    # scheduling order, so two runs agree to ~1e-8, not bitwise
+    np.testing.assert_allclose(ps, pw, rtol=1e-6, atol=0)
+    np.testing.assert_array_equal(bs[[0, 1, 2, 8]], bw[[0, 1, 2, 8]])
+    errs, pow_err = b_errors(bs, bw)
+    assert max(errs) < 1e-6 and pow_err < 1e-12, (errs, pow_err)
