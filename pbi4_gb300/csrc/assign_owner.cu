@@ -117,15 +117,62 @@ struct PrepOut {
     int w;
 };
 
+// first_and_h for both grids from one FP64 product and sum, v = N p + 1 (the
+// reference's two roundings; FP64 is a slow pipe on this part).  The shifted
+// grid's v - 1/2 is exact, and floor(v), v - floor(v) and its half-cell
+// variants are read from v's bits as integers, exactly; each offset then takes
+// the single FP32 rounding first_and_h gives it, so cells and offsets are
+// bit-identical to it.  v outside [1, 2^20) (positions outside [0, 1]) takes
+// first_and_h.
+__device__ __forceinline__ void first_cells(double p, int N, int nintp, bool interlaced, int &f0, float &h0, int &f1,
+                                            float &h1) {
+    const double v = (double)N * p + 1.0;
+    if (!(v >= 1.0 && v < 1048576.0)) {
+        first_and_h(p, N, nintp, false, !interlaced, f0, h0);
+        if (interlaced) first_and_h(p, N, nintp, true, false, f1, h1);
+        else { f1 = f0; h1 = 0.f; }
+        return;
+    }
+    const long long bits = __double_as_longlong(v);
+    const int sh = 52 - ((int)(bits >> 52) - 1023);  // fraction bits of v: 33..52
+    const long long mant = (bits & 0xFFFFFFFFFFFFFLL) | (1LL << 52);
+    const long long one = 1LL << sh, half = one >> 1;
+    const int iv = (int)(mant >> sh);                 // floor(v)
+    const long long fr = mant & (one - 1);            // (v - floor(v)) 2^sh
+    const bool up = fr >= half;                       // v - floor(v) >= 1/2
+    const float scale = __int_as_float((127 - sh) << 23);  // 2^-sh
+    auto off = [&](long long x) { return __ll2float_rn(x) * scale; };
+    auto cell = [&](int t) {
+        int f = wrap_cell(t, N);
+        if (f < 0) f += N;
+        return (f < 0 || f >= N) ? 0 : f;
+    };
+    const int ivs = up ? iv : iv - 1;                 // floor(v - 1/2)
+    const long long frs = up ? fr - half : fr + half;  // (v - 1/2 - floor(v - 1/2)) 2^sh
+    if (nintp == 4) {
+        f0 = cell(iv - 2); h0 = off(fr);
+        f1 = cell(ivs - 2); h1 = off(frs);
+    } else if (nintp == 3) {
+        // nint(v) = floor(v) + up; nint(v - 1/2) = floor(v)
+        f0 = cell(iv + (up ? 1 : 0) - 2); h0 = off(up ? fr - one : fr);
+        f1 = cell(iv - 2); h1 = off(fr - half);
+    } else if (nintp == 2) {
+        f0 = cell(iv); h0 = off((!interlaced && up) ? fr - one : fr);
+        f1 = cell(ivs); h1 = off(frs);
+    } else {
+        f0 = cell(iv + (up ? 1 : 0) - 1); h0 = 0.f;
+        f1 = cell(iv - 1); h1 = 0.f;
+    }
+    if (!interlaced) { f1 = f0; h1 = 0.f; }
+}
+
 __device__ __forceinline__ PRec make_rec(const double *__restrict__ pos, int64_t stride, int64_t i, int N, int nintp,
                                          int interlaced, int lo[3]) {
     PRec r;
     int f[2][3];
     for (int c = 0; c < 3; c++) {
         const double p = pos[(size_t)c * stride + i];
-        first_and_h(p, N, nintp, false, !interlaced, f[0][c], r.h[0][c]);
-        if (interlaced) first_and_h(p, N, nintp, true, false, f[1][c], r.h[1][c]);
-        else { f[1][c] = f[0][c]; r.h[1][c] = 0.f; }
+        first_cells(p, N, nintp, interlaced != 0, f[0][c], r.h[0][c], f[1][c], r.h[1][c]);
         // the shifted grid starts at the same cell or one below (circularly)
         lo[c] = (interlaced && f[1][c] == (f[0][c] == 0 ? N - 1 : f[0][c] - 1)) ? f[1][c] : f[0][c];
     }
@@ -146,9 +193,14 @@ __global__ void owner_count_kernel(int N, int nintp, int interlaced, int64_t npa
         int tx[2], ty[2], tz[2];
         const int nx = axis_tiles(lo[0], w, N, nt, tx), ny = axis_tiles(lo[1], w, N, nt, ty),
                   nz = axis_tiles(lo[2], w, N, nt, tz);
+        // the first tile of every particle: one atomic per distinct tile of the warp
+        // (neighbouring particles of a catalogue often share it)
+        const int t0 = (tz[0] * nt + ty[0]) * nt + tx[0];
+        const unsigned same = __match_any_sync(__activemask(), t0);
+        if ((int)(threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(count + t0, (unsigned)__popc(same));
         for (int c = 0; c < nz; c++)
             for (int b = 0; b < ny; b++)
-                for (int a = 0; a < nx; a++) atomicAdd(count + (tz[c] * nt + ty[b]) * nt + tx[a], 1u);
+                for (int a = (b | c) ? 0 : 1; a < nx; a++) atomicAdd(count + (tz[c] * nt + ty[b]) * nt + tx[a], 1u);
     }
 }
 
@@ -204,9 +256,20 @@ __global__ void owner_scatter_kernel(int N, int nintp, int interlaced, int64_t n
         const int nx = axis_tiles(lo[0], w, N, nt, tx), ny = axis_tiles(lo[1], w, N, nt, ty),
                   nz = axis_tiles(lo[2], w, N, nt, tz);
         const float wt = weight ? (float)weight[i] : 1.f;
+        // the first tile: one atomic per distinct tile of the warp, the lanes that
+        // share it take consecutive slots in lane order
+        const int t0 = (tz[0] * nt + ty[0]) * nt + tx[0];
+        const unsigned act = __activemask();
+        const unsigned same = __match_any_sync(act, t0);
+        const int lead = __ffs(same) - 1, lane = (int)(threadIdx.x & 31);
+        unsigned d0 = 0;
+        if (lane == lead) d0 = atomicAdd(cursor + t0, (unsigned)__popc(same));
+        d0 = __shfl_sync(same, d0, lead) + (unsigned)__popc(same & ((1u << lane) - 1u));
+        sorted[d0] = r;
+        if (wsorted) wsorted[d0] = wt;
         for (int c = 0; c < nz; c++)
             for (int b = 0; b < ny; b++)
-                for (int a = 0; a < nx; a++) {
+                for (int a = (b | c) ? 0 : 1; a < nx; a++) {
                     const unsigned d = atomicAdd(cursor + (tz[c] * nt + ty[b]) * nt + tx[a], 1u);
                     sorted[d] = r;
                     if (wsorted) wsorted[d] = wt;
@@ -219,7 +282,7 @@ __global__ void owner_scatter_kernel(int N, int nintp, int interlaced, int64_t n
 // its lanes take the G * NI^3 (grid, cell) pairs, so the cell indices and the
 // weight polynomials fold to constants and shifts.
 template <int NI, int G>
-__global__ void __launch_bounds__(kThreads) owner_tile_kernel(int N, int nt, const unsigned int *__restrict__ start,
+__global__ void __launch_bounds__(kThreads, 2) owner_tile_kernel(int N, int nt, const unsigned int *__restrict__ start,
                                                                const PRec *__restrict__ sorted,
                                                                const float *__restrict__ wsorted, float scale,
                                                                float inv_scale, float *__restrict__ out1,
@@ -259,9 +322,20 @@ __global__ void __launch_bounds__(kThreads) owner_tile_kernel(int N, int nt, con
             py[it] = axis_poly<NI>(cj[it]);
             pz[it] = axis_poly<NI>(cl[it] < 0 ? 0 : cl[it]);
         }
+        // the next record of the warp is loaded while this one is added
+        PRec rn;
+        float wn = 1.f;
+        if (b + warp < e) {
+            rn = sorted[b + warp];
+            if (wsorted) wn = wsorted[b + warp];
+        }
         for (unsigned k = b + warp; k < e; k += nwarps) {
-            const PRec r = sorted[k];
-            const float wt = wsorted ? wsorted[k] : 1.f;
+            const PRec r = rn;
+            const float wt = wn;
+            if (k + nwarps < e) {
+                rn = sorted[k + nwarps];
+                if (wsorted) wn = wsorted[k + nwarps];
+            }
             int cell[G][NIT];
             int q[G][NIT];
             bool ok[G][NIT];

@@ -111,17 +111,20 @@ __device__ __forceinline__ typename Cx<R>::T dsample(const typename Cx<R>::T *__
     return cmk<C>(f1.x + f2.y, f2.x - f1.y);
 }
 
+// orbits t < NH^3 <= 1025^3 < 2^32: 32-bit index arithmetic; ang[i] = the
+// reference's phase angle -pi i / N (powerI4.f90:325-342) rounded to R
 template <class R>
 __global__ void fcomb_interlaced_half_kernel(int N, const typename Cx<R>::T *__restrict__ spec,
                                              typename Cx<R>::T *__restrict__ delta, const R *__restrict__ iW,
-                                             R cf, double piN, const BoxPar *__restrict__ bp) {
+                                             const R *__restrict__ ang, R cf, const BoxPar *__restrict__ bp) {
     const int NH = N / 2 + 1;
     if (bp) cf = (R)bp->fcomb_cf;
     const size_t HC = (size_t)N * N * NH;
     const typename Cx<R>::T *F1 = spec, *F2 = spec + HC;
-    const size_t total = (size_t)NH * NH * NH;
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
-        const int ox = (int)(t % NH), oy = (int)((t / NH) % NH), oz = (int)(t / ((size_t)NH * NH));
+    const unsigned total = (unsigned)NH * NH * NH;
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        const unsigned q = t / NH;
+        const int ox = (int)(t - q * NH), oy = (int)(q % NH), oz = (int)(q / NH);
         const int cx = kneg0(ox, N), cy = kneg0(oy, N), cz = kneg0(oz, N);
         Orbit<R> o;
         o.ex = ox == cx; o.ey = oy == cy; o.ez = oz == cz;
@@ -131,7 +134,7 @@ __global__ void fcomb_interlaced_half_kernel(int N, const typename Cx<R>::T *__r
             o.v[o.key(xs, ys, zs)] = dsample<R>(F1, F2, N, xs ? cx : ox, ys ? cy : oy, zs ? cz : oz);
         }
         const R cfac = cf * iW[ox] * iW[oy] * iW[oz];
-        o.combine((R)(piN * ox), (R)(piN * oy), (R)(piN * oz), cfac);
+        o.combine(ang[ox], ang[oy], ang[oz], cfac);
         // store the orbit's locations inside the half (x = ox; x = cx only if equal)
 #pragma unroll
         for (int s = 0; s < 4; s++) {
@@ -143,15 +146,17 @@ __global__ void fcomb_interlaced_half_kernel(int N, const typename Cx<R>::T *__r
     }
 }
 
-template <class R>
+// I: the cell index type (32-bit when the half spectrum has < 2^31 cells)
+template <class R, class I>
 __global__ void fcomb_plain_half_kernel(int N, const typename Cx<R>::T *__restrict__ spec,
                                         typename Cx<R>::T *__restrict__ delta, const R *__restrict__ iW, R cf,
                                         const BoxPar *__restrict__ bp) {
     const int NH = N / 2 + 1;
     if (bp) cf = (R)bp->fcomb_cf;
-    const size_t HC = (size_t)N * N * NH;
-    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < HC; c += (size_t)gridDim.x * blockDim.x) {
-        const int x = (int)(c % NH), y = (int)((c / NH) % N), z = (int)(c / ((size_t)NH * N));
+    const I HC = (I)N * N * NH;
+    for (I c = blockIdx.x * (I)blockDim.x + threadIdx.x; c < HC; c += (I)gridDim.x * blockDim.x) {
+        const I q = c / NH;
+        const int x = (int)(c - q * NH), y = (int)(q % N), z = (int)(q / N);
         const R f = cf * iW[x] * iW[kabs0(y, N)] * iW[kabs0(z, N)];
         delta[c] = cscale(spec[c], f);
     }
@@ -168,13 +173,18 @@ int fcomb_half(int N, int nintp, bool interlaced, float box, double norm, const 
     const int NH = N / 2 + 1;
     std::vector<double> tW(NH);
     window_table(N, nintp, tW.data());
-    std::vector<R> iW(NH);
-    for (int i = 0; i < NH; i++) iW[i] = (R)(1.0 / tW[i]);
-    // the 1/W table is tiny; it lives in the caller's buffer and is rebuilt only
+    // 1/W, then the interlacing phase angles -pi i / N
+    const double tpiN = (double)kTwoPiF / (double)N;
+    std::vector<R> iW(2 * NH);
+    for (int i = 0; i < NH; i++) {
+        iW[i] = (R)(1.0 / tW[i]);
+        iW[NH + i] = (R)((-tpiN / 2.0) * (double)i);
+    }
+    // the tables are tiny; they live in the caller's buffer and are rebuilt only
     // when (N, nintp, precision) changes
     if (wcache.N != N || wcache.nintp != nintp || wcache.rsize != (int)sizeof(R) || !wcache.buf.p) {
-        PBI4G_CHECK(wcache.buf.ensure(sizeof(R) * NH));
-        PBI4G_CUDA(cudaMemcpyAsync(wcache.buf.p, iW.data(), sizeof(R) * NH, cudaMemcpyHostToDevice, st));
+        PBI4G_CHECK(wcache.buf.ensure(sizeof(R) * 2 * NH));
+        PBI4G_CUDA(cudaMemcpyAsync(wcache.buf.p, iW.data(), sizeof(R) * 2 * NH, cudaMemcpyHostToDevice, st));
         PBI4G_CUDA(cudaStreamSynchronize(st));
         wcache.N = N;
         wcache.nintp = nintp;
@@ -183,13 +193,15 @@ int fcomb_half(int N, int nintp, bool interlaced, float box, double norm, const 
     DevBuf &cache = wcache.buf;
     const double cf = fcomb_cf(interlaced, box, norm);
     if (interlaced) {
-        const double tpiN = (double)kTwoPiF / (double)N;
         const size_t total = (size_t)NH * NH * NH;
-        fcomb_interlaced_half_kernel<R><<<grid_blocks(total, 256), 256, 0, st>>>(N, spec, delta, cache.as<R>(),
-                                                                                 (R)cf, -tpiN / 2.0, bp);
+        fcomb_interlaced_half_kernel<R><<<grid_blocks(total, 256), 256, 0, st>>>(
+            N, spec, delta, cache.as<R>(), cache.as<R>() + NH, (R)cf, bp);
+    } else if (half_cells(N) < ((size_t)1 << 31)) {
+        fcomb_plain_half_kernel<R, unsigned><<<grid_blocks(half_cells(N), 256), 256, 0, st>>>(
+            N, spec, delta, cache.as<R>(), (R)cf, bp);
     } else {
-        fcomb_plain_half_kernel<R><<<grid_blocks(half_cells(N), 256), 256, 0, st>>>(N, spec, delta, cache.as<R>(),
-                                                                                    (R)cf, bp);
+        fcomb_plain_half_kernel<R, size_t><<<grid_blocks(half_cells(N), 256), 256, 0, st>>>(
+            N, spec, delta, cache.as<R>(), (R)cf, bp);
     }
     PBI4G_LAUNCH_CHECK();
     ++*launches;

@@ -235,3 +235,32 @@ def test_plan_density_bit_reproducible(box_uniform, interlacing, nintp):
     est.run_host(np.ascontiguousarray(box_uniform[:, perm]))
     b = est.delta_half()
     assert a.tobytes() == b.tobytes()
+
+
+@pytest.mark.parametrize("nintp", [1, 2, 3, 4])
+@pytest.mark.parametrize("interlacing", [False, True])
+def test_plan_density_fp32_prep_matches_fp64(nintp, interlacing):
+    """The FP32 forms find each particle's first cells and FP32 offsets from one
+    FP64 product (integer fraction bits for the floor, the rounding and the
+    half-cell shift); on positions at cell edges, half cells, 0, 1 - 2^-53 and
+    1 the density equals the FP64 form's to FP32 rounding (a different cell for
+    one particle would show as a 1e-4 error)."""
+    n = 32
+    rng = np.random.default_rng(5)
+    k = np.arange(n + 1, dtype=np.float64)
+    special = np.concatenate([k / n, (k + 0.5) / n, np.nextafter(k / n, 0), np.nextafter((k + 0.5) / n, 1),
+                              [0.0, 1.0 - 2.0 ** -53, 1.0]])
+    special = np.clip(special, 0.0, 1.0)
+    m = special.size
+    pos = np.concatenate([rng.random((3, 3000)),
+                          np.stack([special, rng.permutation(special), special[::-1]])], axis=1)
+    p = ref_params(n, 1000.0, nintp, interlacing, False)
+    out = {}
+    for prec in ("fp32", "fp64"):
+        est = Estimator(EstimatorConfig.from_params(p, precision=prec, do_bispectrum=False))
+        est.run_host(np.ascontiguousarray(pos))
+        out[prec] = est.delta_half()
+        est.close()
+    assert m > 100
+    err = np.max(np.abs(out["fp32"] - out["fp64"])) / np.max(np.abs(out["fp64"]))
+    assert err < 2e-6, err
