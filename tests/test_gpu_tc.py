@@ -80,24 +80,36 @@ def test_tensor_core_forms_repeatable(box_za, precision):
 
 
 @pytest.mark.parametrize("precision", ["fp32", "fp16split", "tf32split", "bf16"])
-def test_map_slabs_match_whole_grid(box_za, precision):
+@pytest.mark.parametrize("grid,nb,multipoles", [(64, 10, True), (128, 16, False)])
+def test_map_slabs_match_whole_grid(box_za, precision, grid, nb, multipoles):
     """A map budget below the whole grid's slab buffers streams the y pass, the
-    x pass and the triangle sums over z-slabs (here with an uneven last slab);
-    the results equal the one-slab run up to the order of the FP64 slab
-    additions, and the counts and k columns are exact."""
-    p = ref_params(64, 1000.0, 4, True, True, kbin=2.0, kcenter=2.0)
-    p["nbins_bisp"] = 10
+    x pass and the triangle sums over z-slabs (here with an uneven last slab;
+    the 128^3 case has map grid 100, where a slab is a multiple of 4 z-planes
+    so that it holds whole 64-point chunks); the results equal the one-slab run
+    up to the order of the FP64 slab additions, and the counts and k columns
+    are exact."""
+    p = ref_params(grid, 1000.0, 4, True, multipoles, kbin=2.0, kcenter=2.0)
+    p["nbins_bisp"] = nb
     whole = Estimator(EstimatorConfig.from_params(p, precision=precision))
     pw, bw = whole.run_host(box_za)
     nm_grid, nmaps = whole.map_grid, whole.nmaps
     assert whole.map_slabs() == (nm_grid, 1)
+    q = 1
+    while (q * nm_grid ** 2) % 64:
+        q *= 2
+    if grid == 128:
+        assert nm_grid % 8 == 4 and q == 4, (nm_grid, q)
     # slab buffers per z-plane: the y pass's output (kxtot Nm complex) + the real maps
     kxtot = whole.map_work()[1] // nm_grid ** 2
-    per_point = {"fp32": 4 * nmaps, "fp16split": 4 * nmaps + 4 * 10, "tf32split": 8 * nmaps + 4 * 10,
-                 "bf16": 2 * nmaps + 4 * 10}[precision]
+    per_point = {"fp32": 4 * nmaps, "fp16split": 4 * nmaps + 4 * nb, "tf32split": 8 * nmaps + 4 * nb,
+                 "bf16": 2 * nmaps + 4 * nb}[precision]
     per_plane = per_point * nm_grid ** 2 + 8 * kxtot * nm_grid
-    mb = next(m for m in range(1, 64) if (m << 20) // per_plane >= 2 and nm_grid % ((m << 20) // per_plane))
-    zs = (mb << 20) // per_plane
+
+    def planes(m):
+        return max(q, (m << 20) // per_plane // q * q)
+
+    mb = next(m for m in range(1, 256) if 2 <= planes(m) < nm_grid and nm_grid % planes(m))
+    zs = planes(mb)
     sl = Estimator(EstimatorConfig.from_params(p, precision=precision, map_budget_mb=mb))
     ps, bs = sl.run_host(box_za)
     assert sl.map_slabs() == (zs, -(-nm_grid // zs)), (sl.map_slabs(), zs)
