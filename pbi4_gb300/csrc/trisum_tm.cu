@@ -120,6 +120,15 @@ template <> struct Form<kFormBF16> {
     static constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kN >> 3) << 17) |
                                        ((uint32_t)(kM >> 4) << 24);
 };
+// A waiter on an mbarrier names the phase by its parity, so each A stage and each
+// accumulator must be consumed by one issuing thread, chunk after chunk: issuer w
+// takes chunks w + k kMmaWarps, which use stage (and accumulator) i % count only if
+// count is a multiple of kMmaWarps.  Otherwise an issuer two phases ahead of a stage
+// would read a stale parity as complete.
+static_assert(kAcc % kMmaWarps == 0, "accumulators per issuer");
+static_assert(Form<kFormTF32>::kAStages % kMmaWarps == 0 && Form<kFormF16>::kAStages % kMmaWarps == 0 &&
+                  Form<kFormBF16>::kAStages % kMmaWarps == 0,
+              "A stages per issuer");
 static_assert(kColA + Form<kFormTF32>::kAStages * Form<kFormTF32>::kACols <= kTmemCols, "TMEM budget");
 static_assert(kColA + Form<kFormF16>::kAStages * Form<kFormF16>::kACols <= kTmemCols, "TMEM budget");
 
