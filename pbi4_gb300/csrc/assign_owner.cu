@@ -31,11 +31,12 @@ namespace {
 
 constexpr int kT = 16;                  // tile edge
 constexpr int kTC = kT * kT * kT;       // 4096 cells
-// padded shared layout of a tile: cell (x, y, z) at z * kPz + y * kPy + x.  With
-// kPy = 20 and kPz = 336 (= 16 mod 32) the 32 lanes of one stencil step,
-// (i, j, l) in [0,4) x [0,4) x [0,2), hit 32 distinct banks: i + 20 j + 16 l mod 32.
+// padded shared layout of a tile's 64-bit sums: cell (x, y, z) at z * kPz + y * kPy + x.
+// A stencil step's lanes are (i, j, l) in [0,4) x [0,4) x [0,2), l = lane / 16; a 64-bit
+// access takes the bank pair 2 (i + 20 j + 16 l) = 2 i + 8 j (mod 32), so each half-warp
+// (one wavefront of 8-byte accesses) touches 16 distinct pairs.
 constexpr int kPy = 20, kPz = 336;
-constexpr int kTCP = kT * kPz;          // 5376 words per tile array
+constexpr int kTCP = kT * kPz;          // 5376 cells per tile array
 constexpr int kThreads = 512;
 
 struct alignas(16) PRec {               // one particle, both grids (32 bytes)
@@ -289,7 +290,7 @@ __global__ void __launch_bounds__(kThreads, 2) owner_tile_kernel(int N, int nt, 
                                                                float *__restrict__ out2,
                                                                unsigned int *__restrict__ next_tile) {
     constexpr int NC = NI * NI * NI;
-    extern __shared__ unsigned acc32[];  // [G][lo, hi][kTCP]
+    extern __shared__ unsigned long long acc64[];  // [G][kTCP]
     const int ntiles = nt * nt * nt;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     __shared__ int s_tile;
@@ -302,7 +303,7 @@ __global__ void __launch_bounds__(kThreads, 2) owner_tile_kernel(int N, int nt, 
         if (tile >= ntiles) break;
         const int tx = tile % nt, ty = (tile / nt) % nt, tz = tile / (nt * nt);
         const int ox = tx * kT, oy = ty * kT, oz = tz * kT;
-        for (int c = threadIdx.x; c < 2 * G * kTCP; c += blockDim.x) acc32[c] = 0u;
+        for (int c = threadIdx.x; c < G * kTCP; c += blockDim.x) acc64[c] = 0ull;
         __syncthreads();
         const unsigned b = start[tile], e = start[tile + 1];
         // per-lane stencil cells of one grid: NIT steps of 32 cells; the (i, j, l)
@@ -358,34 +359,20 @@ __global__ void __launch_bounds__(kThreads, 2) owner_tile_kernel(int N, int nt, 
                     cell[g][it] = lz * kPz + ly * kPy + lx;
                 }
             }
-            // 64-bit fixed-point adds of the sign-extended q as two 32-bit shared
-            // atomics: all low words of the record first (independent), then the high
-            // word with the sign and the carry the returned low word gives, so the
-            // pair sums exactly (mod 2^64).  The high word is touched only on a carry
-            // or a negative weight.
-            unsigned old[G][NIT];
+            // 64-bit fixed-point adds of the sign-extended q (exact mod 2^64)
 #pragma unroll
             for (int g = 0; g < G; g++)
 #pragma unroll
                 for (int it = 0; it < NIT; it++)
-                    if (ok[g][it]) old[g][it] = atomicAdd(acc32 + 2 * g * kTCP + cell[g][it], (unsigned)q[g][it]);
-#pragma unroll
-            for (int g = 0; g < G; g++)
-#pragma unroll
-                for (int it = 0; it < NIT; it++)
-                    if (ok[g][it]) {
-                        const unsigned ql = (unsigned)q[g][it];
-                        const unsigned qh = (q[g][it] < 0 ? 0xFFFFFFFFu : 0u) + (old[g][it] + ql < old[g][it] ? 1u : 0u);
-                        if (qh) atomicAdd(acc32 + (2 * g + 1) * kTCP + cell[g][it], qh);
-                    }
+                    if (ok[g][it])
+                        atomicAdd(acc64 + g * kTCP + cell[g][it], (unsigned long long)(long long)q[g][it]);
         }
         __syncthreads();
         for (int c = threadIdx.x; c < G * kTC; c += blockDim.x) {
             const int g = c / kTC, cc = c % kTC;
             const int x = cc % kT, y = (cc / kT) % kT, z = cc / (kT * kT);
-            const unsigned *alo = acc32 + 2 * g * kTCP;
             const int pc = z * kPz + y * kPy + x;
-            const long long v = (long long)(((unsigned long long)alo[kTCP + pc] << 32) | alo[pc]);
+            const long long v = (long long)acc64[g * kTCP + pc];
             float *out = g ? out2 : out1;
             out[((size_t)(oz + z) * N + (oy + y)) * N + (ox + x)] = (float)v * inv_scale;
         }
@@ -396,7 +383,7 @@ __global__ void __launch_bounds__(kThreads, 2) owner_tile_kernel(int N, int nt, 
 template <int NI, int G>
 static int launch_tile(int N, int nt, const unsigned *start, const PRec *sorted, const float *wsorted, int bits,
                        float *out1, float *out2, unsigned *next_tile, cudaStream_t st) {
-    const size_t smem = sizeof(unsigned) * 2 * G * kTCP;
+    const size_t smem = sizeof(unsigned long long) * G * kTCP;
     PBI4G_CUDA(cudaFuncSetAttribute(owner_tile_kernel<NI, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int ntiles = nt * nt * nt;
     int per_sm = 0;
