@@ -365,18 +365,24 @@ __global__ void __launch_bounds__(kThreads, PF <= 9 ? 4 : 2) map_xpass_kernel(co
         const int nrows = min(32, row_hi - row0);
         int mn = m, rn = r;
         advance(mn, rn);
+        const int kxn = a.info[m].kxn;  // X[k] = 0 for k >= kxn
         __syncthreads();
 #pragma unroll
         for (int i = 0; i < PF; i++) {
             const int k = warp + i * nw;
-            if (k < KX) xr[k * kP + lane] = pre[i];
+            if (k < kxn) xr[k * kP + lane] = pre[i];
         }
         if (tile + (int)gridDim.x < ntiles) fetch(mn, a.row_lo + rn * 32);
         __syncthreads();
         for (int k = warp; k <= M / 2; k += nw) {
             const int kc = M - k;
-            const float2 xk = k < KX ? xr[k * kP + lane] : czero();
-            const float2 xc = (k > 0 && kc < KX) ? xr[kc * kP + lane] : czero();  // X[M - k]
+            if (k >= kxn && kc >= kxn) {  // X[k] = X[M - k] = 0 (k is warp-uniform)
+                buf[perm[k] * kP + lane] = czero();
+                if (k > 0 && kc != k) buf[perm[kc] * kP + lane] = czero();
+                continue;
+            }
+            const float2 xk = k < kxn ? xr[k * kP + lane] : czero();
+            const float2 xc = (k > 0 && kc < kxn) ? xr[kc * kP + lane] : czero();  // X[M - k]
             const float2 ck = make_float2(xc.x, -xc.y), cc = make_float2(xk.x, -xk.y);
             const float2 o1 = fftd::cmul(fftd::csub(xk, ck), xt[k]);
             buf[perm[k] * kP + lane] = fftd::cadd(fftd::cadd(xk, ck), fftd::itimes(o1));
