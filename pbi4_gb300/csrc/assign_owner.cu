@@ -182,6 +182,15 @@ __device__ __forceinline__ PRec make_rec(const double *__restrict__ pos, int64_t
     return r;
 }
 
+// Tile of stencil slot s (steps a = s & 1 in x, b = s >> 1 & 1 in y, c = s >> 2 in z)
+// of a particle whose stencil spans nx x ny x nz tiles; -1 when it has no such slot.
+__device__ __forceinline__ int slot_tile(int s, const int tx[2], const int ty[2], const int tz[2], int nx, int ny,
+                                         int nz, int nt) {
+    const int a = s & 1, b = (s >> 1) & 1, c = s >> 2;
+    if (a >= nx || b >= ny || c >= nz) return -1;
+    return (tz[c] * nt + ty[b]) * nt + tx[a];
+}
+
 __global__ void owner_count_kernel(int N, int nintp, int interlaced, int64_t npart, int64_t stride,
                                    const BoxPar *__restrict__ bp, const double *__restrict__ pos, int nt,
                                    PRec *__restrict__ rec, unsigned int *__restrict__ count) {
@@ -194,14 +203,17 @@ __global__ void owner_count_kernel(int N, int nintp, int interlaced, int64_t npa
         int tx[2], ty[2], tz[2];
         const int nx = axis_tiles(lo[0], w, N, nt, tx), ny = axis_tiles(lo[1], w, N, nt, ty),
                   nz = axis_tiles(lo[2], w, N, nt, tz);
-        // the first tile of every particle: one atomic per distinct tile of the warp
-        // (neighbouring particles of a catalogue often share it)
-        const int t0 = (tz[0] * nt + ty[0]) * nt + tx[0];
-        const unsigned same = __match_any_sync(__activemask(), t0);
-        if ((int)(threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(count + t0, (unsigned)__popc(same));
-        for (int c = 0; c < nz; c++)
-            for (int b = 0; b < ny; b++)
-                for (int a = (b | c) ? 0 : 1; a < nx; a++) atomicAdd(count + (tz[c] * nt + ty[b]) * nt + tx[a], 1u);
+        // slot by slot, one atomic per distinct tile of the warp (neighbouring
+        // particles of a catalogue share their tiles and their tile crossings)
+        const unsigned act = __activemask();
+        const int lane = (int)(threadIdx.x & 31);
+#pragma unroll
+        for (int sl = 0; sl < 8; sl++) {
+            const int t = slot_tile(sl, tx, ty, tz, nx, ny, nz, nt);
+            if (!__any_sync(act, t >= 0)) continue;
+            const unsigned same = __match_any_sync(act, t);
+            if (t >= 0 && lane == __ffs(same) - 1) atomicAdd(count + t, (unsigned)__popc(same));
+        }
     }
 }
 
@@ -257,24 +269,24 @@ __global__ void owner_scatter_kernel(int N, int nintp, int interlaced, int64_t n
         const int nx = axis_tiles(lo[0], w, N, nt, tx), ny = axis_tiles(lo[1], w, N, nt, ty),
                   nz = axis_tiles(lo[2], w, N, nt, tz);
         const float wt = weight ? (float)weight[i] : 1.f;
-        // the first tile: one atomic per distinct tile of the warp, the lanes that
-        // share it take consecutive slots in lane order
-        const int t0 = (tz[0] * nt + ty[0]) * nt + tx[0];
+        // slot by slot (as owner_count_kernel counts them): one atomic per distinct
+        // tile of the warp, the lanes that share it take consecutive places in lane order
         const unsigned act = __activemask();
-        const unsigned same = __match_any_sync(act, t0);
-        const int lead = __ffs(same) - 1, lane = (int)(threadIdx.x & 31);
-        unsigned d0 = 0;
-        if (lane == lead) d0 = atomicAdd(cursor + t0, (unsigned)__popc(same));
-        d0 = __shfl_sync(same, d0, lead) + (unsigned)__popc(same & ((1u << lane) - 1u));
-        sorted[d0] = r;
-        if (wsorted) wsorted[d0] = wt;
-        for (int c = 0; c < nz; c++)
-            for (int b = 0; b < ny; b++)
-                for (int a = (b | c) ? 0 : 1; a < nx; a++) {
-                    const unsigned d = atomicAdd(cursor + (tz[c] * nt + ty[b]) * nt + tx[a], 1u);
-                    sorted[d] = r;
-                    if (wsorted) wsorted[d] = wt;
-                }
+        const int lane = (int)(threadIdx.x & 31);
+#pragma unroll
+        for (int sl = 0; sl < 8; sl++) {
+            const int t = slot_tile(sl, tx, ty, tz, nx, ny, nz, nt);
+            if (!__any_sync(act, t >= 0)) continue;
+            const unsigned same = __match_any_sync(act, t);
+            const int lead = __ffs(same) - 1;
+            unsigned d = 0;
+            if (t >= 0 && lane == lead) d = atomicAdd(cursor + t, (unsigned)__popc(same));
+            d = __shfl_sync(same, d, lead) + (unsigned)__popc(same & ((1u << lane) - 1u));
+            if (t >= 0) {
+                sorted[d] = r;
+                if (wsorted) wsorted[d] = wt;
+            }
+        }
     }
 }
 
