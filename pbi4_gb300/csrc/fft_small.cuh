@@ -1,6 +1,7 @@
 // fft_small.cuh -- building blocks of the shell-map inverse transforms
 // (mapfft.cu): complex helpers, inverse DFTs of 2, 3, 4, 5, 7, 8 and 10 points, and
-// the host-side plan of an in-place mixed-radix decimation-in-frequency FFT.
+// the host-side plan of an in-place mixed-radix decimation-in-frequency FFT
+// (radices 2, 3, 4, 5, 7, 8, 10 and 20).
 //
 // Sign convention: every transform here is an inverse DFT,
 //   X[k] = sum_n x[n] e^{+2 pi i n k / N}   (no 1/N: cuFFT's CUFFT_INVERSE / C2R).
@@ -30,7 +31,7 @@
 namespace pbi4g {
 namespace fftd {
 
-constexpr int kMaxRadix = 10;
+constexpr int kMaxRadix = 20;
 
 __host__ __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __host__ __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
@@ -115,6 +116,26 @@ __host__ __device__ __forceinline__ void dft_small(float2 (&v)[kMaxRadix]) {
             v[(6 * k2) % 10] = a[k2];
             v[(5 + 6 * k2) % 10] = b[k2];
         }
+    } else if constexpr (R == 20) {
+        // prime-factor split 20 = 4 x 5 (no twiddles): n = (5 n1 + 4 n2) mod 20,
+        // 4-point DFTs over n1, then 5-point DFTs over n2; X[k] for k = k1 (mod 4),
+        // k = k2 (mod 5) sits at k = (5 k1 + 16 k2) mod 20
+        float2 c[5][kMaxRadix];
+#pragma unroll
+        for (int n2 = 0; n2 < 5; n2++) {
+#pragma unroll
+            for (int n1 = 0; n1 < 4; n1++) c[n2][n1] = v[(5 * n1 + 4 * n2) % 20];
+            dft_small<4>(c[n2]);
+        }
+#pragma unroll
+        for (int k1 = 0; k1 < 4; k1++) {
+            float2 d[kMaxRadix];
+#pragma unroll
+            for (int n2 = 0; n2 < 5; n2++) d[n2] = c[n2][k1];
+            dft_small<5>(d);
+#pragma unroll
+            for (int k2 = 0; k2 < 5; k2++) v[(5 * k1 + 16 * k2) % 20] = d[k2];
+        }
     } else {
         static_assert(R == 8, "radix");
         // one radix-2 step (n, n + 4) then two 4-point DFTs: even outputs from the
@@ -181,18 +202,32 @@ struct FftPlan {
     std::vector<int> perm;   // [n]: position of X[k]
     std::vector<float2> tw;  // [n]: e^{2 pi i s / n}
 
-    // false when n has a prime factor above 7 (or needs too many stages)
-    bool build(int n) {
-        d = FftDesc();
-        d.n = n;
-        int rest = n;
-        for (int r : {10, 8, 4, 2, 3, 5, 7})
-            while (rest % r == 0) {
-                if (d.nst == kMaxStages) return false;
-                d.rad[d.nst++] = r;
-                rest /= r;
-            }
-        if (rest != 1 || n < 2) return false;
+    // false when n has a prime factor above 7 (or needs too many stages).  Radices
+    // are taken greedily from {10, 8, 4, 2, 3, 5, 7}; with allow20 the factorisation
+    // that starts with 20 is used instead when it has fewer stages (each stage is a
+    // round trip of every point through shared memory).
+    bool build(int n, bool allow20 = false) {
+        auto factor = [&](bool with20, FftDesc &o) {
+            o = FftDesc();
+            o.n = n;
+            int rest = n;
+            if (with20)
+                while (rest % 20 == 0) {
+                    if (o.nst == kMaxStages) return false;
+                    o.rad[o.nst++] = 20;
+                    rest /= 20;
+                }
+            for (int r : {10, 8, 4, 2, 3, 5, 7})
+                while (rest % r == 0) {
+                    if (o.nst == kMaxStages) return false;
+                    o.rad[o.nst++] = r;
+                    rest /= r;
+                }
+            return rest == 1 && n >= 2;
+        };
+        FftDesc alt;
+        if (!factor(false, d)) return false;
+        if (allow20 && factor(true, alt) && alt.nst < d.nst) d = alt;
         ent.clear();
         int L = n;
         for (int s = 0; s < d.nst; s++) {
@@ -247,6 +282,7 @@ inline void run_plan_host(const FftPlan &p, float2 *buf, int pitch, int t) {
                 case 5: dit_butterfly<5>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
                 case 7: dit_butterfly<7>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
                 case 8: dit_butterfly<8>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
+                case 20: dit_butterfly<20>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
                 default: dit_butterfly<10>(buf, pitch, t, e.x, p.d.ls[s], e.y, p.tw.data()); break;
             }
         }

@@ -40,12 +40,19 @@ __device__ __forceinline__ void load_tables(const unsigned char *__restrict__ ta
 }
 
 // the plan's stages, last to first, over the 32 transforms of a tile whose
-// points sit at the permuted positions (ends with a barrier); natural-order output
+// points sit at the permuted positions (ends with a barrier); natural-order output.
+// R20: the plan may hold radix-20 stages (plans built with allow20)
+template <bool R20>
 __device__ __forceinline__ void run_dit(const fftd::FftDesc &fd, float2 *buf, const int2 *ent, const float2 *tw,
                                         int warp, int nw, int lane) {
     for (int s = fd.nst - 1; s >= 0; s--) {
         const int R = fd.rad[s], ls = fd.ls[s], nbf = fd.n / R;
         const int2 *e = ent + fd.eoff[s];
+        if (R20 && R == 20) {
+            for (int j = warp; j < nbf; j += nw) fftd::dit_butterfly<20>(buf, kP, lane, e[j].x, ls, e[j].y, tw);
+            __syncthreads();
+            continue;
+        }
         switch (R) {
             case 10:
                 for (int j = warp; j < nbf; j += nw) fftd::dit_butterfly<10>(buf, kP, lane, e[j].x, ls, e[j].y, tw);
@@ -97,7 +104,7 @@ struct ZArgs {
 // column is kz = kfreq0(i, Nm); a mode is in the shell when k2lo <= |k|^2 <=
 // k2hi (the shell's |k|^2 range, contiguous).  The mask, multipole factor and
 // kx = 0 symmetrisation of build_map_spectra; the multipole factor in FP32.
-__global__ void __launch_bounds__(kThreads) map_zpass_kernel(const ZArgs a) {
+__global__ void __launch_bounds__(kThreads, 4) map_zpass_kernel(const ZArgs a) {
     extern __shared__ __align__(16) unsigned char zsm[];
     const fftd::FftDesc &fd = a.fd;
     const int Nm = a.Nm, N = a.N, nb = a.nb;
@@ -158,7 +165,7 @@ __global__ void __launch_bounds__(kThreads) map_zpass_kernel(const ZArgs a) {
             if (lane == 0 && pw != 0.0) atomicAdd(&spow[s * nb + b - 1], pw);
         }
         __syncthreads();
-        run_dit(fd, buf, ent, tw, warp, nw, lane);
+        run_dit<true>(fd, buf, ent, tw, warp, nw, lane);
         // column c0 + l -> T[tbase + (c0 + l) Nm + z], z along the lanes
         for (int l = warp; l < 32; l += nw) {
             if (c0 + l >= mi.ncol) break;
@@ -190,7 +197,7 @@ struct YArgs {
 // (g = kxc + kx: the flat kx index over all maps, so a tile may span maps); a
 // lane reads column kx of its map, ky in [-r(kx), r(kx)], from T and the
 // transform lands in U[f][y].
-__global__ void __launch_bounds__(kThreads) map_ypass_kernel(const YArgs a) {
+__global__ void __launch_bounds__(kThreads, 4) map_ypass_kernel(const YArgs a) {
     extern __shared__ __align__(16) unsigned char ysm[];
     const fftd::FftDesc &fd = a.fd;
     const int Nm = a.Nm;
@@ -217,7 +224,7 @@ __global__ void __launch_bounds__(kThreads) map_ypass_kernel(const YArgs a) {
             buf[perm[i] * kP + lane] = (ky >= -rc.x && ky <= rc.x) ? __ldcs(in + (ptrdiff_t)ky * Nm) : czero();
         }
         __syncthreads();
-        run_dit(fd, buf, ent, tw, warp, nw, lane);
+        run_dit<true>(fd, buf, ent, tw, warp, nw, lane);
         for (int l = warp; l < 32; l += nw) {
             if (t0 + l >= a.nflat) break;
             float2 *o = a.U + (size_t)(t0 + l) * Nm;
@@ -392,7 +399,7 @@ __global__ void __launch_bounds__(kThreads, PF <= 9 ? 4 : 2) map_xpass_kernel(co
             }
         }
         __syncthreads();
-        run_dit(fd, buf, ent, tw, warp, nw, lane);
+        run_dit<false>(fd, buf, ent, tw, warp, nw, lane);
         if (a.oform < 0) {
             // dense FP32 maps: one warp per row, x[2j], x[2j+1] = z[j]
             for (int l = warp; l < nrows; l += nw) {
@@ -443,7 +450,9 @@ int MapTransform::build(const Shells &s, int nm) {
     Nm = s.Nm;
     nmaps = nm;
     nb = s.nb;
-    if (Nm % 4 || !pz.build(Nm) || !px.build(Nm / 2))
+    // radix 20 in the z / y passes only: the x pass keeps its prefetched
+    // coefficients live across the transform and has no registers to spare
+    if (Nm % 4 || !pz.build(Nm, true) || !px.build(Nm / 2, false))
         return set_error(PBI4G_ERR_UNSUPPORTED, "map transform: map grid %d", Nm);
     // per shell: largest k^2, the kx range and the (kx, ky) columns
     std::vector<int> k2hi(nb, -1), k2lo(nb, -1);
@@ -631,7 +640,7 @@ int map_xpass(const MapTransform &mt, const float2 *work, float *out, const MapP
 
 int fft_plan_host_check(int n, int batch, const float *in, float *out) {
     fftd::FftPlan p;
-    if (!p.build(n)) return set_error(PBI4G_ERR_UNSUPPORTED, "fft plan: %d points", n);
+    if (!p.build(n, true)) return set_error(PBI4G_ERR_UNSUPPORTED, "fft plan: %d points", n);
     std::vector<float2> buf((size_t)n);
     for (int t = 0; t < batch; t++) {
         for (int i = 0; i < n; i++)

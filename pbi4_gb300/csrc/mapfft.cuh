@@ -72,7 +72,7 @@ struct MapPlanes {
 
 struct MapTransform {
     int Nm = 0, nmaps = 0, nb = 0, kxmax = 0;
-    fftd::FftPlan pz;    // Nm points (z and y passes)
+    fftd::FftPlan pz;    // Nm points (z and y passes; radix 20 allowed)
     fftd::FftPlan px;    // Nm / 2 points (x pass)
     DevBuf tab_z, tab_x;  // packed plan tables (twiddles, butterfly entries, output positions)
     DevBuf xtw;           // e^{2 pi i k / Nm}, k < Nm (the x pass's even/odd split)

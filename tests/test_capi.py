@@ -68,10 +68,12 @@ def test_errors_without_device(lib):
     assert out.value > 256 ** 3 * 8
 
 
-@pytest.mark.parametrize("n", [2, 3, 5, 7, 8, 12, 50, 100, 128, 150, 196, 200, 294, 320, 392, 400, 512])
+@pytest.mark.parametrize("n", [2, 3, 5, 7, 8, 12, 20, 40, 50, 60, 100, 128, 140, 150, 196, 200, 240, 294, 320,
+                               392, 400, 480, 512, 640, 8000])
 def test_fft_plan_host(lib, n):
     """The in-place mixed-radix plans of the shell-map transforms (radices 2, 3,
-    4, 5, 7, 8; digit-reversed output positions) against numpy's inverse DFT."""
+    4, 5, 7, 8, 10 and 20; digit-reversed output positions) against numpy's
+    inverse DFT."""
     import numpy as np
     rng = np.random.default_rng(n)
     batch = 3
