@@ -358,7 +358,7 @@ template <class R> struct AccOf { using T = float; };
 template <> struct AccOf<double> { using T = double; };
 
 template <class R, int MODE>
-__global__ void pk_accum_kernel(int N, int nbins, const int *__restrict__ lut, PkExact e, double l0, double l1,
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) pk_accum_kernel(int N, int nbins, const int *__restrict__ lut, PkExact e, double l0, double l1,
                                 double l2, const typename Cx<R>::T *__restrict__ a,
                                 const typename Cx<R>::T *__restrict__ b, const typename Cx<R>::T *__restrict__ c,
                                 double *__restrict__ partial) {
@@ -373,7 +373,12 @@ __global__ void pk_accum_kernel(int N, int nbins, const int *__restrict__ lut, P
     const int nwarps = gridDim.x * wpb;
     const A lf0 = (A)l0, lf1 = (A)l1, lf2 = (A)l2;
     // one warp per (y, z) row; a lane takes 4 consecutive x, along which |k| and so
-    // the bin never decrease: the sums stay in registers until the bin changes
+    // the bin never decrease: the sums stay in registers until the bin changes.  A
+    // lane's table and spectrum loads are issued together before its modes are added;
+    // when N/2 would start a 128-wide step of its own (N = 256), the last lane takes
+    // that Nyquist-plane mode as a fifth, after its four.
+    const bool nyq_tail = N / 2 > 0 && (N / 2) % 128 == 0;
+    const int xend = nyq_tail ? NH - 1 : NH;
     for (int row = blockIdx.x * wpb + (threadIdx.x >> 5); row < N * N; row += nwarps) {
         const int ky = kfreq0(row % N, N), kz = kfreq0(row / N, N);
         const int r2 = ky * ky + kz * kz;
@@ -388,38 +393,54 @@ __global__ void pk_accum_kernel(int N, int nbins, const int *__restrict__ lut, P
                 atomicAdd(&s[2 * nbins + cur - 1], s2);
             }
         };
-        for (int x0 = 4 * lane; x0 < NH; x0 += 128) {
+        using C = typename Cx<R>::T;
+        auto add = [&](int x, int bin, C va, C vb, C vc) {
+            if (bin < 1 || bin > nbins) return;
+            if (bin != cur) {
+                flush();
+                cur = bin;
+                s0 = s1 = s2 = 0;
+            }
+            if (MODE == 0) {
+                s0 += (A)(va.x * vb.x + va.y * vb.y);
+            } else if (MODE == 1) {
+                const int k2 = x * x + r2;
+                const A p = (A)(va.x * va.x + va.y * va.y);
+                const A lk = lf0 * (A)x + lf1 * (A)ky + lf2 * (A)kz;
+                const A mu2 = lk * lk / (A)k2;
+                s0 += p;
+                s1 += p * ((A)-0.5 + (A)1.5 * mu2);
+                s2 += p * ((A)0.375 + mu2 * ((A)-3.75 + (A)4.375 * mu2));
+            } else {
+                s0 += (A)(va.x * va.x + va.y * va.y);
+                s1 += (A)(va.x * vb.x + va.y * vb.y);
+                s2 += (A)(va.x * vc.x + va.y * vc.y);
+            }
+        };
+        auto bin_of = [&](int x) {
+            if (!pk_keep(x, ky, kz)) return 0;
+            int bin = lut[x * x + r2];
+            if (bin < 0) bin = pk_bin_exact(e, x, ky, kz);
+            return bin;
+        };
+        for (int x0 = 4 * lane; x0 < xend; x0 += 128) {
+            int bin[4];
+            C va[4], vb[4], vc[4];
 #pragma unroll
             for (int t = 0; t < 4; t++) {
                 const int x = x0 + t;
-                if (x >= NH || !pk_keep(x, ky, kz)) continue;
-                const int k2 = x * x + r2;
-                int bin = lut[k2];
-                if (bin < 0) bin = pk_bin_exact(e, x, ky, kz);
-                if (bin < 1 || bin > nbins) continue;
-                if (bin != cur) {
-                    flush();
-                    cur = bin;
-                    s0 = s1 = s2 = 0;
-                }
-                const typename Cx<R>::T va = a[off + x];
-                if (MODE == 0) {
-                    const typename Cx<R>::T vb = b[off + x];
-                    s0 += (A)(va.x * vb.x + va.y * vb.y);
-                } else if (MODE == 1) {
-                    const A p = (A)(va.x * va.x + va.y * va.y);
-                    const A lk = lf0 * (A)x + lf1 * (A)ky + lf2 * (A)kz;
-                    const A mu2 = lk * lk / (A)k2;
-                    s0 += p;
-                    s1 += p * ((A)-0.5 + (A)1.5 * mu2);
-                    s2 += p * ((A)0.375 + mu2 * ((A)-3.75 + (A)4.375 * mu2));
-                } else {
-                    const typename Cx<R>::T vb = b[off + x], vc = c[off + x];
-                    s0 += (A)(va.x * va.x + va.y * va.y);
-                    s1 += (A)(va.x * vb.x + va.y * vb.y);
-                    s2 += (A)(va.x * vc.x + va.y * vc.y);
-                }
+                const bool in = x < xend;
+                bin[t] = in ? bin_of(x) : 0;
+                va[t] = in ? a[off + x] : C{};
+                vb[t] = (in && MODE != 1) ? b[off + x] : C{};
+                vc[t] = (in && MODE == 2) ? c[off + x] : C{};
             }
+#pragma unroll
+            for (int t = 0; t < 4; t++) add(x0 + t, bin[t], va[t], vb[t], vc[t]);
+        }
+        if (nyq_tail && lane == 31) {
+            const int x = NH - 1;
+            add(x, bin_of(x), a[off + x], MODE != 1 ? b[off + x] : C{}, MODE == 2 ? c[off + x] : C{});
         }
         flush();
     }
