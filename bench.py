@@ -545,7 +545,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", default="fp16split", choices=["fp32", "fp64", "fp16split", "bf16", "tf32split"])
     ap.add_argument("--no-compare", action="store_true", help="skip the plain-FP32 and FP64 comparison runs")
-    ap.add_argument("--serve-requests", type=int, default=48, help="requests in the serving leg (0: skip)")
+    ap.add_argument("--serve-requests", type=int, default=400, help="requests in the serving leg (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="offered request rate of the serving leg (1/s)")
     ap.add_argument("--serve-npart-max", type=float, default=1e7, help="largest particle count of a served box")
     ap.add_argument("--quick", action="store_true", help="small box (debug only)")
