@@ -114,8 +114,10 @@ def test_map_slabs_match_whole_grid(box_za, precision, grid, nb, multipoles):
     ps, bs = sl.run_host(box_za)
     assert sl.map_slabs() == (zs, -(-nm_grid // zs)), (sl.map_slabs(), zs)
     # P does not depend on the slabs; its FP32 per-block bin sums are added in
-    # scheduling order, so two runs agree to ~1e-8, not bitwise
-    np.testing.assert_allclose(ps, pw, rtol=1e-6, atol=0)
+    # scheduling order, so two runs agree to ~1e-8 of P0, not bitwise
+    np.testing.assert_allclose(ps[:2], pw[:2], rtol=1e-6, atol=0)
+    np.testing.assert_array_equal(ps[4], pw[4])
+    assert np.all(np.abs(ps[2:4] - pw[2:4]) <= 1e-6 * np.abs(pw[1]))  # P2, P4 against P0
     np.testing.assert_array_equal(bs[[0, 1, 2, 8]], bw[[0, 1, 2, 8]])
     errs, pow_err = b_errors(bs, bw)
     assert max(errs) < 1e-6 and pow_err < 1e-12, (errs, pow_err)

@@ -98,3 +98,42 @@ def test_graph_batch_matches_direct():
             scale = np.maximum(np.abs(b_ref[6]), np.abs(b_ref[3] * b_ref[4]))
             assert np.max(np.abs(bouts[k][6] - b_ref[6]) / scale) < 1e-6
     est.close()
+
+
+@pytest.mark.parametrize("precision", ["fp16split", "fp32"])
+def test_two_plans_on_two_streams_match_one(precision):
+    """Two plans of one configuration on two CUDA streams with their boxes in
+    flight together (the two-in-flight form of the throughput figure) give the
+    results each box gets alone on one plan: the k columns and counts identical,
+    the rest within the ordering of the floating-point atomics (1e-6, P2 and P4
+    relative to P0; the mean |k| of a P bin is summed with FP64 atomics once per
+    plan, so two plans agree on it to the last bit only)."""
+    import torch
+    cfg = EstimatorConfig(grid=64, box=1000.0, nintp=4, interlacing=True, multipoles=True, kbin_bs=2.0,
+                          kcenter_bs=2.0, nbins_bs=10, precision=precision)
+    boxes = [synthetic.zeldovich_box(24, 1000.0, seed=40 + k) for k in range(4)]
+    alone = Estimator(cfg)
+    ref = [alone.run_host(b) for b in boxes]
+    alone.close()
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    ests = [Estimator(cfg, stream=s) for s in streams]
+    outs = [[e.alloc_outputs() for _ in range(2)] for e in ests]
+    dpos = [torch.from_numpy(b).cuda() for b in boxes]
+    torch.cuda.synchronize()
+    for k in range(4):  # box k on plan k % 2, output slot k // 2; no host sync between the launches
+        e = ests[k % 2]
+        po, bo = outs[k % 2][k // 2]
+        e.run_device(dpos[k].shape[1], dpos[k], po, bo)
+    torch.cuda.synchronize()
+    for e in ests:
+        e.check()
+    for k in range(4):
+        po, bo = outs[k % 2][k // 2]
+        p, b = po.cpu().numpy(), bo.cpu().numpy()
+        pr, br = ref[k]
+        np.testing.assert_array_equal(b[[0, 1, 2, 8]], br[[0, 1, 2, 8]])
+        np.testing.assert_array_equal(p[4], pr[4])
+        np.testing.assert_allclose(p[:2], pr[:2], rtol=1e-6, atol=0)
+        # P2 and P4 against P0 of the bin (they are small differences of large terms)
+        assert np.all(np.abs(p[2:4] - pr[2:4]) <= 1e-6 * np.abs(pr[1])), np.max(np.abs(p[2:4] - pr[2:4]) / np.abs(pr[1]))
+        np.testing.assert_allclose(b, br, rtol=1e-6, atol=1e-9 * np.max(np.abs(br)))
