@@ -264,3 +264,25 @@ def test_plan_density_fp32_prep_matches_fp64(nintp, interlacing):
     assert m > 100
     err = np.max(np.abs(out["fp32"] - out["fp64"])) / np.max(np.abs(out["fp64"]))
     assert err < 2e-6, err
+
+
+@pytest.mark.parametrize("interlacing,nintp", [(True, 4), (False, 2), (True, 3)])
+def test_plan_density_weighted_fp32_matches_fp64(box_za, interlacing, nintp):
+    """Per-particle weights through the FP32 owner tiles (the fixed-point scale
+    set from the largest weight, one 32-bit value per contribution) against the
+    FP64 form: the density equals it to FP32 rounding; zero weights and a wide
+    weight range included."""
+    rng = np.random.default_rng(21)
+    n = box_za.shape[1]
+    w = rng.uniform(0.5, 1.5, n)
+    w[::7] = 0.0
+    w[5] = 40.0
+    p = ref_params(32, 1000.0, nintp, interlacing, False)
+    out = {}
+    for prec in ("fp32", "fp64"):
+        est = Estimator(EstimatorConfig.from_params(p, precision=prec, do_bispectrum=False))
+        est.run_host(box_za, w)
+        out[prec] = est.delta_half()
+        est.close()
+    err = np.max(np.abs(out["fp32"] - out["fp64"])) / np.max(np.abs(out["fp64"]))
+    assert err < 2e-6, err
