@@ -309,6 +309,7 @@ def run_ours(args):
     ms_one, launches_one, stages, clocks_one = timed(est, pout, bout, args.steps)
     value_one = replicas.throughput(world * args.steps, ms_one / 1e3)
     map_work = est.map_work()
+    tensor_units = est.tensor_units()
 
     # two boxes in flight (the batched form): two plans on two streams take the
     # boxes in turn, so one box's low-occupancy phases (kernel tails, the tile
@@ -417,7 +418,7 @@ def run_ours(args):
 
     from pbi4_gb300 import roofline
     rl, rl_all = roofline.for_stages(stages, args.steps, cfg, npart, itot=itot, map_grid=map_grid, nmaps=nmaps,
-                                     map_work=map_work)
+                                     map_work=map_work, tensor_units=tensor_units)
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:

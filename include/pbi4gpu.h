@@ -174,6 +174,12 @@ int pbi4g_plan_map_work(const pbi4g_plan *plan, int64_t *zcols, int64_t *yplanes
 /* z-planes per slab of the map grid and slabs per box of the last bispectrum
  * run (one slab of map_grid planes without a map budget; 0, 0 before a run). */
 int pbi4g_plan_map_slabs(const pbi4g_plan *plan, int32_t *slab_planes, int32_t *nslabs);
+/* Tensor-core triangle sums of the last bispectrum run: units (one 128-pair x
+ * 64-map tile of the contraction each) and MMA products per K step (3 for the
+ * hi+lo split forms, 1 for BF16); 0, 0 for the CUDA-core forms and before a run.
+ * The executed tensor work per box is units * (map grid)^3 * 128 * 64 * 2 *
+ * products flops, against 2 (map grid)^3 itot sets useful ones. */
+int pbi4g_plan_tensor_units(const pbi4g_plan *plan, int32_t *units, int32_t *products);
 /* Exact integer triangle counts of the plan's binning (computed once, cached). */
 int pbi4g_plan_triangle_counts(pbi4g_plan *plan, int64_t *counts_host);
 

@@ -25,7 +25,7 @@ EXPORTS = [
     "pbi4g_compute_q2k", "pbi4g_compute_q4k", "pbi4g_measure_pk", "pbi4g_measure_pk_multipoles",
     "pbi4g_count_triangles", "pbi4g_measure_bk", "pbi4g_measure_bk_multipoles", "pbi4g_measure_bk_cross",
     "pbi4g_plan_footprint", "pbi4g_plan_create", "pbi4g_plan_destroy", "pbi4g_plan_set_stream",
-    "pbi4g_plan_shape", "pbi4g_plan_map_grid", "pbi4g_plan_map_work", "pbi4g_plan_map_slabs",
+    "pbi4g_plan_shape", "pbi4g_plan_map_grid", "pbi4g_plan_map_work", "pbi4g_plan_map_slabs", "pbi4g_plan_tensor_units",
     "pbi4g_plan_triangle_counts", "pbi4g_plan_density",
     "pbi4g_plan_powerspectrum",
     "pbi4g_plan_bispectrum", "pbi4g_plan_run_device", "pbi4g_plan_run_host", "pbi4g_plan_get_delta_half",
@@ -82,6 +82,7 @@ _SIGS = {
     "pbi4g_plan_map_grid": [_P, ctypes.POINTER(_i32), ctypes.POINTER(_i32)],
     "pbi4g_plan_map_work": [_P, _P, _P],
     "pbi4g_plan_map_slabs": [_P, ctypes.POINTER(_i32), ctypes.POINTER(_i32)],
+    "pbi4g_plan_tensor_units": [_P, ctypes.POINTER(_i32), ctypes.POINTER(_i32)],
     "pbi4g_plan_check": [_P],
     "pbi4g_plan_graph_build": [_P, _i32, _i64],
     "pbi4g_plan_graph_run_host": [_P, _i32, _P, _P, _P, _P],

@@ -391,6 +391,15 @@ int pbi4g_plan_map_slabs(const pbi4g_plan *plan, int32_t *slab_planes, int32_t *
     return PBI4G_OK;
 }
 
+int pbi4g_plan_tensor_units(const pbi4g_plan *plan, int32_t *units, int32_t *products) {
+    if (!plan) return set_error(PBI4G_ERR_INVALID, "null plan");
+    const BkEngine &bk = plan->bk;
+    const bool tc = plan->cfg.do_bispectrum && bk.tc_mode != 0 && bk.tmp_nsets >= 0;
+    if (units) *units = tc ? bk.tmp.nunits : 0;
+    if (products) *products = tc ? (bk.tc_mode == 2 ? 1 : 3) : 0;
+    return PBI4G_OK;
+}
+
 int64_t pbi4g_plan_kernel_launches(const pbi4g_plan *plan) { return plan ? plan->launches : -1; }
 
 int pbi4g_plan_triangle_counts(pbi4g_plan *plan, int64_t *counts_host) {

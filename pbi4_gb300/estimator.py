@@ -123,6 +123,12 @@ class Estimator:
         check(lib().pbi4g_plan_map_slabs(self._h, ctypes.byref(z), ctypes.byref(n)))
         return z.value, n.value
 
+    def tensor_units(self):
+        """(units, products per K step) of the tensor-core triangle sums of the last run."""
+        u, k = ctypes.c_int32(), ctypes.c_int32()
+        check(lib().pbi4g_plan_tensor_units(self._h, ctypes.byref(u), ctypes.byref(k)))
+        return u.value, k.value
+
     # -- lifecycle
     def close(self):
         if getattr(self, "_h", None):

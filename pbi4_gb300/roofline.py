@@ -104,12 +104,16 @@ def _entry(name, bound, amount, avg_ms, pk, traffic):
             "algorithmic_bytes": amount, "avg_ms": round(avg_ms, 4), "peak_source": pk["source"]}
 
 
-def for_stages(stages, steps, cfg, npart, itot=None, map_grid=None, nmaps=None, map_work=None):
+def for_stages(stages, steps, cfg, npart, itot=None, map_grid=None, nmaps=None, map_work=None, tensor_units=None):
     """(dominant, all): the roofline object of the slowest stage among this
-    library's kernels and the list for every timed stage.  Tensor-core triangle
-    sums count the useful flops 2 Nm^3 itot S against the measured bf16 dense
-    peak; HBM stages count their algorithmic bytes.  `traffic` is the per-launch
-    DRAM bytes of the committed ncu capture for this workload, if one exists."""
+    library's kernels and the list for every timed stage (per box: a stage that
+    runs slab by slab adds its launches).  Tensor-core triangle sums count the
+    useful flops 2 Nm^3 itot S against the measured bf16 dense peak; with
+    tensor_units = (units, products) they also report the executed tensor work (every
+    128-pair x 64-map tile of a unit over every point, times the split's products)
+    and the fraction of the tiles' entries that is no triangle sum.  HBM stages count their
+    algorithmic bytes.  `traffic` is the per-launch DRAM bytes of the committed ncu
+    capture for this workload, if one exists."""
     pk = peaks()
     work = dict(stage_work(cfg, npart, map_grid, nmaps, map_work))
     if itot and cfg.precision in ("fp16split", "bf16", "tf32split"):
@@ -121,9 +125,17 @@ def for_stages(stages, steps, cfg, npart, itot=None, map_grid=None, nmaps=None, 
         ms, calls = stages.get(name, (0.0, 0))
         if calls == 0 or ms <= 0:
             continue
-        e = _entry(name, bound, amount, ms / calls, pk, table.get(name))
+        e = _entry(name, bound, amount, ms / max(1, steps), pk, table.get(name))
         if name == "shell_maps_z" and cfg.precision == "fp64":
             e["kernel"] = "build_map_spectra_kernel"
+        if name == "triangle_sums" and tensor_units and tensor_units[0]:
+            units, products = tensor_units
+            executed = float(units) * int(map_grid or cfg.grid) ** 3 * 128 * 64 * 2 * products
+            e["executed_flops"] = executed
+            e["executed_tflops"] = round(executed / (e["avg_ms"] * 1e-3) / 1e12, 1)
+            e["split_products"] = products
+            # entries of the units' (pair, map) tiles that are no (triangle, set) slot
+            e["gemm_recast_waste"] = round(1.0 - amount * products / executed, 4)
         out.append(e)
     if not out:
         return None, []
