@@ -128,10 +128,29 @@ __global__ void fcomb_interlaced_half_kernel(int N, const typename Cx<R>::T *__r
         const int cx = kneg0(ox, N), cy = kneg0(oy, N), cz = kneg0(oz, N);
         Orbit<R> o;
         o.ex = ox == cx; o.ey = oy == cy; o.ez = oz == cz;
+        // the orbit's points (ox or cx, oy or cy, oz or cz) read the four half-spectrum
+        // cells (ox, oy or cy, oz or cz): (ox, Y, Z) directly, (cx, Y, Z) as the mirror
+        // of (ox, -Y, -Z) (dsample's two branches), so each cell is loaded once
+        using C = typename Cx<R>::T;
+        C f1[2][2], f2[2][2];
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            const int ys = c & 1, zs = c >> 1;
+            const size_t off = ((size_t)(zs ? cz : oz) * N + (ys ? cy : oy)) * NH + ox;
+            f1[ys][zs] = F1[off];
+            f2[ys][zs] = F2[off];
+        }
 #pragma unroll
         for (int s = 0; s < 8; s++) {
             const int xs = s & 1, ys = (s >> 1) & 1, zs = s >> 2;
-            o.v[o.key(xs, ys, zs)] = dsample<R>(F1, F2, N, xs ? cx : ox, ys ? cy : oy, zs ? cz : oz);
+            if (xs && o.ex) continue;  // ox = cx: the same points as xs = 0
+            if (!xs) {
+                const C a = f1[ys][zs], b = f2[ys][zs];
+                o.v[o.key(0, ys, zs)] = cmk<C>(a.x - b.y, a.y + b.x);
+            } else {
+                const C a = f1[1 - ys][1 - zs], b = f2[1 - ys][1 - zs];
+                o.v[o.key(1, ys, zs)] = cmk<C>(a.x + b.y, b.x - a.y);
+            }
         }
         const R cfac = cf * iW[ox] * iW[oy] * iW[oz];
         o.combine(ang[ox], ang[oy], ang[oz], cfac);
