@@ -55,13 +55,16 @@ __device__ __forceinline__ void sincos_t(double a, double *s, double *c) { sinco
 // The orbit {ix,icx} x {iy,icy} x {iz,icz} of one iteration of fcomb's
 // interlaced loop, with the reference's write order (powerI4.f90:325-342)
 // applied to an 8-entry local copy.  Where ix == icx (etc.) the two slots are
-// one location and later writes win, exactly as in the Fortran.
-template <class R>
+// one location and later writes win, exactly as in the Fortran.  DISTINCT: the
+// caller has checked that no two slots coincide (ix != icx, iy != icy, iz != icz),
+// so every index is static and the copy stays in registers.
+template <class R, bool DISTINCT = false>
 struct Orbit {
     using C = typename Cx<R>::T;
     C v[8];
-    int ex, ey, ez;
+    int ex = 0, ey = 0, ez = 0;
     __device__ __forceinline__ int key(int xs, int ys, int zs) const {
+        if constexpr (DISTINCT) return xs | (ys << 1) | (zs << 2);
         return (ex ? 0 : xs) | ((ey ? 0 : ys) << 1) | ((ez ? 0 : zs) << 2);
     }
     __device__ __forceinline__ void combine(R xa, R ya, R za, R cfac) {
@@ -126,42 +129,47 @@ __global__ void fcomb_interlaced_half_kernel(int N, const typename Cx<R>::T *__r
         const unsigned q = t / NH;
         const int ox = (int)(t - q * NH), oy = (int)(q % NH), oz = (int)(q / NH);
         const int cx = kneg0(ox, N), cy = kneg0(oy, N), cz = kneg0(oz, N);
-        Orbit<R> o;
-        o.ex = ox == cx; o.ey = oy == cy; o.ez = oz == cz;
-        // the orbit's points (ox or cx, oy or cy, oz or cz) read the four half-spectrum
-        // cells (ox, oy or cy, oz or cz): (ox, Y, Z) directly, (cx, Y, Z) as the mirror
-        // of (ox, -Y, -Z) (dsample's two branches), so each cell is loaded once
-        using C = typename Cx<R>::T;
-        C f1[2][2], f2[2][2];
+        // orbits without coinciding points (all but the kx, ky, kz = 0 and Nyquist planes)
+        // take the register path
+        auto run = [&](auto o) {
+            o.ex = ox == cx; o.ey = oy == cy; o.ez = oz == cz;
+            // the orbit's points (ox or cx, oy or cy, oz or cz) read the four half-spectrum
+            // cells (ox, oy or cy, oz or cz): (ox, Y, Z) directly, (cx, Y, Z) as the mirror
+            // of (ox, -Y, -Z) (dsample's two branches), so each cell is loaded once
+            using C = typename Cx<R>::T;
+            C f1[2][2], f2[2][2];
 #pragma unroll
-        for (int c = 0; c < 4; c++) {
-            const int ys = c & 1, zs = c >> 1;
-            const size_t off = ((size_t)(zs ? cz : oz) * N + (ys ? cy : oy)) * NH + ox;
-            f1[ys][zs] = F1[off];
-            f2[ys][zs] = F2[off];
-        }
-#pragma unroll
-        for (int s = 0; s < 8; s++) {
-            const int xs = s & 1, ys = (s >> 1) & 1, zs = s >> 2;
-            if (xs && o.ex) continue;  // ox = cx: the same points as xs = 0
-            if (!xs) {
-                const C a = f1[ys][zs], b = f2[ys][zs];
-                o.v[o.key(0, ys, zs)] = cmk<C>(a.x - b.y, a.y + b.x);
-            } else {
-                const C a = f1[1 - ys][1 - zs], b = f2[1 - ys][1 - zs];
-                o.v[o.key(1, ys, zs)] = cmk<C>(a.x + b.y, b.x - a.y);
+            for (int c = 0; c < 4; c++) {
+                const int ys = c & 1, zs = c >> 1;
+                const size_t off = ((size_t)(zs ? cz : oz) * N + (ys ? cy : oy)) * NH + ox;
+                f1[ys][zs] = F1[off];
+                f2[ys][zs] = F2[off];
             }
-        }
-        const R cfac = cf * iW[ox] * iW[oy] * iW[oz];
-        o.combine(ang[ox], ang[oy], ang[oz], cfac);
-        // store the orbit's locations inside the half (x = ox; x = cx only if equal)
 #pragma unroll
-        for (int s = 0; s < 4; s++) {
-            const int ys = s & 1, zs = s >> 1;
-            if ((ys && o.ey) || (zs && o.ez)) continue;
-            const int Y = ys ? cy : oy, Z = zs ? cz : oz;
-            delta[((size_t)Z * N + Y) * NH + ox] = o.v[o.key(0, ys, zs)];
-        }
+            for (int s = 0; s < 8; s++) {
+                const int xs = s & 1, ys = (s >> 1) & 1, zs = s >> 2;
+                if (xs && o.ex) continue;  // ox = cx: the same points as xs = 0
+                if (!xs) {
+                    const C a = f1[ys][zs], b = f2[ys][zs];
+                    o.v[o.key(0, ys, zs)] = cmk<C>(a.x - b.y, a.y + b.x);
+                } else {
+                    const C a = f1[1 - ys][1 - zs], b = f2[1 - ys][1 - zs];
+                    o.v[o.key(1, ys, zs)] = cmk<C>(a.x + b.y, b.x - a.y);
+                }
+            }
+            const R cfac = cf * iW[ox] * iW[oy] * iW[oz];
+            o.combine(ang[ox], ang[oy], ang[oz], cfac);
+            // store the orbit's locations inside the half (x = ox; x = cx only if equal)
+#pragma unroll
+            for (int s = 0; s < 4; s++) {
+                const int ys = s & 1, zs = s >> 1;
+                if ((ys && o.ey) || (zs && o.ez)) continue;
+                const int Y = ys ? cy : oy, Z = zs ? cz : oz;
+                delta[((size_t)Z * N + Y) * NH + ox] = o.v[o.key(0, ys, zs)];
+            }
+        };
+        if (ox != cx && oy != cy && oz != cz) run(Orbit<R, true>{});
+        else run(Orbit<R, false>{});
     }
 }
 
