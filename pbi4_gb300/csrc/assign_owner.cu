@@ -290,11 +290,13 @@ __global__ void owner_scatter_kernel(int N, int nintp, int interlaced, int64_t n
     }
 }
 
-// Tile kernel, specialised on the stencil width NI (1..4) and the number of
-// grids G (2 when interlaced): a warp takes one record (particle, tile) and
-// its lanes take the G * NI^3 (grid, cell) pairs, so the cell indices and the
-// weight polynomials fold to constants and shifts.
-template <int NI, int G>
+// Tile kernel, specialised on the stencil width NI (1..4), the number of
+// grids G (2 when interlaced) and the presence of particle weights W: a warp
+// takes one record (particle, tile) and its lanes take the G * NI^3 (grid,
+// cell) pairs, so the cell indices and the weight polynomials fold to
+// constants and shifts.  The fixed-point scale 2^S rides in the z polynomial
+// (a power of two: the products are the same bits as scaling at the end).
+template <int NI, int G, bool W>
 __global__ void __launch_bounds__(kThreads, 2) owner_tile_kernel(int N, int nt, const unsigned int *__restrict__ start,
                                                                const PRec *__restrict__ sorted,
                                                                const float *__restrict__ wsorted, float scale,
@@ -333,21 +335,22 @@ __global__ void __launch_bounds__(kThreads, 2) owner_tile_kernel(int N, int nt, 
             cl[it] = c < NC ? c / (NI * NI) : -1;  // -1: no cell for this lane at this step
             px[it] = axis_poly<NI>(ci[it]);
             py[it] = axis_poly<NI>(cj[it]);
-            pz[it] = axis_poly<NI>(cl[it] < 0 ? 0 : cl[it]);
+            const float4 zc = axis_poly<NI>(cl[it] < 0 ? 0 : cl[it]);
+            pz[it] = make_float4(zc.x * scale, zc.y * scale, zc.z * scale, zc.w * scale);
         }
         // the next record of the warp is loaded while this one is added
         PRec rn;
         float wn = 1.f;
         if (b + warp < e) {
             rn = sorted[b + warp];
-            if (wsorted) wn = wsorted[b + warp];
+            if (W) wn = wsorted[b + warp];
         }
         for (unsigned k = b + warp; k < e; k += nwarps) {
             const PRec r = rn;
             const float wt = wn;
             if (k + nwarps < e) {
                 rn = sorted[k + nwarps];
-                if (wsorted) wn = wsorted[k + nwarps];
+                if (W) wn = wsorted[k + nwarps];
             }
             int cell[G][NIT];
             int q[G][NIT];
@@ -366,8 +369,9 @@ __global__ void __launch_bounds__(kThreads, 2) owner_tile_kernel(int N, int nt, 
                                 (unsigned)lz < (unsigned)kT;
                     // the reference's product order: ((w_x w_y) w_z) weight; wv * 2^S is exact in
                     // FP32 (a power-of-two scale) and |wv| 2^S < 2^30, so q is one 32-bit integer
-                    const float wv = horner(px[xi], hx) * horner(py[xi], hy) * horner(pz[it], hz) * wt;
-                    q[g][it] = __float2int_rn(wv * scale);
+                    float wv = horner(px[xi], hx) * horner(py[xi], hy) * horner(pz[it], hz);
+                    if (W) wv *= wt;
+                    q[g][it] = __float2int_rn(wv);
                     cell[g][it] = lz * kPz + ly * kPy + lx;
                 }
             }
@@ -392,19 +396,27 @@ __global__ void __launch_bounds__(kThreads, 2) owner_tile_kernel(int N, int nt, 
     }
 }
 
+template <int NI, int G, bool W>
+static int launch_tile_w(int N, int nt, const unsigned *start, const PRec *sorted, const float *wsorted, int bits,
+                         float *out1, float *out2, unsigned *next_tile, cudaStream_t st) {
+    const size_t smem = sizeof(unsigned long long) * G * kTCP;
+    auto kern = owner_tile_kernel<NI, G, W>;
+    PBI4G_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int ntiles = nt * nt * nt;
+    int per_sm = 0;
+    PBI4G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem));
+    const int grid = std::min(ntiles, 152 * std::max(1, per_sm));
+    kern<<<grid, kThreads, smem, st>>>(N, nt, start, sorted, wsorted, ldexpf(1.0f, bits), ldexpf(1.0f, -bits), out1,
+                                       out2, next_tile);
+    PBI4G_LAUNCH_CHECK();
+    return PBI4G_OK;
+}
+
 template <int NI, int G>
 static int launch_tile(int N, int nt, const unsigned *start, const PRec *sorted, const float *wsorted, int bits,
                        float *out1, float *out2, unsigned *next_tile, cudaStream_t st) {
-    const size_t smem = sizeof(unsigned long long) * G * kTCP;
-    PBI4G_CUDA(cudaFuncSetAttribute(owner_tile_kernel<NI, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int ntiles = nt * nt * nt;
-    int per_sm = 0;
-    PBI4G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, owner_tile_kernel<NI, G>, kThreads, smem));
-    const int grid = std::min(ntiles, 152 * std::max(1, per_sm));
-    owner_tile_kernel<NI, G><<<grid, kThreads, smem, st>>>(N, nt, start, sorted, wsorted, ldexpf(1.0f, bits),
-                                                           ldexpf(1.0f, -bits), out1, out2, next_tile);
-    PBI4G_LAUNCH_CHECK();
-    return PBI4G_OK;
+    return wsorted ? launch_tile_w<NI, G, true>(N, nt, start, sorted, wsorted, bits, out1, out2, next_tile, st)
+                   : launch_tile_w<NI, G, false>(N, nt, start, sorted, wsorted, bits, out1, out2, next_tile, st);
 }
 
 __global__ void owner_wmax_kernel(int64_t n, const double *__restrict__ w, unsigned long long *__restrict__ out) {
