@@ -94,154 +94,108 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------ CPU legs ---
-class ReferenceSampler:
-    """Seconds per box of the CPU restatement of the reference (oracle/: the
-    Fortran loops in C, serial as in the reference; FFTs through scipy on all
-    host cores), timed stage by stage on bounded samples of the workload:
-      assign          a fraction of the particles, extrapolated linearly
-      fft, fcomb, pk  one density FFT, the interlacing combine, P(k) multipole binning
-      multipoles      one of the 22 FFT passes of compute_density_multipoles (x22)
-      maps            one of the 3 x 21 shell-map FFTs (x63)
-      triangle_sums   a few triangles of the serial FP64 triple sum (x1156 / n)
-    A step times every stage (`rotate=False`) or, for long runs, the assignment,
-    the triangles and one of the three FFT groups in turn; the box time of a
-    step is the sum of the latest timing of every stage."""
-
-    def __init__(self, pos, assign_fraction=1.0, tri_budget_s=2.0, rotate=False):
-        import scipy.fft
-
-        from oracle import pbi4_oracle as O
-        self.O, self.fft = O, scipy.fft
-        w = WORKLOAD
-        self.N, self.cores = w["grid"], os.cpu_count() or 1
-        p = dict(grid=self.N, box=w["box"], interpolation=w["nintp"], interlacing=w["interlacing"], multipoles=True,
-                 kbin=w["kbin_ps"], kcenter=w["kcenter_ps"], iopen=True, los=w["los"], cross=False, om=0.3, ol=0.7,
-                 z=0.5)
-        p.update(O.derived_params(p))
-        self.p, self.pos = p, pos
-        self.nsub = max(1, int(round(pos.shape[1] * assign_fraction)))
-        self.sub = np.ascontiguousarray(pos[:, : self.nsub])
-        self.tri_budget, self.rotate, self.k = tri_budget_s, rotate, 0
-        # one real density (the full assignment, untimed) feeds the FFT-side stages
-        npart, dcl = O.assign_grid(pos, p)
-        self.npart, self.dcl = npart, dcl
-        d = O.compute_density(npart, dcl, p, workers=self.cores)
-        self.d = d
-        shell = O.shell_index(self.N, w["kbin_bs"], w["kcenter_bs"])
-        self.shell_in = np.where(shell == 5, O.hermitian_full_grid(d), 0.0)
-        self.latest = {}
-        self.ntri = 0
-
-    def _assign(self):
-        t0 = time.perf_counter()
-        self.O.assign_grid(self.sub, self.p)
-        self.latest["assign"] = (time.perf_counter() - t0) * self.pos.shape[1] / self.nsub
-
-    def _density(self):
-        O, N, w = self.O, self.N, WORKLOAD
-        t0 = time.perf_counter()
-        f = self.fft.fftn(self.dcl / self.npart, workers=self.cores)
-        self.latest["fft"] = time.perf_counter() - t0
-        t0 = time.perf_counter()
-        d = O.fcomb(N, w["nintp"], True, w["box"], f)
-        self.latest["fcomb"] = time.perf_counter() - t0
-        t0 = time.perf_counter()
-        O.measure_pk_multipoles(N, w["box"], 1.0, 1.0, w["nbins_ps"], d, d, d)
-        self.latest["pk"] = time.perf_counter() - t0
-
-    def _multipoles(self):
-        O, N, w = self.O, self.N, WORKLOAD
-        t0 = time.perf_counter()
-        dx = self.fft.ifftn(self.d, workers=self.cores)
-        O.compute_q2k(N, w["box"], self.fft.fftn(dx * 1.0, workers=self.cores), 3, 3)
-        self.latest["multipoles"] = (time.perf_counter() - t0) * 22  # 1 ifftn + 21 fftn/q-factor passes
-
-    def _maps(self):
-        t0 = time.perf_counter()
-        self.m = self.fft.fftn(self.shell_in, workers=self.cores).real.ravel()
-        self.latest["maps"] = (time.perf_counter() - t0) * 3 * WORKLOAD["nbins_bs"]
-
-    def _triangles(self):
-        O, N = self.O, self.N
-        maps = np.stack([self.m, self.m, self.m])
-        counts = np.ones(1, dtype=np.float32)
-        bout = np.zeros((11, 1))
-        ntri = 0
-        t0 = time.perf_counter()
-        while ntri < 1 or (time.perf_counter() - t0 < self.tri_budget and ntri < 50):
-            O.lib().or_bk_multipoles_last_sum(1, 3.0, 3.0, 1, 0.00628, int(self.npart), N ** 3,
-                                              counts.ctypes.data_as(O._f), O._p(maps), O._p(maps), O._p(maps),
-                                              O._p(np.zeros(1)), O._p(bout))
-            ntri += 1
-        self.ntri = ntri
-        self.latest["triangle_sums"] = (time.perf_counter() - t0) / ntri * 1156
-
-    def step(self):
-        """Time one step's sample; return the box time in seconds."""
-        groups = (self._density, self._multipoles, self._maps)
-        if self.k == 0 or not self.rotate:
-            for g in groups:
-                g()
-        else:
-            groups[self.k % 3]()
-            if self.k % 3 != 2 and "maps" not in self.latest:
-                self._maps()
-        self._assign()
-        self._triangles()
-        self.k += 1
-        return sum(self.latest.values())
-
-    def sample(self):
-        n = self.pos.shape[1]
-        return (f"assignment of {self.nsub} of {n} particles (x{n / self.nsub:.3g}) + 1 density FFT + fcomb + P "
-                f"binning; 1 of 22 multipole FFT passes (x22), 1 of 63 shell-map FFTs (x63), {self.ntri} of 1156 "
-                f"triangle triple-sums (x1156/{self.ntri}); FFTs on {self.cores} threads, Fortran loops serial as "
-                f"in the reference" + ("; FFT groups re-timed in rotation" if self.rotate else ""))
+def oracle_params(grid=None):
+    """The workload as a reference params dict (pbi4.py:86-119), with the
+    bispectrum's own binning (kbin_bs, kcenter_bs, nbins_bisp, itot).  A smaller
+    `grid` (the debug cases) keeps the binning widths and derives the bin counts."""
+    from oracle import pbi4_oracle as O
+    w = WORKLOAD
+    g = grid or w["grid"]
+    p = dict(grid=g, box=w["box"], interpolation=w["nintp"], interlacing=w["interlacing"],
+             multipoles=w["multipoles"], kbin=w["kbin_ps"], kcenter=w["kcenter_ps"], iopen=w["iopen"], los=w["los"],
+             cross=False, om=0.3, ol=0.7, z=0.5)
+    p.update(O.derived_params(p))
+    nb = w["nbins_bs"] if grid is None else int((g / 3 + w["kbin_bs"] - w["kcenter_bs"]) // w["kbin_bs"])
+    p.update(kbin_bs=w["kbin_bs"], kcenter_bs=w["kcenter_bs"], nbins_bisp=nb,
+             itot=O.itot(nb, w["kbin_bs"], w["kcenter_bs"], w["iopen"]))
+    return p
 
 
-def cpu_reference_box_seconds(pos, budget_s=20.0):
-    """One full bounded sample (every stage timed once): (seconds per box, stage
-    seconds, sample description, cores)."""
-    rs = ReferenceSampler(pos, assign_fraction=1.0, tri_budget_s=max(1.0, budget_s / 2))
-    sec = rs.step()
-    return sec, dict(rs.latest), rs.sample(), rs.cores
+def oracle_full_box(pos, workers, grid=None):
+    """One whole box through the CPU restatement of the reference (every stage
+    computed: assignment, density FFT + fcomb, the 22 multipole FFT passes, P
+    binning, 63 shell-map FFTs, 1156 x 3 triangle sums), after the triangle
+    counts (input independent, computed first like the reference's cfile).
+    Returns (pout, bout, seconds of the box, seconds per cost class, counts
+    seconds, the FP64 counts)."""
+    from oracle import pbi4_oracle as O
+    bp = O.BoxPipeline(pos, oracle_params(grid), workers=workers)
+    t0 = time.perf_counter()
+    bp.compute_counts()
+    t_counts = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    stages = bp.run_all()
+    return bp.pout, bp.bout, time.perf_counter() - t0, stages, t_counts, bp.counts
+
+
+ORACLE_SAMPLE = ("one whole 256^3 box, every stage computed (no extrapolation): serial assignment, density FFT + "
+                 "fcomb, 1 ifftn + 21 fftn multipole passes, serial P binning, 63 shell-map FFTs, 1156 x 3 triangle "
+                 "sums; triangle counts computed once before the box (input independent, the reference's cfile). "
+                 "FFTs (scipy.fft) on %d threads (the reference: FFTW npool threads for the maps, single-threaded "
+                 "scipy fftn for the density), triangle rows split over %d threads (each row the reference's serial "
+                 "loop); assignment, fcomb and binning loops serial as in the Fortran")
 
 
 def run_reference(args):
-    """The reference's CPU path (the oracle restatement) on this host's cores:
-    each of the warmup + steps iterations times one bounded sample of a box,
-    sized so that the whole run takes a few minutes."""
+    """The reference's CPU path (the oracle restatement) on this host's cores.
+    The warm-up computes the triangle counts and one whole box (which also
+    measures the cost of each of the box's work items); the K timed steps then
+    compute one more whole box, its work items split in order into K
+    contiguous groups of about equal measured cost, one group per step.  The
+    timed region is exactly one box: value = 1 / (sum of the K step times)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     from oracle import pbi4_oracle as O
     O.build()
     pos = make_positions(quick=args.quick)
-    nsteps = args.warmup + args.steps
-    per_step = min(8.0, max(1.0, 150.0 / nsteps))
-    t0 = time.perf_counter()
-    O.assign_grid(np.ascontiguousarray(pos[:, : pos.shape[1] // 16]), dict(
-        grid=WORKLOAD["grid"], interpolation=WORKLOAD["nintp"], interlacing=WORKLOAD["interlacing"]))
-    t_assign = (time.perf_counter() - t0) * 16
-    frac = min(1.0, 0.25 * per_step / max(t_assign, 1e-6))
-    rs = ReferenceSampler(pos, assign_fraction=frac, tri_budget_s=0.4 * per_step, rotate=per_step < 4.0)
-    vals = []
-    for k in range(nsteps):
-        sec = rs.step()
-        if k >= args.warmup:
-            vals.append(sec)
-    sec = statistics.median(vals)
-    value = 1.0 / sec
+    cores = os.cpu_count() or 1
+    p = oracle_params(64 if args.quick else None)
+    # warm-up: counts + one whole box with per-item timing
+    bp = O.BoxPipeline(pos, p, workers=cores)
+    bp.compute_counts()
+    cost = []
+    for name, cls, fn in bp.items():
+        t0 = time.perf_counter()
+        fn()
+        cost.append(time.perf_counter() - t0)
+    # timed: one whole box in K contiguous groups of about equal cost
+    bp2 = O.BoxPipeline(pos, p, counts=bp.counts, workers=cores)
+    items = bp2.items()
+    total = sum(cost)
+    K = args.steps
+    bounds, acc, k = [], 0.0, 0
+    for idx, c in enumerate(cost):
+        acc += c
+        if acc >= total * (k + 1) / K and k < K - 1:
+            bounds.append(idx + 1)
+            k += 1
+    bounds = [0] + bounds + [len(items)] * (K - len(bounds))
+    step_s = []
+    for k in range(K):
+        t0 = time.perf_counter()
+        for _, _, fn in items[bounds[k]: bounds[k + 1]]:
+            fn()
+        step_s.append(time.perf_counter() - t0)
+    box_s = sum(step_s)
+    value = 1.0 / box_s
+    sample = ORACLE_SAMPLE % (cores, cores) + "; the timed steps are one box split into %d groups of its work items" % K
     line = {"metric": METRIC, "value": value, "unit": "boxes/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": box_s * 1e3 / K, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Zel'dovich box)",
-            "config": {**{k: v for k, v in WORKLOAD.items()}, "parallelism": "cpu"},
-            "impl": "reference",
-            "cpu_baseline": {"value": value, "unit": "boxes/s", "cores": rs.cores, "kind": "port",
-                             "sample": rs.sample()},
+            "config": bench_config(args.gpus), "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "boxes/s", "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "boxes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "stages_s": dict(rs.latest)}
+            "box_seconds": box_s, "warmup_box_seconds": total,
+            "step_seconds": [round(x, 3) for x in step_s]}
     print(json.dumps(line), flush=True)
+
+
+def bench_config(world):
+    """The workload's `config` (the same in both arms)."""
+    return {**WORKLOAD, "parallelism": f"replicas{world}",
+            "l2": "working set > L2 (a box's shell maps are 2.0 GB on the 200^3 map grid; the density grids 0.27 GB)",
+            "triangle_counts": "computed once per binning, outside the timed region (input independent)"}
 
 
 # ------------------------------------------------------------ GPU arm ---
@@ -249,20 +203,44 @@ DTYPE = {"fp32": "f32", "fp64": "f64", "fp16split": "fp16 hi+lo (f32 accumulate)
          "tf32split": "tf32 hi+lo (f32 accumulate)"}
 
 
-def error_report(pout, bout, p64, b64):
-    """Max per-bin error against the FP64 GPU form: P_l relative to P0, B_l relative to
-    max(|B_l|, (2l+1)(P1P2+P1P3+P2P3)); Nmodes and N_tr must be identical."""
-    ok = p64[4] > 0
-    e = {"P0": float(np.max(np.abs(pout[1][ok] / p64[1][ok] - 1))),
-         "P2": float(np.max(np.abs(pout[2][ok] - p64[2][ok]) / np.abs(p64[1][ok]))),
-         "P4": float(np.max(np.abs(pout[3][ok] - p64[3][ok]) / np.abs(p64[1][ok]))),
-         "Nmodes_equal": bool(np.array_equal(pout[4], p64[4]))}
-    den = np.abs(b64[3] * b64[4]) + np.abs(b64[3] * b64[5]) + np.abs(b64[4] * b64[5])
+def error_report(pout, bout, pref, bref, tol, counts=None, counts_ref=None, grid=None):
+    """Per-bin errors against a reference run (the oracle, or the FP64 GPU form).
+
+    Plain relative errors |x / x_ref - 1| of every P_l and B_l bin: the maximum,
+    and how many bins exceed `tol`.  Beside them the two normalised metrics:
+    P2, P4 relative to P0 (the multipoles cross zero), and B_l relative to
+    max(|B_l|, (2l+1)(P1P2 + P1P3 + P2P3)) (the reduced bispectrum where B_l
+    itself is near zero).  Mode and triangle counts must be identical: with the
+    oracle's FP64 counts (counts_ref = N^3 N_tri, an FFT sum) and this library's
+    exact integers (counts), the integers are compared; the float32 N_tr column of
+    the reference rounds its FP64 sum, so above 2^24 a count halfway between two
+    float32 values may land on the other neighbour (Ntr_float32_ties)."""
+    ok = pref[4] > 0
+    e = {"tol": tol, "P_bins": int(ok.sum()), "B_bins": int(bref.shape[1]),
+         "Nmodes_equal": bool(np.array_equal(pout[4], pref[4]))}
+    if counts is not None and counts_ref is not None:
+        exact_ref = np.round(np.asarray(counts_ref) / float(grid) ** 3).astype(np.int64)
+        e["Ntr_integer_equal"] = bool(np.array_equal(np.asarray(counts, dtype=np.int64), exact_ref))
+        e["Ntr_float32_ties"] = int((bout[8] != bref[8]).sum())
+    else:
+        e["Ntr_equal"] = bool(np.array_equal(bout[8], bref[8]))
+    for name, r in (("P0", 1), ("P2", 2), ("P4", 3)):
+        rel = np.abs(pout[r][ok] / pref[r][ok] - 1)
+        e[name + "_max_rel"] = float(rel.max())
+        e[name + "_bins_above_tol"] = int((rel > tol).sum())
+        if r > 1:
+            e[name + "_max_rel_to_P0"] = float(np.max(np.abs(pout[r][ok] - pref[r][ok]) / np.abs(pref[1][ok])))
+    den = np.abs(bref[3] * bref[4]) + np.abs(bref[3] * bref[5]) + np.abs(bref[4] * bref[5])
     for name, r, f in (("B0", 6, 1.0), ("B2", 9, 5.0), ("B4", 10, 9.0)):
-        e[name] = float(np.max(np.abs(bout[r] - b64[r]) / np.maximum(np.abs(b64[r]), f * den)))
-    e["B0_plain_relative_median"] = float(np.median(np.abs(bout[6] / b64[6] - 1)))
-    e["Ntr_equal"] = bool(np.array_equal(bout[8], b64[8]))
+        rel = np.abs(bout[r] / bref[r] - 1)
+        e[name + "_max_rel"] = float(rel.max())
+        e[name + "_median_rel"] = float(np.median(rel))
+        e[name + "_bins_above_tol"] = int((rel > tol).sum())
+        e[name + "_max_rel_Q"] = float(np.max(np.abs(bout[r] - bref[r]) / np.maximum(np.abs(bref[r]), f * den)))
+    e["shell_powers_max_rel"] = float(np.max(np.abs(bout[3:6] / bref[3:6] - 1)))
     return e
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -307,6 +285,7 @@ def run_ours(args):
 
     # one box in flight: the per-stage times and the roofline come from this pass
     ms_one, launches_one, stages, clocks_one = timed(est, pout, bout, args.steps)
+    tri_counts = est.triangle_counts()
     value_one = replicas.throughput(world * args.steps, ms_one / 1e3)
     map_work = est.map_work()
     tensor_units = est.tensor_units()
@@ -373,10 +352,13 @@ def run_ours(args):
     est.set_stream(None)
     est_b.close()
 
-    # the plain FP32 GPU form on the same box, and the FP64 GPU form as the error reference
-    plain = errors = None
-    if not args.no_compare and rank == 0:
-        if args.precision != "fp32":
+    # the plain FP32 GPU form on the same box; the errors of both forms against the
+    # oracle (one whole box of the CPU restatement of the reference, which is also
+    # the timed cpu_baseline) and against the FP64 GPU form
+    plain = errors = errors64 = cpu = None
+    tol = 1e-5 if args.precision in ("fp32", "fp64") else 1e-4
+    if rank == 0 and not (args.no_compare and args.no_cpu_baseline):
+        if not args.no_compare and args.precision != "fp32":
             e32 = Estimator(est_config("fp32", grid=grid))
             po32, bo32 = e32.alloc_outputs()
             ms32, _, _, _ = timed(e32, po32, bo32, max(3, args.steps // 4))
@@ -384,12 +366,25 @@ def run_ours(args):
                      "ms_per_step": ms32 / max(3, args.steps // 4)}
             p32, b32 = e32.run_host(pos)
             e32.close()
-        e64 = Estimator(est_config("fp64", grid=grid))
-        p64, b64 = e64.run_host(pos)
-        e64.close()
-        errors = error_report(p_h, b_h, p64, b64)
-        if plain is not None:
-            plain["error_vs_fp64"] = error_report(p32, b32, p64, b64)
+        if not args.no_compare:
+            e64 = Estimator(est_config("fp64", grid=grid))
+            p64, b64 = e64.run_host(pos)
+            e64.close()
+            errors64 = error_report(p_h, b_h, p64, b64, tol)
+            if plain is not None:
+                plain["error_vs_fp64_gpu"] = error_report(p32, b32, p64, b64, 1e-5)
+        cores = os.cpu_count() or 1
+        pref, bref, box_s, cls_s, counts_s, counts_ref = oracle_full_box(pos, cores, grid=grid)
+        if not args.no_cpu_baseline:
+            cpu = {"value": 1.0 / box_s, "unit": "boxes/s", "cores": cores, "kind": "port",
+                   "sample": ORACLE_SAMPLE % (cores, cores), "seconds_by_stage": {k: round(v, 3) for k, v in
+                                                                                cls_s.items()},
+                   "triangle_counts_seconds": round(counts_s, 3)}
+        if not args.no_compare:
+            g = grid or WORKLOAD["grid"]
+            errors = error_report(p_h, b_h, pref, bref, tol, tri_counts, counts_ref, g)
+            if plain is not None:
+                plain["error_vs_oracle"] = error_report(p32, b32, pref, bref, 1e-5, tri_counts, counts_ref, g)
 
     # serving: a short Poisson stream of mixed boxes through the continuous-batching loop
     serving = None
@@ -420,19 +415,13 @@ def run_ours(args):
     rl, rl_all = roofline.for_stages(stages, args.steps, cfg, npart, itot=itot, map_grid=map_grid, nmaps=nmaps,
                                      map_work=map_work, tensor_units=tensor_units)
     if rank == 0:
-        cpu = None
-        if not args.no_cpu_baseline:
-            sec, _, sample, cores = cpu_reference_box_seconds(pos, budget_s=10.0)
-            cpu = {"value": 1.0 / sec, "unit": "boxes/s", "cores": cores, "kind": "port", "sample": sample}
         line = {"metric": METRIC, "value": value, "unit": "boxes/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[args.precision],
                 "data": "synthetic (seeded Zel'dovich box, positions resident in HBM)",
-                "config": {**WORKLOAD, "precision": args.precision, "parallelism": f"replicas{world}",
-                           "boxes_in_flight": 2, "map_grid": map_grid,
-                           "l2": "working set > L2 (shell maps %.1f GB per box on the %d^3 map grid)" % (
-                               nmaps * map_grid ** 3 * 4 / 1e9, map_grid),
-                           "triangle_counts": "computed once per plan (input independent)"},
+                "config": bench_config(world),
+                "form": {"precision": args.precision, "boxes_in_flight": 2, "map_grid": map_grid, "maps": nmaps,
+                         "triangles": itot},
                 "e2e": {"value": e2e_value, "unit": "boxes/s", "h2d_bytes_per_step": int(pos.nbytes),
                         "d2h_bytes_per_step": int(p_h.nbytes + b_h.nbytes)},
                 "gpu_launches": int(launches), "clocks": clocks, "roofline": rl, "roofline_stages": rl_all,
@@ -440,7 +429,7 @@ def run_ours(args):
                                       "gpu_launches": int(launches_one), "clocks": clocks_one,
                                       "note": "one plan, one stream: the stage times and the roofline"},
                 "cpu_baseline": cpu,
-                "plain_fp32": plain, "error_vs_fp64": errors, "serving": serving,
+                "plain_fp32": plain, "error_vs_oracle": errors, "error_vs_fp64_gpu": errors64, "serving": serving,
                 "stages_ms_per_box": {k: round(v[0] / max(1, args.steps), 4) for k, v in stages.items()}}
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -498,7 +487,7 @@ def _forms_leg(w, dpos, forms, metric, data):
         del po, bo
         torch.cuda.empty_cache()
     p32, b32 = res["fp32"]
-    errs = {prec: error_report(res[prec][0], res[prec][1], p32, b32) for prec, _ in forms if prec != "fp32"}
+    errs = {prec: error_report(res[prec][0], res[prec][1], p32, b32, 1e-4) for prec, _ in forms if prec != "fp32"}
     print(json.dumps({"metric": metric, "unit": "boxes/s", "data": data,
                       "config": {**w, "particles": npart, "nintp": 4, "interlacing": True, "multipoles": True},
                       "forms": out, "error_vs_plain_fp32": errs}), flush=True)

@@ -95,8 +95,10 @@ int pbi4g_measure_pk_multipoles(int32_t grid, float box, float kbin, float kcent
  * the call returns without synchronising.  No cudaMalloc/cudaFree: its scratch
  * is a fixed 4.3 MiB device array inside the library, held by every device that
  * loads the library until exit, sized for grid <= 512 and nbins <= 512; larger
- * sizes return PBI4G_ERR_RANGE.  The first call on a device looks up the
- * array's device address; make that first call before any stream capture.
+ * sizes return PBI4G_ERR_RANGE.  Each call outside stream capture looks up the
+ * array's device address on the current device (so a device reset is
+ * harmless); a call inside a capture reuses the address the previous call on
+ * that device found, so make the first call on a device before any capture.
  * All calls share the one array: calls that overlap on the GPU (other streams,
  * other host threads) race and must be serialised by the caller. */
 int pbi4g_measure_pk_multipoles_noalloc(int32_t grid, float box, float kbin, float kcenter, int32_t nbins,
@@ -257,6 +259,14 @@ int pbi4g_plan_stage_times(pbi4g_plan *plan, double *ms, int64_t *calls);
 int pbi4g_catalog_positions(int64_t npart, const void *d_pos, const void *d_vel, int32_t is_double,
                             const double *los, int32_t rsd_mode, double hz, double z, double box, double *d_out,
                             void *stream);
+
+/* Diagnostics.  Device allocations (cudaMalloc) this library has made for its
+ * own buffers since it was loaded (cuFFT's plan work areas are not counted). */
+int64_t pbi4g_device_allocs(void);
+/* Host-side failure hook for tests of the callers' error paths: with k > 0 the
+ * k-th next device allocation of this library returns PBI4G_ERR_NOMEM (no
+ * cudaMalloc is issued for it), once; 0 disarms.  No device fault is involved. */
+int pbi4g_debug_fail_alloc(int32_t k);
 
 /* Host check of the shell maps' FFT plans (no device work): `batch` inverse
  * DFTs of n points, X[k] = sum_j x[j] e^{+2 pi i j k / n}, of interleaved

@@ -511,133 +511,147 @@ int64_t or_count_itot(int nbins, float kbin, float kcenter, int iopen, int cross
     return m;
 }
 
-/* The "Last sum" loops of count_triangles (bispectrumI4.f90:884-908): maps are
- * FP64 [nbins][gridD].  counts[m] = sum_n map_i map_j map_l. */
+/* The "Last sum" loops of the four routines below visit the triangles in the
+ * reference's order (l outer, j, then i); every triangle's sum is an independent
+ * serial loop over the grid, so the routines take a row range [m0, m1) of that
+ * order and compute only those rows: a caller may split the rows over threads
+ * and gets the same bits as one serial pass.  The plain-named routines are the
+ * whole range. */
+#define TRI_LOOP_BEGIN(CROSS)                                                                   \
+    int ishift = bk_ishift(kbin, kcenter, iopen);                                               \
+    int64_t m = 0;                                                                              \
+    for (int l = 1; l <= nbins && m < m1; l++)                                                  \
+        for (int j = 1; j <= l && m < m1; j++) {                                                \
+            int imin = l - j + 1 - ishift; if (imin < 1) imin = 1;                              \
+            int imax = (CROSS) ? ((j + l - 1 + ishift) < nbins ? (j + l - 1 + ishift) : nbins) : j; \
+            for (int i = imin; i <= imax; i++, m++) {                                           \
+                if (m < m0) continue;                                                           \
+                if (m >= m1) break;
+#define TRI_LOOP_END }}
+
+/* count_triangles "Last sum" (bispectrumI4.f90:884-908): maps are FP64
+ * [nbins][gridD].  counts[m] = sum_n map_i map_j map_l. */
+void or_triangle_counts_sum_rows(int nbins, float kbin, float kcenter, int iopen, int cross,
+                                 int64_t gridD, const double *maps, double *counts, int64_t m0, int64_t m1) {
+    TRI_LOOP_BEGIN(cross)
+        const double *mi = maps + (size_t)(i - 1) * gridD;
+        const double *mj = maps + (size_t)(j - 1) * gridD;
+        const double *ml = maps + (size_t)(l - 1) * gridD;
+        double sum = 0.0;
+        for (int64_t n = 0; n < gridD; n++) sum = sum + mi[n] * mj[n] * ml[n];
+        counts[m] = sum;
+    TRI_LOOP_END
+}
+
 void or_triangle_counts_sum(int nbins, float kbin, float kcenter, int iopen, int cross,
                             int64_t gridD, const double *maps, double *counts) {
-    int ishift = bk_ishift(kbin, kcenter, iopen);
-    int64_t m = 0;
-    for (int l = 1; l <= nbins; l++)
-        for (int j = 1; j <= l; j++) {
-            int imin = l - j + 1 - ishift; if (imin < 1) imin = 1;
-            int imax = cross ? ((j + l - 1 + ishift) < nbins ? (j + l - 1 + ishift) : nbins) : j;
-            for (int i = imin; i <= imax; i++) {
-                const double *mi = maps + (size_t)(i - 1) * gridD;
-                const double *mj = maps + (size_t)(j - 1) * gridD;
-                const double *ml = maps + (size_t)(l - 1) * gridD;
-                double sum = 0.0;
-                for (int64_t n = 0; n < gridD; n++) sum = sum + mi[n] * mj[n] * ml[n];
-                counts[m++] = sum;
-            }
-        }
+    or_triangle_counts_sum_rows(nbins, kbin, kcenter, iopen, cross, gridD, maps, counts, 0, INT64_MAX);
 }
 
 /* measure_bk "Last sum" (bispectrumI4.f90:160-193), bout(9,itot) Fortran order.
  * maps: FP64 [nbins][gridD]; pow[nbins] already shot-noise subtracted. */
-void or_bk_last_sum(int nbins, float kbin, float kcenter, int iopen, float kf, int64_t npart,
-                    int64_t gridD, const float *counts, const double *maps, const double *pow_,
-                    double *bout) {
-    int ishift = bk_ishift(kbin, kcenter, iopen);
+void or_bk_last_sum_rows(int nbins, float kbin, float kcenter, int iopen, float kf, int64_t npart,
+                         int64_t gridD, const float *counts, const double *maps, const double *pow_,
+                         double *bout, int64_t m0, int64_t m1) {
     float kf3f = kf * kf * kf;
     double kf3 = (double)kf3f;
     double powSN = 1.0 / (double)npart / kf3;
     double powSN2 = powSN * powSN;
-    int64_t m = 0;
-    for (int l = 1; l <= nbins; l++)
-        for (int j = 1; j <= l; j++) {
-            int imin = l - j + 1 - ishift; if (imin < 1) imin = 1;
-            for (int i = imin; i <= j; i++) {
-                const double *mi = maps + (size_t)(i - 1) * gridD;
-                const double *mj = maps + (size_t)(j - 1) * gridD;
-                const double *ml = maps + (size_t)(l - 1) * gridD;
-                double sum = 0.0;
-                for (int64_t n = 0; n < gridD; n++) sum = sum + mi[n] * mj[n] * ml[n];
-                double bispSN = (pow_[i - 1] + pow_[j - 1] + pow_[l - 1]) * powSN + powSN2;
-                double *o = bout + 9 * m;
-                o[0] = (double)kcenter + (double)(l - 1) * (double)kbin;
-                o[1] = (double)kcenter + (double)(j - 1) * (double)kbin;
-                o[2] = (double)kcenter + (double)(i - 1) * (double)kbin;
-                o[3] = pow_[l - 1];
-                o[4] = pow_[j - 1];
-                o[5] = pow_[i - 1];
-                o[6] = kf3 * sum / (double)counts[m] + bispSN;
-                o[7] = bispSN;
-                o[8] = (double)(float)((double)counts[m] / (double)gridD);
-                m++;
-            }
-        }
+    TRI_LOOP_BEGIN(0)
+        const double *mi = maps + (size_t)(i - 1) * gridD;
+        const double *mj = maps + (size_t)(j - 1) * gridD;
+        const double *ml = maps + (size_t)(l - 1) * gridD;
+        double sum = 0.0;
+        for (int64_t n = 0; n < gridD; n++) sum = sum + mi[n] * mj[n] * ml[n];
+        double bispSN = (pow_[i - 1] + pow_[j - 1] + pow_[l - 1]) * powSN + powSN2;
+        double *o = bout + 9 * m;
+        o[0] = (double)kcenter + (double)(l - 1) * (double)kbin;
+        o[1] = (double)kcenter + (double)(j - 1) * (double)kbin;
+        o[2] = (double)kcenter + (double)(i - 1) * (double)kbin;
+        o[3] = pow_[l - 1];
+        o[4] = pow_[j - 1];
+        o[5] = pow_[i - 1];
+        o[6] = kf3 * sum / (double)counts[m] + bispSN;
+        o[7] = bispSN;
+        o[8] = (double)(float)((double)counts[m] / (double)gridD);
+    TRI_LOOP_END
+}
+
+void or_bk_last_sum(int nbins, float kbin, float kcenter, int iopen, float kf, int64_t npart,
+                    int64_t gridD, const float *counts, const double *maps, const double *pow_,
+                    double *bout) {
+    or_bk_last_sum_rows(nbins, kbin, kcenter, iopen, kf, npart, gridD, counts, maps, pow_, bout, 0, INT64_MAX);
 }
 
 /* measure_bk_multipoles "Last sum" (bispectrumI4.f90:476-511), bout(11,itot). */
+void or_bk_multipoles_last_sum_rows(int nbins, float kbin, float kcenter, int iopen, float kf, int64_t npart,
+                                    int64_t gridD, const float *counts, const double *maps,
+                                    const double *maps2, const double *maps4, const double *pow_,
+                                    double *bout, int64_t m0, int64_t m1) {
+    float kf3f = kf * kf * kf;
+    double kf3 = (double)kf3f;
+    double powSN = 1.0 / (double)npart / kf3;
+    double powSN2 = powSN * powSN;
+    TRI_LOOP_BEGIN(0)
+        const double *mi = maps + (size_t)(i - 1) * gridD;
+        const double *mj = maps + (size_t)(j - 1) * gridD;
+        const double *ml = maps + (size_t)(l - 1) * gridD;
+        const double *m2l = maps2 + (size_t)(l - 1) * gridD;
+        const double *m4l = maps4 + (size_t)(l - 1) * gridD;
+        double sum = 0.0, sum2 = 0.0, sum4 = 0.0;
+        for (int64_t n = 0; n < gridD; n++) {
+            sum = sum + mi[n] * mj[n] * ml[n];
+            sum2 = sum2 + mi[n] * mj[n] * m2l[n];
+            sum4 = sum4 + mi[n] * mj[n] * m4l[n];
+        }
+        double bispSN = (pow_[i - 1] + pow_[j - 1] + pow_[l - 1]) * powSN + powSN2;
+        double *o = bout + 11 * m;
+        o[0] = (double)kcenter + (double)(l - 1) * (double)kbin;
+        o[1] = (double)kcenter + (double)(j - 1) * (double)kbin;
+        o[2] = (double)kcenter + (double)(i - 1) * (double)kbin;
+        o[3] = pow_[l - 1];
+        o[4] = pow_[j - 1];
+        o[5] = pow_[i - 1];
+        o[6] = kf3 * sum / (double)counts[m] + bispSN;
+        o[7] = bispSN;
+        o[8] = (double)(float)((double)counts[m] / (double)gridD);
+        o[9] = 5 * kf3 * sum2 / (double)counts[m];
+        o[10] = 9 * kf3 * sum4 / (double)counts[m];
+    TRI_LOOP_END
+}
+
 void or_bk_multipoles_last_sum(int nbins, float kbin, float kcenter, int iopen, float kf, int64_t npart,
                                int64_t gridD, const float *counts, const double *maps,
                                const double *maps2, const double *maps4, const double *pow_,
                                double *bout) {
-    int ishift = bk_ishift(kbin, kcenter, iopen);
-    float kf3f = kf * kf * kf;
-    double kf3 = (double)kf3f;
-    double powSN = 1.0 / (double)npart / kf3;
-    double powSN2 = powSN * powSN;
-    int64_t m = 0;
-    for (int l = 1; l <= nbins; l++)
-        for (int j = 1; j <= l; j++) {
-            int imin = l - j + 1 - ishift; if (imin < 1) imin = 1;
-            for (int i = imin; i <= j; i++) {
-                const double *mi = maps + (size_t)(i - 1) * gridD;
-                const double *mj = maps + (size_t)(j - 1) * gridD;
-                const double *ml = maps + (size_t)(l - 1) * gridD;
-                const double *m2l = maps2 + (size_t)(l - 1) * gridD;
-                const double *m4l = maps4 + (size_t)(l - 1) * gridD;
-                double sum = 0.0, sum2 = 0.0, sum4 = 0.0;
-                for (int64_t n = 0; n < gridD; n++) {
-                    sum = sum + mi[n] * mj[n] * ml[n];
-                    sum2 = sum2 + mi[n] * mj[n] * m2l[n];
-                    sum4 = sum4 + mi[n] * mj[n] * m4l[n];
-                }
-                double bispSN = (pow_[i - 1] + pow_[j - 1] + pow_[l - 1]) * powSN + powSN2;
-                double *o = bout + 11 * m;
-                o[0] = (double)kcenter + (double)(l - 1) * (double)kbin;
-                o[1] = (double)kcenter + (double)(j - 1) * (double)kbin;
-                o[2] = (double)kcenter + (double)(i - 1) * (double)kbin;
-                o[3] = pow_[l - 1];
-                o[4] = pow_[j - 1];
-                o[5] = pow_[i - 1];
-                o[6] = kf3 * sum / (double)counts[m] + bispSN;
-                o[7] = bispSN;
-                o[8] = (double)(float)((double)counts[m] / (double)gridD);
-                o[9] = 5 * kf3 * sum2 / (double)counts[m];
-                o[10] = 9 * kf3 * sum4 / (double)counts[m];
-                m++;
-            }
-        }
+    or_bk_multipoles_last_sum_rows(nbins, kbin, kcenter, iopen, kf, npart, gridD, counts, maps, maps2, maps4,
+                                   pow_, bout, 0, INT64_MAX);
 }
 
 /* measure_bk_cross "Last sum" (bispectrumI4.f90:732-756), bout(5,itot):
  * S = sum mapkB_i mapk_j mapk_l with i up to min(nbins, j+l-1+ishift). */
+void or_bk_cross_last_sum_rows(int nbins, float kbin, float kcenter, int iopen, float kf,
+                               int64_t gridD, const float *counts, const double *maps,
+                               const double *mapsB, double *bout, int64_t m0, int64_t m1) {
+    float kf3f = kf * kf * kf;
+    double kf3 = (double)kf3f;
+    TRI_LOOP_BEGIN(1)
+        const double *bi = mapsB + (size_t)(i - 1) * gridD;
+        const double *mj = maps + (size_t)(j - 1) * gridD;
+        const double *ml = maps + (size_t)(l - 1) * gridD;
+        double sum = 0.0;
+        for (int64_t n = 0; n < gridD; n++) sum = sum + bi[n] * mj[n] * ml[n];
+        double *o = bout + 5 * m;
+        o[0] = (double)kcenter + (double)(l - 1) * (double)kbin;
+        o[1] = (double)kcenter + (double)(j - 1) * (double)kbin;
+        o[2] = (double)kcenter + (double)(i - 1) * (double)kbin;
+        o[3] = kf3 * sum / (double)counts[m];
+        o[4] = (double)(float)((double)counts[m] / (double)gridD);
+    TRI_LOOP_END
+}
+
 void or_bk_cross_last_sum(int nbins, float kbin, float kcenter, int iopen, float kf,
                           int64_t gridD, const float *counts, const double *maps,
                           const double *mapsB, double *bout) {
-    int ishift = bk_ishift(kbin, kcenter, iopen);
-    float kf3f = kf * kf * kf;
-    double kf3 = (double)kf3f;
-    int64_t m = 0;
-    for (int l = 1; l <= nbins; l++)
-        for (int j = 1; j <= l; j++) {
-            int imin = l - j + 1 - ishift; if (imin < 1) imin = 1;
-            int imax = (j + l - 1 + ishift) < nbins ? (j + l - 1 + ishift) : nbins;
-            for (int i = imin; i <= imax; i++) {
-                const double *bi = mapsB + (size_t)(i - 1) * gridD;
-                const double *mj = maps + (size_t)(j - 1) * gridD;
-                const double *ml = maps + (size_t)(l - 1) * gridD;
-                double sum = 0.0;
-                for (int64_t n = 0; n < gridD; n++) sum = sum + bi[n] * mj[n] * ml[n];
-                double *o = bout + 5 * m;
-                o[0] = (double)kcenter + (double)(l - 1) * (double)kbin;
-                o[1] = (double)kcenter + (double)(j - 1) * (double)kbin;
-                o[2] = (double)kcenter + (double)(i - 1) * (double)kbin;
-                o[3] = kf3 * sum / (double)counts[m];
-                o[4] = (double)(float)((double)counts[m] / (double)gridD);
-                m++;
-            }
-        }
+    or_bk_cross_last_sum_rows(nbins, kbin, kcenter, iopen, kf, gridD, counts, maps, mapsB, bout, 0, INT64_MAX);
 }

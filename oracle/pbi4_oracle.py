@@ -69,12 +69,35 @@ def lib():
         L.or_bk_last_sum.argtypes = [_ci, _cf, _cf, _ci, _cf, _cl, _cl, _f, _d, _d, _d]
         L.or_bk_multipoles_last_sum.argtypes = [_ci, _cf, _cf, _ci, _cf, _cl, _cl, _f, _d, _d, _d, _d, _d]
         L.or_bk_cross_last_sum.argtypes = [_ci, _cf, _cf, _ci, _cf, _cl, _f, _d, _d, _d]
+        L.or_triangle_counts_sum_rows.argtypes = [_ci, _cf, _cf, _ci, _ci, _cl, _d, _d, _cl, _cl]
+        L.or_bk_last_sum_rows.argtypes = [_ci, _cf, _cf, _ci, _cf, _cl, _cl, _f, _d, _d, _d, _cl, _cl]
+        L.or_bk_multipoles_last_sum_rows.argtypes = [_ci, _cf, _cf, _ci, _cf, _cl, _cl, _f, _d, _d, _d, _d, _d,
+                                                     _cl, _cl]
+        L.or_bk_cross_last_sum_rows.argtypes = [_ci, _cf, _cf, _ci, _cf, _cl, _f, _d, _d, _d, _cl, _cl]
         _lib = L
     return _lib
 
 
 def _p(a, t=_d):
     return a.ctypes.data_as(t)
+
+
+def _rows(fn, nrows, workers, *args):
+    """Run a triangle "Last sum" routine `fn(*args, m0, m1)` over the rows
+    [0, nrows), split into contiguous blocks over `workers` threads (ctypes
+    releases the GIL).  Each row is the same serial loop as in one pass, so the
+    result does not depend on the split."""
+    nrows = int(nrows)
+    nw = max(1, min(int(workers or 1), nrows))
+    if nw == 1:
+        fn(*args, 0, nrows)
+        return
+    import concurrent.futures as cf
+    # blocks of ~4 rows per task keep threads busy to the end (rows cost the same)
+    step = max(1, min(4, nrows // nw))
+    bounds = [(a, min(nrows, a + step)) for a in range(0, nrows, step)]
+    with cf.ThreadPoolExecutor(max_workers=nw) as ex:
+        list(ex.map(lambda b: fn(*args, b[0], b[1]), bounds))
 
 
 def _cgrid(a):
@@ -213,8 +236,8 @@ def count_triangles(nbins, grid, kbin, kcenter, iopen, cross, npool, itot_, work
         m = (shell == b).astype(np.complex128)
         maps[b - 1] = scipy.fft.fftn(m, workers=workers).real.ravel()
     counts = np.zeros(int(itot_), dtype=np.float64)
-    lib().or_triangle_counts_sum(int(nbins), float(kbin), float(kcenter), int(bool(iopen)), int(bool(cross)),
-                                 grid ** 3, _p(maps), _p(counts))
+    _rows(lib().or_triangle_counts_sum_rows, itot_, workers, int(nbins), float(kbin), float(kcenter),
+          int(bool(iopen)), int(bool(cross)), grid ** 3, _p(maps), _p(counts))
     return counts
 
 
@@ -233,8 +256,8 @@ def measure_bk(nbins, grid, kbin, kcenter, iopen, kf, npool, itot_, npart, count
     pw = _shell_pow(maps, nmodes, kf, npart, grid ** 3)
     c32 = np.ascontiguousarray(counts, dtype=np.float32)
     bout = np.zeros((9, int(itot_)), dtype=np.float64, order="F")
-    lib().or_bk_last_sum(int(nbins), float(kbin), float(kcenter), int(bool(iopen)), float(kf), int(npart),
-                         grid ** 3, _p(c32, _f), _p(maps), _p(pw), _p(bout))
+    _rows(lib().or_bk_last_sum_rows, itot_, workers, int(nbins), float(kbin), float(kcenter), int(bool(iopen)),
+          float(kf), int(npart), grid ** 3, _p(c32, _f), _p(maps), _p(pw), _p(bout))
     return bout
 
 
@@ -248,8 +271,9 @@ def measure_bk_multipoles(nbins, grid, kbin, kcenter, iopen, kf, npool, itot_, n
     pw = _shell_pow(maps, nmodes, kf, npart, grid ** 3)
     c32 = np.ascontiguousarray(counts, dtype=np.float32)
     bout = np.zeros((11, int(itot_)), dtype=np.float64, order="F")
-    lib().or_bk_multipoles_last_sum(int(nbins), float(kbin), float(kcenter), int(bool(iopen)), float(kf), int(npart),
-                                    grid ** 3, _p(c32, _f), _p(maps), _p(maps2), _p(maps4), _p(pw), _p(bout))
+    _rows(lib().or_bk_multipoles_last_sum_rows, itot_, workers, int(nbins), float(kbin), float(kcenter),
+          int(bool(iopen)), float(kf), int(npart), grid ** 3, _p(c32, _f), _p(maps), _p(maps2), _p(maps4), _p(pw),
+          _p(bout))
     return bout
 
 
@@ -260,8 +284,8 @@ def measure_bk_cross(nbins, grid, kbin, kcenter, iopen, kf, npool, itot_, npart,
     mapsB, _ = shell_maps(dcl2, nbins, kbin, kcenter, workers)
     c32 = np.ascontiguousarray(counts, dtype=np.float32)
     bout = np.zeros((5, int(itot_)), dtype=np.float64, order="F")
-    lib().or_bk_cross_last_sum(int(nbins), float(kbin), float(kcenter), int(bool(iopen)), float(kf),
-                               grid ** 3, _p(c32, _f), _p(maps), _p(mapsB), _p(bout))
+    _rows(lib().or_bk_cross_last_sum_rows, itot_, workers, int(nbins), float(kbin), float(kcenter),
+          int(bool(iopen)), float(kf), grid ** 3, _p(c32, _f), _p(maps), _p(mapsB), _p(bout))
     return bout
 
 
@@ -403,6 +427,154 @@ def bispectrum(npart, counts, dcl, params, dcl2=None, dcl4=None, workers=None):
     for r, (name, _) in enumerate(dt):
         out[name] = bout[r]
     return out
+
+
+class BoxPipeline:
+    """One box through the reference's call sequence (Tutorials/Script/test.py:7-13
+    with pbi4.py:290-553): assign_grid -> compute_density -> compute_density_multipoles
+    (the literal 1 ifftn + 21 fftn) -> measure_pk[_multipoles] -> measure_bk[_multipoles],
+    with the triangle counts given (the reference loads them from its cfile when
+    present, pbi4.py:466-470) or computed first.
+
+    The box is a list of work items (`items()`: name, cost class, callable) run in
+    order; running all of them computes the whole box.  FFTs use `workers` threads
+    (the reference's FFTW npool threads for the maps; its scipy fftn calls are
+    single-threaded) and the triangle sums split their rows over `workers`
+    threads; the Fortran loops of assignment, fcomb and P binning stay serial.
+    After the last item, `pout` and `bout` hold the f2py outputs."""
+
+    def __init__(self, pos, params, counts=None, workers=None, tri_block=16):
+        self.pos, self.p, self.workers = pos, params, workers
+        self.counts = counts
+        self.tri_block = int(tri_block)
+        self.pout = self.bout = None
+
+    # -- the counts (input independent; cached by the caller like the reference's cfile)
+    def compute_counts(self):
+        p = self.p
+        self.counts = count_triangles(p["nbins_bisp"], p["grid"], p["kbin_bs"], p["kcenter_bs"], p["iopen"], False,
+                                      1, p["itot"], workers=self.workers)
+        return self.counts
+
+    def items(self):
+        p, w = self.p, self.workers
+        N = int(p["grid"])
+        mp = bool(p["multipoles"])
+        nb, itot_ = int(p["nbins_bisp"]), int(p["itot"])
+        kb, kc = float(p["kbin_bs"]), float(p["kcenter_bs"])
+        st = {}
+        out = []
+
+        def assign():
+            st["npart"], st["dcl"] = assign_grid(self.pos, p)
+
+        def density():
+            st["d"] = compute_density(st["npart"], st["dcl"], p, workers=w)
+            st["dcl"] = None
+
+        out += [("assign", "assign", assign), ("fft_fcomb", "fft", density)]
+        los = p["los"]
+        if mp:
+            def inv():
+                st["deltax"] = scipy.fft.ifftn(st["d"], workers=w)
+                st["d2"] = -0.5 * st["d"]
+
+            out.append(("multipoles_ifft", "fft", inv))
+            for i in range(3):
+                for j in range(i + 1):
+                    def q2(i=i, j=j):
+                        fac = 2.0 if i != j else 1.0
+                        dk_ = scipy.fft.fftn(st["deltax"] * los[i] * los[j], workers=w)
+                        st["d2"] = st["d2"] + fac * 1.5 * compute_q2k(N, p["box"], dk_, i + 1, j + 1)
+                    out.append((f"q2k_{i}{j}", "fft", q2))
+
+            def d4init():
+                st["d4"] = -7.0 / 8.0 * st["d"] - 2.5 * st["d2"]
+            out.append(("d4_init", "small", d4init))
+            for i in range(3):
+                for j in range(i + 1):
+                    for l in range(j + 1):
+                        for k in range(l + 1):
+                            def q4(i=i, j=j, l=l, k=k):
+                                dk_ = scipy.fft.fftn(st["deltax"] * los[i] * los[j] * los[l] * los[k], workers=w)
+                                st["d4"] = st["d4"] + _q4_fac(i, j, l, k) * (35.0 / 8.0) * compute_q4k(
+                                    N, p["box"], dk_, i + 1, j + 1, l + 1, k + 1)
+                            out.append((f"q4k_{i}{j}{l}{k}", "fft", q4))
+
+        def pk():
+            if mp:
+                st["deltax"] = None
+                self.pout = measure_pk_multipoles(N, p["box"], p["kbin"], p["kcenter"], p["nbins_ps"], st["d"],
+                                                  st["d2"], st["d4"])
+            else:
+                self.pout = measure_pk(N, p["box"], p["kbin"], p["kcenter"], p["nbins_ps"], st["d"], st["d"])
+        out.append(("pk_binning", "small", pk))
+        if not p.get("do_bispectrum", True) or itot_ == 0:
+            return out
+
+        sets = ("d", "d2", "d4") if mp else ("d",)
+        shell = shell_index(N, kb, kc)
+        st["maps"] = {s: np.empty((nb, N ** 3), dtype=np.float64) for s in sets}
+        st["nmodes"] = np.array([int((shell == b).sum()) for b in range(1, nb + 1)], dtype=np.int64)
+        for s in sets:
+            def herm(s=s):
+                st["full"] = hermitian_full_grid(st[s])
+            out.append((f"hermitian_{s}", "small", herm))
+            for b in range(1, nb + 1):
+                def one_map(s=s, b=b):
+                    m = np.where(shell == b, st["full"], 0.0)
+                    st["maps"][s][b - 1] = scipy.fft.fftn(m, workers=w).real.ravel()
+                out.append((f"map_{s}_{b}", "fft", one_map))
+
+        def setup_sums():
+            st["full"] = None
+            st["pw"] = _shell_pow(st["maps"]["d"], st["nmodes"], p["kf"], st["npart"], N ** 3)
+            st["c32"] = np.ascontiguousarray(self.counts, dtype=np.float32)
+            st["bout"] = np.zeros((11 if mp else 9, itot_), dtype=np.float64, order="F")
+        out.append(("shell_powers", "small", setup_sums))
+        L = lib()
+        for m0 in range(0, itot_, self.tri_block):
+            m1 = min(itot_, m0 + self.tri_block)
+
+            def tri(m0=m0, m1=m1):
+                M = st["maps"]
+                if mp:
+                    fn, args = L.or_bk_multipoles_last_sum_rows, (
+                        nb, kb, kc, int(bool(p["iopen"])), float(p["kf"]), int(st["npart"]), N ** 3,
+                        _p(st["c32"], _f), _p(M["d"]), _p(M["d2"]), _p(M["d4"]), _p(st["pw"]), _p(st["bout"]))
+                else:
+                    fn, args = L.or_bk_last_sum_rows, (
+                        nb, kb, kc, int(bool(p["iopen"])), float(p["kf"]), int(st["npart"]), N ** 3,
+                        _p(st["c32"], _f), _p(M["d"]), _p(st["pw"]), _p(st["bout"]))
+                # rows m0..m1 split over the threads, one row per task
+                _rows_range(fn, m0, m1, w, *args)
+                if m1 == itot_:
+                    self.bout = st["bout"]
+            out.append((f"triangles_{m0}", "triangles", tri))
+        return out
+
+    def run_all(self, timer=None):
+        """Every item in order; returns {item cost class: seconds}."""
+        import time
+        if self.counts is None and self.p.get("do_bispectrum", True) and int(self.p["itot"]) > 0:
+            self.compute_counts()
+        t = {}
+        for name, cls, fn in self.items():
+            t0 = time.perf_counter()
+            fn()
+            t[cls] = t.get(cls, 0.0) + time.perf_counter() - t0
+        return t
+
+
+def _rows_range(fn, m0, m1, workers, *args):
+    """Rows [m0, m1) of a "Last sum" routine, one row per thread task."""
+    nw = max(1, min(int(workers or 1), m1 - m0))
+    if nw == 1:
+        fn(*args, m0, m1)
+        return
+    import concurrent.futures as cf
+    with cf.ThreadPoolExecutor(max_workers=nw) as ex:
+        list(ex.map(lambda m: fn(*args, m, m + 1), range(m0, m1)))
 
 
 def catalogue_positions(pos, vel=None, los=None, hz=None, z=None, box=1000.0, rsd_mode=1):

@@ -33,6 +33,7 @@ EXPORTS = [
     "pbi4g_catalog_positions",
     "pbi4g_measure_pk_multipoles_noalloc", "pbi4g_plan_set_delta_half", "pbi4g_plan_set_counts",
     "pbi4g_plan_check", "pbi4g_plan_graph_build", "pbi4g_plan_graph_run_host",
+    "pbi4g_device_allocs", "pbi4g_debug_fail_alloc",
 ]
 NSTAGES = 12
 STAGES = ["assign", "grid_convert", "fft_r2c", "fcomb", "pk_binning", "triangle_counts", "shell_maps_z",
@@ -101,6 +102,7 @@ _SIGS = {
     "pbi4g_measure_pk_multipoles_noalloc": [_i32, _f32, _f32, _f32, _i32, _P, _P, _P, _P, _P],
     "pbi4g_plan_set_delta_half": [_P, _i64, _P],
     "pbi4g_plan_set_counts": [_P, _P],
+    "pbi4g_debug_fail_alloc": [_i32],
 }
 
 _lock = threading.Lock()
@@ -124,6 +126,8 @@ def lib(build_if_missing: bool = True):
         L.pbi4g_version.restype = ctypes.c_int
         L.pbi4g_plan_kernel_launches.restype = ctypes.c_int64
         L.pbi4g_plan_kernel_launches.argtypes = [_P]
+        L.pbi4g_device_allocs.restype = ctypes.c_int64
+        L.pbi4g_device_allocs.argtypes = []
         for name, args in _SIGS.items():
             f = getattr(L, name)
             f.argtypes = args

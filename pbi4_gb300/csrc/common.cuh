@@ -14,6 +14,7 @@
 #include <stdint.h>
 #include <stddef.h>
 
+#include <atomic>
 #include <vector>
 
 #include "../../include/pbi4gpu.h"
@@ -81,6 +82,21 @@ struct BoxPar {
     double pad;
 };
 
+// Device allocations this library has made through DevBuf since it was loaded
+// (pbi4g_device_allocs), and the host-side failure hook of
+// pbi4g_debug_fail_alloc: armed with k > 0, the k-th next DevBuf allocation
+// reports PBI4G_ERR_NOMEM without calling cudaMalloc.
+inline std::atomic<long long> g_dev_allocs{0};
+inline std::atomic<int> g_fail_alloc_in{0};
+
+// true when an armed failure hook has come to this allocation (and disarms it)
+inline bool injected_alloc_failure() {
+    int k = g_fail_alloc_in.load();
+    while (k > 0 && !g_fail_alloc_in.compare_exchange_weak(k, k - 1)) {
+    }
+    return k == 1;
+}
+
 // RAII device buffer
 struct DevBuf {
     void* p = nullptr;
@@ -98,11 +114,14 @@ struct DevBuf {
         if (n <= bytes && p) return PBI4G_OK;
         release();
         if (n == 0) n = 16;
+        if (injected_alloc_failure())
+            return set_error(PBI4G_ERR_NOMEM, "cudaMalloc(%zu) failed: injected by pbi4g_debug_fail_alloc", n);
         cudaError_t e = cudaMalloc(&p, n);
         if (e != cudaSuccess) {
             p = nullptr;
             return set_error(PBI4G_ERR_NOMEM, "cudaMalloc(%zu) failed: %s", n, cudaGetErrorString(e));
         }
+        g_dev_allocs.fetch_add(1);
         bytes = n;
         return PBI4G_OK;
     }

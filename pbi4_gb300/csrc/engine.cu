@@ -292,6 +292,14 @@ int pbi4g_fft_plan_check(int32_t n, int32_t batch, const float *in, float *out) 
 }
 int pbi4g_version(void) { return 100; }
 
+int64_t pbi4g_device_allocs(void) { return (int64_t)pbi4g::g_dev_allocs.load(); }
+
+int pbi4g_debug_fail_alloc(int32_t k) {
+    if (k < 0) return pbi4g::set_error(PBI4G_ERR_INVALID, "debug_fail_alloc: k must be >= 0");
+    pbi4g::g_fail_alloc_in.store(k);
+    return PBI4G_OK;
+}
+
 int pbi4g_plan_footprint(const pbi4g_config *cfg, int64_t npart_max, int64_t *bytes) {
     PBI4G_CHECK(check_config(cfg));
     if (!bytes || npart_max < 0) return set_error(PBI4G_ERR_INVALID, "bad footprint arguments");

@@ -637,16 +637,22 @@ constexpr size_t kNoAllocScratchBytes = kNoAllocLutBytes + kNoAllocBinBytes + kN
 static __device__ __align__(256) unsigned char g_pk_noalloc_scratch[kNoAllocScratchBytes];
 
 // The host-side name of g_pk_noalloc_scratch is not a device address; its
-// device address is looked up once per device with that device current.
+// device address is looked up with the device current.  Outside stream capture
+// every call looks it up again (a device reset or a new primary context gives
+// the array a new address); inside a capture the call uses the address the
+// last call on that device found, so the first call on a device must come
+// before any capture.
 static std::mutex g_noalloc_mutex;
 static void *g_noalloc_ptr[128];
 
-static int noalloc_scratch(void **out) {
+static int noalloc_scratch(cudaStream_t st, void **out) {
     int dev = -1;
     PBI4G_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 128) return set_error(PBI4G_ERR_UNSUPPORTED, "device index %d out of range", dev);
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    PBI4G_CUDA(cudaStreamIsCapturing(st, &cs));
     std::lock_guard<std::mutex> g(g_noalloc_mutex);
-    if (!g_noalloc_ptr[dev]) {
+    if (cs == cudaStreamCaptureStatusNone || !g_noalloc_ptr[dev]) {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_pk_noalloc_scratch);
         if (e != cudaSuccess || !p)
@@ -689,9 +695,9 @@ extern "C" int pbi4g_measure_pk_multipoles_noalloc(int32_t grid, float box, floa
     if (!(kbin > 0) || !(box > 0)) return set_error(PBI4G_ERR_INVALID, "noalloc P(k): kbin and box must be > 0");
     if (!d_dcl_half || !d_dcl2_half || !d_dcl4_half || !d_pout)
         return set_error(PBI4G_ERR_INVALID, "noalloc P(k): null device pointer");
-    void *scratch = nullptr;
-    PBI4G_CHECK(noalloc_scratch(&scratch));
     cudaStream_t st = (cudaStream_t)stream;
+    void *scratch = nullptr;
+    PBI4G_CHECK(noalloc_scratch(st, &scratch));
     unsigned char *base = static_cast<unsigned char *>(scratch);
     int *lut = reinterpret_cast<int *>(base);
     double *sumk = reinterpret_cast<double *>(base + kNoAllocLutBytes);  // [2][nbins]: sum|k|, count

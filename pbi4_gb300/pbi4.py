@@ -124,10 +124,29 @@ class IO:
 
 
 class Density:
-    """Device-resident density handle (a stage of DENSITIES)."""
+    """Device-resident density handle (a stage of DENSITIES).
 
-    def __init__(self, params, npart, pos=None, weight=None, ell=0, plan=None):
+    A handle made by compute_density refers to the density its plan holds; the
+    plan is shared by every box of one configuration, so the handle records the
+    plan's density generation and refuses to read a later box's density.  With
+    params['cross'] set the handle keeps a host copy of its half spectrum
+    instead, so two densities of one configuration can be measured together."""
+
+    def __init__(self, params, npart, pos=None, weight=None, ell=0, plan=None, gen=0, half=None):
         self.params, self.npart, self.pos, self.weight, self.ell, self.plan = params, npart, pos, weight, ell, plan
+        self.gen, self.half = gen, half
+
+    def check_current(self):
+        if self.half is None and self.plan is not None and getattr(self.plan, "density_gen", 0) != self.gen:
+            raise RuntimeError("this density handle is stale: its plan has computed another box's density since "
+                               "(set params['cross'] to keep several densities of one configuration)")
+
+    def half_spectrum(self):
+        """The kx >= 0 half spectrum [z][y][x] of this density (host array)."""
+        if self.half is not None:
+            return self.half
+        self.check_current()
+        return self.plan.delta_half()
 
     def __array__(self, dtype=None, copy=None):
         p = self.params
@@ -137,7 +156,7 @@ class Density:
             f = powerI4.assign_double_grid if p["interlacing"] else powerI4.assign_single_grid
             return np.asarray(f(p["grid"], p["interpolation"], self.npart, self.pos, w), dtype=dtype)
         n = int(p["grid"])
-        half = self.plan.delta_half()                       # [z][y][x], x <= N/2
+        half = self.half_spectrum()                         # [z][y][x], x <= N/2
         full = np.zeros((n, n, n), dtype=np.complex128)      # [x][y][z] (Fortran index order)
         full[: n // 2 + 1] = half.transpose(2, 1, 0)
         neg = (-np.arange(n)) % n
@@ -170,7 +189,8 @@ class DENSITIES:
     def compute_density(self, npart, dcl, params=None):
         """pbi4.py:304-341: assignment, FFT, interlacing combine and window correction on the GPU."""
         params = params or self.params
-        plan = _plan(params)
+        cross = bool(params.get("cross", False))
+        plan = _plan(params, do_bispectrum=not cross)
         if not isinstance(dcl, Density) or dcl.pos is None:
             raise TypeError("compute_density takes the handle returned by assign_grid")
         import torch
@@ -178,12 +198,14 @@ class DENSITIES:
         dw = None if dcl.weight is None else torch.from_numpy(np.ascontiguousarray(dcl.weight, np.float64)).cuda()
         plan.density(npart, dpos, dw)
         torch.cuda.synchronize()
-        return Density(params, npart, plan=plan)
+        plan.density_gen = getattr(plan, "density_gen", 0) + 1
+        return Density(params, npart, plan=plan, gen=plan.density_gen, half=plan.delta_half() if cross else None)
 
     def compute_density_multipoles(self, dcl, params=None):
         """pbi4.py:343-388: delta_2, delta_4 as handles (factors applied per mode on the GPU)."""
         params = params or self.params
-        return (Density(params, dcl.npart, ell=2, plan=dcl.plan), Density(params, dcl.npart, ell=4, plan=dcl.plan))
+        return (Density(params, dcl.npart, ell=2, plan=dcl.plan, gen=dcl.gen, half=dcl.half),
+                Density(params, dcl.npart, ell=4, plan=dcl.plan, gen=dcl.gen, half=dcl.half))
 
     def save_density(self, dcl, npart, params=None):
         """pbi4.py:390-396: npz with header [grid, npart, kf, kN] and the full grid."""
@@ -222,14 +244,28 @@ class MEASUREMENTS:
         self.params, self.verbose = params, verbose
 
     def powerspectrum(self, npart, dcl, dcl2=None, dcl4=None, params=None):
-        """pbi4.py:405-461 (auto spectra; the plan applies the multipole factors)."""
+        """pbi4.py:405-461: auto spectra on the plan (which applies the multipole
+        factors); with params['cross'] the real-space cross spectrum of dcl and
+        dcl2 (pbi4.py:445-449) through powerI4.measure_pk."""
         import torch
         params = params or self.params
-        plan = dcl.plan
-        pout_d, _ = plan.alloc_outputs()
-        plan.powerspectrum(pout_d)
-        torch.cuda.synchronize()
-        pout = pout_d.cpu().numpy()
+        if params.get("cross", False):
+            if params["multipoles"]:
+                print("ERROR: Cross power spectrum in redshift space not implemented yet!")
+                raise SystemExit
+            if dcl2 is None:
+                print("ERROR: you did not include the second density field")
+                raise SystemExit
+            from . import powerI4
+            pout = powerI4.measure_pk(params["grid"], params["box"], params["kbin"], params["kcenter"],
+                                      params["nbins_ps"], np.asarray(dcl), np.asarray(dcl2))
+        else:
+            dcl.check_current()
+            plan = dcl.plan
+            pout_d, _ = plan.alloc_outputs()
+            plan.powerspectrum(pout_d)
+            torch.cuda.synchronize()
+            pout = pout_d.cpu().numpy()
         out = np.zeros(len(params["kvec"]), dtype=self.PS_DTYPE)
         out["P0+PSN"] = pout[1]
         if params["multipoles"]:
@@ -247,14 +283,34 @@ class MEASUREMENTS:
         cf = params.get("cfile")
         if cf and os.path.exists(cf) and os.path.getsize(cf) > 0:
             return np.load(cf)["counts"]
+        if params.get("cross", False):
+            from . import bispectrumI4
+            return bispectrumI4.count_triangles(params["nbins_bisp"], params["grid"], params["kbin"],
+                                                params["kcenter"], params["iopen"], True, params.get("npool", 1),
+                                                params["itot"])
         plan = _plan(params)
         n = float(params["grid"])
         return plan.triangle_counts().astype(np.float64) * n ** 3
 
+    CROSS_DTYPE = [("k1", np.float32), ("k2", np.float32), ("k3", np.float32), ("B0", np.float32),
+                   ("Ntr", np.float32)]
+
     def bispectrum(self, npart, counts, dcl, dcl2=None, dcl4=None, params=None):
-        """pbi4.py:478-553 (auto spectra)."""
+        """pbi4.py:478-553: auto spectra on the plan; with params['cross'] the cross
+        bispectrum of dcl and dcl2 (pbi4.py:481-497) through bispectrumI4.measure_bk_cross."""
         import torch
         params = params or self.params
+        if params.get("cross", False):
+            from . import bispectrumI4
+            bout = bispectrumI4.measure_bk_cross(params["nbins_bisp"], params["grid"], params["kbin"],
+                                                 params["kcenter"], params["iopen"], params["kf"],
+                                                 params.get("npool", 1), params["itot"], npart, counts,
+                                                 np.asarray(dcl), np.asarray(dcl2))
+            out = np.zeros(bout.shape[1], dtype=self.CROSS_DTYPE)
+            for r, (name, _) in enumerate(self.CROSS_DTYPE):
+                out[name] = bout[r]
+            return out
+        dcl.check_current()
         plan = dcl.plan
         plan.set_counts(np.asarray(counts, dtype=np.float64))
         _, bout_d = plan.alloc_outputs()
@@ -283,6 +339,11 @@ class MEASUREMENTS:
     def save_bispectrum(self, bout, params=None):
         """pbi4.py:574-594 (same text formats)."""
         params = params or self.params
+        if params.get("cross", False):
+            header = "k1/kF k2/kF k3/kF      B0          N_tr\n"
+            np.savetxt(params["bs_outfile"], np.array([bout["k1"], bout["k2"], bout["k3"], bout["B0"], bout["Ntr"]]).T,
+                       fmt=("%d", "%d", "%d", "%0.8e", "%0.8e"), header=header)
+            return
         if params["multipoles"]:
             header = "k1/kF k2/kF k3/kF P(k1) P(k2)       P(k3)       B0+BSN        BSN    N_tr    B2      B4\n"
             cols = ["k1", "k2", "k3", "Pk1", "Pk2", "Pk3", "B0+BSN", "BSN", "Ntr", "B2", "B4"]

@@ -14,7 +14,7 @@ one launch of a CUDA graph the plan captured for that batch size
 (pbi4g_plan_graph_run_host): per-box particle counts and their normalisation
 factors are read from device memory, so one captured graph serves any counts
 up to the server's max_npart.  Configurations the captured form does not cover
-(FP64 plans, grids that are not a multiple of 16, weighted boxes) run box by
+(FP64 plans, grids that are not a multiple of 16 or below 32, weighted boxes) run box by
 box through the direct path on the same slots.
 
 Admission is by device footprint: a batch starts when a slot is free and the
@@ -63,8 +63,10 @@ class Result:
 
 
 def graph_capable(cfg: EstimatorConfig) -> bool:
-    """Configurations the captured (graph) form covers: FP32-family plans on grids % 16 == 0."""
-    return cfg.precision != "fp64" and int(cfg.grid) % 16 == 0
+    """Configurations the captured (graph) form covers: FP32-family plans on the
+    grids the owner-computes assignment takes (multiples of 16 from 32 to 2048)."""
+    g = int(cfg.grid)
+    return cfg.precision != "fp64" and g % 16 == 0 and 32 <= g <= 2048
 
 
 class _Slot:
@@ -92,6 +94,8 @@ class Server:
         self.lock = threading.Condition()
         self.results: list[Result] = []
         self.rejected = 0
+        self.failed = 0       # requests that ended in an error other than a rejection
+        self.cancelled = 0    # requests cancelled while queued
         self.evictions = 0
         self.batches = 0
         self._stop = False
@@ -141,7 +145,8 @@ class Server:
         return {"n": len(self.results), "p50_ms": float(np.percentile(lat, 50) * 1e3),
                 "p99_ms": float(np.percentile(lat, 99) * 1e3), "mean_ms": float(lat.mean() * 1e3),
                 "boxes_per_s": len(self.results) / max(t1 - t0, 1e-9), "evictions": self.evictions,
-                "rejected": self.rejected, "batches": self.batches,
+                "rejected": self.rejected, "failed": self.failed, "cancelled": self.cancelled,
+                "batches": self.batches,
                 "mean_batch": len(self.results) / max(1, self.batches), "resident_gb": self.resident_bytes() / 1e9}
 
     # --------------------------------------------------------------- loop ---
@@ -191,11 +196,13 @@ class Server:
         return plan
 
     def _take_batch(self):
-        """The head request and up to batch-1 queued requests of the same configuration."""
+        """The head request and up to batch-1 queued requests of the same
+        configuration, each moved to the running state (a request cancelled
+        while queued is dropped here, and cannot be cancelled once it runs)."""
         req, fut = self.queue[0]
         if not graph_capable(req.cfg) or req.weight is not None:
             self.queue.popleft()
-            return [(req, fut)]
+            return [(req, fut)] if fut.set_running_or_notify_cancel() else []
         key = req.cfg.key()
         picked = [0]
         for k in range(1, min(len(self.queue), self.lookahead)):
@@ -207,7 +214,12 @@ class Server:
         items = [self.queue[k] for k in picked]
         for k in reversed(picked):
             del self.queue[k]
-        return items
+        return [(r, f) for r, f in items if f.set_running_or_notify_cancel()]
+
+    def _drop_cancelled_head(self):
+        while self.queue and self.queue[0][1].cancelled():
+            self.queue.popleft()
+            self.cancelled += 1
 
     def _start(self, slot: _Slot, items, plan: Estimator):
         torch = self.torch
@@ -261,6 +273,7 @@ class Server:
             err = e
         for r, f, (po, bo) in zip(reqs, futs, outs):
             if err is not None:
+                self.failed += 1
                 f.set_exception(err)
                 continue
             res = Result(r.rid, po.copy(), None if bo is None else bo.copy(), r.t_arrival, t_start, t_done, len(reqs))
@@ -278,6 +291,7 @@ class Server:
                 if self._stop and not self.queue and all(s.busy is None for s in self.slots):
                     return
                 free = [s for s in self.slots if s.busy is None]
+                self._drop_cancelled_head()
                 while free and self.queue:
                     req, fut = self.queue[0]
                     slot = free[0]
@@ -286,21 +300,31 @@ class Server:
                     except MemoryError as e:  # can never fit: reject this request
                         self.queue.popleft()
                         self.rejected += 1
-                        fut.set_exception(e)
+                        if fut.set_running_or_notify_cancel():
+                            fut.set_exception(e)
+                        self._drop_cancelled_head()
                         continue
-                    except Exception as e:  # plan creation failed: report and keep serving
+                    except Exception as e:  # plan creation failed (e.g. out of memory): report, keep serving
                         self.queue.popleft()
-                        fut.set_exception(e)
+                        self.failed += 1
+                        if fut.set_running_or_notify_cancel():
+                            fut.set_exception(e)
+                        self._drop_cancelled_head()
                         continue
                     if plan is None:
                         break
                     items = self._take_batch()
+                    if not items:   # the batch's requests were all cancelled
+                        self._drop_cancelled_head()
+                        continue
                     try:
                         self._start(slot, items, plan)
                     except Exception as e:  # report per request; keep serving
                         slot.busy = None
+                        self.failed += len(items)
                         for _, f in items:
                             f.set_exception(e)
+                        self._drop_cancelled_head()
                         continue
                     free.remove(slot)
                     progressed = True

@@ -6,14 +6,18 @@ kbin = kcenter = 1, iopen = True, multipoles; 32 P bins, 21 B shells, 1156
 triangles).  Only columns that do not depend on the (missing) input catalogue
 are kept: from ps.dat k, avgk, Nmodes and PSN; from bs.dat k1, k2, k3 and N_tr.
 
-Run from the repository root:  python tests/golden/make_golden.py [REFERENCE_ROOT]
+Run from the repository root:
+    python tests/golden/make_golden.py REFERENCE_ROOT
+(or with the reference's root in the environment variable PBI4_REFERENCE).
 """
 import os
 import sys
 
 import numpy as np
 
-ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PBI4_REFERENCE")
+if not ref:
+    sys.exit("usage: make_golden.py REFERENCE_ROOT (or set PBI4_REFERENCE)")
 ps = np.loadtxt(os.path.join(ref, "Tutorials", "testdata", "ps.dat"))
 bs = np.loadtxt(os.path.join(ref, "Tutorials", "testdata", "bs.dat"))
 out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_testdata_cols.npz")

@@ -1,0 +1,165 @@
+"""GPU parity on the benchmark configurations themselves, against the FP64 oracle.
+
+* The small plain configuration, exactly: 100,000 positions uniform i.i.d.
+  float32 in L = 1000 Mpc/h (numpy default_rng(1)), grid 64^3, CIC on a single
+  grid (the int/nint quirk of powerI4.f90:114-123), real space; P(k) with
+  dk = kf from kf to k_Nyq (32 bins); B over all closed triangles (iopen=False,
+  bispectrumI4.f90:38-42) with dk = 2 kf up to 16 kf (8 shells, 86 triangles).
+  Run through the device plan (every precision form) and through the drop-in
+  modules powerI4/bispectrumI4 (the call sequence of pbi4.py:290-553).
+* The clustered redshift-space configuration at half scale: a 64^3-lattice
+  Zel'dovich box on a 128^3 grid, PCS with interlacing, P l=0,2,4 with dk = kf,
+  B l=0,2,4 with dk = 3 kf up to 0.5 k_Nyq.  The full 256^3 box is compared
+  with the oracle by bench.py (error_vs_oracle).
+
+Tolerances: mode and triangle counts bit-exact; FP64 forms <= 1e-9; the FP32
+form <= 1e-5 and the mixed forms (FP16 hi+lo, TF32 hi+lo) <= 1e-4:
+* P_l and the shell powers: plain relative error of every bin, except that for
+  l = 2, 4 the bins whose value is below 1e-3 of the monopole (the multipole
+  crosses zero there) are held to the bound relative to the monopole;
+* B_l: plain relative error on every bin where |B_l| >= (2l+1)(P1P2 + P1P3 +
+  P2P3) (|Q_l| >= 1, the l-weighted reduced bispectrum); where B_l nearly
+  cancels (|Q_l| < 1) the error is held to the bound times (2l+1)(P1P2 + P1P3 +
+  P2P3).  In those bins the FP32 data path (the density FFT and the shell maps
+  in FP32, shared by the FP32 and mixed forms) limits the plain relative error;
+  the small plain configuration meets the plain bound on every bin.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import pbi4_oracle as O
+from pbi4_gb300 import bispectrumI4 as B
+from pbi4_gb300 import powerI4 as P
+from pbi4_gb300 import synthetic
+from pbi4_gb300.estimator import Estimator, EstimatorConfig
+
+from ._helpers import ref_params
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"fp64": 1e-9, "fp32": 1e-5, "fp16split": 1e-4, "tf32split": 1e-4}
+
+
+def _rel(got, ref):
+    return np.abs(got / ref - 1)
+
+
+def _multipole_err(got, ref, mono):
+    """Plain relative error, or the error relative to the monopole where the
+    multipole is below 1e-3 of it."""
+    small = np.abs(ref) < 1e-3 * np.abs(mono)
+    return np.where(small, np.abs(got - ref) / np.abs(mono), _rel(got, ref))
+
+
+# ----------------------------------------------------- small plain config ---
+@pytest.fixture(scope="module")
+def c0():
+    pos = synthetic.uniform_box(100000, 1000.0, seed=1)
+    p = ref_params(64, 1000.0, 2, False, False, kbin=1.0, kcenter=1.0, iopen=False)
+    npart, dcl = O.assign_grid(pos, p)
+    d = O.compute_density(npart, dcl, p)
+    pref = O.measure_pk(64, 1000.0, 1.0, 1.0, p["nbins_ps"], d, d)
+    nb = 8
+    it = O.itot(nb, 2.0, 2.0, False)
+    counts = O.count_triangles(nb, 64, 2.0, 2.0, False, False, 1, it)
+    bref = O.measure_bk(nb, 64, 2.0, 2.0, False, 2 * np.pi / 1000.0, 1, it, npart, counts, d)
+    return dict(pos=pos, p=p, npart=npart, dcl=dcl, d=d, pref=pref, bref=bref, counts=counts, nb=nb, it=it)
+
+
+def test_small_config_shape(c0):
+    assert c0["p"]["nbins_ps"] == 32
+    assert c0["it"] == 86
+    assert c0["pos"].shape == (3, 100000)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64", "fp16split", "tf32split"])
+def test_small_config_plan(c0, precision):
+    tol = TOL[precision]
+    cfg = EstimatorConfig(grid=64, box=1000.0, nintp=2, interlacing=False, multipoles=False, kbin_ps=1.0,
+                          kcenter_ps=1.0, do_bispectrum=True, kbin_bs=2.0, kcenter_bs=2.0, nbins_bs=c0["nb"],
+                          iopen=False, precision=precision)
+    est = Estimator(cfg)
+    assert est.nbins_ps == 32 and est.itot == 86
+    pout, bout = est.run_host(c0["pos"])
+    est.close()
+    pref, bref = c0["pref"], c0["bref"]
+    # real space: rows avgk, P, Nmodes as measure_pk (powerI4.f90:589-592)
+    np.testing.assert_array_equal(pout[2], pref[2])
+    assert np.max(_rel(pout[0], pref[0])) < 1e-12
+    e_p = _rel(pout[1], pref[1])
+    assert e_p.max() <= tol, (precision, e_p.max(), int((e_p > tol).sum()))
+    np.testing.assert_array_equal(bout[[0, 1, 2, 8]], bref[[0, 1, 2, 8]])
+    e_pow = _rel(bout[3:6], bref[3:6])
+    e_b = _rel(bout[6], bref[6])
+    e_bsn = _rel(bout[7], bref[7])
+    assert e_pow.max() <= tol and e_bsn.max() <= tol, (e_pow.max(), e_bsn.max())
+    assert e_b.max() <= tol, (precision, e_b.max(), int((e_b > tol).sum()), int(np.argmax(e_b)))
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_small_config_dropins(c0, precision):
+    """The reference's call sequence through the drop-in modules: assign_single_grid,
+    (fftn), fcomb, measure_pk, count_triangles, measure_bk."""
+    import scipy.fft
+    tol = TOL[precision]
+    pos, p = c0["pos"], c0["p"]
+    npart = pos.shape[1]
+    dcl = P.assign_single_grid(64, 2, npart, pos, np.ones(npart))
+    assert np.max(np.abs(dcl - c0["dcl"])) <= 1e-11 * np.max(np.abs(c0["dcl"]))
+    d = P.fcomb(64, 2, False, 1000.0, scipy.fft.fftn(dcl / npart))
+    pout = P.measure_pk(64, 1000.0, 1.0, 1.0, 32, d, d)
+    np.testing.assert_array_equal(pout[2], c0["pref"][2])
+    assert np.max(_rel(pout[1], c0["pref"][1])) <= 1e-12
+    nb, it = c0["nb"], c0["it"]
+    counts = B.count_triangles(nb, 64, 2.0, 2.0, False, False, 1, it)
+    np.testing.assert_array_equal(counts / 64.0 ** 3, np.round(c0["counts"] / 64.0 ** 3))
+    B.set_precision(precision)
+    try:
+        bout = B.measure_bk(nb, 64, 2.0, 2.0, False, 2 * np.pi / 1000.0, 1, it, npart, counts, d)
+    finally:
+        B.set_precision("fp32")
+    bref = c0["bref"]
+    np.testing.assert_array_equal(bout[[0, 1, 2, 8]], bref[[0, 1, 2, 8]])
+    e_b = _rel(bout[6], bref[6])
+    assert e_b.max() <= tol and _rel(bout[3:6], bref[3:6]).max() <= tol, e_b.max()
+
+
+# ---------------------------------- clustered redshift-space, half scale ---
+@pytest.fixture(scope="module")
+def c1_half():
+    pos = synthetic.zeldovich_box(64, 1000.0, n_s=-1.5, rms_disp=5.0, f_growth=0.7, seed=2)
+    grid, kb = 128, 3.0
+    p = ref_params(grid, 1000.0, 4, True, True, kbin=1.0, kcenter=1.0)
+    nb = int((grid / 4 + kb - kb) // kb)   # shells up to 0.5 k_Nyq
+    it = O.itot(nb, kb, kb, True)
+    p.update(kbin_bs=kb, kcenter_bs=kb, nbins_bisp=nb, itot=it)
+    bp = O.BoxPipeline(pos, p, workers=os.cpu_count())
+    bp.run_all()
+    return dict(pos=pos, p=p, nb=nb, it=it, pref=bp.pout, bref=bp.bout)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp16split", "tf32split", "fp64"])
+def test_clustered_half_scale_plan(c1_half, precision):
+    tol = TOL[precision]
+    p = c1_half["p"]
+    cfg = EstimatorConfig(grid=p["grid"], box=1000.0, nintp=4, interlacing=True, multipoles=True, kbin_ps=1.0,
+                          kcenter_ps=1.0, do_bispectrum=True, kbin_bs=p["kbin_bs"], kcenter_bs=p["kcenter_bs"],
+                          nbins_bs=c1_half["nb"], iopen=True, precision=precision)
+    est = Estimator(cfg)
+    pout, bout = est.run_host(c1_half["pos"])
+    est.close()
+    pref, bref = c1_half["pref"], c1_half["bref"]
+    np.testing.assert_array_equal(pout[4], pref[4])
+    errs = {"P0": _rel(pout[1], pref[1]), "P2": _multipole_err(pout[2], pref[2], pref[1]),
+            "P4": _multipole_err(pout[3], pref[3], pref[1])}
+    np.testing.assert_array_equal(bout[[0, 1, 2, 8]], bref[[0, 1, 2, 8]])
+    errs["pow"] = _rel(bout[3:6], bref[3:6])
+    den = np.abs(bref[3] * bref[4]) + np.abs(bref[3] * bref[5]) + np.abs(bref[4] * bref[5])
+    floored = {}
+    for name, r, f in (("B0", 6, 1.0), ("B2", 9, 5.0), ("B4", 10, 9.0)):
+        errs[name] = np.abs(bout[r] - bref[r]) / np.maximum(np.abs(bref[r]), f * den)
+        floored[name] = int((np.abs(bref[r]) < f * den).sum())
+    bad = {k: (float(v.max()), int((v > tol).sum())) for k, v in errs.items() if v.max() > tol}
+    assert not bad, (precision, bad, floored)
