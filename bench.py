@@ -290,50 +290,52 @@ def run_ours(args):
     map_work = est.map_work()
     tensor_units = est.tensor_units()
 
-    # two boxes in flight (the batched form): two plans on two streams take the
-    # boxes in turn, so one box's low-occupancy phases (kernel tails, the tile
-    # scan, the small kernels) overlap the other's work
-    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    # K boxes in flight (the batched form): K plans on K streams take the boxes
+    # in turn, so one box's low-occupancy phases (kernel tails, the tile scan,
+    # the small kernels) overlap the others' work
+    K = max(1, args.boxes_in_flight)
+    streams = [torch.cuda.Stream() for _ in range(K)]
     est.set_stream(streams[0])
-    est_b = Estimator(cfg, stream=streams[1])
-    ests = [est, est_b]
-    outs = [(pout, bout), est_b.alloc_outputs()]
+    ests = [est] + [Estimator(cfg, stream=streams[k]) for k in range(1, K)]
+    outs = [(pout, bout)] + [e.alloc_outputs() for e in ests[1:]]
     for e, (po, bo) in zip(ests, outs):
         for _ in range(args.warmup):
             e.run_device(npart, dpos, po, bo)
     torch.cuda.synchronize()
-    l0 = est.launches + est_b.launches
-    start, stop, joined = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
-                           torch.cuda.Event())
+    l0 = sum(e.launches for e in ests)
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    joined = [torch.cuda.Event() for _ in range(K)]
     barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         start.record(streams[0])
-        streams[1].wait_event(start)
+        for k in range(1, K):
+            streams[k].wait_event(start)
         for i in range(args.steps):
-            ests[i % 2].run_device(npart, dpos, *outs[i % 2])
-        joined.record(streams[1])
-        streams[0].wait_event(joined)
+            ests[i % K].run_device(npart, dpos, *outs[i % K])
+        for k in range(1, K):
+            joined[k].record(streams[k])
+            streams[0].wait_event(joined[k])
         stop.record(streams[0])
         torch.cuda.synchronize()
     barrier()
     for e in ests:
         e.check()
     ms_max = replicas.max_over_ranks(start.elapsed_time(stop))
-    launches = est.launches + est_b.launches - l0
+    launches = sum(e.launches for e in ests) - l0
     clocks = clk.summary()
     value = replicas.throughput(world * args.steps, ms_max / 1e3)
 
     # e2e: host (pinned) positions in, host results out, through the C-ABI call
-    # (pbi4g_plan_run_host), two callers (host threads, one plan and stream each)
-    # so one box's copies overlap the other's kernels
+    # (pbi4g_plan_run_host), K callers (host threads, one plan and stream each)
+    # so one box's copies overlap the others' kernels
     import threading as _th
     hpos = torch.from_numpy(pos).pin_memory().numpy()
     for e in ests:
         for _ in range(2):
             e.run_host(hpos)
-    e2e_steps = max(2, args.steps // 2)
-    results = [[], []]
+    e2e_steps = max(K, args.steps // 2)
+    results = [[] for _ in range(K)]
 
     def caller(k, n):
         for _ in range(n):
@@ -341,7 +343,7 @@ def run_ours(args):
 
     barrier()
     t0 = time.perf_counter()
-    th = [_th.Thread(target=caller, args=(k, (e2e_steps + 1 - k) // 2)) for k in range(2)]
+    th = [_th.Thread(target=caller, args=(k, len(range(k, e2e_steps, K)))) for k in range(K)]
     for t in th:
         t.start()
     for t in th:
@@ -350,7 +352,8 @@ def run_ours(args):
     e2e_value = replicas.throughput(world * e2e_steps, e2e_s)
     p_h, b_h = results[0][-1]
     est.set_stream(None)
-    est_b.close()
+    for e in ests[1:]:
+        e.close()
 
     # the plain FP32 GPU form on the same box; the errors of both forms against the
     # oracle (one whole box of the CPU restatement of the reference, which is also
@@ -397,14 +400,21 @@ def run_ours(args):
                                           precision=args.precision)
         live = serve_workload.run_stream(reqs, hbm_budget_gb=200.0, slots=3, batch=4, realtime=True)
         sat = serve_workload.run_stream(reqs, hbm_budget_gb=200.0, slots=3, batch=4, realtime=False)
-        serial = serve_workload.run_serial_plain(reqs)
+        n_serial = min(len(reqs), 500)
+        serial = serve_workload.run_serial_plain(reqs[:n_serial])
+        r3 = lambda x: round(x, 3)
         serving = {"requests": live["n"], "offered_rate_hz": args.serve_rate,
-                   "p50_ms": round(live["p50_ms"], 3), "p99_ms": round(live["p99_ms"], 3),
+                   "p50_ms": r3(live["p50_ms"]), "p99_ms": r3(live["p99_ms"]),
+                   "queue_p50_ms": r3(live["queue_p50_ms"]), "queue_p99_ms": r3(live["queue_p99_ms"]),
+                   "service_p50_ms": r3(live["service_p50_ms"]), "service_p99_ms": r3(live["service_p99_ms"]),
+                   "p99_tail": {k: (r3(v) if isinstance(v, float) else v) for k, v in live["tail"].items()},
+                   "plans_built_during_stream": live["plans_built"], "evictions": live["evictions"],
                    "boxes_per_s_offered_load": round(live["boxes_per_s"], 2),
                    "boxes_per_s_saturated": round(sat["boxes_per_s"], 2),
-                   "p50_ms_saturated": round(sat["p50_ms"], 3), "p99_ms_saturated": round(sat["p99_ms"], 3),
+                   "p50_ms_saturated": r3(sat["p50_ms"]), "p99_ms_saturated": r3(sat["p99_ms"]),
                    "mean_graph_batch_saturated": round(sat["mean_batch"], 2),
                    "serial_plain_fp32_boxes_per_s": round(serial["boxes_per_s"], 2),
+                   "serial_plain_fp32_sample": f"the first {n_serial} requests",
                    "workload": "Poisson arrivals; grid in {128,192,256,384}; npart log-uniform [1e5, %.0e]; uniform "
                                "or Zel'dovich (P~k^n, n in [-2,-1]) positions; CIC/TSC/PCS; interlacing on/off; P-only "
                                "or P+B (dk=2kf to 0.5 kNyq); plans warmed before the stream (resident plans); "
@@ -420,7 +430,7 @@ def run_ours(args):
                 "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[args.precision],
                 "data": "synthetic (seeded Zel'dovich box, positions resident in HBM)",
                 "config": bench_config(world),
-                "form": {"precision": args.precision, "boxes_in_flight": 2, "map_grid": map_grid, "maps": nmaps,
+                "form": {"precision": args.precision, "boxes_in_flight": K, "map_grid": map_grid, "maps": nmaps,
                          "triangles": itot},
                 "e2e": {"value": e2e_value, "unit": "boxes/s", "h2d_bytes_per_step": int(pos.nbytes),
                         "d2h_bytes_per_step": int(p_h.nbytes + b_h.nbytes)},
@@ -445,10 +455,11 @@ LARGE_BOX = dict(workload="zeldovich_1024_pcs_interlaced_P024_B024_51shells", la
                  kbin_bs=4.0, kcenter_bs=4.0, nbins_bs=51, map_budget_mb=24576)
 
 
-def _forms_leg(w, dpos, forms, metric, data):
+def _forms_leg(w, dpos, forms, metric, data, ref="fp32", print_line=True):
     """Time each (precision, steps) of `forms` on the device-resident box dpos
     (after one untimed run that builds tables, counts and buffers) and report
-    errors of the mixed forms against the plain FP32 form."""
+    the errors of the other forms against the form `ref` (the plain FP32 form,
+    or the FP64 GPU form)."""
     import torch
     from pbi4_gb300.estimator import Estimator, EstimatorConfig
     npart = int(dpos.shape[1])
@@ -486,28 +497,39 @@ def _forms_leg(w, dpos, forms, metric, data):
         est.close()
         del po, bo
         torch.cuda.empty_cache()
-    p32, b32 = res["fp32"]
-    errs = {prec: error_report(res[prec][0], res[prec][1], p32, b32, 1e-4) for prec, _ in forms if prec != "fp32"}
-    print(json.dumps({"metric": metric, "unit": "boxes/s", "data": data,
-                      "config": {**w, "particles": npart, "nintp": 4, "interlacing": True, "multipoles": True},
-                      "forms": out, "error_vs_plain_fp32": errs}), flush=True)
+    pr, br = res[ref]
+    errs = {prec: error_report(res[prec][0], res[prec][1], pr, br, 1e-5 if prec == "fp32" else 1e-4)
+            for prec, _ in forms if prec != ref}
+    line = {"metric": metric, "unit": "boxes/s", "data": data,
+            "config": {**w, "particles": npart, "nintp": 4, "interlacing": True, "multipoles": True},
+            "forms": out, ("error_vs_plain_fp32" if ref == "fp32" else "error_vs_fp64_gpu"): errs}
+    if print_line:
+        print(json.dumps(line), flush=True)
+    return line
 
 
 def run_precision_form(args):
     """The 512^3 precision form: a 256^3-lattice Zel'dovich box in L = 2000 Mpc/h,
     grid 512^3, PCS interlaced, P l=0,2,4 (dk = kf), B l=0,2,4 with dk = 2 kf up to
     0.6 k_Nyq (76 shells, 228 maps on the 480^3 map grid).  The FP16 hi+lo and BF16
-    tensor-core forms run beside the plain FP32 form; errors are reported against
-    the plain FP32 form (an FP64 run of this box would need ~200 GB of FP64 maps and
-    a minute of FP64 triangle sums)."""
+    tensor-core forms run beside the plain FP32 form, with their errors against
+    it; then the FP16 hi+lo and plain FP32 forms run beside the FP64 GPU form on
+    the first 40 shells (all 76 in FP64 would need about 200 GB of FP64 maps),
+    with their errors against FP64."""
     import torch
     from pbi4_gb300 import synthetic
     w = PRECISION_FORM
     pos = synthetic.zeldovich_box(w["lattice"], w["box"], n_s=-1.5, rms_disp=5.0, f_growth=0.7, seed=2)
     dpos = torch.from_numpy(pos).cuda()
-    _forms_leg(w, dpos, (("fp16split", 2), ("bf16", 2), ("fp32", 1)),
-               "P+B boxes/s @512^3 PCS interlaced, 76 shells (precision form)",
-               "synthetic (seeded Zel'dovich box, positions resident in HBM)")
+    data = "synthetic (seeded Zel'dovich box, positions resident in HBM)"
+    full = _forms_leg(w, dpos, (("fp16split", 2), ("bf16", 2), ("fp32", 1)),
+                      "P+B boxes/s @512^3 PCS interlaced, 76 shells (precision form)", data, print_line=False)
+    # FP64 reference on a stated subset: the first 40 of the 76 shells (k up to
+    # 0.32 k_Nyq; the FP64 maps of all 76 would need about 200 GB)
+    sub = _forms_leg({**w, "nbins_bs": 40, "workload": w["workload"] + "_first40shells"}, dpos,
+                     (("fp16split", 2), ("fp32", 1), ("fp64", 1)), "", data, ref="fp64", print_line=False)
+    full["fp64_subset"] = {"shells": 40, "forms": sub["forms"], "error_vs_fp64_gpu": sub["error_vs_fp64_gpu"]}
+    print(json.dumps(full), flush=True)
 
 
 def run_large_box(args):
@@ -515,16 +537,24 @@ def run_large_box(args):
     generated on the device) in L = 3000 Mpc/h, grid 1024^3, PCS interlaced, P
     l=0,2,4 (dk = kf), B l=0,2,4 with dk = 4 kf up to 0.4 k_Nyq (51 shells).  The
     FP16 hi+lo form runs beside the plain FP32 form with a 24 GiB budget for the
-    slab-sized map buffers; errors against the plain FP32 form."""
+    slab-sized map buffers, with its errors against the plain FP32 form; then both
+    run beside the FP64 GPU form on the first 25 shells, with their errors against
+    FP64."""
     import torch
     from pbi4_gb300 import synthetic
     w = LARGE_BOX
     dpos = synthetic.zeldovich_box_device(w["lattice"], w["box"], n_s=-1.5, rms_disp=5.0, f_growth=0.7, seed=4)
     torch.cuda.synchronize()
     torch.cuda.empty_cache()
-    _forms_leg(w, dpos, (("fp16split", 2), ("fp32", 1)),
-               "P+B boxes/s @1024^3 PCS interlaced, 51 shells (large single box)",
-               "synthetic (seeded Zel'dovich box generated on the device, positions resident in HBM)")
+    data = "synthetic (seeded Zel'dovich box generated on the device, positions resident in HBM)"
+    full = _forms_leg(w, dpos, (("fp16split", 2), ("fp32", 1)),
+                      "P+B boxes/s @1024^3 PCS interlaced, 51 shells (large single box)", data, print_line=False)
+    # FP64 reference on a stated subset: the first 25 of the 51 shells (k up to
+    # 0.2 k_Nyq; the FP64 maps of all 51 would need over 300 GB)
+    sub = _forms_leg({**w, "nbins_bs": 25, "workload": w["workload"] + "_first25shells"}, dpos,
+                     (("fp16split", 2), ("fp32", 1), ("fp64", 1)), "", data, ref="fp64", print_line=False)
+    full["fp64_subset"] = {"shells": 25, "forms": sub["forms"], "error_vs_fp64_gpu": sub["error_vs_fp64_gpu"]}
+    print(json.dumps(full), flush=True)
 
 
 def main():
@@ -535,9 +565,11 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", default="fp16split", choices=["fp32", "fp64", "fp16split", "bf16", "tf32split"])
     ap.add_argument("--no-compare", action="store_true", help="skip the plain-FP32 and FP64 comparison runs")
-    ap.add_argument("--serve-requests", type=int, default=400, help="requests in the serving leg (0: skip)")
+    ap.add_argument("--serve-requests", type=int, default=2000, help="requests in the serving leg (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="offered request rate of the serving leg (1/s)")
     ap.add_argument("--serve-npart-max", type=float, default=1e7, help="largest particle count of a served box")
+    ap.add_argument("--boxes-in-flight", type=int, default=2,
+                    help="plans (one stream each) taking the timed boxes in turn")
     ap.add_argument("--quick", action="store_true", help="small box (debug only)")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: 64^3 particles on a 128^3 grid (same kernels, a few hundred MB)")

@@ -268,6 +268,15 @@ int64_t pbi4g_device_allocs(void);
  * cudaMalloc is issued for it), once; 0 disarms.  No device fault is involved. */
 int pbi4g_debug_fail_alloc(int32_t k);
 
+/* Diagnostic limit of the plan's tensor-core triangle sums: after `polls`
+ * polls (non-blocking) a main-loop barrier wait gives up, so that the waits run
+ * out on healthy work and the launch takes its abort path (every role stops,
+ * the copies and tensor-core work in flight are waited for with the normal
+ * limit, tensor memory is freed) and the call returns PBI4G_ERR_TIMEOUT.  0
+ * restores the normal limit (about 4 million polls).  For tests of the callers'
+ * error handling; no device fault is involved. */
+int pbi4g_plan_debug_wait_limit(pbi4g_plan *plan, int64_t polls);
+
 /* Host check of the shell maps' FFT plans (no device work): `batch` inverse
  * DFTs of n points, X[k] = sum_j x[j] e^{+2 pi i j k / n}, of interleaved
  * complex FP32 rows in[t][n][2] -> out[t][n][2], computed on the CPU with the

@@ -45,7 +45,13 @@ def up_to_date() -> bool:
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
-    if not force and up_to_date():
+    """Compile and link the library (in parallel, one nvcc per .cu).  Extra
+    nvcc flags (e.g. -D tuning macros) may come from the environment variable
+    PBI4G_NVCC_EXTRA; the library is rebuilt when they change."""
+    extra = os.environ.get("PBI4G_NVCC_EXTRA", "").split()
+    stamp = os.path.join(OUT, "nvcc_extra.txt")
+    prev = open(stamp).read() if os.path.exists(stamp) else ""
+    if not force and up_to_date() and prev == " ".join(extra):
         return LIB
     os.makedirs(OUT, exist_ok=True)
     nv = nvcc()
@@ -53,7 +59,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     def compile_one(src):
         obj = os.path.join(OUT, os.path.basename(src)[:-3] + ".o")
-        cmd = [nv, *ARCH, *NVCC_FLAGS, "-c", src, "-o", obj]
+        cmd = [nv, *ARCH, *NVCC_FLAGS, *extra, "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}\n{r.stderr}")
@@ -69,6 +75,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    with open(stamp, "w") as f:
+        f.write(" ".join(extra))
     return LIB
 
 

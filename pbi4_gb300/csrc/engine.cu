@@ -644,6 +644,12 @@ int pbi4g_plan_check(pbi4g_plan *p) {
     return p->cfg.do_bispectrum ? p->bk.check(p->st) : PBI4G_OK;
 }
 
+int pbi4g_plan_debug_wait_limit(pbi4g_plan *p, int64_t polls) {
+    if (!p || polls < 0) return set_error(PBI4G_ERR_INVALID, "debug_wait_limit: null plan or negative limit");
+    p->bk.tmp.wait_limit = polls > 0xFFFFFFFFLL ? 0u : (uint32_t)polls;
+    return PBI4G_OK;
+}
+
 int pbi4g_plan_enable_timing(pbi4g_plan *p, int32_t enable) {
     if (!p) return set_error(PBI4G_ERR_INVALID, "null plan");
     p->prof.on = enable != 0;

@@ -168,19 +168,38 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *tm, in
         : "memory");
 }
 
-// Bounded wait that also gives up once another role has aborted.
-__device__ __forceinline__ bool wait_or_abort(uint64_t *bar, uint32_t parity, volatile int *abort_flag) {
-    for (uint32_t i = 0; i < kWaitLimit; i++) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if ((i & 255) == 255 && *abort_flag) return false;
+// Suspend-time hint of the main-loop waits (ns; 0: plain polling).
+#ifndef PBI4G_TM_WAIT_HINT_NS
+#define PBI4G_TM_WAIT_HINT_NS 0
+#endif
+
+// Bounded wait of the main loop that also gives up once another role has
+// aborted: kWaitLimit polls.  The diagnostic instantiation (D) polls `limit`
+// times without blocking instead, so that such waits run out on healthy work
+// (pbi4g_plan_debug_wait_limit); everything else in the kernel is the same.
+template <bool D>
+__device__ __forceinline__ bool wait_or_abort(uint64_t *bar, uint32_t parity, volatile int *abort_flag,
+                                              uint32_t limit) {
+    if constexpr (D) {
+        for (uint32_t i = 0; i < limit; i++)
+            if (mbar_test_wait(bar, parity)) return true;
+        return false;
+    } else {
+        for (uint32_t i = 0; i < kWaitLimit; i++) {
+            if (PBI4G_TM_WAIT_HINT_NS > 0 ? mbar_try_wait_sleep(bar, parity, PBI4G_TM_WAIT_HINT_NS)
+                                          : mbar_try_wait(bar, parity))
+                return true;
+            if ((i & 255) == 255 && *abort_flag) return false;
+        }
+        return false;
     }
-    return false;
 }
 
 // The same, with one answer for the whole warp (the tcgen05 loads and stores
 // that follow are warp-collective: every lane takes the same branch).
-__device__ __forceinline__ bool warp_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag) {
-    return __all_sync(0xffffffffu, wait_or_abort(bar, parity, abort_flag));
+template <bool D>
+__device__ __forceinline__ bool warp_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag, uint32_t limit) {
+    return __all_sync(0xffffffffu, wait_or_abort<D>(bar, parity, abort_flag, limit));
 }
 
 // Barrier parity of the completion, for chunk i, of a barrier used every `every` chunks.
@@ -229,9 +248,10 @@ struct TmArgs {
     const int *mexp;       // FP16 form: per-map exponent e, map stored times 2^e (|M| 2^e <= 2^14)
     double *partial;       // [ksplit][nslots]
     int *err;              // set to 1 when a bounded wait gives up
+    uint32_t wait_limit;   // polls of a main-loop wait (kWaitLimit unless a diagnostic limit is set)
 };
 
-template <int F>
+template <int F, bool D>
 __global__ void __launch_bounds__(kThreads, 1)
     trisum_tm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmBh,
                      const __grid_constant__ CUtensorMap tmBl, const TmArgs a) {
@@ -302,9 +322,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         Ring rs(grp, nst);  // stage and full-barrier phase of chunk i
         for (int i = grp; i < n; i += kGroups, rs.step(kGroups, nst)) {
             const int s = rs.idx, as = i % AST;
-            if (!warp_wait(&full[s], (uint32_t)rs.phase, abort_flag)) { fail(); break; }
+            if (!warp_wait<D>(&full[s], (uint32_t)rs.phase, abort_flag, a.wait_limit)) { fail(); break; }
             // the A stage is free once the MMAs of chunk i - AST completed (MMAs complete in order)
-            if (i >= AST && !warp_wait(&done[(i - AST) % kDone], ph(i - AST, kDone), abort_flag)) {
+            if (i >= AST && !warp_wait<D>(&done[(i - AST) % kDone], ph(i - AST, kDone), abort_flag, a.wait_limit)) {
                 fail();
                 break;
             }
@@ -325,13 +345,22 @@ __global__ void __launch_bounds__(kThreads, 1)
                                     *reinterpret_cast<const float4 *>(blk + pr.x * 128 + ((c ^ (pr.x & 7)) << 4));
                                 const float4 v =
                                     *reinterpret_cast<const float4 *>(blk + pr.y * 128 + ((c ^ (pr.y & 7)) << 4));
-                                const float p[4] = {u.x * v.x, u.y * v.y, u.z * v.z, u.w * v.w};
-#pragma unroll
-                                for (int e = 0; e < 4; e++) {
-                                    const uint32_t h = __float_as_uint(p[e]) & kTfMask;
-                                    hi[4 * c4 + e] = h;
-                                    lo[4 * c4 + e] = __float_as_uint(p[e] - __uint_as_float(h));
-                                }
+                                const float2 p01 = __fmul2_rn(make_float2(u.x, u.y), make_float2(v.x, v.y));
+                                const float2 p23 = __fmul2_rn(make_float2(u.z, u.w), make_float2(v.z, v.w));
+                                const float2 h01 = make_float2(__uint_as_float(__float_as_uint(p01.x) & kTfMask),
+                                                               __uint_as_float(__float_as_uint(p01.y) & kTfMask));
+                                const float2 h23 = make_float2(__uint_as_float(__float_as_uint(p23.x) & kTfMask),
+                                                               __uint_as_float(__float_as_uint(p23.y) & kTfMask));
+                                const float2 l01 = __fadd2_rn(p01, make_float2(-h01.x, -h01.y));
+                                const float2 l23 = __fadd2_rn(p23, make_float2(-h23.x, -h23.y));
+                                hi[4 * c4 + 0] = __float_as_uint(h01.x);
+                                hi[4 * c4 + 1] = __float_as_uint(h01.y);
+                                hi[4 * c4 + 2] = __float_as_uint(h23.x);
+                                hi[4 * c4 + 3] = __float_as_uint(h23.y);
+                                lo[4 * c4 + 0] = __float_as_uint(l01.x);
+                                lo[4 * c4 + 1] = __float_as_uint(l01.y);
+                                lo[4 * c4 + 2] = __float_as_uint(l23.x);
+                                lo[4 * c4 + 3] = __float_as_uint(l23.y);
                             }
                         } else {
 #pragma unroll
@@ -386,7 +415,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         bool ok = true;
         for (int i = 0; i < n; i++) {
             const int b = i % kAcc;
-            if (!warp_wait(&done[i % kDone], ph(i, kDone), abort_flag)) { fail(); ok = false; break; }
+            if (!warp_wait<D>(&done[i % kDone], ph(i, kDone), abort_flag, a.wait_limit)) { fail(); ok = false; break; }
             tc_fence_after();
 #pragma unroll
             for (int h = 0; h < 2; h++) {
@@ -449,9 +478,9 @@ __global__ void __launch_bounds__(kThreads, 1)
             Ring rs(mw, nst);
             for (int i = mw; i < n; i += kMmaWarps, rs.step(kMmaWarps, nst)) {
                 const int b = i % kAcc, as = i % AST, s = rs.idx;
-                if (i >= kAcc && !wait_or_abort(&accfree[b], ph(i - kAcc, kAcc), abort_flag)) { ok = false; break; }
-                if (!wait_or_abort(&full[s], (uint32_t)rs.phase, abort_flag)) { ok = false; break; }  // B tiles
-                if (!wait_or_abort(&prod[as], ph(i, AST), abort_flag)) { ok = false; break; }  // A stage
+                if (i >= kAcc && !wait_or_abort<D>(&accfree[b], ph(i - kAcc, kAcc), abort_flag, a.wait_limit)) { ok = false; break; }
+                if (!wait_or_abort<D>(&full[s], (uint32_t)rs.phase, abort_flag, a.wait_limit)) { ok = false; break; }  // B tiles
+                if (!wait_or_abort<D>(&prod[as], ph(i, AST), abort_flag, a.wait_limit)) { ok = false; break; }  // A stage
                 tc_fence_after();
                 // descriptors advance by 16-byte units within the stage (no carry out of the address field)
                 const uint64_t db = sw128_desc(smem_u32(stage_ptr(s)) + kBlocks * a.ablock);
@@ -499,8 +528,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             // stage s is free once the producers took the pair factors of chunk j - nst
             // (the ring's previous phase) and the MMAs of that chunk (which read its B
             // tiles) completed
-            if (j >= nst && (!wait_or_abort(&sfree[s], (uint32_t)(rs.phase ^ 1), abort_flag) ||
-                             !wait_or_abort(&done[(j - nst) % kDone], ph(j - nst, kDone), abort_flag))) {
+            if (j >= nst && (!wait_or_abort<D>(&sfree[s], (uint32_t)(rs.phase ^ 1), abort_flag, a.wait_limit) ||
+                             !wait_or_abort<D>(&done[(j - nst) % kDone], ph(j - nst, kDone), abort_flag, a.wait_limit))) {
                 ok = false;
                 break;
             }
@@ -522,11 +551,10 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
             issued = j + 1;
         }
-        if (!ok) {
-            fail();
-            // copies in flight land (bounded) before the shared memory goes away
-            for (int j = std::max(0, issued - nst); j < issued; j++) mbar_wait(&full[j % nst], ph(j, nst));
-        }
+        if (!ok) fail();
+        // copies in flight land (bounded) before the shared memory goes away: after an
+        // abort of any role, and (already complete, so at once) at a normal end
+        for (int j = std::max(0, issued - nst); j < issued; j++) mbar_wait(&full[j % nst], ph(j, nst));
     }
     tc_fence_before();
     __syncthreads();
@@ -669,8 +697,9 @@ bool tm_supported(const Shells &sh) {
 template <int F>
 static int launch_tm(const CUtensorMap &tmA, const CUtensorMap &tmBh, const CUtensorMap &tmBl, const TmArgs &a,
                      size_t smem, int grid, cudaStream_t st) {
-    PBI4G_CUDA(cudaFuncSetAttribute(trisum_tm_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    trisum_tm_kernel<F><<<grid, kThreads, smem, st>>>(tmA, tmBh, tmBl, a);
+    auto kern = a.wait_limit < kWaitLimit ? trisum_tm_kernel<F, true> : trisum_tm_kernel<F, false>;
+    PBI4G_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<grid, kThreads, smem, st>>>(tmA, tmBh, tmBl, a);
     PBI4G_LAUNCH_CHECK();
     return PBI4G_OK;
 }
@@ -749,6 +778,7 @@ int triangle_sums_tm(const Shells &sh, TmPlan &tp, const MapPlanes &pl, DevBuf &
     PBI4G_CHECK(partial.ensure(sizeof(double) * (size_t)a.ksplit * tp.nslots));
     a.partial = partial.as<double>();
     a.err = tp.err.as<int>();
+    a.wait_limit = tp.wait_limit > 0 && tp.wait_limit < kWaitLimit ? tp.wait_limit : kWaitLimit;
     PBI4G_CUDA(cudaMemsetAsync(tp.err.p, 0, sizeof(int), st));
     const int grid = tp.nunits * a.ksplit;
     PBI4G_CHECK(tp.kahan.ensure(sizeof(float) * 2 * kN * kM * (size_t)grid));

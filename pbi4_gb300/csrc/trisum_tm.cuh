@@ -12,6 +12,7 @@ struct TmPlan {
     DevBuf units, prow, slots, err;
     DevBuf mexp;     // FP16 form: per-map power-of-two exponents
     DevBuf kahan;    // per-CTA running sums of the contraction (L2-resident scratch)
+    uint32_t wait_limit = 0;  // diagnostic: polls before a main-loop wait gives up (0: the default)
     int build(const Shells &sh, int nsets);
 };
 

@@ -56,10 +56,22 @@ class Result:
     t_start: float
     t_done: float
     batch: int = 1
+    plan_s: float = 0.0     # seconds the loop spent building the batch's plan (0: resident)
+    evictions: int = 0      # plans evicted to make room for it
 
     @property
     def latency(self) -> float:
         return self.t_done - self.t_arrival
+
+    @property
+    def queue_s(self) -> float:
+        """Arrival to the batch's start on a slot (includes the plan build)."""
+        return self.t_start - self.t_arrival
+
+    @property
+    def service_s(self) -> float:
+        """The batch's start on its slot to its completion being seen by the loop."""
+        return self.t_done - self.t_start
 
 
 def graph_capable(cfg: EstimatorConfig) -> bool:
@@ -97,6 +109,7 @@ class Server:
         self.failed = 0       # requests that ended in an error other than a rejection
         self.cancelled = 0    # requests cancelled while queued
         self.evictions = 0
+        self.plans_built = 0
         self.batches = 0
         self._stop = False
         self._thread = threading.Thread(target=self._loop, daemon=True)
@@ -121,6 +134,7 @@ class Server:
             for cfg in cfgs:
                 if self._plan_for(cfg, self.slots[0]) is None:
                     break
+            self.plans_built = 0  # counts the plans built while serving
         self.torch.cuda.synchronize()
 
     def close(self, wait: bool = True):
@@ -137,16 +151,33 @@ class Server:
         return sum(self.plan_bytes.values())
 
     def stats(self) -> dict:
+        """Latency percentiles and throughput of the completed requests, with the
+        latency split into queue wait (arrival to the batch's start, plan build
+        included) and service (start to completion), and what the slowest 1% of
+        requests waited on."""
         if not self.results:
             return {"n": 0}
         lat = np.array([r.latency for r in self.results])
+        q = np.array([r.queue_s for r in self.results])
+        sv = np.array([r.service_s for r in self.results])
         t0 = min(r.t_arrival for r in self.results)
         t1 = max(r.t_done for r in self.results)
+        p99 = float(np.percentile(lat, 99))
+        tail = [r for r in self.results if r.latency >= p99]
         return {"n": len(self.results), "p50_ms": float(np.percentile(lat, 50) * 1e3),
-                "p99_ms": float(np.percentile(lat, 99) * 1e3), "mean_ms": float(lat.mean() * 1e3),
+                "p99_ms": p99 * 1e3, "mean_ms": float(lat.mean() * 1e3),
+                "queue_p50_ms": float(np.percentile(q, 50) * 1e3), "queue_p99_ms": float(np.percentile(q, 99) * 1e3),
+                "service_p50_ms": float(np.percentile(sv, 50) * 1e3),
+                "service_p99_ms": float(np.percentile(sv, 99) * 1e3),
+                "tail": {"requests": len(tail), "queue_ms": float(np.mean([r.queue_s for r in tail]) * 1e3),
+                         "service_ms": float(np.mean([r.service_s for r in tail]) * 1e3),
+                         "with_plan_build": sum(1 for r in tail if r.plan_s > 0),
+                         "plan_build_ms": float(np.mean([r.plan_s for r in tail]) * 1e3),
+                         "evictions": sum(r.evictions for r in tail),
+                         "mean_batch": float(np.mean([r.batch for r in tail]))},
                 "boxes_per_s": len(self.results) / max(t1 - t0, 1e-9), "evictions": self.evictions,
                 "rejected": self.rejected, "failed": self.failed, "cancelled": self.cancelled,
-                "batches": self.batches,
+                "batches": self.batches, "plans_built": self.plans_built,
                 "mean_batch": len(self.results) / max(1, self.batches), "resident_gb": self.resident_bytes() / 1e9}
 
     # --------------------------------------------------------------- loop ---
@@ -193,6 +224,7 @@ class Server:
             plan.graph_build(self.batch, self.max_npart)
         self.plans[key] = plan
         self.plan_bytes[key] = need
+        self.plans_built += 1
         return plan
 
     def _take_batch(self):
@@ -221,7 +253,7 @@ class Server:
             self.queue.popleft()
             self.cancelled += 1
 
-    def _start(self, slot: _Slot, items, plan: Estimator):
+    def _start(self, slot: _Slot, items, plan: Estimator, plan_s: float = 0.0, evicted: int = 0):
         torch = self.torch
         reqs = [r for r, _ in items]
         futs = [f for _, f in items]
@@ -260,10 +292,10 @@ class Server:
         ev.record(slot.stream)
         self.batches += 1
         # every buffer of the batch in flight stays alive until its event completes
-        slot.busy = (reqs, futs, plan, ev, (outs, keep), t_start)
+        slot.busy = (reqs, futs, plan, ev, (outs, keep), t_start, plan_s, evicted)
 
     def _finish(self, slot: _Slot):
-        reqs, futs, plan, ev, (outs, _), t_start = slot.busy
+        reqs, futs, plan, ev, (outs, _), t_start, plan_s, evicted = slot.busy
         slot.busy = None
         t_done = time.perf_counter()
         err = None
@@ -276,7 +308,8 @@ class Server:
                 self.failed += 1
                 f.set_exception(err)
                 continue
-            res = Result(r.rid, po.copy(), None if bo is None else bo.copy(), r.t_arrival, t_start, t_done, len(reqs))
+            res = Result(r.rid, po.copy(), None if bo is None else bo.copy(), r.t_arrival, t_start, t_done, len(reqs),
+                         plan_s, evicted)
             self.results.append(res)
             f.set_result(res)
 
@@ -295,6 +328,7 @@ class Server:
                 while free and self.queue:
                     req, fut = self.queue[0]
                     slot = free[0]
+                    t_plan, ev0, built0 = time.perf_counter(), self.evictions, self.plans_built
                     try:
                         plan = self._plan_for(req.cfg, slot)
                     except MemoryError as e:  # can never fit: reject this request
@@ -317,8 +351,9 @@ class Server:
                     if not items:   # the batch's requests were all cancelled
                         self._drop_cancelled_head()
                         continue
+                    plan_s = time.perf_counter() - t_plan if self.plans_built > built0 else 0.0
                     try:
-                        self._start(slot, items, plan)
+                        self._start(slot, items, plan, plan_s, self.evictions - ev0)
                     except Exception as e:  # report per request; keep serving
                         slot.busy = None
                         self.failed += len(items)
