@@ -43,13 +43,46 @@ def peaks():
 
 def traffic_table():
     """Per-launch DRAM bytes of each stage from the committed ncu summary, if present,
-    keyed by "grid<N>_<precision>" of the workload it was measured (and scaled) for."""
+    keyed by "grid<N>_<precision>" of the workload it was measured (and scaled) for:
+    {stage: {"bytes": B, "source": hash of the kernel's sources when captured}}."""
     p = os.path.join(ROOT, "profiles", "dram_bytes.json")
     try:
         with open(p) as f:
             return json.load(f)
     except Exception:
         return {}
+
+
+# the source files each stage's kernels are built from (pbi4_gb300/csrc)
+SOURCES = {"assign": ("assign_owner.cu", "assign_owner.cuh"), "assign_sort": ("assign_owner.cu", "assign_owner.cuh"),
+           "fcomb": ("spectrum.cu",), "pk_binning": ("spectrum.cu",),
+           "shell_maps_z": ("mapfft.cu", "fft_small.cuh"), "shell_maps_y": ("mapfft.cu", "fft_small.cuh"),
+           "shell_maps_x": ("mapfft.cu", "fft_small.cuh"), "triangle_sums": ("trisum_tm.cu", "tc_ptx.cuh")}
+
+
+def source_hash(stage):
+    """First 16 hex digits of the SHA-256 of the stage's kernel sources (None if unknown)."""
+    import hashlib
+    files = SOURCES.get(stage)
+    if not files:
+        return None
+    h = hashlib.sha256()
+    for f in files:
+        p = os.path.join(ROOT, "pbi4_gb300", "csrc", f)
+        if not os.path.exists(p):
+            return None
+        with open(p, "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:16]
+
+
+def measured_traffic(table, stage):
+    """The captured per-launch DRAM bytes of a stage, or None when there is none or
+    the kernel's sources changed since the capture (the figure would be stale)."""
+    t = table.get(stage)
+    if isinstance(t, dict) and t.get("source") and t.get("source") == source_hash(stage):
+        return t.get("bytes")
+    return None
 
 
 def stage_work(cfg, npart, map_grid=None, nmaps=None, map_work=None):
@@ -113,7 +146,8 @@ def for_stages(stages, steps, cfg, npart, itot=None, map_grid=None, nmaps=None, 
     128-pair x 64-map tile of a unit over every point, times the split's products)
     and the fraction of the tiles' entries that is no triangle sum.  HBM stages count their
     algorithmic bytes.  `traffic` is the per-launch DRAM bytes of the committed ncu
-    capture for this workload, if one exists."""
+    capture for this workload, if one exists and the kernel's sources are those it
+    was captured from (else null)."""
     pk = peaks()
     work = dict(stage_work(cfg, npart, map_grid, nmaps, map_work))
     if itot and cfg.precision in ("fp16split", "bf16", "tf32split"):
@@ -125,7 +159,7 @@ def for_stages(stages, steps, cfg, npart, itot=None, map_grid=None, nmaps=None, 
         ms, calls = stages.get(name, (0.0, 0))
         if calls == 0 or ms <= 0:
             continue
-        e = _entry(name, bound, amount, ms / max(1, steps), pk, table.get(name))
+        e = _entry(name, bound, amount, ms / max(1, steps), pk, measured_traffic(table, name))
         if name == "shell_maps_z" and cfg.precision == "fp64":
             e["kernel"] = "build_map_spectra_kernel"
         if name == "triangle_sums" and tensor_units and tensor_units[0]:
