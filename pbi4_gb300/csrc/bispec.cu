@@ -29,6 +29,36 @@ constexpr int kTQ = 8;   // q maps per thread tile
 constexpr int kGroupThreads = 256;
 
 // ------------------------------------------------------------- Shells ---
+// Smallest multiple of 4 above 3 kmax that the map transform handles fast
+// (5-smooth, or 7-smooth when that is more than 5% smaller), else N.
+int map_grid_for_kmax(int N, int kmax) {
+    auto smooth = [](int n, int fmax) {
+        for (int f : {2, 3, 5, 7})
+            if (f <= fmax)
+                while (n % f == 0) n /= f;
+        return n == 1;
+    };
+    int n5 = 0, n7 = 0;
+    for (int n = 4; n < N && (!n5 || !n7); n += 4) {
+        if (n <= 3 * kmax) continue;
+        if (!n7 && smooth(n, 7)) n7 = n;
+        if (!n5 && smooth(n, 5)) n5 = n;
+    }
+    if (n5) return (n7 && n7 < 0.95 * n5) ? n7 : n5;
+    return n7 ? n7 : N;
+}
+
+int shell_map_grid(int N, float kbin, float kcenter, int nb) {
+    const double kck = (double)(kcenter / kbin);
+    const int h = N / 2, k2max = 3 * h * h;
+    int kmax = 0;
+    for (int k2 = 0; k2 <= k2max; k2++) {
+        const long long b = llround(sqrt((double)k2) / (double)kbin - kck - (double)FLT_MIN) + 1;
+        if (b >= 1 && b <= nb) kmax = std::max(kmax, (int)floor(sqrt((double)k2)));
+    }
+    return map_grid_for_kmax(N, kmax);
+}
+
 int Shells::build(int N_, float kbin_, float kcenter_, int nb_, int iopen_, int cross_, cudaStream_t st) {
     if (N == N_ && kbin == kbin_ && kcenter == kcenter_ && nb == nb_ && iopen == iopen_ && cross == cross_ && lut.p)
         return PBI4G_OK;
@@ -65,23 +95,7 @@ int Shells::build(int N_, float kbin_, float kcenter_, int nb_, int iopen_, int 
     kmax = 0;
     for (int k2 = 0; k2 <= k2max; k2++)
         if (lut_h[k2]) kmax = std::max(kmax, (int)floor(sqrt((double)k2)));
-    // smallest multiple of 4 above 3 kmax that cuFFT handles fast: 5-smooth,
-    // or 7-smooth when that is more than 5% smaller
-    auto smooth = [](int n, int fmax) {
-        for (int f : {2, 3, 5, 7})
-            if (f <= fmax)
-                while (n % f == 0) n /= f;
-        return n == 1;
-    };
-    int n5 = 0, n7 = 0;
-    for (int n = 4; n < N && (!n5 || !n7); n += 4) {
-        if (n <= 3 * kmax) continue;
-        if (!n7 && smooth(n, 7)) n7 = n;
-        if (!n5 && smooth(n, 5)) n5 = n;
-    }
-    Nm = N;
-    if (n5) Nm = (n7 && n7 < 0.95 * n5) ? n7 : n5;
-    else if (n7) Nm = n7;
+    Nm = map_grid_for_kmax(N, kmax);
     ishift = (int)(kcenter / kbin) + (iopen ? 1 : 0);  // bispectrumI4.f90:38-42
     tri.clear();
     for (int l = 1; l <= nb; l++)

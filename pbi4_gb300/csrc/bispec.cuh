@@ -29,6 +29,12 @@ struct Shells {
     int build(int N, float kbin, float kcenter, int nb, int iopen, int cross, cudaStream_t st);
 };
 
+// Grid of the shell maps for shells whose modes reach |k_axis| <= kmax (the
+// smallest FFT-friendly multiple of 4 above 3 kmax, at most N), and the same
+// from the binning (what Shells::build sets as Nm), host only.
+int map_grid_for_kmax(int N, int kmax);
+int shell_map_grid(int N, float kbin, float kcenter, int nb);
+
 // Sparse "pair x q" contraction S[slot] = sum_x P_a(x) P_b(x) Q(x) arranged as
 // register tiles; built once per (shells, number of q sets).
 struct TriPlan {

@@ -60,15 +60,22 @@ void Prof::end(cudaStream_t st) {
     cur_stage = -1;
 }
 
-size_t BkEngine::footprint(int N, int nb, int nsets, int cross, bool fp64, size_t budget) {
-    const size_t HC = half_cells(N);  // upper bound: the map grid is at most N
+size_t BkEngine::footprint(int N, float kbin, float kcenter, int nb, int nsets, int cross, int precision,
+                           size_t budget) {
+    const bool fp64 = precision == PBI4G_PREC_FP64;
+    const int Nm = shell_map_grid(N, kbin, kcenter, nb);  // the maps' grid, as the plan will choose it
+    const size_t HC = half_cells(Nm), FC = full_cells(Nm);
     const int nm = cross ? 2 * nb : nsets * nb;
     const size_t cs = fp64 ? 16 : 8;
     // FP64: half spectra + a cuFFT work area of about one batch of the same size;
-    // FP32: the pruned transform's intermediates (at most two half-spectrum sets)
-    // + the real maps of one slab (upper estimates)
+    // FP32 forms: the pruned transform's intermediates (at most two half-spectrum
+    // sets) + the real maps or operand planes of one slab (upper estimates)
     const size_t maps = (size_t)nm * HC * cs;
-    return 2 * maps + (fp64 ? 0 : (budget ? std::min(maps, budget) : maps)) + (size_t)nb * 8 + ((size_t)1 << 26);
+    const int tc = tc_mode_of(precision);
+    const size_t per_point = tc == 3 ? 8 : (tc == 2 ? 2 : 4);  // bytes per map and point
+    const size_t dense = (size_t)nm * FC * per_point + (tc ? (size_t)nb * FC * 4 : 0);
+    return 2 * maps + (fp64 ? 0 : (budget ? std::min(dense, budget) : dense)) + (size_t)nb * 8 +
+           ((size_t)1 << 26);
 }
 
 int BkEngine::slab_planes(int Nm, size_t per_plane, size_t budget) {
@@ -311,7 +318,8 @@ int pbi4g_plan_footprint(const pbi4g_config *cfg, int64_t npart_max, int64_t *by
     b += 2 * G * HC * cs;  // cuFFT work area (upper estimate)
     b += (size_t)npart_max * 32 + 5 * (size_t)cfg->nbins_ps * 8 * 1300;
     if (cfg->do_bispectrum) {
-        b += BkEngine::footprint(N, cfg->nbins_bs, cfg->multipoles ? 3 : 1, 0, fp64, (size_t)cfg->map_budget_mb << 20);
+        b += BkEngine::footprint(N, cfg->kbin_bs, cfg->kcenter_bs, cfg->nbins_bs, cfg->multipoles ? 3 : 1, 0,
+                                 cfg->precision, (size_t)cfg->map_budget_mb << 20);
         b += (size_t)FC * 8 * (size_t)0;  // counts use a temporary FP64 map set, freed after the first box
     }
     *bytes = (int64_t)b;

@@ -46,7 +46,8 @@ struct BkEngine {
         if (inv) cufftDestroy(inv);
     }
     int nmaps() const { return cross ? 2 * sh.nb : nsets * sh.nb; }
-    static size_t footprint(int N, int nb, int nsets, int cross, bool fp64, size_t map_budget = 0);
+    static size_t footprint(int N, float kbin, float kcenter, int nb, int nsets, int cross, int precision,
+                            size_t map_budget = 0);
     // z-planes per slab on map grid Nm for `per_plane` bytes of slab buffers a z-plane
     static int slab_planes(int Nm, size_t per_plane, size_t budget);
     // PBI4G_ERR_TIMEOUT if a bounded wait of a tensor-core launch gave up (synchronises st)
