@@ -327,23 +327,25 @@ def run_ours(args):
     value = replicas.throughput(world * args.steps, ms_max / 1e3)
 
     # e2e: host (pinned) positions in, host results out, through the C-ABI call
-    # (pbi4g_plan_run_host), K callers (host threads, one plan and stream each)
+    # (pbi4g_plan_run_host), C callers (host threads, one plan and stream each)
     # so one box's copies overlap the others' kernels
     import threading as _th
+    C = max(1, args.e2e_callers)
+    eps = ests[:C] + [Estimator(cfg, stream=torch.cuda.Stream()) for _ in range(C - len(ests))]
     hpos = torch.from_numpy(pos).pin_memory().numpy()
-    for e in ests:
+    for e in eps:
         for _ in range(2):
             e.run_host(hpos)
-    e2e_steps = max(K, args.steps // 2)
-    results = [[] for _ in range(K)]
+    e2e_steps = max(C, args.steps)
+    results = [[] for _ in range(C)]
 
     def caller(k, n):
         for _ in range(n):
-            results[k].append(ests[k].run_host(hpos))
+            results[k].append(eps[k].run_host(hpos))
 
     barrier()
     t0 = time.perf_counter()
-    th = [_th.Thread(target=caller, args=(k, len(range(k, e2e_steps, K)))) for k in range(K)]
+    th = [_th.Thread(target=caller, args=(k, len(range(k, e2e_steps, C)))) for k in range(C)]
     for t in th:
         t.start()
     for t in th:
@@ -352,7 +354,7 @@ def run_ours(args):
     e2e_value = replicas.throughput(world * e2e_steps, e2e_s)
     p_h, b_h = results[0][-1]
     est.set_stream(None)
-    for e in ests[1:]:
+    for e in set(ests[1:] + eps[1:]):
         e.close()
 
     # the plain FP32 GPU form on the same box; the errors of both forms against the
@@ -432,7 +434,7 @@ def run_ours(args):
                 "config": bench_config(world),
                 "form": {"precision": args.precision, "boxes_in_flight": K, "map_grid": map_grid, "maps": nmaps,
                          "triangles": itot},
-                "e2e": {"value": e2e_value, "unit": "boxes/s", "h2d_bytes_per_step": int(pos.nbytes),
+                "e2e": {"value": e2e_value, "unit": "boxes/s", "callers": C, "h2d_bytes_per_step": int(pos.nbytes),
                         "d2h_bytes_per_step": int(p_h.nbytes + b_h.nbytes)},
                 "gpu_launches": int(launches), "clocks": clocks, "roofline": rl, "roofline_stages": rl_all,
                 "one_box_in_flight": {"value": value_one, "unit": "boxes/s", "ms_per_step": ms_one / args.steps,
@@ -570,6 +572,8 @@ def main():
     ap.add_argument("--serve-npart-max", type=float, default=1e7, help="largest particle count of a served box")
     ap.add_argument("--boxes-in-flight", type=int, default=2,
                     help="plans (one stream each) taking the timed boxes in turn")
+    ap.add_argument("--e2e-callers", type=int, default=4,
+                    help="host threads (one plan and stream each) calling run_host in the e2e leg")
     ap.add_argument("--quick", action="store_true", help="small box (debug only)")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: 64^3 particles on a 128^3 grid (same kernels, a few hundred MB)")
