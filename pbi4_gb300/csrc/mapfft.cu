@@ -23,6 +23,17 @@ namespace {
 
 constexpr int kP = 33;        // shared pitch (float2) between the points of a tile
 constexpr int kThreads = 256;
+// CTAs per SM each pass is compiled for (registers per thread = 65536 / (256 x this)); build-time
+// tuning macros, the defaults measured best
+#ifndef PBI4G_ZPASS_MINB
+#define PBI4G_ZPASS_MINB 4
+#endif
+#ifndef PBI4G_YPASS_MINB
+#define PBI4G_YPASS_MINB 4
+#endif
+#ifndef PBI4G_XPASS_MINB
+#define PBI4G_XPASS_MINB 4
+#endif
 
 __device__ __forceinline__ float2 czero() { return make_float2(0.f, 0.f); }
 
@@ -104,7 +115,7 @@ struct ZArgs {
 // column is kz = kfreq0(i, Nm); a mode is in the shell when k2lo <= |k|^2 <=
 // k2hi (the shell's |k|^2 range, contiguous).  The mask, multipole factor and
 // kx = 0 symmetrisation of build_map_spectra; the multipole factor in FP32.
-__global__ void __launch_bounds__(kThreads, 4) map_zpass_kernel(const ZArgs a) {
+__global__ void __launch_bounds__(kThreads, PBI4G_ZPASS_MINB) map_zpass_kernel(const ZArgs a) {
     extern __shared__ __align__(16) unsigned char zsm[];
     const fftd::FftDesc &fd = a.fd;
     const int Nm = a.Nm, N = a.N, nb = a.nb;
@@ -197,7 +208,7 @@ struct YArgs {
 // (g = kxc + kx: the flat kx index over all maps, so a tile may span maps); a
 // lane reads column kx of its map, ky in [-r(kx), r(kx)], from T and the
 // transform lands in U[f][y].
-__global__ void __launch_bounds__(kThreads, 4) map_ypass_kernel(const YArgs a) {
+__global__ void __launch_bounds__(kThreads, PBI4G_YPASS_MINB) map_ypass_kernel(const YArgs a) {
     extern __shared__ __align__(16) unsigned char ysm[];
     const fftd::FftDesc &fd = a.fd;
     const int Nm = a.Nm;
@@ -331,7 +342,7 @@ __device__ __forceinline__ void store_planes(const XArgs &a, const float2 *buf, 
 // coefficient rows a warp prefetches into registers for the next tile
 // (kxmax <= PF * warps).
 template <int PF>
-__global__ void __launch_bounds__(kThreads, PF <= 9 ? 4 : 2) map_xpass_kernel(const XArgs a) {
+__global__ void __launch_bounds__(kThreads, PF <= 9 ? PBI4G_XPASS_MINB : 2) map_xpass_kernel(const XArgs a) {
     extern __shared__ __align__(16) unsigned char xsm[];
     const fftd::FftDesc &fd = a.fd;
     const int Nm = a.Nm, M = fd.n, KX = a.kxmax;

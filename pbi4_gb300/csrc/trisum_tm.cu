@@ -76,7 +76,10 @@ constexpr int kMmaWarp = kProdWarps + kDrainWarps;
 constexpr int kMmaWarps = 2;     // MMA issuers, chunks alternating (a thread's MMAs of a chunk stay in order)
 constexpr int kTmaWarp = kMmaWarp + kMmaWarps;
 constexpr int kThreads = (kTmaWarp + 1) * 32;  // 608
-constexpr int kFold = 16;        // chunks summed in registers before a Kahan fold
+#ifndef PBI4G_TM_FOLD
+#define PBI4G_TM_FOLD 16
+#endif
+constexpr int kFold = PBI4G_TM_FOLD;  // chunks summed in registers before a Kahan fold
 constexpr int kFoldGroup = 8;    // scratch values a drain thread folds per batch of loads
 constexpr int kAcc = 4;          // TMEM accumulators (one chunk each)
 constexpr int kDone = 16;        // per-chunk MMA completion barriers (ring)
