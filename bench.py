@@ -411,6 +411,8 @@ def run_ours(args):
                    "service_p50_ms": r3(live["service_p50_ms"]), "service_p99_ms": r3(live["service_p99_ms"]),
                    "p99_tail": {k: (r3(v) if isinstance(v, float) else v) for k, v in live["tail"].items()},
                    "plans_built_during_stream": live["plans_built"], "evictions": live["evictions"],
+                   "failed_requests": live["failed_requests"] + sat["failed_requests"],
+                   "errors": sorted(set(live["errors"] + sat["errors"])),
                    "boxes_per_s_offered_load": round(live["boxes_per_s"], 2),
                    "boxes_per_s_saturated": round(sat["boxes_per_s"], 2),
                    "p50_ms_saturated": r3(sat["p50_ms"]), "p99_ms_saturated": r3(sat["p99_ms"]),

@@ -6,7 +6,19 @@
 namespace pbi4g {
 namespace tcx {
 
-constexpr uint32_t kWaitLimit = 1u << 22;  // try_wait polls before a wait gives up
+// A bounded wait gives up after kWaitNs of device time (the global nanosecond
+// timer, read every 256 polls): long beyond any healthy wait of these kernels,
+// however busy the GPU, and still an end when a phase never completes.
+// kWaitLimit bounds a diagnostic poll count (pbi4g_plan_debug_wait_limit).
+constexpr uint32_t kWaitNs = 2000000000u;
+constexpr uint32_t kWaitLimit = 1u << 22;
+
+// low 32 bits of the global timer (ns): differences below 2^32 ns (4.3 s) are exact
+__device__ __forceinline__ uint32_t global_ns() {
+    uint32_t t;
+    asm volatile("mov.u32 %0, %globaltimer_lo;" : "=r"(t));
+    return t;
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -54,11 +66,14 @@ __device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t *bar, uint32_t pari
     return ok != 0;
 }
 
-// Bounded wait on an mbarrier phase; false if the limit ran out.
+// Bounded wait on an mbarrier phase; false if kWaitNs ran out.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-    for (uint32_t i = 0; i < kWaitLimit; i++)
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint32_t t0 = global_ns();
+    for (uint32_t i = 1;; i++) {
         if (mbar_try_wait(bar, parity)) return true;
-    return false;
+        if ((i & 255) == 0 && global_ns() - t0 > kWaitNs) return false;
+    }
 }
 
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }

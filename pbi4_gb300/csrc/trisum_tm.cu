@@ -38,7 +38,7 @@
 //     so keeping each accumulation to one chunk keeps that error near 1e-6;
 //   * two drain warpgroups (32 accumulator columns each) add each chunk's
 //     accumulator into FP32 registers (round to nearest) and fold those into a
-//     Kahan-compensated sum every 16 chunks (kept in shared memory), then write the final sums (FP64,
+//     Kahan-compensated sum every 16 chunks (in shared memory when it fits), then write the final sums (FP64,
 //     scaled back by the FP16 exponents) of the triangle slots.
 // Every wait is bounded: a wait that runs out sets an abort flag that ends all
 // roles, records the error for the host, and the CTA waits (bounded) for its
@@ -177,8 +177,9 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *tm, in
 #endif
 
 // Bounded wait of the main loop that also gives up once another role has
-// aborted: kWaitLimit polls.  The diagnostic instantiation (D) polls `limit`
-// times without blocking instead, so that such waits run out on healthy work
+// aborted: kWaitNs of device time (the abort flag and the timer read every 256
+// polls).  The diagnostic instantiation (D) polls `limit` times without
+// blocking instead, so that such waits run out on healthy work
 // (pbi4g_plan_debug_wait_limit); everything else in the kernel is the same.
 template <bool D>
 __device__ __forceinline__ bool wait_or_abort(uint64_t *bar, uint32_t parity, volatile int *abort_flag,
@@ -188,13 +189,14 @@ __device__ __forceinline__ bool wait_or_abort(uint64_t *bar, uint32_t parity, vo
             if (mbar_test_wait(bar, parity)) return true;
         return false;
     } else {
-        for (uint32_t i = 0; i < kWaitLimit; i++) {
+        if (mbar_try_wait(bar, parity)) return true;
+        const uint32_t t0 = global_ns();
+        for (uint32_t i = 1;; i++) {
             if (PBI4G_TM_WAIT_HINT_NS > 0 ? mbar_try_wait_sleep(bar, parity, PBI4G_TM_WAIT_HINT_NS)
                                           : mbar_try_wait(bar, parity))
                 return true;
-            if ((i & 255) == 255 && *abort_flag) return false;
+            if ((i & 255) == 0 && (*abort_flag || global_ns() - t0 > kWaitNs)) return false;
         }
-        return false;
     }
 }
 
@@ -240,33 +242,11 @@ __device__ __forceinline__ void pack_prod2(float u0, float v0, float u1, float v
     }
 }
 
-// Where the drain keeps its Kahan running sums: shared memory (1, measured 5%
-// faster at 256^3: the folds no longer wait on L2 round trips; three fewer
-// pipeline stages fit) or an L2-resident global scratch (0, loads and stores
-// that bypass L1)
-#ifndef PBI4G_TM_KAHAN_SMEM
-#define PBI4G_TM_KAHAN_SMEM 1
-#endif
-__device__ __forceinline__ float kahan_load(const float *p) {
-#if PBI4G_TM_KAHAN_SMEM
-    return *p;
-#else
-    return __ldcg(p);
-#endif
-}
-__device__ __forceinline__ void kahan_store(float *p, float v) {
-#if PBI4G_TM_KAHAN_SMEM
-    *p = v;
-#else
-    __stcg(p, v);
-#endif
-}
-
 struct TmArgs {
     long long nchunks;     // points / kKC, rounded up
     int nunits, ksplit, nslots, nA, nstages, nmaps;
     uint32_t stage_bytes, ablock;
-    float *kahan;          // [grid][2][kN][kM] running sums of each CTA when not in shared memory
+    float *kahan;          // [grid][2][kN][kM] running sums of each CTA, or null: in shared memory
     const int2 *units;     // (M tile, N tile) per unit
     const int2 *prow;      // [nunits][kM] staged rows (i, j) of each pair's factors, (-1, -1) for none
     const int *slots;      // [nunits][kM][kN] output slot or -1
@@ -298,12 +278,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     int2 *prow_s = reinterpret_cast<int2 *>(tmem_slot + 4);
     int *qexp_s = reinterpret_cast<int *>(prow_s + kM);  // [kN] FP16 exponent of each B row
     // running sums of the drain: [kN][kM], then the compensation; in shared memory
-    // after the tables, or in an L2-resident global scratch per CTA
-#if PBI4G_TM_KAHAN_SMEM
-    float *run_g = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(qexp_s + kN) + 15) & ~(uintptr_t)15);
-#else
-    float *run_g = a.kahan + (size_t)blockIdx.x * 2 * kN * kM;
-#endif
+    // after the tables (a.kahan null), or in a global scratch per CTA (each thread
+    // reads back only what it wrote)
+    float *run_g = a.kahan ? a.kahan + (size_t)blockIdx.x * 2 * kN * kM
+                           : reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(qexp_s + kN) + 15) & ~(uintptr_t)15);
     float *comp_g = run_g + kN * kM;
 
     const int unit = blockIdx.x % a.nunits, split = blockIdx.x / a.nunits;
@@ -466,8 +444,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                     float rv[kFoldGroup], cv[kFoldGroup];
 #pragma unroll
                     for (int e = 0; e < kFoldGroup; e++) {
-                        rv[e] = kahan_load(run_g + (c0 + h + e) * kM + row);
-                        cv[e] = kahan_load(comp_g + (c0 + h + e) * kM + row);
+                        rv[e] = run_g[(c0 + h + e) * kM + row];
+                        cv[e] = comp_g[(c0 + h + e) * kM + row];
                     }
 #pragma unroll
                     for (int e = 0; e < kFoldGroup; e++) {
@@ -479,8 +457,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                     }
 #pragma unroll
                     for (int e = 0; e < kFoldGroup; e++) {
-                        kahan_store(run_g + (c0 + h + e) * kM + row, rv[e]);
-                        kahan_store(comp_g + (c0 + h + e) * kM + row, cv[e]);
+                        run_g[(c0 + h + e) * kM + row] = rv[e];
+                        comp_g[(c0 + h + e) * kM + row] = cv[e];
                     }
                 }
             }
@@ -795,9 +773,13 @@ int triangle_sums_tm(const Shells &sh, TmPlan &tp, const MapPlanes &pl, DevBuf &
     const int btiles = form == 0 ? Form<kFormTF32>::kBTiles : (form == 1 ? Form<kFormF16>::kBTiles : 1);
     a.stage_bytes = kBlocks * a.ablock + (uint32_t)btiles * kBTile;
     // barriers, TMEM address, abort flag, pair table, B-row exponents
-    const size_t tail = 8 * (2 * kMaxStages + 4 + kDone + kAcc) + 16 + sizeof(int2) * kM + sizeof(int) * kN +
-                        (PBI4G_TM_KAHAN_SMEM ? 16 + sizeof(float) * 2 * kN * kM : 0);
-    const size_t fixed = 1024 + tail;
+    // the drain's Kahan sums live in shared memory when four or more stages fit
+    // beside them (5% faster at 256^3 than an L2 scratch: the folds no longer wait
+    // on L2 round trips), else in a global scratch
+    const size_t kahan_bytes = 16 + sizeof(float) * 2 * kN * kM;
+    const size_t tail0 = 8 * (2 * kMaxStages + 4 + kDone + kAcc) + 16 + sizeof(int2) * kM + sizeof(int) * kN;
+    const bool kahan_smem = 1024 + tail0 + kahan_bytes + 4 * (size_t)a.stage_bytes <= 227 * 1024;
+    const size_t fixed = 1024 + tail0 + (kahan_smem ? kahan_bytes : 0);
     a.nstages = kMaxStages;
     while (a.nstages > 3 && fixed + (size_t)a.nstages * a.stage_bytes > 227 * 1024) a.nstages--;
     const size_t smem = fixed + (size_t)a.nstages * a.stage_bytes;
@@ -813,8 +795,11 @@ int triangle_sums_tm(const Shells &sh, TmPlan &tp, const MapPlanes &pl, DevBuf &
     a.wait_limit = tp.wait_limit > 0 && tp.wait_limit < kWaitLimit ? tp.wait_limit : kWaitLimit;
     PBI4G_CUDA(cudaMemsetAsync(tp.err.p, 0, sizeof(int), st));
     const int grid = tp.nunits * a.ksplit;
-    if (!PBI4G_TM_KAHAN_SMEM) PBI4G_CHECK(tp.kahan.ensure(sizeof(float) * 2 * kN * kM * (size_t)grid));
-    a.kahan = tp.kahan.as<float>();
+    a.kahan = nullptr;
+    if (!kahan_smem) {
+        PBI4G_CHECK(tp.kahan.ensure(sizeof(float) * 2 * kN * kM * (size_t)grid));
+        a.kahan = tp.kahan.as<float>();
+    }
     if (form == 0) PBI4G_CHECK(launch_tm<kFormTF32>(tmA, tmBh, tmBl, a, smem, grid, st));
     else if (form == 1) PBI4G_CHECK(launch_tm<kFormF16>(tmA, tmBh, tmBl, a, smem, grid, st));
     else PBI4G_CHECK(launch_tm<kFormBF16>(tmA, tmBh, tmBl, a, smem, grid, st));

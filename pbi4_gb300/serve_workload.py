@@ -77,10 +77,16 @@ def run_stream(reqs, hbm_budget_gb=200.0, slots=3, batch=4, max_npart=None, warm
                 time.sleep(t - now)
         r.t_arrival = time.perf_counter()
         futs.append(srv.submit(r))
+    errors = []
     for f in futs:
-        f.result(timeout=1800)
+        try:
+            f.result(timeout=1800)
+        except Exception as e:  # a failed request is counted and reported, the stream goes on
+            errors.append(f"{type(e).__name__}: {e}")
     st = srv.stats()
     srv.close()
+    st["errors"] = sorted(set(errors))[:5]
+    st["failed_requests"] = len(errors)
     return st
 
 
