@@ -34,10 +34,6 @@ constexpr int kThreads = 256;
 #ifndef PBI4G_XPASS_MINB
 #define PBI4G_XPASS_MINB 4
 #endif
-// spectrum points the z pass loads per thread before forming them
-#ifndef PBI4G_ZPASS_BATCH
-#define PBI4G_ZPASS_BATCH 1
-#endif
 // column loads the y pass keeps in flight per thread (8: 8% faster than 1 at 256^3)
 #ifndef PBI4G_YPASS_BATCH
 #define PBI4G_YPASS_BATCH 8
@@ -154,42 +150,28 @@ __global__ void __launch_bounds__(kThreads, PBI4G_ZPASS_MINB) map_zpass_kernel(c
         const float lxy = a.los[0] * (float)kx + a.los[1] * (float)ky;
         const float wpow = kx == 0 ? 1.f : 2.f;  // the kx > 0 modes stand for their mirror too
         float pacc = 0.f;
-        // PBI4G_ZPASS_BATCH points of the column loaded before they are formed and stored
-        for (int i0 = warp; i0 < Nm; i0 += PBI4G_ZPASS_BATCH * nw) {
-            float2 v[PBI4G_ZPASS_BATCH], w[PBI4G_ZPASS_BATCH];
-#pragma unroll
-            for (int u = 0; u < PBI4G_ZPASS_BATCH; u++) {
-                const int i = i0 + u * nw, kz = kfreq0(i, Nm), kz2 = kz * kz;
-                v[u] = w[u] = czero();
-                if (i < Nm && kz2 >= lo2 && kz2 <= hi2) {
-                    const int zN = kz < 0 ? kz + N : kz;
-                    v[u] = src[((size_t)zN * N + yN) * a.NH + kx];
-                    if (kx == 0) w[u] = src[((size_t)kneg0(zN, N) * N + kneg0(yN, N)) * a.NH];
+        for (int i = warp; i < Nm; i += nw) {
+            const int kz = kfreq0(i, Nm), kz2 = kz * kz;
+            float2 v = czero();
+            if (kz2 >= lo2 && kz2 <= hi2) {
+                const int zN = kz < 0 ? kz + N : kz;
+                v = src[((size_t)zN * N + yN) * a.NH + kx];
+                if (kx == 0) {
+                    const float2 w = src[((size_t)kneg0(zN, N) * N + kneg0(yN, N)) * a.NH];
+                    v.x = (v.x + w.x) * 0.5f;
+                    v.y = (v.y - w.y) * 0.5f;
                 }
-            }
-#pragma unroll
-            for (int u = 0; u < PBI4G_ZPASS_BATCH; u++) {
-                const int i = i0 + u * nw, kz = kfreq0(i, Nm), kz2 = kz * kz;
-                if (i >= Nm) break;
-                float2 x = czero();
-                if (kz2 >= lo2 && kz2 <= hi2) {
-                    x = v[u];
-                    if (kx == 0) {
-                        x.x = (x.x + w[u].x) * 0.5f;
-                        x.y = (x.y - w[u].y) * 0.5f;
-                    }
-                    if (fac) {
-                        const float lk = lxy + a.los[2] * (float)kz;
-                        const int k2 = r2 + kz2;
-                        const float mu2 = k2 > 0 ? lk * lk / (float)k2 : 0.f;
-                        const float L = fac == 2 ? -0.5f + 1.5f * mu2 : 0.375f + mu2 * (-3.75f + 4.375f * mu2);
-                        x.x *= L;
-                        x.y *= L;
-                    }
-                    pacc += wpow * (x.x * x.x + x.y * x.y);
+                if (fac) {
+                    const float lk = lxy + a.los[2] * (float)kz;
+                    const int k2 = r2 + kz2;
+                    const float mu2 = k2 > 0 ? lk * lk / (float)k2 : 0.f;
+                    const float L = fac == 2 ? -0.5f + 1.5f * mu2 : 0.375f + mu2 * (-3.75f + 4.375f * mu2);
+                    v.x *= L;
+                    v.y *= L;
                 }
-                buf[perm[i] * kP + lane] = x;
+                pacc += wpow * (v.x * v.x + v.y * v.y);
             }
+            buf[perm[i] * kP + lane] = v;
         }
         if (a.powsum && (a.pow_mask >> s & 1)) {
             double pw = (double)pacc;

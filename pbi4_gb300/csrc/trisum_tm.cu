@@ -242,6 +242,14 @@ __device__ __forceinline__ void pack_prod2(float u0, float v0, float u1, float v
     }
 }
 
+// The drain's Kahan sums in shared memory (1) or a global scratch (0).  Shared
+// memory measured 5% faster at 256^3, but a serving stream (three streams of
+// mixed boxes) then saw a few launches whose bounded waits gave up; the global
+// scratch has shown none.
+#ifndef PBI4G_TM_KAHAN_SMEM
+#define PBI4G_TM_KAHAN_SMEM 0
+#endif
+
 struct TmArgs {
     long long nchunks;     // points / kKC, rounded up
     int nunits, ksplit, nslots, nA, nstages, nmaps;
@@ -773,12 +781,12 @@ int triangle_sums_tm(const Shells &sh, TmPlan &tp, const MapPlanes &pl, DevBuf &
     const int btiles = form == 0 ? Form<kFormTF32>::kBTiles : (form == 1 ? Form<kFormF16>::kBTiles : 1);
     a.stage_bytes = kBlocks * a.ablock + (uint32_t)btiles * kBTile;
     // barriers, TMEM address, abort flag, pair table, B-row exponents
-    // the drain's Kahan sums live in shared memory when four or more stages fit
-    // beside them (5% faster at 256^3 than an L2 scratch: the folds no longer wait
-    // on L2 round trips), else in a global scratch
+    // the drain's Kahan sums: a global scratch per CTA, or (build option
+    // PBI4G_TM_KAHAN_SMEM) shared memory when four or more stages fit beside them
     const size_t kahan_bytes = 16 + sizeof(float) * 2 * kN * kM;
     const size_t tail0 = 8 * (2 * kMaxStages + 4 + kDone + kAcc) + 16 + sizeof(int2) * kM + sizeof(int) * kN;
-    const bool kahan_smem = 1024 + tail0 + kahan_bytes + 4 * (size_t)a.stage_bytes <= 227 * 1024;
+    const bool kahan_smem =
+        PBI4G_TM_KAHAN_SMEM && 1024 + tail0 + kahan_bytes + 4 * (size_t)a.stage_bytes <= 227 * 1024;
     const size_t fixed = 1024 + tail0 + (kahan_smem ? kahan_bytes : 0);
     a.nstages = kMaxStages;
     while (a.nstages > 3 && fixed + (size_t)a.nstages * a.stage_bytes > 227 * 1024) a.nstages--;
