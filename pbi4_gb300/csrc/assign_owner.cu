@@ -290,12 +290,71 @@ __global__ void owner_scatter_kernel(int N, int nintp, int interlaced, int64_t n
     }
 }
 
+// PCS records in columns: a half-warp takes one (particle, grid) pair of a
+// record, lane (j, i) = (l >> 2 & 3, l & 3) of it the z column of cells
+// (i, j, 0..3).  The x and y weights and their product are formed once per
+// column, the z weights per cell, in the same order as the cell mapping,
+// ((w_x w_y) w_z) weight, so every q is the same integer.  Two grids: the
+// halves take grids 0 and 1 of one record; one grid: two records.  Each
+// half-warp's 16 cells of a z step fall on 16 distinct bank pairs (2 i + 8 j).
+template <int G, bool W>
+__device__ __forceinline__ void pcs_columns(unsigned b, unsigned e, int warp, int nwarps, int lane, int N, int ox,
+                                            int oy, int oz, float scale, const PRec *__restrict__ sorted,
+                                            const float *__restrict__ wsorted, unsigned long long *acc64) {
+    const int half = lane >> 4, ci = lane & 3, cj = (lane >> 2) & 3;
+    const int g = G == 2 ? half : 0;
+    const float4 px = axis_poly<4>(ci), py = axis_poly<4>(cj);
+    float4 pz[4];
+#pragma unroll
+    for (int l = 0; l < 4; l++) {
+        const float4 zc = axis_poly<4>(l);
+        pz[l] = make_float4(zc.x * scale, zc.y * scale, zc.z * scale, zc.w * scale);
+    }
+    constexpr int RPW = G == 2 ? 1 : 2;  // records per warp step
+    const unsigned step = (unsigned)(RPW * nwarps);
+    const unsigned first = b + (unsigned)(RPW * warp) + (G == 2 ? 0u : (unsigned)half);
+    // the next record of the half-warp is loaded while this one is added
+    PRec rn = {};
+    float wn = 1.f;
+    if (first < e) {
+        rn = sorted[first];
+        if (W) wn = wsorted[first];
+    }
+    for (unsigned k0 = b + (unsigned)(RPW * warp); k0 < e; k0 += step) {
+        const unsigned k = k0 + (G == 2 ? 0u : (unsigned)half);
+        const bool valid = k < e;
+        const PRec r = rn;
+        const float wt = wn;
+        if (k + step < e) {
+            rn = sorted[k + step];
+            if (W) wn = wsorted[k + step];
+        }
+        const unsigned pf = g ? r.f[1] : r.f[0];
+        const float hx = g ? r.h[1][0] : r.h[0][0], hy = g ? r.h[1][1] : r.h[0][1], hz = g ? r.h[1][2] : r.h[0][2];
+        const int lx = tile_offset((int)(pf & 2047), ox, N) + ci;
+        const int ly = tile_offset((int)((pf >> 11) & 2047), oy, N) + cj;
+        const int dz = tile_offset((int)(pf >> 22), oz, N);
+        const bool okxy = valid && (unsigned)lx < (unsigned)kT && (unsigned)ly < (unsigned)kT;
+        const float wxy = horner(px, hx) * horner(py, hy);
+        unsigned long long *col = acc64 + g * kTCP + ly * kPy + lx;
+#pragma unroll
+        for (int l = 0; l < 4; l++) {
+            const int lz = dz + l;
+            float wv = wxy * horner(pz[l], hz);
+            if (W) wv *= wt;
+            const int q = __float2int_rn(wv);
+            if (okxy && (unsigned)lz < (unsigned)kT) atomicAdd(col + lz * kPz, (unsigned long long)(long long)q);
+        }
+    }
+}
+
 // Tile kernel, specialised on the stencil width NI (1..4), the number of
-// grids G (2 when interlaced) and the presence of particle weights W: a warp
-// takes one record (particle, tile) and its lanes take the G * NI^3 (grid,
-// cell) pairs, so the cell indices and the weight polynomials fold to
-// constants and shifts.  The fixed-point scale 2^S rides in the z polynomial
-// (a power of two: the products are the same bits as scaling at the end).
+// grids G (2 when interlaced) and the presence of particle weights W: below
+// PCS a warp takes one record (particle, tile) and its lanes take the
+// G * NI^3 (grid, cell) pairs, so the cell indices and the weight polynomials
+// fold to constants and shifts; PCS takes the column mapping above.  The
+// fixed-point scale 2^S rides in the z polynomial (a power of two: the
+// products are the same bits as scaling at the end).
 template <int NI, int G, bool W>
 __global__ void __launch_bounds__(kThreads, 2) owner_tile_kernel(int N, int nt, const unsigned int *__restrict__ start,
                                                                const PRec *__restrict__ sorted,
@@ -320,68 +379,73 @@ __global__ void __launch_bounds__(kThreads, 2) owner_tile_kernel(int N, int nt, 
         for (int c = threadIdx.x; c < G * kTCP; c += blockDim.x) acc64[c] = 0ull;
         __syncthreads();
         const unsigned b = start[tile], e = start[tile + 1];
-        // per-lane stencil cells of one grid: NIT steps of 32 cells; the (i, j, l)
-        // of a lane and its weight polynomials are the same for every record
-        constexpr int NIT = (NC + 31) / 32;
-        // with NI^2 dividing 32 (NI = 1, 2, 4) a lane's x and y cells are the same at every step
-        constexpr bool kXYFixed = 32 % (NI * NI) == 0;
-        int ci[NIT], cj[NIT], cl[NIT];
-        float4 px[NIT], py[NIT], pz[NIT];
+        if constexpr (NI == 4) {
+            pcs_columns<G, W>(b, e, warp, nwarps, lane, N, ox, oy, oz, scale, sorted, wsorted, acc64);
+        } else {
+            // per-lane stencil cells of one grid: NIT steps of 32 cells; the (i, j, l)
+            // of a lane and its weight polynomials are the same for every record
+            constexpr int NIT = (NC + 31) / 32;
+            // with NI^2 dividing 32 (NI = 1, 2, 4) a lane's x and y cells are the same at every step
+            constexpr bool kXYFixed = 32 % (NI * NI) == 0;
+            int ci[NIT], cj[NIT], cl[NIT];
+            float4 px[NIT], py[NIT], pz[NIT];
 #pragma unroll
-        for (int it = 0; it < NIT; it++) {
-            const int c = it * 32 + lane;
-            ci[it] = c % NI;
-            cj[it] = (c / NI) % NI;
-            cl[it] = c < NC ? c / (NI * NI) : -1;  // -1: no cell for this lane at this step
-            px[it] = axis_poly<NI>(ci[it]);
-            py[it] = axis_poly<NI>(cj[it]);
-            const float4 zc = axis_poly<NI>(cl[it] < 0 ? 0 : cl[it]);
-            pz[it] = make_float4(zc.x * scale, zc.y * scale, zc.z * scale, zc.w * scale);
-        }
-        // the next record of the warp is loaded while this one is added
-        PRec rn;
-        float wn = 1.f;
-        if (b + warp < e) {
-            rn = sorted[b + warp];
-            if (W) wn = wsorted[b + warp];
-        }
-        for (unsigned k = b + warp; k < e; k += nwarps) {
-            const PRec r = rn;
-            const float wt = wn;
-            if (k + nwarps < e) {
-                rn = sorted[k + nwarps];
-                if (W) wn = wsorted[k + nwarps];
+            for (int it = 0; it < NIT; it++) {
+                const int c = it * 32 + lane;
+                ci[it] = c % NI;
+                cj[it] = (c / NI) % NI;
+                cl[it] = c < NC ? c / (NI * NI) : -1;  // -1: no cell for this lane at this step
+                px[it] = axis_poly<NI>(ci[it]);
+                py[it] = axis_poly<NI>(cj[it]);
+                const float4 zc = axis_poly<NI>(cl[it] < 0 ? 0 : cl[it]);
+                pz[it] = make_float4(zc.x * scale, zc.y * scale, zc.z * scale, zc.w * scale);
             }
-            int cell[G][NIT];
-            int q[G][NIT];
-            bool ok[G][NIT];
-#pragma unroll
-            for (int g = 0; g < G; g++) {
-                const unsigned pf = r.f[g];
-                const int dx = tile_offset((int)(pf & 2047), ox, N), dy = tile_offset((int)((pf >> 11) & 2047), oy, N),
-                          dz = tile_offset((int)(pf >> 22), oz, N);
-                const float hx = r.h[g][0], hy = r.h[g][1], hz = r.h[g][2];
-#pragma unroll
-                for (int it = 0; it < NIT; it++) {
-                    const int xi = kXYFixed ? 0 : it;  // folds to one evaluation per record when fixed
-                    const int lx = dx + ci[xi], ly = dy + cj[xi], lz = dz + cl[it];
-                    ok[g][it] = cl[it] >= 0 && (unsigned)lx < (unsigned)kT && (unsigned)ly < (unsigned)kT &&
-                                (unsigned)lz < (unsigned)kT;
-                    // the reference's product order: ((w_x w_y) w_z) weight; wv * 2^S is exact in
-                    // FP32 (a power-of-two scale) and |wv| 2^S < 2^30, so q is one 32-bit integer
-                    float wv = horner(px[xi], hx) * horner(py[xi], hy) * horner(pz[it], hz);
-                    if (W) wv *= wt;
-                    q[g][it] = __float2int_rn(wv);
-                    cell[g][it] = lz * kPz + ly * kPy + lx;
+            // the next record of the warp is loaded while this one is added
+            PRec rn;
+            float wn = 1.f;
+            if (b + warp < e) {
+                rn = sorted[b + warp];
+                if (W) wn = wsorted[b + warp];
+            }
+            for (unsigned k = b + warp; k < e; k += nwarps) {
+                const PRec r = rn;
+                const float wt = wn;
+                if (k + nwarps < e) {
+                    rn = sorted[k + nwarps];
+                    if (W) wn = wsorted[k + nwarps];
                 }
+                int cell[G][NIT];
+                int q[G][NIT];
+                bool ok[G][NIT];
+#pragma unroll
+                for (int g = 0; g < G; g++) {
+                    const unsigned pf = r.f[g];
+                    const int dx = tile_offset((int)(pf & 2047), ox, N);
+                    const int dy = tile_offset((int)((pf >> 11) & 2047), oy, N);
+                    const int dz = tile_offset((int)(pf >> 22), oz, N);
+                    const float hx = r.h[g][0], hy = r.h[g][1], hz = r.h[g][2];
+#pragma unroll
+                    for (int it = 0; it < NIT; it++) {
+                        const int xi = kXYFixed ? 0 : it;  // folds to one evaluation per record when fixed
+                        const int lx = dx + ci[xi], ly = dy + cj[xi], lz = dz + cl[it];
+                        ok[g][it] = cl[it] >= 0 && (unsigned)lx < (unsigned)kT && (unsigned)ly < (unsigned)kT &&
+                                    (unsigned)lz < (unsigned)kT;
+                        // the reference's product order: ((w_x w_y) w_z) weight; wv * 2^S is exact in
+                        // FP32 (a power-of-two scale) and |wv| 2^S < 2^30, so q is one 32-bit integer
+                        float wv = horner(px[xi], hx) * horner(py[xi], hy) * horner(pz[it], hz);
+                        if (W) wv *= wt;
+                        q[g][it] = __float2int_rn(wv);
+                        cell[g][it] = lz * kPz + ly * kPy + lx;
+                    }
+                }
+                // 64-bit fixed-point adds of the sign-extended q (exact mod 2^64)
+#pragma unroll
+                for (int g = 0; g < G; g++)
+#pragma unroll
+                    for (int it = 0; it < NIT; it++)
+                        if (ok[g][it])
+                            atomicAdd(acc64 + g * kTCP + cell[g][it], (unsigned long long)(long long)q[g][it]);
             }
-            // 64-bit fixed-point adds of the sign-extended q (exact mod 2^64)
-#pragma unroll
-            for (int g = 0; g < G; g++)
-#pragma unroll
-                for (int it = 0; it < NIT; it++)
-                    if (ok[g][it])
-                        atomicAdd(acc64 + g * kTCP + cell[g][it], (unsigned long long)(long long)q[g][it]);
         }
         __syncthreads();
         for (int c = threadIdx.x; c < G * kTC; c += blockDim.x) {

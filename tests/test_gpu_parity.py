@@ -236,7 +236,7 @@ def test_plan_bispectrum(box_za, precision, tol, multipoles):
     assert all(e < t for e, t in zip(errs, lim)) and pw < tol, (errs, pw)
 
 
-@pytest.mark.parametrize("interlacing,nintp", [(True, 4), (False, 2), (True, 3)])
+@pytest.mark.parametrize("interlacing,nintp", [(True, 4), (False, 4), (False, 2), (True, 3)])
 def test_plan_density_bit_reproducible(box_uniform, interlacing, nintp):
     """The plan's density (fixed-point tiles, then FFT) is bit-identical for any particle order."""
     p = ref_params(64, 1000.0, nintp, interlacing, False)
@@ -278,7 +278,7 @@ def test_plan_density_fp32_prep_matches_fp64(nintp, interlacing):
     assert err < 2e-6, err
 
 
-@pytest.mark.parametrize("interlacing,nintp", [(True, 4), (False, 2), (True, 3)])
+@pytest.mark.parametrize("interlacing,nintp", [(True, 4), (False, 4), (False, 2), (True, 3)])
 def test_plan_density_weighted_fp32_matches_fp64(box_za, interlacing, nintp):
     """Per-particle weights through the FP32 owner tiles (the fixed-point scale
     set from the largest weight, one 32-bit value per contribution) against the
