@@ -44,6 +44,22 @@ struct alignas(16) PRec {               // one particle, both grids (32 bytes)
     float h[2][3];                      // cell offset per grid and axis
 };
 
+// One particle's stencil on one grid, relative to one tile (16 bytes): pack =
+// base + kBias | x mask << 13 | y mask << 17 | z mask << 21, with base the
+// padded offset (z kPz + y kPy + x) of the stencil's first cell from the tile
+// origin and bit i of an axis mask set when the stencil's cell i on that axis
+// lies inside the tile (pack 0: no cell inside).  The scatter writes them, so
+// the tile kernel's lanes test one bit pattern and add one offset per cell.
+struct alignas(16) PCell {
+    int pack;
+    float h[3];
+};
+struct alignas(16) PTile {              // a sorted record (particle, tile), both grids (32 bytes)
+    PCell g[2];
+};
+constexpr int kBias = 2048;             // a stencil with a cell inside starts at [-3, 15] per axis: base + kBias in [977, 7403]
+constexpr int kMX = 13, kMY = 17, kMZ = 21;
+
 __device__ __forceinline__ unsigned int pack3(int x, int y, int z) {
     return (unsigned)x | ((unsigned)y << 11) | ((unsigned)z << 22);
 }
@@ -112,11 +128,6 @@ __device__ __forceinline__ int axis_tiles(int lo, int w, int N, int nt, int t[2]
     t[1] = hi / kT;
     return t[1] == t[0] ? 1 : 2;
 }
-
-struct PrepOut {
-    int lo[3];
-    int w;
-};
 
 // first_and_h for both grids from one FP64 product and sum, v = N p + 1 (the
 // reference's two roundings; FP64 is a slow pipe on this part).  The shifted
@@ -252,9 +263,24 @@ __global__ void owner_scan_kernel(int ntiles, const unsigned int *__restrict__ c
     if (threadIdx.x == 0) start[ntiles] = carry;
 }
 
+// Offset d of a stencil's first cell from a tile origin on one axis (tile_offset)
+// and the mask of its NI cells d .. d + NI - 1 that fall inside the tile.
+__device__ __forceinline__ unsigned axis_mask(int d, int NI) {
+    const int lo = max(0, -d), hi = min(NI - 1, kT - 1 - d);
+    return lo <= hi ? ((2u << hi) - 1u) & ~((1u << lo) - 1u) : 0u;
+}
+
+__device__ __forceinline__ int cell_pack(unsigned f, int ox, int oy, int oz, int N, int NI) {
+    const int dx = tile_offset((int)(f & 2047), ox, N), dy = tile_offset((int)((f >> 11) & 2047), oy, N);
+    const int dz = tile_offset((int)(f >> 22), oz, N);
+    const unsigned mx = axis_mask(dx, NI), my = axis_mask(dy, NI), mz = axis_mask(dz, NI);
+    if (!mx || !my || !mz) return 0;
+    return (dz * kPz + dy * kPy + dx + kBias) | (int)(mx << kMX | my << kMY | mz << kMZ);
+}
+
 __global__ void owner_scatter_kernel(int N, int nintp, int interlaced, int64_t npart, const BoxPar *__restrict__ bp,
                                      int nt, const PRec *__restrict__ rec, const double *__restrict__ weight,
-                                     unsigned int *__restrict__ cursor, PRec *__restrict__ sorted,
+                                     unsigned int *__restrict__ cursor, PTile *__restrict__ sorted,
                                      float *__restrict__ wsorted) {
     const int w = nintp + (interlaced ? 1 : 0);
     const int64_t n = bp ? bp->npart : npart;
@@ -283,7 +309,16 @@ __global__ void owner_scatter_kernel(int N, int nintp, int interlaced, int64_t n
             if (t >= 0 && lane == lead) d = atomicAdd(cursor + t, (unsigned)__popc(same));
             d = __shfl_sync(same, d, lead) + (unsigned)__popc(same & ((1u << lane) - 1u));
             if (t >= 0) {
-                sorted[d] = r;
+                const int ox = tx[sl & 1] * kT, oy = ty[(sl >> 1) & 1] * kT, oz = tz[sl >> 2] * kT;
+                PTile o;
+#pragma unroll
+                for (int g = 0; g < 2; g++) {
+                    o.g[g].pack = (g == 0 || interlaced) ? cell_pack(r.f[g], ox, oy, oz, N, nintp) : 0;
+                    o.g[g].h[0] = r.h[g][0];
+                    o.g[g].h[1] = r.h[g][1];
+                    o.g[g].h[2] = r.h[g][2];
+                }
+                sorted[d] = o;
                 if (wsorted) wsorted[d] = wt;
             }
         }
@@ -298,9 +333,9 @@ __global__ void owner_scatter_kernel(int N, int nintp, int interlaced, int64_t n
 // halves take grids 0 and 1 of one record; one grid: two records.  Each
 // half-warp's 16 cells of a z step fall on 16 distinct bank pairs (2 i + 8 j).
 template <int G, bool W>
-__device__ __forceinline__ void pcs_columns(unsigned b, unsigned e, int warp, int nwarps, int lane, int N, int ox,
-                                            int oy, int oz, float scale, const PRec *__restrict__ sorted,
-                                            const float *__restrict__ wsorted, unsigned long long *acc64) {
+__device__ __forceinline__ void pcs_columns(unsigned b, unsigned e, int warp, int nwarps, int lane, float scale,
+                                            const PTile *__restrict__ sorted, const float *__restrict__ wsorted,
+                                            unsigned long long *acc64) {
     const int half = lane >> 4, ci = lane & 3, cj = (lane >> 2) & 3;
     const int g = G == 2 ? half : 0;
     const float4 px = axis_poly<4>(ci), py = axis_poly<4>(cj);
@@ -310,40 +345,35 @@ __device__ __forceinline__ void pcs_columns(unsigned b, unsigned e, int warp, in
         const float4 zc = axis_poly<4>(l);
         pz[l] = make_float4(zc.x * scale, zc.y * scale, zc.z * scale, zc.w * scale);
     }
+    const int need = (1 << (kMX + ci)) | (1 << (kMY + cj));  // the column's x and y cells
+    const int loff = g * kTCP + cj * kPy + ci - kBias;  // the column's cell offset less the bias
     constexpr int RPW = G == 2 ? 1 : 2;  // records per warp step
-    const unsigned step = (unsigned)(RPW * nwarps);
-    const unsigned first = b + (unsigned)(RPW * warp) + (G == 2 ? 0u : (unsigned)half);
+    const unsigned step = (unsigned)(RPW * nwarps), off = G == 2 ? 0u : (unsigned)half;
     // the next record of the half-warp is loaded while this one is added
-    PRec rn = {};
+    PCell cn = {};
     float wn = 1.f;
-    if (first < e) {
-        rn = sorted[first];
-        if (W) wn = wsorted[first];
+    if (b + (unsigned)(RPW * warp) + off < e) {
+        cn = sorted[b + (unsigned)(RPW * warp) + off].g[g];
+        if (W) wn = wsorted[b + (unsigned)(RPW * warp) + off];
     }
-    for (unsigned k0 = b + (unsigned)(RPW * warp); k0 < e; k0 += step) {
-        const unsigned k = k0 + (G == 2 ? 0u : (unsigned)half);
-        const bool valid = k < e;
-        const PRec r = rn;
+    for (unsigned k = b + (unsigned)(RPW * warp) + off; k - off < e; k += step) {
+        const PCell c = cn;
         const float wt = wn;
         if (k + step < e) {
-            rn = sorted[k + step];
+            cn = sorted[k + step].g[g];
             if (W) wn = wsorted[k + step];
         }
-        const unsigned pf = g ? r.f[1] : r.f[0];
-        const float hx = g ? r.h[1][0] : r.h[0][0], hy = g ? r.h[1][1] : r.h[0][1], hz = g ? r.h[1][2] : r.h[0][2];
-        const int lx = tile_offset((int)(pf & 2047), ox, N) + ci;
-        const int ly = tile_offset((int)((pf >> 11) & 2047), oy, N) + cj;
-        const int dz = tile_offset((int)(pf >> 22), oz, N);
-        const bool okxy = valid && (unsigned)lx < (unsigned)kT && (unsigned)ly < (unsigned)kT;
-        const float wxy = horner(px, hx) * horner(py, hy);
-        unsigned long long *col = acc64 + g * kTCP + ly * kPy + lx;
+        // k >= e (the second record of a one-grid step past the end): pack 0
+        const int pk = k < e ? c.pack : 0;
+        const bool okxy = (pk & need) == need;
+        const float wxy = horner(px, c.h[0]) * horner(py, c.h[1]);
+        unsigned long long *col = acc64 + (loff + (pk & ((1 << kMX) - 1)));
 #pragma unroll
         for (int l = 0; l < 4; l++) {
-            const int lz = dz + l;
-            float wv = wxy * horner(pz[l], hz);
+            float wv = wxy * horner(pz[l], c.h[2]);
             if (W) wv *= wt;
             const int q = __float2int_rn(wv);
-            if (okxy && (unsigned)lz < (unsigned)kT) atomicAdd(col + lz * kPz, (unsigned long long)(long long)q);
+            if (okxy && (pk >> (kMZ + l) & 1)) atomicAdd(col + l * kPz, (unsigned long long)(long long)q);
         }
     }
 }
@@ -357,7 +387,7 @@ __device__ __forceinline__ void pcs_columns(unsigned b, unsigned e, int warp, in
 // products are the same bits as scaling at the end).
 template <int NI, int G, bool W>
 __global__ void __launch_bounds__(kThreads, 2) owner_tile_kernel(int N, int nt, const unsigned int *__restrict__ start,
-                                                               const PRec *__restrict__ sorted,
+                                                               const PTile *__restrict__ sorted,
                                                                const float *__restrict__ wsorted, float scale,
                                                                float inv_scale, float *__restrict__ out1,
                                                                float *__restrict__ out2,
@@ -380,35 +410,35 @@ __global__ void __launch_bounds__(kThreads, 2) owner_tile_kernel(int N, int nt, 
         __syncthreads();
         const unsigned b = start[tile], e = start[tile + 1];
         if constexpr (NI == 4) {
-            pcs_columns<G, W>(b, e, warp, nwarps, lane, N, ox, oy, oz, scale, sorted, wsorted, acc64);
+            pcs_columns<G, W>(b, e, warp, nwarps, lane, scale, sorted, wsorted, acc64);
         } else {
             // per-lane stencil cells of one grid: NIT steps of 32 cells; the (i, j, l)
-            // of a lane and its weight polynomials are the same for every record
+            // of a lane, its cell offset, its bit pattern and its weight polynomials
+            // are the same for every record
             constexpr int NIT = (NC + 31) / 32;
-            // with NI^2 dividing 32 (NI = 1, 2, 4) a lane's x and y cells are the same at every step
-            constexpr bool kXYFixed = 32 % (NI * NI) == 0;
-            int ci[NIT], cj[NIT], cl[NIT];
+            int need[NIT], loff[NIT];
             float4 px[NIT], py[NIT], pz[NIT];
 #pragma unroll
             for (int it = 0; it < NIT; it++) {
                 const int c = it * 32 + lane;
-                ci[it] = c % NI;
-                cj[it] = (c / NI) % NI;
-                cl[it] = c < NC ? c / (NI * NI) : -1;  // -1: no cell for this lane at this step
-                px[it] = axis_poly<NI>(ci[it]);
-                py[it] = axis_poly<NI>(cj[it]);
-                const float4 zc = axis_poly<NI>(cl[it] < 0 ? 0 : cl[it]);
+                const int ci = c % NI, cj = (c / NI) % NI, cl = c < NC ? c / (NI * NI) : 0;
+                // no cell for this lane at this step: a bit no pack has
+                need[it] = c < NC ? (1 << (kMX + ci)) | (1 << (kMY + cj)) | (1 << (kMZ + cl)) : (1 << 30);
+                loff[it] = cl * kPz + cj * kPy + ci - kBias;
+                px[it] = axis_poly<NI>(ci);
+                py[it] = axis_poly<NI>(cj);
+                const float4 zc = axis_poly<NI>(cl);
                 pz[it] = make_float4(zc.x * scale, zc.y * scale, zc.z * scale, zc.w * scale);
             }
             // the next record of the warp is loaded while this one is added
-            PRec rn;
+            PTile rn;
             float wn = 1.f;
             if (b + warp < e) {
                 rn = sorted[b + warp];
                 if (W) wn = wsorted[b + warp];
             }
             for (unsigned k = b + warp; k < e; k += nwarps) {
-                const PRec r = rn;
+                const PTile r = rn;
                 const float wt = wn;
                 if (k + nwarps < e) {
                     rn = sorted[k + nwarps];
@@ -419,23 +449,17 @@ __global__ void __launch_bounds__(kThreads, 2) owner_tile_kernel(int N, int nt, 
                 bool ok[G][NIT];
 #pragma unroll
                 for (int g = 0; g < G; g++) {
-                    const unsigned pf = r.f[g];
-                    const int dx = tile_offset((int)(pf & 2047), ox, N);
-                    const int dy = tile_offset((int)((pf >> 11) & 2047), oy, N);
-                    const int dz = tile_offset((int)(pf >> 22), oz, N);
-                    const float hx = r.h[g][0], hy = r.h[g][1], hz = r.h[g][2];
+                    const int pk = r.g[g].pack;
+                    const float hx = r.g[g].h[0], hy = r.g[g].h[1], hz = r.g[g].h[2];
 #pragma unroll
                     for (int it = 0; it < NIT; it++) {
-                        const int xi = kXYFixed ? 0 : it;  // folds to one evaluation per record when fixed
-                        const int lx = dx + ci[xi], ly = dy + cj[xi], lz = dz + cl[it];
-                        ok[g][it] = cl[it] >= 0 && (unsigned)lx < (unsigned)kT && (unsigned)ly < (unsigned)kT &&
-                                    (unsigned)lz < (unsigned)kT;
+                        ok[g][it] = (pk & need[it]) == need[it];
                         // the reference's product order: ((w_x w_y) w_z) weight; wv * 2^S is exact in
                         // FP32 (a power-of-two scale) and |wv| 2^S < 2^30, so q is one 32-bit integer
-                        float wv = horner(px[xi], hx) * horner(py[xi], hy) * horner(pz[it], hz);
+                        float wv = horner(px[it], hx) * horner(py[it], hy) * horner(pz[it], hz);
                         if (W) wv *= wt;
                         q[g][it] = __float2int_rn(wv);
-                        cell[g][it] = lz * kPz + ly * kPy + lx;
+                        cell[g][it] = (pk & ((1 << kMX) - 1)) + loff[it];
                     }
                 }
                 // 64-bit fixed-point adds of the sign-extended q (exact mod 2^64)
@@ -461,7 +485,7 @@ __global__ void __launch_bounds__(kThreads, 2) owner_tile_kernel(int N, int nt, 
 }
 
 template <int NI, int G, bool W>
-static int launch_tile_w(int N, int nt, const unsigned *start, const PRec *sorted, const float *wsorted, int bits,
+static int launch_tile_w(int N, int nt, const unsigned *start, const PTile *sorted, const float *wsorted, int bits,
                          float *out1, float *out2, unsigned *next_tile, cudaStream_t st) {
     const size_t smem = sizeof(unsigned long long) * G * kTCP;
     auto kern = owner_tile_kernel<NI, G, W>;
@@ -477,7 +501,7 @@ static int launch_tile_w(int N, int nt, const unsigned *start, const PRec *sorte
 }
 
 template <int NI, int G>
-static int launch_tile(int N, int nt, const unsigned *start, const PRec *sorted, const float *wsorted, int bits,
+static int launch_tile(int N, int nt, const unsigned *start, const PTile *sorted, const float *wsorted, int bits,
                        float *out1, float *out2, unsigned *next_tile, cudaStream_t st) {
     return wsorted ? launch_tile_w<NI, G, true>(N, nt, start, sorted, wsorted, bits, out1, out2, next_tile, st)
                    : launch_tile_w<NI, G, false>(N, nt, start, sorted, wsorted, bits, out1, out2, next_tile, st);
@@ -507,7 +531,7 @@ int OwnerWork::ensure(int N, int64_t npart) {
     PBI4G_CHECK(cursor.ensure((ntiles + 1) * 4));
     PBI4G_CHECK(rec.ensure(n * sizeof(PRec)));
     // a record per (particle, touched tile): at most 8 per particle
-    PBI4G_CHECK(sorted.ensure(8 * n * sizeof(PRec)));
+    PBI4G_CHECK(sorted.ensure(8 * n * sizeof(PTile)));
     PBI4G_CHECK(wsorted.ensure(8 * n * 4));
     PBI4G_CHECK(wmax.ensure(8));
     return PBI4G_OK;
@@ -515,7 +539,7 @@ int OwnerWork::ensure(int N, int64_t npart) {
 
 size_t OwnerWork::footprint(int N, int64_t npart) {
     const size_t nt = (size_t)(N / kT);
-    return 3 * (nt * nt * nt + 2) * 4 + (size_t)npart * (sizeof(PRec) + 8 * (sizeof(PRec) + 4)) + 64;
+    return 3 * (nt * nt * nt + 2) * 4 + (size_t)npart * (sizeof(PRec) + 8 * (sizeof(PTile) + 4)) + 64;
 }
 
 int assign_owner(OwnerWork &wk, int N, int nintp, bool interlaced, int64_t npart, const double *d_pos,
@@ -560,11 +584,11 @@ int assign_owner(OwnerWork &wk, int N, int nintp, bool interlaced, int64_t npart
     PBI4G_LAUNCH_CHECK();
     owner_scatter_kernel<<<grid_blocks(npart, 256), 256, 0, st>>>(
         N, nintp, interlaced, npart, bp, nt, static_cast<const PRec *>(wk.rec.p), d_weight, wk.cursor.as<unsigned int>(),
-        static_cast<PRec *>(wk.sorted.p), d_weight ? wk.wsorted.as<float>() : nullptr);
+        static_cast<PTile *>(wk.sorted.p), d_weight ? wk.wsorted.as<float>() : nullptr);
     PBI4G_LAUNCH_CHECK();
     const size_t FC = full_cells(N);
     const unsigned *st_ = wk.start.as<unsigned int>();
-    const PRec *so = static_cast<const PRec *>(wk.sorted.p);
+    const PTile *so = static_cast<const PTile *>(wk.sorted.p);
     const float *ws = d_weight ? wk.wsorted.as<float>() : nullptr;
     float *o2 = interlaced ? out + FC : nullptr;
     unsigned *nx = wk.count.as<unsigned int>() + ntiles + 1;
