@@ -31,14 +31,15 @@
 //     them straight into a tensor-memory A stage with tcgen05.st (the A operand
 //     never touches shared memory);
 //   * an MMA warp issues the MMAs (A in TMEM, B from the stage) into one of
-//     four TMEM accumulators, a fresh one per chunk, and commits them to a
+//     two TMEM accumulators, a fresh one per chunk, and commits them to a
 //     per-chunk completion barrier that frees the A stage, the accumulator and
 //     (with the producers' release) the shared-memory stage.  The tensor core
 //     adds the products of one instruction to the accumulator with truncation,
 //     so keeping each accumulation to one chunk keeps that error near 1e-6;
 //   * two drain warpgroups (32 accumulator columns each) add each chunk's
 //     accumulator into FP32 registers (round to nearest) and fold those into a
-//     Kahan-compensated sum every 16 chunks (in shared memory when it fits), then write the final sums (FP64,
+//     Kahan-compensated sum every 16 chunks (kept in the TMEM columns the
+//     accumulators and A stages leave free), then write the final sums (FP64,
 //     scaled back by the FP16 exponents) of the triangle slots.
 // Every wait is bounded: a wait that runs out sets an abort flag that ends all
 // roles, records the error for the host, and the CTA waits (bounded) for its
@@ -80,8 +81,15 @@ constexpr int kThreads = (kTmaWarp + 1) * 32;  // 608
 #define PBI4G_TM_FOLD 16
 #endif
 constexpr int kFold = PBI4G_TM_FOLD;  // chunks summed in registers before a Kahan fold
-constexpr int kFoldGroup = 8;    // scratch values a drain thread folds per batch of loads
-constexpr int kAcc = 4;          // TMEM accumulators (one chunk each)
+constexpr int kFoldGroup = 8;    // running sums a drain thread folds per batch of loads (one TMEM x8 load)
+// TMEM accumulators (one chunk each) and the FP16 form's A stages (build-time tuning)
+#ifndef PBI4G_TM_ACC
+#define PBI4G_TM_ACC 2
+#endif
+#ifndef PBI4G_TM_F16_ASTAGES
+#define PBI4G_TM_F16_ASTAGES 4
+#endif
+constexpr int kAcc = PBI4G_TM_ACC;
 constexpr int kDone = 16;        // per-chunk MMA completion barriers (ring)
 constexpr uint32_t kColAcc = 0;  // kAcc accumulators of kN columns, then the A stages
 constexpr uint32_t kColA = kAcc * kN;
@@ -106,7 +114,7 @@ template <> struct Form<kFormTF32> {
 // FP16 split: A stage = 32 hi + 32 lo packed columns, 4 K-steps of 16, 3 products
 template <> struct Form<kFormF16> {
     static constexpr uint32_t kACols = kKC;
-    static constexpr int kAStages = 4;
+    static constexpr int kAStages = PBI4G_TM_F16_ASTAGES;
     static constexpr int kBTiles = 2;  // hi, lo: 64 FP16 points per 128-byte row
     static constexpr int kKStep = 16;
     static constexpr bool kSplit = true;
@@ -242,29 +250,22 @@ __device__ __forceinline__ void pack_prod2(float u0, float v0, float u1, float v
     }
 }
 
-// The drain's Kahan sums in shared memory (1) or a global scratch (0).  Shared
-// memory measured 5% faster at 256^3, but a serving stream (three streams of
-// mixed boxes) then saw a few launches whose bounded waits gave up; the global
-// scratch has shown none.
-#ifndef PBI4G_TM_KAHAN_SMEM
-#define PBI4G_TM_KAHAN_SMEM 0
-#endif
-// the scratch is read back by the thread that wrote it: L1-bypassing loads and
-// stores for the global scratch (plain accesses were 4% slower), plain ones for
-// shared memory
-__device__ __forceinline__ float kahan_load(const float *p) {
-    return PBI4G_TM_KAHAN_SMEM ? *p : __ldcg(p);
-}
-__device__ __forceinline__ void kahan_store(float *p, float v) {
-    if (PBI4G_TM_KAHAN_SMEM) *p = v;
-    else __stcg(p, v);
+// The drain's Kahan sums live in the TMEM columns the accumulators and A stages
+// leave free when there are 2 kN of them (every form with two accumulators),
+// else in an L2-resident global scratch per CTA.  In TMEM the folds cost no L2
+// round trips: with two accumulators the triangle sums at 256^3 took 1.00 ms
+// against 1.08 ms for four accumulators and the sums in L2 (two A stages instead
+// of four: 1.33 ms).
+template <int F>
+constexpr bool kahan_in_tmem() {
+    return kColA + (uint32_t)Form<F>::kAStages * Form<F>::kACols + 2 * kN <= kTmemCols;
 }
 
 struct TmArgs {
     long long nchunks;     // points / kKC, rounded up
     int nunits, ksplit, nslots, nA, nstages, nmaps;
     uint32_t stage_bytes, ablock;
-    float *kahan;          // [grid][2][kN][kM] running sums of each CTA, or null: in shared memory
+    float *kahan;          // [grid][2][kN][kM] running sums of each CTA (forms whose sums do not fit in TMEM)
     const int2 *units;     // (M tile, N tile) per unit
     const int2 *prow;      // [nunits][kM] staged rows (i, j) of each pair's factors, (-1, -1) for none
     const int *slots;      // [nunits][kM][kN] output slot or -1
@@ -295,16 +296,13 @@ __global__ void __launch_bounds__(kThreads, 1)
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
     int2 *prow_s = reinterpret_cast<int2 *>(tmem_slot + 4);
     int *qexp_s = reinterpret_cast<int *>(prow_s + kM);  // [kN] FP16 exponent of each B row
-    // running sums of the drain: [kN][kM], then the compensation; in shared memory
-    // after the tables (a.kahan null), or in a global scratch per CTA (each thread
-    // reads back only what it wrote)
-#if PBI4G_TM_KAHAN_SMEM
-    float *run_g = a.kahan ? a.kahan + (size_t)blockIdx.x * 2 * kN * kM
-                           : reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(qexp_s + kN) + 15) & ~(uintptr_t)15);
-#else
-    float *run_g = a.kahan + (size_t)blockIdx.x * 2 * kN * kM;
-#endif
-    float *comp_g = run_g + kN * kM;
+    // running sums of the drain, then the compensation: TMEM columns kColK .. kColK + 2 kN
+    // of the thread's lane, or [kN][kM] floats each in a global scratch per CTA (each
+    // thread reads back only what it wrote)
+    constexpr bool KT = kahan_in_tmem<F>();
+    constexpr uint32_t kColK = kColA + (uint32_t)AST * FM::kACols;
+    float *run_g = KT ? nullptr : a.kahan + (size_t)blockIdx.x * 2 * kN * kM;
+    float *comp_g = KT ? nullptr : run_g + kN * kM;
 
     const int unit = blockIdx.x % a.nunits, split = blockIdx.x / a.nunits;
     const int2 U = a.units[unit];
@@ -431,19 +429,32 @@ __global__ void __launch_bounds__(kThreads, 1)
     } else if (warp < kMmaWarp) {
         // ---------------------------------------------------------------- drain
         // each chunk's accumulator is added into FP32 registers (round to nearest);
-        // every kFold chunks those are folded into a Kahan-compensated sum kept in
-        // shared memory ([column][row]) (or an L2-resident scratch), written out at the end
+        // every kFold chunks those are folded into a Kahan-compensated sum (in TMEM, or
+        // an L2-resident scratch), written out at the end
         const int quad = warp & 3, cgrp = (warp - kProdWarps) >> 2;
         const int row = quad * 32 + lane, c0 = 32 * cgrp;
         const uint32_t lane_addr = tmem + ((uint32_t)(quad * 32) << 16);
+        const uint32_t krun = lane_addr + kColK + (uint32_t)c0, kcomp = krun + kN;
         float mid[32];
 #pragma unroll
-        for (int e = 0; e < 32; e++) {
-            mid[e] = 0.f;
-            run_g[(c0 + e) * kM + row] = 0.f;
-            comp_g[(c0 + e) * kM + row] = 0.f;
+        for (int e = 0; e < 32; e++) mid[e] = 0.f;
+        if constexpr (KT) {
+            const uint32_t z[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+#pragma unroll
+            for (int h = 0; h < 32; h += 8) {
+                tmem_st8(krun + h, z);
+                tmem_st8(kcomp + h, z);
+            }
+            tmem_wait_st();
+        } else {
+#pragma unroll
+            for (int e = 0; e < 32; e++) {
+                run_g[(c0 + e) * kM + row] = 0.f;
+                comp_g[(c0 + e) * kM + row] = 0.f;
+            }
         }
         bool ok = true;
+#pragma unroll 1
         for (int i = 0; i < n; i++) {
             const int b = i % kAcc;
             if (!warp_wait<D>(&done[i % kDone], ph(i, kDone), abort_flag, a.wait_limit)) { fail(); ok = false; break; }
@@ -459,42 +470,78 @@ __global__ void __launch_bounds__(kThreads, 1)
             tc_fence_before();
             mbar_arrive(&accfree[b]);
             if ((i + 1) % kFold == 0 || i == n - 1) {
-                // each group's scratch loads are issued before its first store, so the
-                // fold costs a few L2 round trips
+                // each group's loads are issued before its first store, so the fold
+                // costs a few TMEM (or L2) round trips
 #pragma unroll
                 for (int h = 0; h < 32; h += kFoldGroup) {
-                    float rv[kFoldGroup], cv[kFoldGroup];
+                    if constexpr (KT) {
+                        uint32_t rr[kFoldGroup], cc[kFoldGroup];
+                        tmem_ld8(krun + h, rr);
+                        tmem_ld8(kcomp + h, cc);
+                        tmem_wait_ld();
 #pragma unroll
-                    for (int e = 0; e < kFoldGroup; e++) {
-                        rv[e] = kahan_load(run_g + (c0 + h + e) * kM + row);
-                        cv[e] = kahan_load(comp_g + (c0 + h + e) * kM + row);
-                    }
+                        for (int e = 0; e < kFoldGroup; e++) {
+                            const float rv = __uint_as_float(rr[e]), y = mid[h + e] - __uint_as_float(cc[e]);
+                            const float t2 = rv + y;
+                            cc[e] = __float_as_uint((t2 - rv) - y);
+                            rr[e] = __float_as_uint(t2);
+                            mid[h + e] = 0.f;
+                        }
+                        tmem_st8(krun + h, rr);
+                        tmem_st8(kcomp + h, cc);
+                    } else {
+                        float rv[kFoldGroup], cv[kFoldGroup];
 #pragma unroll
-                    for (int e = 0; e < kFoldGroup; e++) {
-                        const float y = mid[h + e] - cv[e];
-                        const float t2 = rv[e] + y;
-                        cv[e] = (t2 - rv[e]) - y;
-                        rv[e] = t2;
-                        mid[h + e] = 0.f;
-                    }
+                        for (int e = 0; e < kFoldGroup; e++) {
+                            rv[e] = __ldcg(run_g + (c0 + h + e) * kM + row);
+                            cv[e] = __ldcg(comp_g + (c0 + h + e) * kM + row);
+                        }
 #pragma unroll
-                    for (int e = 0; e < kFoldGroup; e++) {
-                        kahan_store(run_g + (c0 + h + e) * kM + row, rv[e]);
-                        kahan_store(comp_g + (c0 + h + e) * kM + row, cv[e]);
+                        for (int e = 0; e < kFoldGroup; e++) {
+                            const float y = mid[h + e] - cv[e];
+                            const float t2 = rv[e] + y;
+                            cv[e] = (t2 - rv[e]) - y;
+                            rv[e] = t2;
+                            mid[h + e] = 0.f;
+                        }
+#pragma unroll
+                        for (int e = 0; e < kFoldGroup; e++) {
+                            __stcg(run_g + (c0 + h + e) * kM + row, rv[e]);
+                            __stcg(comp_g + (c0 + h + e) * kM + row, cv[e]);
+                        }
                     }
                 }
+                if constexpr (KT) tmem_wait_st();  // the next fold reads these columns back
             }
         }
         if (__all_sync(0xffffffffu, ok && !*abort_flag)) {
             const int *sl = a.slots + ((size_t)unit * kM + row) * kN;
             const int2 pr = prow_s[row];
             const int pe = (F == kFormF16 && pr.x >= 0) ? a.mexp[pr.x] + a.mexp[pr.y] - 14 : 0;
+            if constexpr (KT) {
+#pragma unroll 1
+                for (int h = 0; h < 32; h += 8) {
+                    uint32_t rr[8], cc[8];
+                    tmem_ld8(krun + h, rr);
+                    tmem_ld8(kcomp + h, cc);
+                    tmem_wait_ld();
+#pragma unroll
+                    for (int e = 0; e < 8; e++) {
+                        const int slot = sl[c0 + h + e];
+                        if (slot < 0) continue;
+                        const double v = (double)__uint_as_float(rr[e]) - (double)__uint_as_float(cc[e]);
+                        a.partial[(size_t)split * a.nslots + slot] =
+                            F == kFormF16 ? ldexp(v, -(pe + qexp_s[c0 + h + e])) : v;
+                    }
+                }
+            } else {
 #pragma unroll 4
-            for (int e = 0; e < 32; e++) {
-                const int slot = sl[c0 + e];
-                if (slot < 0) continue;
-                const double v = (double)run_g[(c0 + e) * kM + row] - (double)comp_g[(c0 + e) * kM + row];
-                a.partial[(size_t)split * a.nslots + slot] = F == kFormF16 ? ldexp(v, -(pe + qexp_s[c0 + e])) : v;
+                for (int e = 0; e < 32; e++) {
+                    const int slot = sl[c0 + e];
+                    if (slot < 0) continue;
+                    const double v = (double)run_g[(c0 + e) * kM + row] - (double)comp_g[(c0 + e) * kM + row];
+                    a.partial[(size_t)split * a.nslots + slot] = F == kFormF16 ? ldexp(v, -(pe + qexp_s[c0 + e])) : v;
+                }
             }
         }
     } else if (warp < kTmaWarp) {
@@ -795,13 +842,7 @@ int triangle_sums_tm(const Shells &sh, TmPlan &tp, const MapPlanes &pl, DevBuf &
     const int btiles = form == 0 ? Form<kFormTF32>::kBTiles : (form == 1 ? Form<kFormF16>::kBTiles : 1);
     a.stage_bytes = kBlocks * a.ablock + (uint32_t)btiles * kBTile;
     // barriers, TMEM address, abort flag, pair table, B-row exponents
-    // the drain's Kahan sums: a global scratch per CTA, or (build option
-    // PBI4G_TM_KAHAN_SMEM) shared memory when four or more stages fit beside them
-    const size_t kahan_bytes = 16 + sizeof(float) * 2 * kN * kM;
-    const size_t tail0 = 8 * (2 * kMaxStages + 4 + kDone + kAcc) + 16 + sizeof(int2) * kM + sizeof(int) * kN;
-    const bool kahan_smem =
-        PBI4G_TM_KAHAN_SMEM && 1024 + tail0 + kahan_bytes + 4 * (size_t)a.stage_bytes <= 227 * 1024;
-    const size_t fixed = 1024 + tail0 + (kahan_smem ? kahan_bytes : 0);
+    const size_t fixed = 1024 + 8 * (2 * kMaxStages + 4 + kDone + kAcc) + 16 + sizeof(int2) * kM + sizeof(int) * kN;
     a.nstages = kMaxStages;
     while (a.nstages > 3 && fixed + (size_t)a.nstages * a.stage_bytes > 227 * 1024) a.nstages--;
     const size_t smem = fixed + (size_t)a.nstages * a.stage_bytes;
@@ -818,7 +859,9 @@ int triangle_sums_tm(const Shells &sh, TmPlan &tp, const MapPlanes &pl, DevBuf &
     PBI4G_CUDA(cudaMemsetAsync(tp.err.p, 0, sizeof(int), st));
     const int grid = tp.nunits * a.ksplit;
     a.kahan = nullptr;
-    if (!kahan_smem) {
+    const bool kt = form == 0 ? kahan_in_tmem<kFormTF32>()
+                              : (form == 1 ? kahan_in_tmem<kFormF16>() : kahan_in_tmem<kFormBF16>());
+    if (!kt) {  // the running sums do not fit beside the accumulators and A stages in TMEM
         PBI4G_CHECK(tp.kahan.ensure(sizeof(float) * 2 * kN * kM * (size_t)grid));
         a.kahan = tp.kahan.as<float>();
     }
