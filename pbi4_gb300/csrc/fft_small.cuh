@@ -33,13 +33,46 @@ namespace fftd {
 
 constexpr int kMaxRadix = 20;
 
-__host__ __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__host__ __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// Complex helpers.  Device code forms additions, subtractions and products by
+// a real number with the packed FP32 pair instructions (each element rounded as
+// the scalar operation rounds it: about a third fewer FP instructions in the
+// DFTs below); host code (the plan check) uses scalar arithmetic.
+__host__ __device__ __forceinline__ float2 cadd(float2 a, float2 b) {
+#ifdef __CUDA_ARCH__
+    return __fadd2_rn(a, b);
+#else
+    return make_float2(a.x + b.x, a.y + b.y);
+#endif
+}
+__host__ __device__ __forceinline__ float2 csub(float2 a, float2 b) {
+#ifdef __CUDA_ARCH__
+    return __ffma2_rn(b, make_float2(-1.f, -1.f), a);  // a - b, one rounding
+#else
+    return make_float2(a.x - b.x, a.y - b.y);
+#endif
+}
+__host__ __device__ __forceinline__ float2 cscale(float2 a, float s) {
+#ifdef __CUDA_ARCH__
+    return __fmul2_rn(a, make_float2(s, s));
+#else
+    return make_float2(s * a.x, s * a.y);
+#endif
+}
+// a + c b for a real c (one rounding per element)
+__host__ __device__ __forceinline__ float2 caxpy(float c, float2 b, float2 a) {
+#ifdef __CUDA_ARCH__
+    return __ffma2_rn(make_float2(c, c), b, a);
+#else
+    return make_float2(std::fma(c, b.x, a.x), std::fma(c, b.y, a.y));
+#endif
+}
 __host__ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 __host__ __device__ __forceinline__ float2 itimes(float2 a) { return make_float2(-a.y, a.x); }  // i a
-__host__ __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(s * a.x, s * a.y); }
+// a + i w and a - i w (the rotation swaps components: scalar)
+__host__ __device__ __forceinline__ float2 cadd_i(float2 a, float2 w) { return make_float2(a.x - w.y, a.y + w.x); }
+__host__ __device__ __forceinline__ float2 csub_i(float2 a, float2 w) { return make_float2(a.x + w.y, a.y - w.x); }
 
 // inverse DFT of R points in place: v[q] <- sum_r v[r] e^{+2 pi i q r / R}
 template <int R>
@@ -51,32 +84,32 @@ __host__ __device__ __forceinline__ void dft_small(float2 (&v)[kMaxRadix]) {
     } else if constexpr (R == 3) {
         const float c = -0.5f, sn = 0.8660254037844386f;
         const float2 b = cadd(v[1], v[2]), d = csub(v[1], v[2]);
-        const float2 t = make_float2(v[0].x + c * b.x, v[0].y + c * b.y);
-        const float2 u = itimes(cscale(d, sn));
+        const float2 t = caxpy(c, b, v[0]);
+        const float2 w = cscale(d, sn);
         v[0] = cadd(v[0], b);
-        v[1] = cadd(t, u);
-        v[2] = csub(t, u);
+        v[1] = cadd_i(t, w);
+        v[2] = csub_i(t, w);
     } else if constexpr (R == 4) {
         const float2 s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
-        const float2 s13 = cadd(v[1], v[3]), d13 = itimes(csub(v[1], v[3]));
+        const float2 s13 = cadd(v[1], v[3]), d13 = csub(v[1], v[3]);
         v[0] = cadd(s02, s13);
         v[2] = csub(s02, s13);
-        v[1] = cadd(d02, d13);
-        v[3] = csub(d02, d13);
+        v[1] = cadd_i(d02, d13);
+        v[3] = csub_i(d02, d13);
     } else if constexpr (R == 5) {
         const float c1 = 0.30901699437494745f, c2 = -0.8090169943749475f;
         const float s1 = 0.9510565162951535f, s2 = 0.5877852522924731f;
         const float2 b1 = cadd(v[1], v[4]), b2 = cadd(v[2], v[3]);
         const float2 d1 = csub(v[1], v[4]), d2 = csub(v[2], v[3]);
-        const float2 t1 = make_float2(v[0].x + c1 * b1.x + c2 * b2.x, v[0].y + c1 * b1.y + c2 * b2.y);
-        const float2 t2 = make_float2(v[0].x + c2 * b1.x + c1 * b2.x, v[0].y + c2 * b1.y + c1 * b2.y);
-        const float2 u1 = itimes(make_float2(s1 * d1.x + s2 * d2.x, s1 * d1.y + s2 * d2.y));
-        const float2 u2 = itimes(make_float2(s2 * d1.x - s1 * d2.x, s2 * d1.y - s1 * d2.y));
+        const float2 t1 = caxpy(c2, b2, caxpy(c1, b1, v[0]));
+        const float2 t2 = caxpy(c1, b2, caxpy(c2, b1, v[0]));
+        const float2 w1 = caxpy(s2, d2, cscale(d1, s1));
+        const float2 w2 = caxpy(-s1, d2, cscale(d1, s2));
         v[0] = cadd(v[0], cadd(b1, b2));
-        v[1] = cadd(t1, u1);
-        v[4] = csub(t1, u1);
-        v[2] = cadd(t2, u2);
-        v[3] = csub(t2, u2);
+        v[1] = cadd_i(t1, w1);
+        v[4] = csub_i(t1, w1);
+        v[2] = cadd_i(t2, w2);
+        v[3] = csub_i(t2, w2);
     } else if constexpr (R == 7) {
         // pairs (r, 7 - r): X[q] = v0 + sum_k cos(2 pi k q / 7) b_k + i sum_k sin(2 pi k q / 7) d_k
         const float c1 = 0.6234898018587336f, c2 = -0.22252093395631434f, c3 = -0.900968867902419f;
@@ -84,19 +117,19 @@ __host__ __device__ __forceinline__ void dft_small(float2 (&v)[kMaxRadix]) {
         const float2 b1 = cadd(v[1], v[6]), b2 = cadd(v[2], v[5]), b3 = cadd(v[3], v[4]);
         const float2 d1 = csub(v[1], v[6]), d2 = csub(v[2], v[5]), d3 = csub(v[3], v[4]);
         const float2 x0 = v[0];
-        const float2 t1 = make_float2(x0.x + c1 * b1.x + c2 * b2.x + c3 * b3.x, x0.y + c1 * b1.y + c2 * b2.y + c3 * b3.y);
-        const float2 t2 = make_float2(x0.x + c2 * b1.x + c3 * b2.x + c1 * b3.x, x0.y + c2 * b1.y + c3 * b2.y + c1 * b3.y);
-        const float2 t3 = make_float2(x0.x + c3 * b1.x + c1 * b2.x + c2 * b3.x, x0.y + c3 * b1.y + c1 * b2.y + c2 * b3.y);
-        const float2 u1 = itimes(make_float2(s1 * d1.x + s2 * d2.x + s3 * d3.x, s1 * d1.y + s2 * d2.y + s3 * d3.y));
-        const float2 u2 = itimes(make_float2(s2 * d1.x - s3 * d2.x - s1 * d3.x, s2 * d1.y - s3 * d2.y - s1 * d3.y));
-        const float2 u3 = itimes(make_float2(s3 * d1.x - s1 * d2.x + s2 * d3.x, s3 * d1.y - s1 * d2.y + s2 * d3.y));
+        const float2 t1 = caxpy(c3, b3, caxpy(c2, b2, caxpy(c1, b1, x0)));
+        const float2 t2 = caxpy(c1, b3, caxpy(c3, b2, caxpy(c2, b1, x0)));
+        const float2 t3 = caxpy(c2, b3, caxpy(c1, b2, caxpy(c3, b1, x0)));
+        const float2 w1 = caxpy(s3, d3, caxpy(s2, d2, cscale(d1, s1)));
+        const float2 w2 = caxpy(-s1, d3, caxpy(-s3, d2, cscale(d1, s2)));
+        const float2 w3 = caxpy(s2, d3, caxpy(-s1, d2, cscale(d1, s3)));
         v[0] = cadd(x0, cadd(b1, cadd(b2, b3)));
-        v[1] = cadd(t1, u1);
-        v[6] = csub(t1, u1);
-        v[2] = cadd(t2, u2);
-        v[5] = csub(t2, u2);
-        v[3] = cadd(t3, u3);
-        v[4] = csub(t3, u3);
+        v[1] = cadd_i(t1, w1);
+        v[6] = csub_i(t1, w1);
+        v[2] = cadd_i(t2, w2);
+        v[5] = csub_i(t2, w2);
+        v[3] = cadd_i(t3, w3);
+        v[4] = csub_i(t3, w3);
     } else if constexpr (R == 10) {
         // prime-factor split 10 = 2 x 5 (no twiddles): n = (5 n1 + 2 n2) mod 10,
         // X[k] with k = k1 (mod 2), k = k2 (mod 5): 2-point DFTs over n1, then

@@ -313,9 +313,8 @@ __device__ __forceinline__ void store_planes(const XArgs &a, const float2 *buf, 
             unsigned hw[P], lw[P];
 #pragma unroll
             for (int i = 0; i < P; i++) {
-                const __half2 h = __floats2half2_rn(v[i].x, v[i].y);
-                const float2 hb = __half22float2(h);
-                const __half2 g = __floats2half2_rn(v[i].x - hb.x, v[i].y - hb.y);
+                const __half2 h = __float22half2_rn(v[i]);
+                const __half2 g = __float22half2_rn(fftd::csub(v[i], __half22float2(h)));
                 hw[i] = *reinterpret_cast<const unsigned *>(&h);
                 lw[i] = *reinterpret_cast<const unsigned *>(&g);
             }
@@ -325,7 +324,7 @@ __device__ __forceinline__ void store_planes(const XArgs &a, const float2 *buf, 
             unsigned hw[P];
 #pragma unroll
             for (int i = 0; i < P; i++) {
-                const __nv_bfloat162 h = __floats2bfloat162_rn(v[i].x, v[i].y);
+                const __nv_bfloat162 h = __float22bfloat162_rn(v[i]);
                 hw[i] = *reinterpret_cast<const unsigned *>(&h);
             }
             store_words<P>(reinterpret_cast<__nv_bfloat16 *>(a.bhi) + ib, hw);
@@ -335,7 +334,7 @@ __device__ __forceinline__ void store_planes(const XArgs &a, const float2 *buf, 
             for (int i = 0; i < P; i++) {
                 h[i] = make_float2(__uint_as_float(__float_as_uint(v[i].x) & 0xFFFFE000u),
                                    __uint_as_float(__float_as_uint(v[i].y) & 0xFFFFE000u));
-                lo[i] = make_float2(v[i].x - h[i].x, v[i].y - h[i].y);
+                lo[i] = fftd::csub(v[i], h[i]);
             }
             store_floats<P>(reinterpret_cast<float *>(a.bhi) + ib, h);
             store_floats<P>(reinterpret_cast<float *>(a.blo) + ib, lo);
@@ -417,10 +416,10 @@ __global__ void __launch_bounds__(kThreads, PF <= 9 ? PBI4G_XPASS_MINB : 2) map_
             const float2 xc = (k > 0 && kc < kxn) ? xr[kc * kP + lane] : czero();  // X[M - k]
             const float2 ck = make_float2(xc.x, -xc.y), cc = make_float2(xk.x, -xk.y);
             const float2 o1 = fftd::cmul(fftd::csub(xk, ck), xt[k]);
-            buf[perm[k] * kP + lane] = fftd::cadd(fftd::cadd(xk, ck), fftd::itimes(o1));
+            buf[perm[k] * kP + lane] = fftd::cadd_i(fftd::cadd(xk, ck), o1);
             if (k > 0 && kc != k) {
                 const float2 o2 = fftd::cmul(fftd::csub(xc, cc), xt[kc]);
-                buf[perm[kc] * kP + lane] = fftd::cadd(fftd::cadd(xc, cc), fftd::itimes(o2));
+                buf[perm[kc] * kP + lane] = fftd::cadd_i(fftd::cadd(xc, cc), o2);
             }
         }
         __syncthreads();
