@@ -26,7 +26,7 @@
 //   * a TMA warp loads each chunk's B tile(s) (64 maps x 64 points, 128-byte
 //     swizzled: the K-major operand layout itself) and the FP32 set-0 maps of
 //     the chunk into a ring of shared-memory stages;
-//   * two producer warpgroups take the chunks in turn (thread = TMEM lane =
+//   * three producer warpgroups take the chunks in turn (thread = TMEM lane =
 //     pair row): they form the 64 products of their pair, split them and store
 //     them straight into a tensor-memory A stage with tcgen05.st (the A operand
 //     never touches shared memory);
@@ -70,13 +70,13 @@ constexpr int kKB = 32;          // FP32 values per 128-byte swizzle row (one K 
 constexpr int kBlocks = 2;       // K blocks per chunk
 constexpr int kKC = kKB * kBlocks;  // grid points per chunk
 constexpr int kMaxStages = 10;   // TMA staging slots (released by the producers and the MMAs)
-constexpr int kGroups = 2;       // producer warpgroups, chunks assigned round robin
+constexpr int kGroups = 3;       // producer warpgroups, chunks assigned round robin (2: 8% slower at 256^3)
 constexpr int kProdWarps = 4 * kGroups;
 constexpr int kDrainWarps = 8;   // two warpgroups, 32 accumulator columns each
 constexpr int kMmaWarp = kProdWarps + kDrainWarps;
 constexpr int kMmaWarps = 2;     // MMA issuers, chunks alternating (a thread's MMAs of a chunk stay in order)
 constexpr int kTmaWarp = kMmaWarp + kMmaWarps;
-constexpr int kThreads = (kTmaWarp + 1) * 32;  // 608
+constexpr int kThreads = (kTmaWarp + 1) * 32;  // 736
 #ifndef PBI4G_TM_FOLD
 #define PBI4G_TM_FOLD 16
 #endif
@@ -404,25 +404,30 @@ __global__ void __launch_bounds__(kThreads, 1)
                         tmem_st16(lane_addr + col + kKC, lo);
                     }
                 } else {
-                    // 32 points -> 16 packed columns (point 2c in the low half of column c)
-                    uint32_t hi[16], lo[16];
-                    if (pr.x >= 0) {
+                    // 32 points -> 16 packed columns (point 2c in the low half of column c), in
+                    // two halves of 16 points (fewer live registers: 23 warps fit in 80 each)
 #pragma unroll
-                        for (int c = 0; c < 8; c++) {
-                            const float4 u =
-                                *reinterpret_cast<const float4 *>(blk + pr.x * 128 + ((c ^ (pr.x & 7)) << 4));
-                            const float4 v =
-                                *reinterpret_cast<const float4 *>(blk + pr.y * 128 + ((c ^ (pr.y & 7)) << 4));
-                            pack_prod2<F>(u.x, v.x, u.y, v.y, hi[2 * c], lo[2 * c]);
-                            pack_prod2<F>(u.z, v.z, u.w, v.w, hi[2 * c + 1], lo[2 * c + 1]);
+                    for (int q8 = 0; q8 < 2; q8++) {
+                        uint32_t hi[8], lo[8];
+                        if (pr.x >= 0) {
+#pragma unroll
+                            for (int c4 = 0; c4 < 4; c4++) {
+                                const int c = 4 * q8 + c4;
+                                const float4 u =
+                                    *reinterpret_cast<const float4 *>(blk + pr.x * 128 + ((c ^ (pr.x & 7)) << 4));
+                                const float4 v =
+                                    *reinterpret_cast<const float4 *>(blk + pr.y * 128 + ((c ^ (pr.y & 7)) << 4));
+                                pack_prod2<F>(u.x, v.x, u.y, v.y, hi[2 * c4], lo[2 * c4]);
+                                pack_prod2<F>(u.z, v.z, u.w, v.w, hi[2 * c4 + 1], lo[2 * c4 + 1]);
+                            }
+                        } else {
+#pragma unroll
+                            for (int e = 0; e < 8; e++) hi[e] = lo[e] = 0u;
                         }
-                    } else {
-#pragma unroll
-                        for (int e = 0; e < 16; e++) hi[e] = lo[e] = 0u;
+                        const uint32_t col = acol + (uint32_t)(kb * (kKB / 2) + 8 * q8);
+                        tmem_st8(lane_addr + col, hi);
+                        if (FM::kSplit) tmem_st8(lane_addr + col + kKC / 2, lo);
                     }
-                    const uint32_t col = acol + (uint32_t)(kb * (kKB / 2));
-                    tmem_st16(lane_addr + col, hi);
-                    if (FM::kSplit) tmem_st16(lane_addr + col + kKC / 2, lo);
                 }
             }
             mbar_arrive(&sfree[s]);  // the stage's pair factors are consumed
