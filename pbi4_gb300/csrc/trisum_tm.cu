@@ -91,6 +91,7 @@ constexpr int kFoldGroup = 8;    // running sums a drain thread folds per batch 
 #endif
 constexpr int kAcc = PBI4G_TM_ACC;
 constexpr int kDone = 16;        // per-chunk MMA completion barriers (ring)
+constexpr int kMaxAStages = 6;   // producer -> MMA barriers (one per A stage)
 constexpr uint32_t kColAcc = 0;  // kAcc accumulators of kN columns, then the A stages
 constexpr uint32_t kColA = kAcc * kN;
 constexpr uint32_t kTmemCols = 512;
@@ -137,6 +138,10 @@ template <> struct Form<kFormBF16> {
 // count is a multiple of kMmaWarps.  Otherwise an issuer two phases ahead of a stage
 // would read a stale parity as complete.
 static_assert(kAcc % kMmaWarps == 0, "accumulators per issuer");
+// the producer -> MMA barriers (one per A stage) are an array of kMaxAStages
+static_assert(Form<kFormTF32>::kAStages <= kMaxAStages && Form<kFormF16>::kAStages <= kMaxAStages &&
+                  Form<kFormBF16>::kAStages <= kMaxAStages,
+              "A stages beyond the barrier array");
 static_assert(Form<kFormTF32>::kAStages % kMmaWarps == 0 && Form<kFormF16>::kAStages % kMmaWarps == 0 &&
                   Form<kFormBF16>::kAStages % kMmaWarps == 0,
               "A stages per issuer");
@@ -294,7 +299,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     // producers, drain), accfree per accumulator (drain -> MMA)
     // smem: nst stages | barriers and tables
     uint64_t *bars = reinterpret_cast<uint64_t *>(base + (size_t)nst * a.stage_bytes);
-    uint64_t *full = bars, *sfree = full + kMaxStages, *prod = sfree + kMaxStages, *done = prod + 4;
+    uint64_t *full = bars, *sfree = full + kMaxStages, *prod = sfree + kMaxStages, *done = prod + kMaxAStages;
     uint64_t *accfree = done + kDone;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(accfree + kAcc);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
@@ -324,7 +329,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             mbar_init(&full[s], 1);
             mbar_init(&sfree[s], 128);  // the warpgroup that consumed the stage's pair factors
         }
-        for (int s = 0; s < 4; s++) mbar_init(&prod[s], 128);  // one warpgroup per chunk
+        for (int s = 0; s < kMaxAStages; s++) mbar_init(&prod[s], 128);  // one warpgroup per chunk
         for (int s = 0; s < kDone; s++) mbar_init(&done[s], 1);
         for (int s = 0; s < kAcc; s++) mbar_init(&accfree[s], kDrainWarps * 32);
         *abort_flag = 0;
@@ -851,7 +856,8 @@ int triangle_sums_tm(const Shells &sh, TmPlan &tp, const MapPlanes &pl, DevBuf &
     const int btiles = form == 0 ? Form<kFormTF32>::kBTiles : (form == 1 ? Form<kFormF16>::kBTiles : 1);
     a.stage_bytes = kBlocks * a.ablock + (uint32_t)btiles * kBTile;
     // barriers, TMEM address, abort flag, pair table, B-row exponents
-    const size_t fixed = 1024 + 8 * (2 * kMaxStages + 4 + kDone + kAcc) + 16 + sizeof(int2) * kM + sizeof(int) * kN;
+    const size_t fixed =
+        1024 + 8 * (2 * kMaxStages + kMaxAStages + kDone + kAcc) + 16 + sizeof(int2) * kM + sizeof(int) * kN;
     a.nstages = kMaxStages;
     while (a.nstages > 3 && fixed + (size_t)a.nstages * a.stage_bytes > 227 * 1024) a.nstages--;
     const size_t smem = fixed + (size_t)a.nstages * a.stage_bytes;
