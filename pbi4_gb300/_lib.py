@@ -34,6 +34,7 @@ EXPORTS = [
     "pbi4g_measure_pk_multipoles_noalloc", "pbi4g_plan_set_delta_half", "pbi4g_plan_set_counts",
     "pbi4g_plan_check", "pbi4g_plan_graph_build", "pbi4g_plan_graph_run_host",
     "pbi4g_device_allocs", "pbi4g_debug_fail_alloc", "pbi4g_plan_debug_wait_limit",
+    "pbi4g_scratch_footprint", "pbi4g_scratch_create", "pbi4g_scratch_destroy", "pbi4g_plan_use_scratch",
 ]
 NSTAGES = 12
 STAGES = ["assign", "grid_convert", "fft_r2c", "fcomb", "pk_binning", "triangle_counts", "shell_maps_z",
@@ -104,6 +105,10 @@ _SIGS = {
     "pbi4g_plan_set_counts": [_P, _P],
     "pbi4g_debug_fail_alloc": [_i32],
     "pbi4g_plan_debug_wait_limit": [_P, _i64],
+    "pbi4g_scratch_footprint": [_i32, _i64, ctypes.POINTER(_i64)],
+    "pbi4g_scratch_create": [_i32, _i64, ctypes.POINTER(_P)],
+    "pbi4g_scratch_destroy": [_P],
+    "pbi4g_plan_use_scratch": [_P, _P],
 }
 
 _lock = threading.Lock()

@@ -57,6 +57,18 @@ struct alignas(16) PCell {
 struct alignas(16) PTile {              // a sorted record (particle, tile), both grids (32 bytes)
     PCell g[2];
 };
+// The buffers of an OwnerWork as the kernels see them.  Direct launches take
+// them by value; the captured form (IND) reads them from the plan's device block
+// (owner_ptrs_host), so its graphs follow the plan to another OwnerWork.  Read
+// through the block the tile kernel measured 3% slower at 256^3, which is why
+// the direct launches keep the kernel parameters.
+struct OwnerPtrs {
+    unsigned int *count, *start, *cursor;  // count: [ntiles + 2], the last two the tile counter
+    PRec *rec;
+    PTile *sorted;
+    float *wsorted;
+};
+static_assert(sizeof(OwnerPtrs) <= kOwnerPtrBytes, "owner pointer block");
 constexpr int kBias = 2048;             // a stencil with a cell inside starts at [-3, 15] per axis: base + kBias in [977, 7403]
 constexpr int kMX = 13, kMY = 17, kMZ = 21;
 
@@ -202,9 +214,12 @@ __device__ __forceinline__ int slot_tile(int s, const int tx[2], const int ty[2]
     return (tz[c] * nt + ty[b]) * nt + tx[a];
 }
 
+template <bool IND>
 __global__ void owner_count_kernel(int N, int nintp, int interlaced, int64_t npart, int64_t stride,
                                    const BoxPar *__restrict__ bp, const double *__restrict__ pos, int nt,
-                                   PRec *__restrict__ rec, unsigned int *__restrict__ count) {
+                                   const OwnerPtrs ov, const OwnerPtrs *__restrict__ op) {
+    PRec *__restrict__ rec = IND ? op->rec : ov.rec;
+    unsigned int *__restrict__ count = IND ? op->count : ov.count;
     const int w = nintp + (interlaced ? 1 : 0);  // cells spanned from the lowest first cell
     const int64_t n = bp ? bp->npart : npart;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -228,8 +243,10 @@ __global__ void owner_count_kernel(int N, int nintp, int interlaced, int64_t npa
     }
 }
 
-__global__ void owner_scan_kernel(int ntiles, const unsigned int *__restrict__ count, unsigned int *__restrict__ start,
-                                  unsigned int *__restrict__ cursor) {
+template <bool IND>
+__global__ void owner_scan_kernel(int ntiles, const OwnerPtrs ov, const OwnerPtrs *__restrict__ op) {
+    const unsigned int *__restrict__ count = IND ? op->count : ov.count;
+    unsigned int *__restrict__ start = IND ? op->start : ov.start, *__restrict__ cursor = IND ? op->cursor : ov.cursor;
     __shared__ unsigned int warp_tot[32];
     __shared__ unsigned int carry;
     if (threadIdx.x == 0) carry = 0;
@@ -278,10 +295,14 @@ __device__ __forceinline__ int cell_pack(unsigned f, int ox, int oy, int oz, int
     return (dz * kPz + dy * kPy + dx + kBias) | (int)(mx << kMX | my << kMY | mz << kMZ);
 }
 
+template <bool IND>
 __global__ void owner_scatter_kernel(int N, int nintp, int interlaced, int64_t npart, const BoxPar *__restrict__ bp,
-                                     int nt, const PRec *__restrict__ rec, const double *__restrict__ weight,
-                                     unsigned int *__restrict__ cursor, PTile *__restrict__ sorted,
-                                     float *__restrict__ wsorted) {
+                                     int nt, const OwnerPtrs ov, const OwnerPtrs *__restrict__ op,
+                                     const double *__restrict__ weight) {
+    const PRec *__restrict__ rec = IND ? op->rec : ov.rec;
+    unsigned int *__restrict__ cursor = IND ? op->cursor : ov.cursor;
+    PTile *__restrict__ sorted = IND ? op->sorted : ov.sorted;
+    float *__restrict__ wsorted = weight ? (IND ? op->wsorted : ov.wsorted) : nullptr;
     const int w = nintp + (interlaced ? 1 : 0);
     const int64_t n = bp ? bp->npart : npart;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -332,6 +353,24 @@ __global__ void owner_scatter_kernel(int N, int nintp, int interlaced, int64_t n
 // ((w_x w_y) w_z) weight, so every q is the same integer.  Two grids: the
 // halves take grids 0 and 1 of one record; one grid: two records.  Each
 // half-warp's 16 cells of a z step fall on 16 distinct bank pairs (2 i + 8 j).
+// Read-only loads of the sorted records (their pointers come from the pointer
+// block, so the compiler cannot infer that the kernel never writes them).
+__device__ __forceinline__ PCell ld_cell(const PCell *p) {
+    const int4 v = __ldg(reinterpret_cast<const int4 *>(p));
+    PCell c;
+    c.pack = v.x;
+    c.h[0] = __int_as_float(v.y);
+    c.h[1] = __int_as_float(v.z);
+    c.h[2] = __int_as_float(v.w);
+    return c;
+}
+__device__ __forceinline__ PTile ld_tile(const PTile *p) {
+    PTile t;
+    t.g[0] = ld_cell(&p->g[0]);
+    t.g[1] = ld_cell(&p->g[1]);
+    return t;
+}
+
 template <int G, bool W>
 __device__ __forceinline__ void pcs_columns(unsigned b, unsigned e, int warp, int nwarps, int lane, float scale,
                                             const PTile *__restrict__ sorted, const float *__restrict__ wsorted,
@@ -353,15 +392,15 @@ __device__ __forceinline__ void pcs_columns(unsigned b, unsigned e, int warp, in
     PCell cn = {};
     float wn = 1.f;
     if (b + (unsigned)(RPW * warp) + off < e) {
-        cn = sorted[b + (unsigned)(RPW * warp) + off].g[g];
-        if (W) wn = wsorted[b + (unsigned)(RPW * warp) + off];
+        cn = ld_cell(&sorted[b + (unsigned)(RPW * warp) + off].g[g]);
+        if (W) wn = __ldg(&wsorted[b + (unsigned)(RPW * warp) + off]);
     }
     for (unsigned k = b + (unsigned)(RPW * warp) + off; k - off < e; k += step) {
         const PCell c = cn;
         const float wt = wn;
         if (k + step < e) {
-            cn = sorted[k + step].g[g];
-            if (W) wn = wsorted[k + step];
+            cn = ld_cell(&sorted[k + step].g[g]);
+            if (W) wn = __ldg(&wsorted[k + step]);
         }
         // k >= e (the second record of a one-grid step past the end): pack 0
         const int pk = k < e ? c.pack : 0;
@@ -385,16 +424,18 @@ __device__ __forceinline__ void pcs_columns(unsigned b, unsigned e, int warp, in
 // fold to constants and shifts; PCS takes the column mapping above.  The
 // fixed-point scale 2^S rides in the z polynomial (a power of two: the
 // products are the same bits as scaling at the end).
-template <int NI, int G, bool W>
-__global__ void __launch_bounds__(kThreads, 2) owner_tile_kernel(int N, int nt, const unsigned int *__restrict__ start,
-                                                               const PTile *__restrict__ sorted,
-                                                               const float *__restrict__ wsorted, float scale,
+template <int NI, int G, bool W, bool IND>
+__global__ void __launch_bounds__(kThreads, 2) owner_tile_kernel(int N, int nt, const OwnerPtrs ov,
+                                                               const OwnerPtrs *__restrict__ op, float scale,
                                                                float inv_scale, float *__restrict__ out1,
-                                                               float *__restrict__ out2,
-                                                               unsigned int *__restrict__ next_tile) {
+                                                               float *__restrict__ out2) {
     constexpr int NC = NI * NI * NI;
     extern __shared__ unsigned long long acc64[];  // [G][kTCP]
     const int ntiles = nt * nt * nt;
+    const unsigned int *__restrict__ start = IND ? op->start : ov.start;
+    const PTile *__restrict__ sorted = IND ? op->sorted : ov.sorted;
+    const float *__restrict__ wsorted = W ? (IND ? op->wsorted : ov.wsorted) : nullptr;
+    unsigned int *next_tile = (IND ? op->count : ov.count) + ntiles + 1;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     __shared__ int s_tile;
     // tiles are handed out dynamically (their particle loads differ by orders of
@@ -408,7 +449,7 @@ __global__ void __launch_bounds__(kThreads, 2) owner_tile_kernel(int N, int nt, 
         const int ox = tx * kT, oy = ty * kT, oz = tz * kT;
         for (int c = threadIdx.x; c < G * kTCP; c += blockDim.x) acc64[c] = 0ull;
         __syncthreads();
-        const unsigned b = start[tile], e = start[tile + 1];
+        const unsigned b = __ldg(&start[tile]), e = __ldg(&start[tile + 1]);
         if constexpr (NI == 4) {
             pcs_columns<G, W>(b, e, warp, nwarps, lane, scale, sorted, wsorted, acc64);
         } else {
@@ -434,15 +475,15 @@ __global__ void __launch_bounds__(kThreads, 2) owner_tile_kernel(int N, int nt, 
             PTile rn;
             float wn = 1.f;
             if (b + warp < e) {
-                rn = sorted[b + warp];
-                if (W) wn = wsorted[b + warp];
+                rn = ld_tile(&sorted[b + warp]);
+                if (W) wn = __ldg(&wsorted[b + warp]);
             }
             for (unsigned k = b + warp; k < e; k += nwarps) {
                 const PTile r = rn;
                 const float wt = wn;
                 if (k + nwarps < e) {
-                    rn = sorted[k + nwarps];
-                    if (W) wn = wsorted[k + nwarps];
+                    rn = ld_tile(&sorted[k + nwarps]);
+                    if (W) wn = __ldg(&wsorted[k + nwarps]);
                 }
                 int cell[G][NIT];
                 int q[G][NIT];
@@ -484,27 +525,34 @@ __global__ void __launch_bounds__(kThreads, 2) owner_tile_kernel(int N, int nt, 
     }
 }
 
-template <int NI, int G, bool W>
-static int launch_tile_w(int N, int nt, const unsigned *start, const PTile *sorted, const float *wsorted, int bits,
-                         float *out1, float *out2, unsigned *next_tile, cudaStream_t st) {
+template <int NI, int G, bool W, bool IND>
+static int launch_tile_w(int N, int nt, const OwnerPtrs &ov, const OwnerPtrs *op, int bits, float *out1, float *out2,
+                         cudaStream_t st) {
     const size_t smem = sizeof(unsigned long long) * G * kTCP;
-    auto kern = owner_tile_kernel<NI, G, W>;
+    auto kern = owner_tile_kernel<NI, G, W, IND>;
     PBI4G_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int ntiles = nt * nt * nt;
     int per_sm = 0;
     PBI4G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem));
     const int grid = std::min(ntiles, 152 * std::max(1, per_sm));
-    kern<<<grid, kThreads, smem, st>>>(N, nt, start, sorted, wsorted, ldexpf(1.0f, bits), ldexpf(1.0f, -bits), out1,
-                                       out2, next_tile);
+    kern<<<grid, kThreads, smem, st>>>(N, nt, ov, op, ldexpf(1.0f, bits), ldexpf(1.0f, -bits), out1, out2);
     PBI4G_LAUNCH_CHECK();
     return PBI4G_OK;
 }
 
 template <int NI, int G>
-static int launch_tile(int N, int nt, const unsigned *start, const PTile *sorted, const float *wsorted, int bits,
-                       float *out1, float *out2, unsigned *next_tile, cudaStream_t st) {
-    return wsorted ? launch_tile_w<NI, G, true>(N, nt, start, sorted, wsorted, bits, out1, out2, next_tile, st)
-                   : launch_tile_w<NI, G, false>(N, nt, start, sorted, wsorted, bits, out1, out2, next_tile, st);
+static int launch_tile(int N, int nt, const OwnerPtrs &ov, const OwnerPtrs *op, bool weighted, int bits, float *out1,
+                       float *out2, cudaStream_t st) {
+    // the captured form takes no weights
+    if (op) return launch_tile_w<NI, G, false, true>(N, nt, ov, op, bits, out1, out2, st);
+    return weighted ? launch_tile_w<NI, G, true, false>(N, nt, ov, op, bits, out1, out2, st)
+                    : launch_tile_w<NI, G, false, false>(N, nt, ov, op, bits, out1, out2, st);
+}
+
+// zero the tile counts and the tile counter (through the pointer block)
+__global__ void owner_zero_kernel(const OwnerPtrs *__restrict__ op, int n) {  // the captured form
+    unsigned int *count = op->count;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) count[i] = 0u;
 }
 
 __global__ void owner_wmax_kernel(int64_t n, const double *__restrict__ w, unsigned long long *__restrict__ out) {
@@ -522,7 +570,21 @@ __global__ void owner_wmax_kernel(int64_t n, const double *__restrict__ w, unsig
 
 bool owner_supported(int N) { return N % kT == 0 && N >= 2 * kT && N <= 2048; }
 
+bool OwnerWork::fits(int N, int64_t npart) const {
+    const int nt = N / kT;
+    const size_t ntiles = (size_t)nt * nt * nt;
+    const size_t n = (size_t)(npart > 0 ? npart : 1);
+    return count.p && count.bytes >= (ntiles + 2) * 4 && start.bytes >= (ntiles + 1) * 4 &&
+           cursor.bytes >= (ntiles + 1) * 4 && rec.bytes >= n * sizeof(PRec) && sorted.bytes >= 8 * n * sizeof(PTile) &&
+           wsorted.bytes >= 8 * n * 4 && wmax.bytes >= 8;
+}
+
 int OwnerWork::ensure(int N, int64_t npart) {
+    if (fixed) {
+        if (fits(N, npart)) return PBI4G_OK;
+        return set_error(PBI4G_ERR_RANGE, "shared assignment scratch too small for grid %d, %lld particles", N,
+                         (long long)npart);
+    }
     const int nt = N / kT;
     const size_t ntiles = (size_t)nt * nt * nt;
     const size_t n = (size_t)(npart > 0 ? npart : 1);
@@ -537,22 +599,44 @@ int OwnerWork::ensure(int N, int64_t npart) {
     return PBI4G_OK;
 }
 
+void OwnerWork::release() {
+    for (DevBuf *b : {&count, &start, &cursor, &key, &rec, &sorted, &wsorted, &wmax}) b->release();
+}
+
 size_t OwnerWork::footprint(int N, int64_t npart) {
     const size_t nt = (size_t)(N / kT);
     return 3 * (nt * nt * nt + 2) * 4 + (size_t)npart * (sizeof(PRec) + 8 * (sizeof(PTile) + 4)) + 64;
 }
 
-int assign_owner(OwnerWork &wk, int N, int nintp, bool interlaced, int64_t npart, const double *d_pos,
-                 const double *d_weight, float *out, cudaStream_t st, int64_t *launches, int64_t stride,
-                 const BoxPar *bp, Prof *prof, int tile_stage, int sort_stage) {
+void owner_ptrs_host(const OwnerWork &wk, unsigned char (&block)[kOwnerPtrBytes]) {
+    OwnerPtrs o;
+    o.count = wk.count.as<unsigned int>();
+    o.start = wk.start.as<unsigned int>();
+    o.cursor = wk.cursor.as<unsigned int>();
+    o.rec = static_cast<PRec *>(wk.rec.p);
+    o.sorted = static_cast<PTile *>(wk.sorted.p);
+    o.wsorted = wk.wsorted.as<float>();
+    memset(block, 0, kOwnerPtrBytes);
+    memcpy(block, &o, sizeof(o));
+}
+
+int assign_owner(OwnerWork &wk, const void *d_ptrs, int N, int nintp, bool interlaced, int64_t npart,
+                 const double *d_pos, const double *d_weight, float *out, cudaStream_t st, int64_t *launches,
+                 int64_t stride, const BoxPar *bp, Prof *prof, int tile_stage, int sort_stage) {
     Prof none;
     Prof &pf = prof ? *prof : none;
     if (stride <= 0) stride = npart;
     if (!owner_supported(N)) return set_error(PBI4G_ERR_UNSUPPORTED, "owner assignment needs grid %% 16 == 0");
-    if (nintp < 1 || nintp > 4 || npart < 1 || !d_pos)
+    if (nintp < 1 || nintp > 4 || npart < 1 || !d_pos || !d_ptrs)
         return set_error(PBI4G_ERR_INVALID, "assign: nintp=%d npart=%lld", nintp, (long long)npart);
     if (npart >= (int64_t)0x1fffffffLL) return set_error(PBI4G_ERR_RANGE, "assign: npart >= 2^29");
-    PBI4G_CHECK(wk.ensure(N, npart));
+    // the caller has sized wk (and, for the captured form, written its pointers to d_ptrs)
+    if (!wk.fits(N, npart)) return set_error(PBI4G_ERR_INVALID, "assign: work buffers not sized for this box");
+    unsigned char blk[kOwnerPtrBytes];
+    owner_ptrs_host(wk, blk);
+    OwnerPtrs ov;
+    memcpy(&ov, blk, sizeof(ov));
+    const OwnerPtrs *op = bp ? static_cast<const OwnerPtrs *>(d_ptrs) : nullptr;  // the captured form
     double wmax = 1.0;
     if (d_weight && bp) return set_error(PBI4G_ERR_UNSUPPORTED, "captured assignment takes no weights");
     if (d_weight) {
@@ -574,36 +658,44 @@ int assign_owner(OwnerWork &wk, int N, int nintp, bool interlaced, int64_t npart
     if (bits < 8) return set_error(PBI4G_ERR_RANGE, "assign: particle weights up to %g", wmax);
     const int nt = N / kT, ntiles = nt * nt * nt;
     pf.begin(sort_stage, st);
-    PBI4G_CUDA(cudaMemsetAsync(wk.count.p, 0, (size_t)(ntiles + 2) * 4, st));  // counts and the tile counter
-    owner_count_kernel<<<grid_blocks(npart, 256), 256, 0, st>>>(N, nintp, interlaced, npart, stride, bp, d_pos, nt,
-                                                                static_cast<PRec *>(wk.rec.p),
-                                                                wk.count.as<unsigned int>());
-    PBI4G_LAUNCH_CHECK();
-    owner_scan_kernel<<<1, 1024, 0, st>>>(ntiles, wk.count.as<unsigned int>(), wk.start.as<unsigned int>(),
-                                          wk.cursor.as<unsigned int>());
-    PBI4G_LAUNCH_CHECK();
-    owner_scatter_kernel<<<grid_blocks(npart, 256), 256, 0, st>>>(
-        N, nintp, interlaced, npart, bp, nt, static_cast<const PRec *>(wk.rec.p), d_weight, wk.cursor.as<unsigned int>(),
-        static_cast<PTile *>(wk.sorted.p), d_weight ? wk.wsorted.as<float>() : nullptr);
+    // counts and the tile counter
+    if (op) {
+        owner_zero_kernel<<<grid_blocks(ntiles + 2, 256, 152 * 4), 256, 0, st>>>(op, ntiles + 2);
+        PBI4G_LAUNCH_CHECK();
+        ++*launches;
+        owner_count_kernel<true><<<grid_blocks(npart, 256), 256, 0, st>>>(N, nintp, interlaced, npart, stride, bp,
+                                                                          d_pos, nt, ov, op);
+        PBI4G_LAUNCH_CHECK();
+        owner_scan_kernel<true><<<1, 1024, 0, st>>>(ntiles, ov, op);
+        PBI4G_LAUNCH_CHECK();
+        owner_scatter_kernel<true><<<grid_blocks(npart, 256), 256, 0, st>>>(N, nintp, interlaced, npart, bp, nt, ov,
+                                                                            op, d_weight);
+    } else {
+        PBI4G_CUDA(cudaMemsetAsync(wk.count.p, 0, (size_t)(ntiles + 2) * 4, st));
+        owner_count_kernel<false><<<grid_blocks(npart, 256), 256, 0, st>>>(N, nintp, interlaced, npart, stride, bp,
+                                                                           d_pos, nt, ov, op);
+        PBI4G_LAUNCH_CHECK();
+        owner_scan_kernel<false><<<1, 1024, 0, st>>>(ntiles, ov, op);
+        PBI4G_LAUNCH_CHECK();
+        owner_scatter_kernel<false><<<grid_blocks(npart, 256), 256, 0, st>>>(N, nintp, interlaced, npart, bp, nt, ov,
+                                                                             op, d_weight);
+    }
     PBI4G_LAUNCH_CHECK();
     const size_t FC = full_cells(N);
-    const unsigned *st_ = wk.start.as<unsigned int>();
-    const PTile *so = static_cast<const PTile *>(wk.sorted.p);
-    const float *ws = d_weight ? wk.wsorted.as<float>() : nullptr;
+    const bool wt = d_weight != nullptr;
     float *o2 = interlaced ? out + FC : nullptr;
-    unsigned *nx = wk.count.as<unsigned int>() + ntiles + 1;
     pf.end(st);
     pf.begin(tile_stage, st);
     int rc = PBI4G_OK;
     switch (nintp * 2 + (interlaced ? 1 : 0)) {
-        case 2: rc = launch_tile<1, 1>(N, nt, st_, so, ws, bits, out, o2, nx, st); break;
-        case 3: rc = launch_tile<1, 2>(N, nt, st_, so, ws, bits, out, o2, nx, st); break;
-        case 4: rc = launch_tile<2, 1>(N, nt, st_, so, ws, bits, out, o2, nx, st); break;
-        case 5: rc = launch_tile<2, 2>(N, nt, st_, so, ws, bits, out, o2, nx, st); break;
-        case 6: rc = launch_tile<3, 1>(N, nt, st_, so, ws, bits, out, o2, nx, st); break;
-        case 7: rc = launch_tile<3, 2>(N, nt, st_, so, ws, bits, out, o2, nx, st); break;
-        case 8: rc = launch_tile<4, 1>(N, nt, st_, so, ws, bits, out, o2, nx, st); break;
-        default: rc = launch_tile<4, 2>(N, nt, st_, so, ws, bits, out, o2, nx, st); break;
+        case 2: rc = launch_tile<1, 1>(N, nt, ov, op, wt, bits, out, o2, st); break;
+        case 3: rc = launch_tile<1, 2>(N, nt, ov, op, wt, bits, out, o2, st); break;
+        case 4: rc = launch_tile<2, 1>(N, nt, ov, op, wt, bits, out, o2, st); break;
+        case 5: rc = launch_tile<2, 2>(N, nt, ov, op, wt, bits, out, o2, st); break;
+        case 6: rc = launch_tile<3, 1>(N, nt, ov, op, wt, bits, out, o2, st); break;
+        case 7: rc = launch_tile<3, 2>(N, nt, ov, op, wt, bits, out, o2, st); break;
+        case 8: rc = launch_tile<4, 1>(N, nt, ov, op, wt, bits, out, o2, st); break;
+        default: rc = launch_tile<4, 2>(N, nt, ov, op, wt, bits, out, o2, st); break;
     }
     pf.end(st);
     PBI4G_CHECK(rc);

@@ -235,6 +235,12 @@ template int BkEngine::run<double>(const double2 *const[3], const int[3], const 
 using namespace pbi4g;
 
 // ================================================================ plan ===
+// Assignment buffers shared by the plans that run on one stream (a serving slot).
+struct pbi4g_scratch {
+    OwnerWork wk;
+    int bound = 0;  // plans using it
+};
+
 struct pbi4g_plan {
     pbi4g_config cfg;
     cudaStream_t st = 0;
@@ -242,7 +248,12 @@ struct pbi4g_plan {
     bool fp64 = false;
     int N = 0, G = 1;
     AssignWork aw;
-    OwnerWork ow;
+    OwnerWork ow;               // the plan's own assignment buffers
+    OwnerWork *ow_cur = &ow;    // the buffers in use: ow or a shared scratch (pbi4g_plan_use_scratch)
+    DevBuf optr;                // the owner kernels' pointer block (owner_ptrs_host of *ow_cur)
+    unsigned char optr_host[kOwnerPtrBytes] = {};
+    bool optr_valid = false;
+    pbi4g_scratch *scratch = nullptr;  // the shared scratch in use, if any
     DevBuf real_grids, spec, delta;
     DevBuf pos_stage, w_stage, pout_d, bout_d;
     cufftHandle fwd = 0;
@@ -365,7 +376,68 @@ int pbi4g_plan_create(const pbi4g_config *cfg, pbi4g_plan **out) {
 }
 
 int pbi4g_plan_destroy(pbi4g_plan *plan) {
+    if (plan && plan->scratch) plan->scratch->bound--;
     delete plan;
+    return PBI4G_OK;
+}
+
+int pbi4g_scratch_footprint(int32_t grid_max, int64_t npart_max, int64_t *bytes) {
+    if (!bytes || npart_max < 1 || !owner_supported(grid_max))
+        return set_error(PBI4G_ERR_INVALID, "scratch footprint: grid %d (a multiple of 16 in [32, 2048]), %lld particles",
+                         grid_max, (long long)npart_max);
+    *bytes = (int64_t)OwnerWork::footprint(grid_max, npart_max);
+    return PBI4G_OK;
+}
+
+int pbi4g_scratch_create(int32_t grid_max, int64_t npart_max, pbi4g_scratch **out) {
+    int64_t b = 0;
+    PBI4G_CHECK(pbi4g_scratch_footprint(grid_max, npart_max, &b));
+    if (!out) return set_error(PBI4G_ERR_INVALID, "null scratch handle");
+    auto *sc = new (std::nothrow) pbi4g_scratch();
+    if (!sc) return set_error(PBI4G_ERR_NOMEM, "scratch object");
+    const int rc = sc->wk.ensure(grid_max, npart_max);
+    if (rc != PBI4G_OK) {
+        delete sc;
+        return rc;
+    }
+    sc->wk.fixed = true;
+    *out = sc;
+    return PBI4G_OK;
+}
+
+int pbi4g_scratch_destroy(pbi4g_scratch *scratch) {
+    if (!scratch) return PBI4G_OK;
+    if (scratch->bound > 0)
+        return set_error(PBI4G_ERR_INVALID, "scratch still in use by %d plan(s)", scratch->bound);
+    delete scratch;
+    return PBI4G_OK;
+}
+
+static int owner_bind(pbi4g_plan *p, int64_t npart);
+
+int pbi4g_plan_use_scratch(pbi4g_plan *plan, pbi4g_scratch *scratch) {
+    if (!plan) return set_error(PBI4G_ERR_INVALID, "null plan");
+    if (plan->fp64 || !owner_supported(plan->N)) return PBI4G_OK;  // no owner-computes assignment in this form
+    if (scratch == plan->scratch && plan->optr_valid) return PBI4G_OK;
+    OwnerWork *w = scratch ? &scratch->wk : &plan->ow;
+    const int64_t cap = std::max<int64_t>(1, plan->g.cap);
+    if (scratch && !w->fits(plan->N, cap))
+        return set_error(PBI4G_ERR_RANGE, "scratch too small for grid %d and %lld particles", plan->N,
+                         (long long)cap);
+    OwnerWork *prev = plan->ow_cur;
+    plan->ow_cur = w;
+    const int rc = owner_bind(plan, cap);
+    if (rc != PBI4G_OK) {  // keep the previous binding; the next run writes its block again
+        plan->ow_cur = prev;
+        plan->optr_valid = false;
+        return rc;
+    }
+    if (plan->scratch) plan->scratch->bound--;
+    plan->scratch = scratch;
+    if (scratch) {
+        scratch->bound++;
+        plan->ow.release();  // the plan's own buffers (idle plan: the caller's contract)
+    }
     return PBI4G_OK;
 }
 
@@ -425,6 +497,25 @@ int pbi4g_plan_triangle_counts(pbi4g_plan *plan, int64_t *counts_host) {
     return PBI4G_OK;
 }
 
+// Size the plan's assignment buffers in use (*ow_cur) for npart particles and
+// point its pointer block at them (a stream-ordered copy, only when they changed).
+static int owner_bind(pbi4g_plan *p, int64_t npart) {
+    PBI4G_CHECK(p->ow_cur->ensure(p->N, npart));
+    unsigned char blk[kOwnerPtrBytes];
+    owner_ptrs_host(*p->ow_cur, blk);
+    if (p->optr_valid && memcmp(blk, p->optr_host, kOwnerPtrBytes) == 0) return PBI4G_OK;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    PBI4G_CUDA(cudaStreamIsCapturing(p->st, &cs));
+    if (cs != cudaStreamCaptureStatusNone)
+        return set_error(PBI4G_ERR_INVALID, "assignment buffers changed during a capture");
+    PBI4G_CHECK(p->optr.ensure(kOwnerPtrBytes));
+    memcpy(p->optr_host, blk, kOwnerPtrBytes);
+    // the copy reads optr_host before the call returns (pageable source)
+    PBI4G_CUDA(cudaMemcpyAsync(p->optr.p, p->optr_host, kOwnerPtrBytes, cudaMemcpyHostToDevice, p->st));
+    p->optr_valid = true;
+    return PBI4G_OK;
+}
+
 // One box's density.  bp == nullptr: npart particles at d_pos (rows of npart).
 // bp != nullptr (captured form): npart is the slot capacity (rows of npart), the
 // particle count and the normalisation come from bp on the device.
@@ -432,8 +523,11 @@ static int density_impl(pbi4g_plan *p, int64_t npart, const double *d_pos, const
     const int N = p->N;
     int bits;
     if (!p->fp64 && owner_supported(N)) {
-        // FP32 grids straight from the owner-computes tiles (fixed-point sums in shared memory)
-        PBI4G_CHECK(assign_owner(p->ow, N, p->cfg.nintp, p->G == 2, npart, d_pos, d_weight,
+        // FP32 grids straight from the owner-computes tiles (fixed-point sums in shared memory);
+        // a captured box uses the binding made before the capture
+        if (!bp) PBI4G_CHECK(owner_bind(p, npart));
+        if (!p->optr_valid) return set_error(PBI4G_ERR_INVALID, "assignment buffers not bound before capture");
+        PBI4G_CHECK(assign_owner(*p->ow_cur, p->optr.p, N, p->cfg.nintp, p->G == 2, npart, d_pos, d_weight,
                                  p->real_grids.as<float>(), p->st, &p->launches, npart, bp, &p->prof, 0, 11));
     } else {
         if (bp) return set_error(PBI4G_ERR_UNSUPPORTED, "captured form needs the owner-computes assignment");
@@ -538,7 +632,7 @@ int pbi4g_plan_graph_build(pbi4g_plan *p, int32_t batch, int64_t npart_cap) {
     // positions at 0 (valid, in [0, 1)); one direct box sizes every buffer and
     // builds the lazy tables (windows, shells, triangle counts, cuFFT plans)
     PBI4G_CUDA(cudaMemsetAsync(g.pos.p, 0, sizeof(double) * 3 * (size_t)npart_cap * batch, p->st));
-    PBI4G_CHECK(p->ow.ensure(p->N, npart_cap));
+    if (!p->fp64 && owner_supported(p->N)) PBI4G_CHECK(owner_bind(p, npart_cap));
     PBI4G_CHECK(pbi4g_plan_run_device(p, 1, g.pos.as<double>(), nullptr, g.pout.as<double>(),
                                       g.bout_n ? g.bout.as<double>() : nullptr));
     PBI4G_CUDA(cudaStreamSynchronize(p->st));
@@ -595,6 +689,8 @@ int pbi4g_plan_graph_run_host(pbi4g_plan *p, int32_t nboxes, const int64_t *npar
         g.hpar[b] = BoxPar{(long long)npart[b], fcomb_cf(p->G == 2, p->cfg.box, (double)npart[b]),
                            bk_pow_sn(kf, npart[b]), 0.0};
     }
+    // the assignment's pointer block holds the buffers in use (rebound after a failed change)
+    if (!p->fp64 && owner_supported(p->N)) PBI4G_CHECK(owner_bind(p, g.cap));
     if (!g.exec[nboxes - 1]) PBI4G_CHECK(graph_capture(p, nboxes));
     for (int b = 0; b < nboxes; b++)
         PBI4G_CUDA(cudaMemcpy2DAsync(g.pos.as<double>() + (size_t)b * 3 * g.cap, sizeof(double) * g.cap, pos[b],

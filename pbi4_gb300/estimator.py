@@ -92,8 +92,50 @@ def footprint(cfg: EstimatorConfig, npart_max: int) -> int:
     return int(out.value)
 
 
+def uses_owner_work(cfg: EstimatorConfig) -> bool:
+    """Whether a plan for cfg assigns with the owner-computes tiles, whose record
+    buffers a shared AssignScratch can hold (the FP32 and tensor-core forms on
+    grids that are multiples of 16 in [32, 2048])."""
+    g = int(cfg.grid)
+    return cfg.precision != "fp64" and g % 16 == 0 and 32 <= g <= 2048
+
+
+def scratch_footprint(grid_max: int, npart_max: int) -> int:
+    """Device bytes of an AssignScratch for grids up to grid_max and npart_max particles."""
+    out = ctypes.c_int64()
+    check(lib().pbi4g_scratch_footprint(int(grid_max), int(npart_max), ctypes.byref(out)))
+    return int(out.value)
+
+
+class AssignScratch:
+    """Assignment buffers shared by plans that run one after another on one stream
+    (a serving slot): the per-tile particle records, up to 8 per particle, that
+    each plan otherwise owns (pbi4g_scratch_*).  It never grows: a box above
+    grid_max or npart_max fails.  Plans that share one must not run concurrently."""
+
+    def __init__(self, grid_max: int, npart_max: int):
+        h = ctypes.c_void_p()
+        check(lib().pbi4g_scratch_create(int(grid_max), int(npart_max), ctypes.byref(h)))
+        self._h = h
+        self.grid_max, self.npart_max = int(grid_max), int(npart_max)
+        self.bytes = scratch_footprint(grid_max, npart_max)
+
+    def close(self):
+        """Free the buffers; raises while a plan still uses them."""
+        if getattr(self, "_h", None):
+            check(lib().pbi4g_scratch_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Estimator:
     stream = None  # the stream object last given to set_stream (serving bookkeeping)
+    scratch = None  # the AssignScratch in use (None: the plan's own buffers)
 
     def __init__(self, cfg: EstimatorConfig, stream=None):
         self.cfg = cfg
@@ -134,6 +176,7 @@ class Estimator:
         if getattr(self, "_h", None):
             lib().pbi4g_plan_destroy(self._h)
             self._h = None
+            self.scratch = None
 
     def __del__(self):
         try:
@@ -145,6 +188,15 @@ class Estimator:
         """stream: a torch.cuda.Stream, an integer cudaStream_t, or None (legacy default)."""
         s = getattr(stream, "cuda_stream", stream)
         check(lib().pbi4g_plan_set_stream(self._h, s))
+
+    def use_scratch(self, scratch):
+        """Assign through a shared AssignScratch (None: the plan's own buffers).  The
+        plan must be idle; its captured graphs follow the binding.  A no-op for the
+        FP64 form, which has no such buffers."""
+        if scratch is self.scratch:
+            return
+        check(lib().pbi4g_plan_use_scratch(self._h, scratch._h if scratch is not None else None))
+        self.scratch = scratch  # keeps the scratch alive while the plan uses it
 
     def enable_timing(self, on: bool = True):
         check(lib().pbi4g_plan_enable_timing(self._h, int(bool(on))))

@@ -29,10 +29,12 @@ def init(backend: str | None = None):
     """Join the process group when WORLD_SIZE > 1 and return (world, rank, local_rank).
 
     backend defaults to "nccl" when CUDA is available, else "gloo".  On CUDA the
-    process is bound to its LOCAL_RANK device first."""
+    process is bound to its LOCAL_RANK device first, when that device exists (a
+    gloo group of more ranks than GPUs, as in the CPU tests, binds none)."""
     world, rank, local = env()
-    if torch.cuda.is_available():
-        torch.cuda.set_device(local if world > 1 else 0)
+    dev = local if world > 1 else 0
+    if torch.cuda.is_available() and dev < torch.cuda.device_count():
+        torch.cuda.set_device(dev)
     if world > 1 and not dist.is_initialized():
         dist.init_process_group(backend or ("nccl" if torch.cuda.is_available() else "gloo"))
     return world, rank, local

@@ -19,7 +19,10 @@ box through the direct path on the same slots.
 
 Admission is by device footprint: a batch starts when a slot is free and the
 plan it needs fits under the HBM budget; idle plans are evicted least recently
-used to make room, and a request whose plan can never fit is rejected.  Each
+used to make room, and a request whose plan can never fit is rejected.  The
+plans that run on one slot share its assignment record buffers (AssignScratch,
+3.2 GB at 10^7 particles), so a resident plan holds only its grids, tables and
+maps.  Each
 batch is issued asynchronously on its slot's stream (pageable positions are
 staged by the driver, outputs land in pinned buffers) followed by an event; the
 loop thread polls events, so new requests are admitted while others run.
@@ -35,7 +38,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from .estimator import Estimator, EstimatorConfig, footprint
+from .estimator import AssignScratch, Estimator, EstimatorConfig, footprint, scratch_footprint, uses_owner_work
 
 
 @dataclass
@@ -82,15 +85,16 @@ def graph_capable(cfg: EstimatorConfig) -> bool:
 
 
 class _Slot:
-    def __init__(self, torch, idx):
+    def __init__(self, torch, idx, scratch=None):
         self.idx = idx
         self.stream = torch.cuda.Stream()
+        self.scratch = scratch  # assignment buffers of the plans that run on this slot
         self.busy = None   # (requests, futures, plan, event, keep-alive objects, t_start)
 
 
 class Server:
     def __init__(self, hbm_budget_bytes: int, slots: int = 4, device: int = 0, max_npart: int = 10_000_000,
-                 batch: int = 4, lookahead: int = 64):
+                 batch: int = 4, lookahead: int = 64, shared_scratch: bool = True, scratch_grid_max: int = 1024):
         import torch
         self.torch = torch
         torch.cuda.set_device(device)
@@ -98,7 +102,14 @@ class Server:
         self.max_npart = int(max_npart)
         self.batch = int(batch)
         self.lookahead = int(lookahead)
-        self.slots = [_Slot(torch, k) for k in range(slots)]
+        # one set of assignment record buffers per slot, shared by every plan up to
+        # scratch_grid_max that runs there (a plan's own would be 3.2 GB at 10^7
+        # particles), counted as resident; larger grids keep their own
+        self.shared_scratch = bool(shared_scratch)
+        self.scratch_grid_max = int(scratch_grid_max)
+        self.slots = [_Slot(torch, k, AssignScratch(self.scratch_grid_max, self.max_npart)
+                            if self.shared_scratch else None) for k in range(slots)]
+        self.fixed_bytes = sum(sl.scratch.bytes for sl in self.slots if sl.scratch is not None)
         # (cfg key, instance) -> plan, least recently used first
         self.plans: "collections.OrderedDict[tuple, Estimator]" = collections.OrderedDict()
         self.plan_bytes: dict[tuple, int] = {}
@@ -146,9 +157,13 @@ class Server:
         for p in self.plans.values():
             p.close()
         self.plans.clear()
+        for sl in self.slots:
+            if sl.scratch is not None:
+                sl.scratch.close()
+                sl.scratch = None
 
     def resident_bytes(self) -> int:
-        return sum(self.plan_bytes.values())
+        return self.fixed_bytes + sum(self.plan_bytes.values())
 
     def stats(self) -> dict:
         """Latency percentiles and throughput of the completed requests, with the
@@ -183,9 +198,17 @@ class Server:
     # --------------------------------------------------------------- loop ---
     def _footprint(self, cfg: EstimatorConfig) -> int:
         need = footprint(cfg, self.max_npart)
+        if self._shares(cfg):
+            need -= scratch_footprint(cfg.grid, self.max_npart)  # held by the slots' scratch
         if graph_capable(cfg):
             need += self.batch * 3 * self.max_npart * 8
         return need
+
+    def _shares(self, cfg: EstimatorConfig) -> bool:
+        return self.shared_scratch and uses_owner_work(cfg) and int(cfg.grid) <= self.scratch_grid_max
+
+    def _scratch_for(self, cfg: EstimatorConfig, slot: _Slot):
+        return slot.scratch if self._shares(cfg) else None
 
     def _busy(self, plan) -> bool:
         return any(s.busy is not None and s.busy[2] is plan for s in self.slots)
@@ -200,11 +223,13 @@ class Server:
                 if plan.stream is not slot.stream:
                     plan.set_stream(slot.stream)
                     plan.stream = slot.stream
+                plan.use_scratch(self._scratch_for(cfg, slot))
                 return plan
         key = (ck, max((k[1] for k in insts), default=-1) + 1)
         need = self._footprint(cfg)
-        if need > self.budget:
-            raise MemoryError(f"plan footprint {need / 1e9:.2f} GB exceeds the HBM budget {self.budget / 1e9:.2f} GB")
+        if need + self.fixed_bytes > self.budget:
+            raise MemoryError(f"plan footprint {need / 1e9:.2f} GB (beside {self.fixed_bytes / 1e9:.2f} GB of slot "
+                              f"scratch) exceeds the HBM budget {self.budget / 1e9:.2f} GB")
         # evict idle plans (least recently used first) until the new one fits
         while self.resident_bytes() + need > self.budget:
             victim = None
@@ -220,6 +245,7 @@ class Server:
             self.torch.cuda.empty_cache()
         plan = Estimator(cfg, stream=slot.stream)
         plan.stream = slot.stream
+        plan.use_scratch(self._scratch_for(cfg, slot))
         if graph_capable(cfg):
             plan.graph_build(self.batch, self.max_npart)
         self.plans[key] = plan

@@ -68,6 +68,19 @@ def test_errors_without_device(lib):
     assert out.value > 256 ** 3 * 8
 
 
+def test_scratch_footprint_without_device(lib):
+    """The shared assignment scratch's size is the plan's own record buffers'
+    (a plan that shares one leaves exactly that much out), and bad arguments are
+    rejected on the host."""
+    out = ctypes.c_int64()
+    assert lib.pbi4g_scratch_footprint(1024, 10 ** 7, ctypes.byref(out)) == 0
+    # 32-byte particle record, up to 8 tile records of 32 bytes and their weights
+    assert out.value == 3 * ((1024 // 16) ** 3 + 2) * 4 + 10 ** 7 * (32 + 8 * (32 + 4)) + 64
+    assert lib.pbi4g_scratch_footprint(40, 1000, ctypes.byref(out)) == 1  # not a multiple of 16
+    assert lib.pbi4g_scratch_footprint(64, 0, ctypes.byref(out)) == 1
+    assert b"scratch" in lib.pbi4g_last_error()
+
+
 @pytest.mark.parametrize("n", [2, 3, 5, 7, 8, 12, 20, 40, 50, 60, 100, 128, 140, 150, 196, 200, 240, 294, 320,
                                392, 400, 480, 512, 640, 8000])
 def test_fft_plan_host(lib, n):
