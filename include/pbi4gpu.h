@@ -165,19 +165,22 @@ int pbi4g_plan_set_stream(pbi4g_plan *plan, void *stream);
 
 /* Shared assignment scratch.  The FP32 and tensor-core forms count-sort the
  * particles into per-tile records (up to 8 per particle: 3.2 GB at 10^7
- * particles) in buffers each plan owns.  Plans that run one after another on one
- * stream (a serving slot) can share one scratch instead: pbi4g_plan_use_scratch
- * points the plan's assignment at it and frees the plan's own buffers, and NULL
- * returns the plan to its own.  The plan must be idle; its captured graphs follow
- * the binding (the kernels read the buffer addresses from a per-plan device
- * block, rewritten on the plan's stream when the binding changes).  A scratch
- * never grows: a box above its grid or particle count fails with PBI4G_ERR_RANGE.
- * Plans sharing a scratch must not run concurrently.  The FP64 form has no such
- * buffers (use_scratch is a no-op).  destroy fails while plans still use it.
- * Replaces nothing in the reference (its Fortran assignment needs no scratch). */
+ * particles) in buffers each plan owns, and the captured form holds `batch` position
+ * slots of its capacity.  Plans that run one after another on one stream (a
+ * serving slot) can share one scratch instead: pbi4g_plan_use_scratch points the
+ * plan's assignment at it and frees the plan's own buffers (and its position slots
+ * when the scratch holds `boxes` >= the plan's batch of at least its capacity), and
+ * NULL returns the plan to its own.  The plan must be idle; its captured graphs
+ * follow the binding (the kernels read the record addresses from a per-plan device
+ * block, rewritten on the plan's stream when the binding changes, and each box's
+ * position slot from its per-launch parameters).  A scratch never grows: a box
+ * above its grid or particle count fails with PBI4G_ERR_RANGE.  Plans sharing a
+ * scratch must not run concurrently.  The FP64 form has no such buffers
+ * (use_scratch is a no-op).  destroy fails while plans still use it.  Replaces
+ * nothing in the reference (its Fortran assignment needs no scratch). */
 typedef struct pbi4g_scratch pbi4g_scratch;
-int pbi4g_scratch_footprint(int32_t grid_max, int64_t npart_max, int64_t *bytes);
-int pbi4g_scratch_create(int32_t grid_max, int64_t npart_max, pbi4g_scratch **out);
+int pbi4g_scratch_footprint(int32_t grid_max, int64_t npart_max, int32_t boxes, int64_t *bytes);
+int pbi4g_scratch_create(int32_t grid_max, int64_t npart_max, int32_t boxes, pbi4g_scratch **out);
 int pbi4g_scratch_destroy(pbi4g_scratch *scratch);
 int pbi4g_plan_use_scratch(pbi4g_plan *plan, pbi4g_scratch *scratch);
 /* Output sizes: pout is (5, nbins_ps), bout is (brows, itot), Fortran order. */

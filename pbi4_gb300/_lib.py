@@ -105,8 +105,8 @@ _SIGS = {
     "pbi4g_plan_set_counts": [_P, _P],
     "pbi4g_debug_fail_alloc": [_i32],
     "pbi4g_plan_debug_wait_limit": [_P, _i64],
-    "pbi4g_scratch_footprint": [_i32, _i64, ctypes.POINTER(_i64)],
-    "pbi4g_scratch_create": [_i32, _i64, ctypes.POINTER(_P)],
+    "pbi4g_scratch_footprint": [_i32, _i64, _i32, ctypes.POINTER(_i64)],
+    "pbi4g_scratch_create": [_i32, _i64, _i32, ctypes.POINTER(_P)],
     "pbi4g_scratch_destroy": [_P],
     "pbi4g_plan_use_scratch": [_P, _P],
 }

@@ -216,8 +216,10 @@ __device__ __forceinline__ int slot_tile(int s, const int tx[2], const int ty[2]
 
 template <bool IND>
 __global__ void owner_count_kernel(int N, int nintp, int interlaced, int64_t npart, int64_t stride,
-                                   const BoxPar *__restrict__ bp, const double *__restrict__ pos, int nt,
+                                   const BoxPar *__restrict__ bp, const double *__restrict__ pos_arg, int nt,
                                    const OwnerPtrs ov, const OwnerPtrs *__restrict__ op) {
+    // the captured form reads the box's position slot from its BoxPar
+    const double *__restrict__ pos = (IND && bp) ? bp->pos : pos_arg;
     PRec *__restrict__ rec = IND ? op->rec : ov.rec;
     unsigned int *__restrict__ count = IND ? op->count : ov.count;
     const int w = nintp + (interlaced ? 1 : 0);  // cells spanned from the lowest first cell

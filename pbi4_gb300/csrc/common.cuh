@@ -77,9 +77,9 @@ inline size_t full_cells(int N) { return (size_t)N * N * N; }
 // direct path passes by value.
 struct BoxPar {
     long long npart;
-    double fcomb_cf;  // interlacing / window normalisation over npart (fcomb_half)
-    double pow_sn;    // 1 / npart / kf^3 (bk_finalize)
-    double pad;
+    double fcomb_cf;    // interlacing / window normalisation over npart (fcomb_half)
+    double pow_sn;      // 1 / npart / kf^3 (bk_finalize)
+    const double *pos;  // the box's positions, rows of the capacity (read by the captured assignment)
 };
 
 // Device allocations this library has made through DevBuf since it was loaded

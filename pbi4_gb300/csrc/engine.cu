@@ -238,7 +238,10 @@ using namespace pbi4g;
 // Assignment buffers shared by the plans that run on one stream (a serving slot).
 struct pbi4g_scratch {
     OwnerWork wk;
-    int bound = 0;  // plans using it
+    DevBuf pos;         // graph position slots: [boxes][3][cap] float64
+    int boxes = 0;
+    int64_t cap = 0;
+    int bound = 0;      // plans using it
 };
 
 struct pbi4g_plan {
@@ -381,26 +384,30 @@ int pbi4g_plan_destroy(pbi4g_plan *plan) {
     return PBI4G_OK;
 }
 
-int pbi4g_scratch_footprint(int32_t grid_max, int64_t npart_max, int64_t *bytes) {
-    if (!bytes || npart_max < 1 || !owner_supported(grid_max))
-        return set_error(PBI4G_ERR_INVALID, "scratch footprint: grid %d (a multiple of 16 in [32, 2048]), %lld particles",
-                         grid_max, (long long)npart_max);
-    *bytes = (int64_t)OwnerWork::footprint(grid_max, npart_max);
+int pbi4g_scratch_footprint(int32_t grid_max, int64_t npart_max, int32_t boxes, int64_t *bytes) {
+    if (!bytes || npart_max < 1 || boxes < 0 || boxes > 64 || !owner_supported(grid_max))
+        return set_error(PBI4G_ERR_INVALID,
+                         "scratch footprint: grid %d (a multiple of 16 in [32, 2048]), %lld particles, %d boxes",
+                         grid_max, (long long)npart_max, boxes);
+    *bytes = (int64_t)(OwnerWork::footprint(grid_max, npart_max) + sizeof(double) * 3 * (size_t)npart_max * boxes);
     return PBI4G_OK;
 }
 
-int pbi4g_scratch_create(int32_t grid_max, int64_t npart_max, pbi4g_scratch **out) {
+int pbi4g_scratch_create(int32_t grid_max, int64_t npart_max, int32_t boxes, pbi4g_scratch **out) {
     int64_t b = 0;
-    PBI4G_CHECK(pbi4g_scratch_footprint(grid_max, npart_max, &b));
+    PBI4G_CHECK(pbi4g_scratch_footprint(grid_max, npart_max, boxes, &b));
     if (!out) return set_error(PBI4G_ERR_INVALID, "null scratch handle");
     auto *sc = new (std::nothrow) pbi4g_scratch();
     if (!sc) return set_error(PBI4G_ERR_NOMEM, "scratch object");
-    const int rc = sc->wk.ensure(grid_max, npart_max);
+    int rc = sc->wk.ensure(grid_max, npart_max);
+    if (rc == PBI4G_OK && boxes > 0) rc = sc->pos.ensure(sizeof(double) * 3 * (size_t)npart_max * boxes);
     if (rc != PBI4G_OK) {
         delete sc;
         return rc;
     }
     sc->wk.fixed = true;
+    sc->boxes = boxes;
+    sc->cap = npart_max;
     *out = sc;
     return PBI4G_OK;
 }
@@ -414,6 +421,22 @@ int pbi4g_scratch_destroy(pbi4g_scratch *scratch) {
 }
 
 static int owner_bind(pbi4g_plan *p, int64_t npart);
+
+// Whether the plan's scratch holds its graph position slots (batch boxes of cap particles).
+static bool scratch_holds_slots(const pbi4g_plan *p) {
+    return p->scratch && p->g.batch > 0 && p->scratch->boxes >= p->g.batch && p->scratch->cap >= p->g.cap;
+}
+
+// The graph position slots in use: the scratch's, or the plan's own (allocated on demand).
+static int pos_slots(pbi4g_plan *p, double **slots) {
+    if (scratch_holds_slots(p)) {
+        *slots = p->scratch->pos.as<double>();
+        return PBI4G_OK;
+    }
+    PBI4G_CHECK(p->g.pos.ensure(sizeof(double) * 3 * (size_t)p->g.cap * p->g.batch));
+    *slots = p->g.pos.as<double>();
+    return PBI4G_OK;
+}
 
 int pbi4g_plan_use_scratch(pbi4g_plan *plan, pbi4g_scratch *scratch) {
     if (!plan) return set_error(PBI4G_ERR_INVALID, "null plan");
@@ -437,6 +460,7 @@ int pbi4g_plan_use_scratch(pbi4g_plan *plan, pbi4g_scratch *scratch) {
     if (scratch) {
         scratch->bound++;
         plan->ow.release();  // the plan's own buffers (idle plan: the caller's contract)
+        if (scratch_holds_slots(plan)) plan->g.pos.release();
     }
     return PBI4G_OK;
 }
@@ -624,16 +648,17 @@ int pbi4g_plan_graph_build(pbi4g_plan *p, int32_t batch, int64_t npart_cap) {
     g.cap = npart_cap;
     g.pout_n = (size_t)5 * p->cfg.nbins_ps;
     g.bout_n = p->cfg.do_bispectrum ? (size_t)(p->cfg.multipoles ? 11 : 9) * p->bk.sh.itot : 0;
-    PBI4G_CHECK(g.pos.ensure(sizeof(double) * 3 * (size_t)npart_cap * batch));
     PBI4G_CHECK(g.pout.ensure(sizeof(double) * g.pout_n * batch));
     PBI4G_CHECK(g.bout.ensure(sizeof(double) * std::max<size_t>(1, g.bout_n) * batch));
     PBI4G_CHECK(g.par.ensure(sizeof(BoxPar) * batch));
-    g.hpar.assign(batch, BoxPar{1, fcomb_cf(p->G == 2, p->cfg.box, 1.0), bk_pow_sn(plan_kf(p), 1), 0.0});
+    g.hpar.assign(batch, BoxPar{1, fcomb_cf(p->G == 2, p->cfg.box, 1.0), bk_pow_sn(plan_kf(p), 1), nullptr});
+    if (!p->fp64 && owner_supported(p->N)) PBI4G_CHECK(owner_bind(p, npart_cap));
+    double *slots = nullptr;  // the scratch's position slots, or the plan's own
+    PBI4G_CHECK(pos_slots(p, &slots));
     // positions at 0 (valid, in [0, 1)); one direct box sizes every buffer and
     // builds the lazy tables (windows, shells, triangle counts, cuFFT plans)
-    PBI4G_CUDA(cudaMemsetAsync(g.pos.p, 0, sizeof(double) * 3 * (size_t)npart_cap * batch, p->st));
-    if (!p->fp64 && owner_supported(p->N)) PBI4G_CHECK(owner_bind(p, npart_cap));
-    PBI4G_CHECK(pbi4g_plan_run_device(p, 1, g.pos.as<double>(), nullptr, g.pout.as<double>(),
+    PBI4G_CUDA(cudaMemsetAsync(slots, 0, sizeof(double) * 3 * (size_t)npart_cap, p->st));
+    PBI4G_CHECK(pbi4g_plan_run_device(p, 1, slots, nullptr, g.pout.as<double>(),
                                       g.bout_n ? g.bout.as<double>() : nullptr));
     PBI4G_CUDA(cudaStreamSynchronize(p->st));
     return p->cfg.do_bispectrum ? p->bk.check(p->st) : PBI4G_OK;
@@ -641,6 +666,8 @@ int pbi4g_plan_graph_build(pbi4g_plan *p, int32_t batch, int64_t npart_cap) {
 
 static int graph_capture(pbi4g_plan *p, int nboxes) {
     auto &g = p->g;
+    double *slots = nullptr;  // (the captured assignment reads each box's slot from its BoxPar)
+    PBI4G_CHECK(pos_slots(p, &slots));
     const bool prof_on = p->prof.on;
     p->prof.on = false;  // no timing events inside a graph
     cudaGraph_t graph = nullptr;
@@ -649,7 +676,7 @@ static int graph_capture(pbi4g_plan *p, int nboxes) {
     int rc = PBI4G_OK;
     for (int b = 0; b < nboxes && rc == PBI4G_OK; b++) {
         const BoxPar *bp = g.par.as<BoxPar>() + b;
-        const double *pos = g.pos.as<double>() + (size_t)b * 3 * g.cap;
+        const double *pos = slots + (size_t)b * 3 * g.cap;
         double *po = g.pout.as<double>() + (size_t)b * g.pout_n;
         double *bo = g.bout.as<double>() + (size_t)b * g.bout_n;
         rc = density_impl(p, g.cap, pos, nullptr, bp);
@@ -687,15 +714,19 @@ int pbi4g_plan_graph_run_host(pbi4g_plan *p, int32_t nboxes, const int64_t *npar
             return set_error(PBI4G_ERR_RANGE, "box %d: npart %lld outside 1..%lld", b, (long long)npart[b],
                              (long long)g.cap);
         g.hpar[b] = BoxPar{(long long)npart[b], fcomb_cf(p->G == 2, p->cfg.box, (double)npart[b]),
-                           bk_pow_sn(kf, npart[b]), 0.0};
+                           bk_pow_sn(kf, npart[b]), nullptr};
     }
     // the assignment's pointer block holds the buffers in use (rebound after a failed change)
     if (!p->fp64 && owner_supported(p->N)) PBI4G_CHECK(owner_bind(p, g.cap));
     if (!g.exec[nboxes - 1]) PBI4G_CHECK(graph_capture(p, nboxes));
-    for (int b = 0; b < nboxes; b++)
-        PBI4G_CUDA(cudaMemcpy2DAsync(g.pos.as<double>() + (size_t)b * 3 * g.cap, sizeof(double) * g.cap, pos[b],
+    double *slots = nullptr;  // the scratch's position slots, or the plan's own
+    PBI4G_CHECK(pos_slots(p, &slots));
+    for (int b = 0; b < nboxes; b++) {
+        g.hpar[b].pos = slots + (size_t)b * 3 * g.cap;
+        PBI4G_CUDA(cudaMemcpy2DAsync(slots + (size_t)b * 3 * g.cap, sizeof(double) * g.cap, pos[b],
                                      sizeof(double) * npart[b], sizeof(double) * npart[b], 3, cudaMemcpyHostToDevice,
                                      p->st));
+    }
     PBI4G_CUDA(cudaMemcpyAsync(g.par.p, g.hpar.data(), sizeof(BoxPar) * nboxes, cudaMemcpyHostToDevice, p->st));
     PBI4G_CUDA(cudaGraphLaunch(g.exec[nboxes - 1], p->st));
     p->launches += g.exec_launches[nboxes - 1];

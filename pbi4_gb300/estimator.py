@@ -100,25 +100,27 @@ def uses_owner_work(cfg: EstimatorConfig) -> bool:
     return cfg.precision != "fp64" and g % 16 == 0 and 32 <= g <= 2048
 
 
-def scratch_footprint(grid_max: int, npart_max: int) -> int:
-    """Device bytes of an AssignScratch for grids up to grid_max and npart_max particles."""
+def scratch_footprint(grid_max: int, npart_max: int, boxes: int = 0) -> int:
+    """Device bytes of an AssignScratch for grids up to grid_max, npart_max particles
+    and `boxes` graph position slots."""
     out = ctypes.c_int64()
-    check(lib().pbi4g_scratch_footprint(int(grid_max), int(npart_max), ctypes.byref(out)))
+    check(lib().pbi4g_scratch_footprint(int(grid_max), int(npart_max), int(boxes), ctypes.byref(out)))
     return int(out.value)
 
 
 class AssignScratch:
     """Assignment buffers shared by plans that run one after another on one stream
     (a serving slot): the per-tile particle records, up to 8 per particle, that
-    each plan otherwise owns (pbi4g_scratch_*).  It never grows: a box above
-    grid_max or npart_max fails.  Plans that share one must not run concurrently."""
+    each plan otherwise owns, and `boxes` position slots for their captured graphs
+    (pbi4g_scratch_*).  It never grows: a box above grid_max or npart_max fails.
+    Plans that share one must not run concurrently."""
 
-    def __init__(self, grid_max: int, npart_max: int):
+    def __init__(self, grid_max: int, npart_max: int, boxes: int = 0):
         h = ctypes.c_void_p()
-        check(lib().pbi4g_scratch_create(int(grid_max), int(npart_max), ctypes.byref(h)))
+        check(lib().pbi4g_scratch_create(int(grid_max), int(npart_max), int(boxes), ctypes.byref(h)))
         self._h = h
-        self.grid_max, self.npart_max = int(grid_max), int(npart_max)
-        self.bytes = scratch_footprint(grid_max, npart_max)
+        self.grid_max, self.npart_max, self.boxes = int(grid_max), int(npart_max), int(boxes)
+        self.bytes = scratch_footprint(grid_max, npart_max, boxes)
 
     def close(self):
         """Free the buffers; raises while a plan still uses them."""

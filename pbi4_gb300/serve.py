@@ -107,7 +107,7 @@ class Server:
         # particles), counted as resident; larger grids keep their own
         self.shared_scratch = bool(shared_scratch)
         self.scratch_grid_max = int(scratch_grid_max)
-        self.slots = [_Slot(torch, k, AssignScratch(self.scratch_grid_max, self.max_npart)
+        self.slots = [_Slot(torch, k, AssignScratch(self.scratch_grid_max, self.max_npart, self.batch)
                             if self.shared_scratch else None) for k in range(slots)]
         self.fixed_bytes = sum(sl.scratch.bytes for sl in self.slots if sl.scratch is not None)
         # (cfg key, instance) -> plan, least recently used first
@@ -200,8 +200,8 @@ class Server:
         need = footprint(cfg, self.max_npart)
         if self._shares(cfg):
             need -= scratch_footprint(cfg.grid, self.max_npart)  # held by the slots' scratch
-        if graph_capable(cfg):
-            need += self.batch * 3 * self.max_npart * 8
+        elif graph_capable(cfg):
+            need += self.batch * 3 * self.max_npart * 8  # its own graph position slots
         return need
 
     def _shares(self, cfg: EstimatorConfig) -> bool:

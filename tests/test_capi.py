@@ -73,11 +73,15 @@ def test_scratch_footprint_without_device(lib):
     (a plan that shares one leaves exactly that much out), and bad arguments are
     rejected on the host."""
     out = ctypes.c_int64()
-    assert lib.pbi4g_scratch_footprint(1024, 10 ** 7, ctypes.byref(out)) == 0
+    assert lib.pbi4g_scratch_footprint(1024, 10 ** 7, 0, ctypes.byref(out)) == 0
     # 32-byte particle record, up to 8 tile records of 32 bytes and their weights
-    assert out.value == 3 * ((1024 // 16) ** 3 + 2) * 4 + 10 ** 7 * (32 + 8 * (32 + 4)) + 64
-    assert lib.pbi4g_scratch_footprint(40, 1000, ctypes.byref(out)) == 1  # not a multiple of 16
-    assert lib.pbi4g_scratch_footprint(64, 0, ctypes.byref(out)) == 1
+    records = 3 * ((1024 // 16) ** 3 + 2) * 4 + 10 ** 7 * (32 + 8 * (32 + 4)) + 64
+    assert out.value == records
+    assert lib.pbi4g_scratch_footprint(1024, 10 ** 7, 4, ctypes.byref(out)) == 0
+    assert out.value == records + 4 * 3 * 10 ** 7 * 8  # and four graph position slots
+    assert lib.pbi4g_scratch_footprint(40, 1000, 0, ctypes.byref(out)) == 1  # not a multiple of 16
+    assert lib.pbi4g_scratch_footprint(64, 0, 0, ctypes.byref(out)) == 1
+    assert lib.pbi4g_scratch_footprint(64, 1000, -1, ctypes.byref(out)) == 1
     assert b"scratch" in lib.pbi4g_last_error()
 
 

@@ -1,6 +1,7 @@
 """Shared assignment scratch (pbi4g_scratch_*, pbi4g_plan_use_scratch).
 
-A plan that assigns through a shared scratch, or moves between scratches, gives
+A plan that assigns through a shared scratch (with or without the graph
+position slots), or moves between scratches, gives
 its boxes the same density as with its own buffers, bit for bit: the records
 are the same, only their addresses change.  P and B then agree within the
 ordering of the floating-point atomics of the P bins and shell powers (1e-6);
@@ -64,8 +65,10 @@ def test_scratch_follows_captured_graphs():
         alone.close()
     est = Estimator(CFG_B, stream=torch.cuda.Stream())
     est.graph_build(4, cap)
-    scratches = [AssignScratch(64, cap), AssignScratch(256, 4 * cap)]
-    for sc in [None, scratches[0], scratches[1], None, scratches[0]]:
+    # records only (positions stay in the plan's own slots), and records with four
+    # position slots (the plan's own are freed)
+    scratches = [AssignScratch(64, cap), AssignScratch(256, 4 * cap, boxes=4)]
+    for sc in [None, scratches[0], scratches[1], None, scratches[1], scratches[0]]:
         est.use_scratch(sc)
         pouts = [np.empty((5, est.nbins_ps), order="F") for _ in boxes]
         bouts = [np.empty((est.brows, est.itot), order="F") for _ in boxes]
