@@ -11,7 +11,7 @@ struct TmPlan {
     int nsets = 1, npairs = 0, nslots = 0, nunits = 0, nA = 0;
     DevBuf units, prow, slots, err;
     DevBuf mexp;     // FP16 form: per-map power-of-two exponents
-    DevBuf kahan;    // per-CTA running sums when the kernel keeps them outside shared memory
+    DevBuf kahan;    // per-CTA running sums when they do not fit in TMEM beside the accumulators
     uint32_t wait_limit = 0;  // diagnostic: polls before a main-loop wait gives up (0: the default)
     int build(const Shells &sh, int nsets);
 };
