@@ -30,7 +30,9 @@ namespace pbi4g {
 template <class W>
 __device__ __forceinline__ void axis_stencil(double p, int N, int nintp, bool shifted, bool cic_nint, int &first,
                                              W w[4]) {
-    double v = (double)N * p + 1.0;  // vr = dble(Nv)*pos + 1
+    // vr = dble(Nv)*pos + 1 with the product and the sum rounded separately (no FMA
+    // contraction), as the oracle's ISO C and an FMA-free Fortran build compute it
+    double v = __dadd_rn(__dmul_rn((double)N, p), 1.0);
     if (shifted) v = v - 0.5;       // vt = vr - 0.5
     double h;
     if (nintp == 4) {

@@ -85,7 +85,7 @@ __device__ __forceinline__ int wrap_cell(long long t, int N) {
 }
 
 __device__ __forceinline__ void first_and_h(double p, int N, int nintp, bool shifted, bool cic_nint, int &f, float &h) {
-    double v = (double)N * p + 1.0;
+    double v = __dadd_rn(__dmul_rn((double)N, p), 1.0);  // two roundings, as in assign.cu
     if (shifted) v = v - 0.5;
     long long iv;
     double hh;
@@ -150,7 +150,7 @@ __device__ __forceinline__ int axis_tiles(int lo, int w, int N, int nt, int t[2]
 // first_and_h.
 __device__ __forceinline__ void first_cells(double p, int N, int nintp, bool interlaced, int &f0, float &h0, int &f1,
                                             float &h1) {
-    const double v = (double)N * p + 1.0;
+    const double v = __dadd_rn(__dmul_rn((double)N, p), 1.0);  // two roundings, as in assign.cu
     if (!(v >= 1.0 && v < 1048576.0)) {
         first_and_h(p, N, nintp, false, !interlaced, f0, h0);
         if (interlaced) first_and_h(p, N, nintp, true, false, f1, h1);
