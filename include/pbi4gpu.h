@@ -176,8 +176,10 @@ int pbi4g_plan_set_stream(pbi4g_plan *plan, void *stream);
  * position slot from its per-launch parameters).  A scratch never grows: a box
  * above its grid or particle count fails with PBI4G_ERR_RANGE.  Plans sharing a
  * scratch must not run concurrently.  The FP64 form has no such buffers
- * (use_scratch is a no-op).  destroy fails while plans still use it.  Replaces
- * nothing in the reference (its Fortran assignment needs no scratch). */
+ * (use_scratch is a no-op).  destroy fails while plans still use it.  Binding,
+ * destroying a bound plan and destroying a scratch keep a count of its plans:
+ * call them from one host thread.  Replaces nothing in the reference (its
+ * Fortran assignment needs no scratch). */
 typedef struct pbi4g_scratch pbi4g_scratch;
 int pbi4g_scratch_footprint(int32_t grid_max, int64_t npart_max, int32_t boxes, int64_t *bytes);
 int pbi4g_scratch_create(int32_t grid_max, int64_t npart_max, int32_t boxes, pbi4g_scratch **out);
